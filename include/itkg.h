@@ -1,0 +1,219 @@
+/*
+ * itkg.h -- C ABI of the GB300 (sm_103a) separable Gaussian path.
+ *
+ * This is the boundary a host binding (Rust `extern "C"`, C++, Python ctypes)
+ * calls in place of itk-rs's CPU implementation of GaussianFilter.  Types and
+ * functions mirror the reference's pipeline API for that path:
+ *
+ *   itkg_region      <-> Region<D>                      (src/image.rs:12-15)
+ *   itkg_image       <-> Image<P, D> + device residency (src/image.rs:82-87)
+ *   itkg_gaussian_*  <-> GaussianFilter<S>               (src/filters/gaussian.rs:13-91)
+ *   itkg_stream_full <-> stream_full                     (src/source.rs:81-98)
+ *   itkg_split_region<-> split_region                    (src/region_splitter.rs:17-48)
+ *
+ * Conventions
+ *   - Axis 0 is the fastest-varying axis (image.rs:111-120).  `dim` is D (1..3).
+ *   - Every call returns an itkg_status; ITKG_SUCCESS is 0.  On failure,
+ *     itkg_last_error() returns a message for the calling thread.  Where the
+ *     reference panics (a buffer that does not cover the region a filter must
+ *     read, capacity overflow for absurd radii) this ABI returns
+ *     ITKG_ERROR_INVALID_ARGUMENT instead.
+ *   - `stream` is an opaque cudaStream_t (NULL = legacy default stream).
+ *     Device work is enqueued on it; calls that touch host buffers synchronise
+ *     it before returning.
+ *   - No CUDA or framework types appear in signatures: plain pointers, sizes.
+ */
+#ifndef ITKG_H
+#define ITKG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ITKG_ABI_VERSION 1
+#define ITKG_MAX_DIM 3
+
+typedef enum itkg_status {
+    ITKG_SUCCESS = 0,
+    ITKG_ERROR_INVALID_ARGUMENT = 1, /* bad descriptor, region not covered, ... */
+    ITKG_ERROR_UNSUPPORTED = 2,      /* dtype / dimension combination not provided */
+    ITKG_ERROR_CUDA = 3,             /* CUDA runtime or driver error */
+    ITKG_ERROR_OUT_OF_MEMORY = 4,
+    ITKG_ERROR_NO_DEVICE = 5,        /* no usable sm_103 device */
+    ITKG_ERROR_TIMEOUT = 6           /* a bounded device-side wait expired */
+} itkg_status;
+
+/* Storage type of one pixel component. */
+typedef enum itkg_dtype {
+    ITKG_F32 = 0,
+    ITKG_I16 = 1,  /* read path: exact cast to f32 (UnaryFilter(i16 -> f32)) */
+    ITKG_U8 = 2,   /* read: cast to f32 (or u8 pixel arithmetic); write: round+clamp */
+    ITKG_BF16 = 3, /* storage only; arithmetic is f32 */
+    ITKG_F16 = 4   /* storage only; arithmetic is f32 */
+} itkg_dtype;
+
+/* Where `itkg_image::data` lives. */
+typedef enum itkg_location {
+    ITKG_DEVICE = 0, /* device pointer on the current CUDA device */
+    ITKG_HOST = 1    /* host pointer (pinned or pageable); staged by the library */
+} itkg_location;
+
+/* Pixel arithmetic of the filter. */
+typedef enum itkg_arithmetic {
+    /* f32 arithmetic: NumericPixel for f32 (src/pixel.rs:416-421) and, per
+     * component, VecPixel<f32,3> (src/pixel.rs:479-495).  i16/u8/bf16/f16
+     * inputs are converted exactly to f32 on load, which is the reference's
+     * UnaryFilter(p as f32) -> GaussianFilter<f32> chain
+     * (examples/blur_png.rs:35-37, tests/blur_png.rs:38-40). */
+    ITKG_ARITH_F32 = 0,
+    /* GaussianFilter<Image<u8>>: per tap round(x as f64 * w).clamp(0,255)
+     * as u8, u8 accumulator with wrapping adds (src/pixel.rs:430-435).
+     * Requires u8 input and u8 output. */
+    ITKG_ARITH_PIXEL_U8 = 1
+} itkg_arithmetic;
+
+/* Rounding discipline of the f32 arithmetic. */
+typedef enum itkg_rounding {
+    /* Bit-exact with the reference: acc = 0; acc = acc + x * (f32)w in
+     * ascending tap order, products and sums rounded separately, f32
+     * intermediates between passes (src/filters/conv.rs:26-36). */
+    ITKG_ROUND_REFERENCE = 0,
+    /* acc = fma(x, w, acc) in the same tap order; within 1e-5 normwise
+     * relative of the reference (typically ~1e-7). */
+    ITKG_ROUND_FMA = 1
+} itkg_rounding;
+
+/* Kernel selection. */
+typedef enum itkg_algorithm {
+    ITKG_ALGO_AUTO = 0,     /* fused when the radius fits a fused tile, else per-axis */
+    ITKG_ALGO_FUSED = 1,    /* fail with ITKG_ERROR_UNSUPPORTED if no fused kernel fits */
+    ITKG_ALGO_PER_AXIS = 2  /* D separate passes through an f32 scratch buffer */
+} itkg_algorithm;
+
+/* Region<D> (src/image.rs:12-15): index[d], size[d] for d < dim. */
+typedef struct itkg_region {
+    int64_t index[ITKG_MAX_DIM];
+    uint64_t size[ITKG_MAX_DIM];
+} itkg_region;
+
+/* Image<P, D> (src/image.rs:82-87) with an explicit, possibly padded, layout.
+ * Pixel (i0, i1, i2) of the buffered region lives at
+ *   data + (i0 - region.index[0]) * pitch[0]
+ *        + (i1 - region.index[1]) * pitch[1] + (i2 - region.index[2]) * pitch[2]
+ * pitch[0] must equal components * sizeof(dtype) (packed pixels). */
+typedef struct itkg_image {
+    int32_t dim;
+    int32_t dtype;      /* itkg_dtype */
+    int32_t components; /* 1 = scalar, 3 = VecPixel<_, 3> (interleaved) */
+    int32_t location;   /* itkg_location */
+    itkg_region region; /* buffered region (BufferedRegion) */
+    int64_t pitch[ITKG_MAX_DIM]; /* bytes between neighbours along each axis */
+    double spacing[ITKG_MAX_DIM];
+    double origin[ITKG_MAX_DIM];
+    void *data;
+} itkg_image;
+
+/* GaussianFilter { source, sigma } (src/filters/gaussian.rs:13-17) plus the
+ * GPU execution choices. Zero-initialised params = reference rounding, f32
+ * arithmetic, automatic kernel choice. */
+typedef struct itkg_gaussian_params {
+    double sigma;       /* standard deviation in physical units */
+    int32_t arithmetic; /* itkg_arithmetic */
+    int32_t rounding;   /* itkg_rounding */
+    int32_t algorithm;  /* itkg_algorithm */
+    int32_t reserved;   /* must be 0 */
+} itkg_gaussian_params;
+
+/* ---- library ----------------------------------------------------------- */
+
+int32_t itkg_abi_version(void);
+/* Message of the last failing call on this thread ("" if none). */
+const char *itkg_last_error(void);
+/* Name of the kernel the last successful filter call on this thread ran. */
+const char *itkg_last_kernel(void);
+/* Number of CUDA kernels this library has launched in this process. */
+uint64_t itkg_launch_counter(void);
+
+/* ---- host-side geometry (no device needed) ------------------------------ */
+
+/* GaussianFilter::kernel_radius (gaussian.rs:24-27): ceil(3*sigma/spacing)
+ * with Rust's saturating float->usize cast (NaN and negatives give 0). */
+uint64_t itkg_kernel_radius(double sigma, double spacing);
+
+/* GaussianFilter::build_kernel (gaussian.rs:29-40): 2*radius+1 f64 weights. */
+itkg_status itkg_build_kernel(double sigma_pixels, uint64_t radius, double *weights_out);
+
+/* Region::padded_per_axis (image.rs:28-37). */
+itkg_status itkg_region_padded_per_axis(const itkg_region *r, int32_t dim,
+                                        const uint64_t *radii, itkg_region *out);
+/* Region::clipped_to (image.rs:52-64). */
+itkg_status itkg_region_clipped_to(const itkg_region *r, int32_t dim,
+                                   const itkg_region *bounds, itkg_region *out);
+
+/* GaussianFilter::input_region_for_output (gaussian.rs:52-57). */
+itkg_status itkg_gaussian_input_region_for_output(const itkg_region *output_region,
+                                                  const itkg_region *largest, int32_t dim,
+                                                  const double *spacing, double sigma,
+                                                  itkg_region *input_region);
+
+/* split_region (region_splitter.rs:17-48). Writes at most `capacity` pieces and
+ * stores the number of pieces split_region yields in *count. */
+itkg_status itkg_split_region(const itkg_region *region, int32_t dim, uint64_t num_pieces,
+                              itkg_region *pieces, uint64_t capacity, uint64_t *count);
+
+/* ---- device memory helpers ---------------------------------------------- */
+
+itkg_status itkg_device_count(int32_t *count);
+itkg_status itkg_set_device(int32_t device);
+itkg_status itkg_device_alloc(size_t bytes, void **ptr);
+itkg_status itkg_device_free(void *ptr);
+itkg_status itkg_host_alloc_pinned(size_t bytes, void **ptr);
+itkg_status itkg_host_free_pinned(void *ptr);
+/* kind: 0 host->device, 1 device->host, 2 device->device, 3 default (UVA). */
+itkg_status itkg_memcpy(void *dst, const void *src, size_t bytes, int32_t kind, void *stream);
+itkg_status itkg_memset_device(void *dst, int32_t value, size_t bytes, void *stream);
+itkg_status itkg_stream_synchronize(void *stream);
+
+/* Fill *img for a freshly allocated device image of `region`, with rows and
+ * slices padded to 128-byte multiples (TMA-friendly), and allocate it. */
+itkg_status itkg_image_alloc_device(itkg_image *img, int32_t dim, int32_t dtype,
+                                    int32_t components, const itkg_region *region,
+                                    const double *spacing, const double *origin);
+itkg_status itkg_image_free(itkg_image *img);
+
+/* Image::copy_from (image.rs:133-140): copy src->region into dst, whose
+ * buffered region must contain it.  Either side may be host or device; the
+ * call returns after the copy completes. */
+itkg_status itkg_image_copy_from(itkg_image *dst, const itkg_image *src, void *stream);
+
+/* ---- the filter ----------------------------------------------------------
+ * GaussianFilter<S>::generate_region(requested) (gaussian.rs:59-91).
+ *   input     the upstream's output: its buffered region must contain
+ *             input_region_for_output(requested) (the reference requests
+ *             exactly that region from its source, gaussian.rs:71-72)
+ *   largest   source.largest_region(): the clamp-to-edge bounds
+ *   requested region to produce; must lie inside `largest`
+ *   output    buffered region must contain `requested`; only `requested` is
+ *             written (stream_full writes pieces in place)
+ * Spacing is taken from input->spacing. */
+itkg_status itkg_gaussian_generate_region(const itkg_image *input, const itkg_region *largest,
+                                          const itkg_region *requested,
+                                          const itkg_gaussian_params *params,
+                                          itkg_image *output, void *stream);
+
+/* stream_full(&GaussianFilter{input, sigma}, num_pieces) (source.rs:81-98):
+ * output (region == largest) is filled piece by piece along axis D-1.  With a
+ * host-resident input and output, only one halo-padded input slab and one
+ * output slab are resident on the device at a time (out-of-core streaming). */
+itkg_status itkg_stream_full(const itkg_image *input, const itkg_region *largest,
+                             const itkg_gaussian_params *params, uint64_t num_pieces,
+                             itkg_image *output, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ITKG_H */

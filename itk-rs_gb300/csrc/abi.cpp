@@ -1,0 +1,692 @@
+// C-ABI implementation: validation, region geometry, host staging and kernel
+// dispatch for GaussianFilter::generate_region and stream_full.
+//
+// Region geometry follows the reference exactly:
+//   kernel_radius            src/filters/gaussian.rs:24-27
+//   build_kernel             src/filters/gaussian.rs:29-40
+//   input_region_for_output  src/filters/gaussian.rs:52-57
+//   generate_region passes   src/filters/gaussian.rs:59-91
+//   padded_per_axis/clipped  src/image.rs:28-64
+//   split_region             src/region_splitter.rs:17-48
+//   stream_full              src/source.rs:81-98
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "internal.hpp"
+
+namespace itkg {
+
+namespace {
+thread_local std::string t_error;
+thread_local std::string t_kernel;
+}  // namespace
+
+itkg_status set_error(itkg_status st, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  t_error = buf;
+  return st;
+}
+
+void set_last_kernel(const char* name) { t_kernel = name; }
+
+namespace {
+std::atomic<uint64_t> g_launches{0};
+}  // namespace
+
+void note_launch(const char* name) {
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  t_kernel = name;
+}
+
+static itkg_status cuda_status(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return ITKG_SUCCESS;
+  cudaGetLastError();  // clear sticky-free errors
+  if (e == cudaErrorMemoryAllocation)
+    return set_error(ITKG_ERROR_OUT_OF_MEMORY, "%s: %s", what, cudaGetErrorString(e));
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver)
+    return set_error(ITKG_ERROR_NO_DEVICE, "%s: %s", what, cudaGetErrorString(e));
+  return set_error(ITKG_ERROR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define ITKG_CUDA(call)                                   \
+  do {                                                    \
+    cudaError_t e_ = (call);                              \
+    if (e_ != cudaSuccess) return cuda_status(e_, #call); \
+  } while (0)
+
+#define ITKG_TRY(expr)                        \
+  do {                                        \
+    itkg_status s_ = (expr);                  \
+    if (s_ != ITKG_SUCCESS) return s_;        \
+  } while (0)
+
+// ---- scratch: one memory pool per device, never trimmed --------------------
+namespace {
+std::mutex g_pool_mu;
+std::vector<cudaMemPool_t> g_pools;  // indexed by device
+}  // namespace
+
+static itkg_status device_pool(cudaMemPool_t* out) {
+  int dev = 0;
+  ITKG_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(g_pool_mu);
+  if ((int)g_pools.size() <= dev) g_pools.resize(dev + 1, nullptr);
+  if (!g_pools[dev]) {
+    cudaMemPoolProps props;
+    std::memset(&props, 0, sizeof props);
+    props.allocType = cudaMemAllocationTypePinned;
+    props.handleTypes = cudaMemHandleTypeNone;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t pool;
+    ITKG_CUDA(cudaMemPoolCreate(&pool, &props));
+    uint64_t thr = UINT64_MAX;
+    ITKG_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
+    g_pools[dev] = pool;
+  }
+  *out = g_pools[dev];
+  return ITKG_SUCCESS;
+}
+
+itkg_status scratch_alloc(void** p, size_t bytes, void* stream) {
+  cudaMemPool_t pool;
+  ITKG_TRY(device_pool(&pool));
+  if (bytes == 0) bytes = 256;
+  ITKG_CUDA(cudaMallocFromPoolAsync(p, bytes, pool, static_cast<cudaStream_t>(stream)));
+  return ITKG_SUCCESS;
+}
+
+void scratch_free(void* p, void* stream) {
+  if (p) cudaFreeAsync(p, static_cast<cudaStream_t>(stream));
+}
+
+// ---- geometry helpers ---------------------------------------------------------
+static uint64_t kernel_radius(double sigma, double spacing) {
+  const double c = std::ceil(3.0 * (sigma / spacing));
+  if (!(c > 0.0)) return 0;  // NaN and non-positive saturate to 0
+  if (c >= 18446744073709551615.0) return UINT64_MAX;
+  return (uint64_t)c;
+}
+
+static void build_kernel(double sigma_px, uint64_t radius, double* out) {
+  const uint64_t len = 2 * radius + 1;
+  for (uint64_t i = 0; i < len; ++i) {
+    const double x = (double)i - (double)radius;
+    const double t = x / sigma_px;
+    out[i] = std::exp(-0.5 * (t * t));
+  }
+  double sum = 0.0;
+  for (uint64_t i = 0; i < len; ++i) sum += out[i];
+  for (uint64_t i = 0; i < len; ++i) out[i] /= sum;
+}
+
+static itkg_region padded(const itkg_region& r, int D, const uint64_t* radii) {
+  itkg_region o = r;
+  for (int d = 0; d < D; ++d) {
+    o.index[d] -= (int64_t)radii[d];
+    o.size[d] += 2 * radii[d];
+  }
+  return o;
+}
+
+static itkg_region clipped(const itkg_region& r, int D, const itkg_region& b) {
+  itkg_region o = r;
+  for (int d = 0; d < D; ++d) {
+    const int64_t se = r.index[d] + (int64_t)r.size[d];
+    const int64_t be = b.index[d] + (int64_t)b.size[d];
+    const int64_t s = std::max(r.index[d], b.index[d]);
+    const int64_t e = std::min(se, be);
+    o.index[d] = s;
+    o.size[d] = e > s ? (uint64_t)(e - s) : 0;
+  }
+  return o;
+}
+
+static uint64_t region_len(const itkg_region& r, int D) {
+  uint64_t n = 1;
+  for (int d = 0; d < D; ++d) n *= r.size[d];
+  return n;
+}
+
+static bool region_contains(const itkg_region& outer, const itkg_region& inner, int D) {
+  for (int d = 0; d < D; ++d) {
+    if (inner.size[d] == 0) return true;
+    if (inner.index[d] < outer.index[d]) return false;
+    if (inner.index[d] + (int64_t)inner.size[d] > outer.index[d] + (int64_t)outer.size[d])
+      return false;
+  }
+  return true;
+}
+
+// Fill unused trailing axes so kernels can treat every image as 3-D.
+static itkg_region full3(const itkg_region& r, int D) {
+  itkg_region o = r;
+  for (int d = D; d < kMaxDim; ++d) {
+    o.index[d] = 0;
+    o.size[d] = 1;
+  }
+  return o;
+}
+
+static itkg_status validate_image(const itkg_image* im, const char* name) {
+  if (!im) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "%s is NULL", name);
+  if (im->dim < 1 || im->dim > kMaxDim)
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "%s: dim %d not in 1..3", name, im->dim);
+  if (dtype_size(im->dtype) == 0)
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "%s: unknown dtype %d", name, im->dtype);
+  if (im->components != 1 && im->components != 3)
+    return set_error(ITKG_ERROR_UNSUPPORTED, "%s: components must be 1 or 3", name);
+  if (im->location != ITKG_DEVICE && im->location != ITKG_HOST)
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "%s: unknown location", name);
+  const int64_t pb = (int64_t)im->components * dtype_size(im->dtype);
+  if (im->pitch[0] != pb)
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "%s: pitch[0]=%lld must equal the pixel size %lld",
+                     name, (long long)im->pitch[0], (long long)pb);
+  for (int d = 1; d < im->dim; ++d)
+    if (im->pitch[d] <= 0 || im->pitch[d] % dtype_size(im->dtype) != 0)
+      return set_error(ITKG_ERROR_INVALID_ARGUMENT, "%s: pitch[%d] invalid", name, d);
+  if (!im->data && region_len(im->region, im->dim) != 0)
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "%s: data is NULL", name);
+  return ITKG_SUCCESS;
+}
+
+// Normalised device view of an image (3-D, pitches for unused axes = 0).
+static void origin_pitch(const itkg_image& im, int64_t* origin, int64_t* pitch) {
+  for (int d = 0; d < kMaxDim; ++d) {
+    origin[d] = d < im.dim ? im.region.index[d] : 0;
+    pitch[d] = d < im.dim ? im.pitch[d] : 0;
+  }
+}
+
+// Dense layout with rows and slices padded to `align` bytes.
+static void dense_layout(itkg_image* im, int align) {
+  const int64_t pb = (int64_t)im->components * dtype_size(im->dtype);
+  im->pitch[0] = pb;
+  int64_t row = (int64_t)im->region.size[0] * pb;
+  if (align > 1) row = (row + align - 1) / align * align;
+  if (row == 0) row = align > 1 ? align : pb;
+  im->pitch[1] = row;
+  im->pitch[2] = row * (int64_t)(im->dim >= 2 ? std::max<uint64_t>(im->region.size[1], 1) : 1);
+  for (int d = im->dim; d < kMaxDim; ++d) im->pitch[d] = d == 1 ? row : im->pitch[d];
+}
+
+static size_t image_bytes(const itkg_image& im) {
+  if (region_len(im.region, im.dim) == 0) return 0;
+  size_t last = 0;
+  for (int d = 0; d < im.dim; ++d) last += (size_t)(im.region.size[d] - 1) * (size_t)im.pitch[d];
+  return last + (size_t)im.pitch[0];
+}
+
+// Copy `reg` between two images (any locations) with 2-D copies per slice, or
+// one copy when both sides are contiguous over the region.
+static itkg_status copy_region(const itkg_image& dst, const itkg_image& src, const itkg_region& reg0,
+                               cudaStream_t s) {
+  const int D = src.dim;
+  const itkg_region reg = full3(reg0, D);
+  if (region_len(reg, D) == 0) return ITKG_SUCCESS;
+  int64_t so[3], sp[3], dof[3], dp[3];
+  origin_pitch(src, so, sp);
+  origin_pitch(dst, dof, dp);
+  const size_t pb = (size_t)src.pitch[0];
+  const size_t width = (size_t)reg.size[0] * pb;
+  auto sptr = [&](int64_t y, int64_t z) {
+    return static_cast<const char*>(src.data) + (reg.index[0] - so[0]) * sp[0] +
+           (y - so[1]) * sp[1] + (z - so[2]) * sp[2];
+  };
+  auto dptr = [&](int64_t y, int64_t z) {
+    return static_cast<char*>(dst.data) + (reg.index[0] - dof[0]) * dp[0] + (y - dof[1]) * dp[1] +
+           (z - dof[2]) * dp[2];
+  };
+  const uint64_t ny = reg.size[1], nz = reg.size[2];
+  // whole region contiguous on both sides?
+  const bool rows_dense = (D < 2 || ((size_t)sp[1] == width && (size_t)dp[1] == width));
+  const bool slices_dense =
+      (D < 3 || ((size_t)sp[2] == width * ny && (size_t)dp[2] == width * ny));
+  if (rows_dense && slices_dense) {
+    ITKG_CUDA(cudaMemcpyAsync(dptr(reg.index[1], reg.index[2]), sptr(reg.index[1], reg.index[2]),
+                              width * ny * nz, cudaMemcpyDefault, s));
+    return ITKG_SUCCESS;
+  }
+  for (uint64_t z = 0; z < nz; ++z) {
+    const int64_t az = reg.index[2] + (int64_t)z;
+    const size_t spitch = D >= 2 ? (size_t)sp[1] : width;
+    const size_t dpitch = D >= 2 ? (size_t)dp[1] : width;
+    ITKG_CUDA(cudaMemcpy2DAsync(dptr(reg.index[1], az), dpitch, sptr(reg.index[1], az), spitch,
+                                width, ny, cudaMemcpyDefault, s));
+  }
+  return ITKG_SUCCESS;
+}
+
+struct Plan {
+  int D = 0;
+  uint64_t radii[kMaxDim] = {0, 0, 0};
+  std::vector<double> w64[kMaxDim];
+  std::vector<float> w32[kMaxDim];
+  itkg_region in_reg;
+};
+
+static itkg_status make_plan(const itkg_image& in, const itkg_region& requested, const itkg_region& largest,
+                             double sigma, Plan* p) {
+  const int D = in.dim;
+  p->D = D;
+  for (int d = 0; d < D; ++d) {
+    const uint64_t r = kernel_radius(sigma, in.spacing[d]);
+    if (r > (1u << 20))
+      return set_error(ITKG_ERROR_INVALID_ARGUMENT,
+                       "kernel radius %llu on axis %d (sigma=%g, spacing=%g) is not allocatable",
+                       (unsigned long long)r, d, sigma, in.spacing[d]);
+    p->radii[d] = r;
+    p->w64[d].resize(2 * r + 1);
+    build_kernel(sigma / in.spacing[d], r, p->w64[d].data());
+    p->w32[d].resize(2 * r + 1);
+    for (size_t k = 0; k < p->w64[d].size(); ++k) p->w32[d][k] = (float)p->w64[d][k];
+  }
+  p->in_reg = clipped(padded(requested, D, p->radii), D, largest);
+  return ITKG_SUCCESS;
+}
+
+// ---- per-axis execution (D passes through scratch) --------------------------
+static itkg_status run_per_axis(const itkg_image& in, const itkg_region& largest,
+                                const itkg_region& requested, const itkg_gaussian_params& prm,
+                                const Plan& plan, const itkg_image& out, cudaStream_t s) {
+  const int D = in.dim;
+  const bool u8pix = prm.arithmetic == ITKG_ARITH_PIXEL_U8;
+  const int scratch_dtype = u8pix ? ITKG_U8 : ITKG_F32;
+  // intermediate regions (gaussian.rs:79-85)
+  itkg_region regs[kMaxDim];
+  size_t max_bytes = 0;
+  for (int a = 0; a < D; ++a) {
+    if (a + 1 < D) {
+      uint64_t rem[kMaxDim] = {0, 0, 0};
+      for (int d = a + 1; d < D; ++d) rem[d] = plan.radii[d];
+      regs[a] = clipped(padded(requested, D, rem), D, largest);
+      const size_t bytes = region_len(regs[a], D) * (size_t)in.components * dtype_size(scratch_dtype);
+      max_bytes = std::max(max_bytes, bytes);
+    } else {
+      regs[a] = requested;
+    }
+  }
+  void* bufs[2] = {nullptr, nullptr};
+  if (D > 1) {
+    ITKG_TRY(scratch_alloc(&bufs[0], max_bytes, s));
+    if (D > 2) {
+      itkg_status st = scratch_alloc(&bufs[1], max_bytes, s);
+      if (st != ITKG_SUCCESS) {
+        scratch_free(bufs[0], s);
+        return st;
+      }
+    }
+  }
+  itkg_image cur = in;
+  itkg_status st = ITKG_SUCCESS;
+  for (int a = 0; a < D && st == ITKG_SUCCESS; ++a) {
+    itkg_image nxt;
+    if (a + 1 < D) {
+      std::memset(&nxt, 0, sizeof nxt);
+      nxt.dim = D;
+      nxt.dtype = scratch_dtype;
+      nxt.components = in.components;
+      nxt.region = regs[a];
+      dense_layout(&nxt, 1);
+      nxt.data = bufs[a & 1];
+    } else {
+      nxt = out;
+    }
+    AxisArgs args;
+    std::memset(&args, 0, sizeof args);
+    args.src = cur.data;
+    args.dst = nxt.data;
+    origin_pitch(cur, args.src_origin, args.src_pitch);
+    origin_pitch(nxt, args.dst_origin, args.dst_pitch);
+    const itkg_region o3 = full3(regs[a], D);
+    for (int d = 0; d < kMaxDim; ++d) {
+      args.out_index[d] = o3.index[d];
+      args.out_size[d] = (int64_t)o3.size[d];
+    }
+    args.lo = largest.index[a];
+    args.hi = largest.index[a] + (int64_t)largest.size[a] - 1;
+    args.axis = a;
+    args.radius = (int32_t)plan.radii[a];
+    args.comps = in.components;
+    if (u8pix) {
+      st = launch_conv_axis_u8(args, plan.w64[a].data(), s);
+    } else {
+      const int in_dt = a == 0 ? in.dtype : ITKG_F32;
+      const int out_dt = a + 1 < D ? ITKG_F32 : out.dtype;
+      st = launch_conv_axis_f32(args, plan.w32[a].data(), in_dt, out_dt, prm.rounding, s);
+    }
+    cur = nxt;
+  }
+  scratch_free(bufs[0], s);
+  scratch_free(bufs[1], s);
+  if (st == ITKG_SUCCESS) set_last_kernel(u8pix ? "per_axis_u8_pixel" : prm.rounding == ITKG_ROUND_REFERENCE ? "per_axis_f32_ref" : "per_axis_f32_fma");
+  return st;
+}
+
+static itkg_status check_params(const itkg_gaussian_params* prm) {
+  if (!prm) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "params is NULL");
+  if (prm->arithmetic != ITKG_ARITH_F32 && prm->arithmetic != ITKG_ARITH_PIXEL_U8)
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "unknown arithmetic %d", prm->arithmetic);
+  if (prm->rounding != ITKG_ROUND_REFERENCE && prm->rounding != ITKG_ROUND_FMA)
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "unknown rounding %d", prm->rounding);
+  if (prm->algorithm < ITKG_ALGO_AUTO || prm->algorithm > ITKG_ALGO_PER_AXIS)
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "unknown algorithm %d", prm->algorithm);
+  if (prm->reserved != 0) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "reserved must be 0");
+  return ITKG_SUCCESS;
+}
+
+// Device-resident input and output.
+static itkg_status generate_device(const itkg_image& in, const itkg_region& largest,
+                                   const itkg_region& requested, const itkg_gaussian_params& prm,
+                                   const Plan& plan, const itkg_image& out, cudaStream_t s) {
+  const int D = in.dim;
+  if (prm.arithmetic != ITKG_ARITH_PIXEL_U8 && prm.algorithm != ITKG_ALGO_PER_AXIS) {
+    FusedGeom g;
+    std::memset(&g, 0, sizeof g);
+    g.src = in.data;
+    g.dst = out.data;
+    origin_pitch(in, g.src_origin, g.src_pitch);
+    origin_pitch(out, g.dst_origin, g.dst_pitch);
+    const itkg_region r3 = full3(requested, D);
+    const itkg_region l3 = full3(largest, D);
+    for (int d = 0; d < kMaxDim; ++d) {
+      g.req_index[d] = r3.index[d];
+      g.req_size[d] = (int64_t)r3.size[d];
+      g.lo[d] = l3.index[d];
+      g.hi[d] = l3.index[d] + (int64_t)l3.size[d] - 1;
+      g.radius[d] = d < D ? (int32_t)plan.radii[d] : 0;
+    }
+    g.dim = D;
+    g.comps = in.components;
+    g.in_dtype = in.dtype;
+    g.out_dtype = out.dtype;
+    g.rounding = prm.rounding;
+    const float* w[kMaxDim] = {nullptr, nullptr, nullptr};
+    for (int d = 0; d < D; ++d) w[d] = plan.w32[d].data();
+    itkg_status st = launch_fused(g, w, s, /*dry_run=*/true);
+    if (st == ITKG_SUCCESS) return launch_fused(g, w, s, false);
+    if (prm.algorithm == ITKG_ALGO_FUSED)
+      return set_error(ITKG_ERROR_UNSUPPORTED, "no fused kernel covers this geometry");
+  }
+  return run_per_axis(in, largest, requested, prm, plan, out, s);
+}
+
+static itkg_status generate_region(const itkg_image* input, const itkg_region* largest,
+                                   const itkg_region* requested, const itkg_gaussian_params* prm,
+                                   const itkg_image* output, cudaStream_t s) {
+  ITKG_TRY(validate_image(input, "input"));
+  ITKG_TRY(validate_image(output, "output"));
+  ITKG_TRY(check_params(prm));
+  if (!largest || !requested) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "region is NULL");
+  const int D = input->dim;
+  if (output->dim != D) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "input/output dim differ");
+  if (output->components != input->components)
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "input/output components differ");
+  if (prm->arithmetic == ITKG_ARITH_PIXEL_U8) {
+    if (input->dtype != ITKG_U8 || output->dtype != ITKG_U8)
+      return set_error(ITKG_ERROR_INVALID_ARGUMENT, "u8 pixel arithmetic needs u8 input and output");
+  } else if (output->dtype == ITKG_I16) {
+    return set_error(ITKG_ERROR_UNSUPPORTED, "i16 output is not provided (the reference has no i16 NumericPixel)");
+  }
+  if (region_len(*requested, D) == 0) return ITKG_SUCCESS;
+  if (!region_contains(*largest, *requested, D))
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "requested region lies outside the largest region");
+  if (!region_contains(output->region, *requested, D))
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "output buffer does not contain the requested region");
+  Plan plan;
+  ITKG_TRY(make_plan(*input, *requested, *largest, prm->sigma, &plan));
+  if (!region_contains(input->region, plan.in_reg, D))
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT,
+                     "input buffer does not cover input_region_for_output(requested)");
+
+  const bool host_in = input->location == ITKG_HOST;
+  const bool host_out = output->location == ITKG_HOST;
+  if (!host_in && !host_out) return generate_device(*input, *largest, *requested, *prm, plan, *output, s);
+
+  // Stage host buffers through stream-ordered scratch.
+  itkg_image din = *input, dout = *output;
+  void* pin = nullptr;
+  void* pout = nullptr;
+  itkg_status st = ITKG_SUCCESS;
+  if (host_in) {
+    din.location = ITKG_DEVICE;
+    din.region = plan.in_reg;
+    dense_layout(&din, 16);
+    st = scratch_alloc(&pin, image_bytes(din), s);
+    if (st == ITKG_SUCCESS) {
+      din.data = pin;
+      st = copy_region(din, *input, plan.in_reg, s);
+    }
+  }
+  if (st == ITKG_SUCCESS && host_out) {
+    dout.location = ITKG_DEVICE;
+    dout.region = *requested;
+    dense_layout(&dout, 16);
+    st = scratch_alloc(&pout, image_bytes(dout), s);
+    if (st == ITKG_SUCCESS) dout.data = pout;
+  }
+  if (st == ITKG_SUCCESS) st = generate_device(din, *largest, *requested, *prm, plan, dout, s);
+  if (st == ITKG_SUCCESS && host_out) st = copy_region(*output, dout, *requested, s);
+  scratch_free(pin, s);
+  scratch_free(pout, s);
+  if (st == ITKG_SUCCESS) {
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_status(e, "cudaStreamSynchronize");
+  }
+  return st;
+}
+
+}  // namespace itkg
+
+using namespace itkg;
+
+extern "C" {
+
+int32_t itkg_abi_version(void) { return ITKG_ABI_VERSION; }
+const char* itkg_last_error(void) { return t_error.c_str(); }
+const char* itkg_last_kernel(void) { return t_kernel.c_str(); }
+uint64_t itkg_launch_counter(void) { return g_launches.load(std::memory_order_relaxed); }
+
+uint64_t itkg_kernel_radius(double sigma, double spacing) { return kernel_radius(sigma, spacing); }
+
+itkg_status itkg_build_kernel(double sigma_pixels, uint64_t radius, double* weights_out) {
+  if (!weights_out) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "weights_out is NULL");
+  if (radius > (1u << 20)) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "radius too large");
+  build_kernel(sigma_pixels, radius, weights_out);
+  return ITKG_SUCCESS;
+}
+
+itkg_status itkg_region_padded_per_axis(const itkg_region* r, int32_t dim, const uint64_t* radii,
+                                        itkg_region* out) {
+  if (!r || !radii || !out || dim < 1 || dim > kMaxDim)
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "bad argument");
+  *out = padded(*r, dim, radii);
+  return ITKG_SUCCESS;
+}
+
+itkg_status itkg_region_clipped_to(const itkg_region* r, int32_t dim, const itkg_region* bounds,
+                                   itkg_region* out) {
+  if (!r || !bounds || !out || dim < 1 || dim > kMaxDim)
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "bad argument");
+  *out = clipped(*r, dim, *bounds);
+  return ITKG_SUCCESS;
+}
+
+itkg_status itkg_gaussian_input_region_for_output(const itkg_region* output_region,
+                                                  const itkg_region* largest, int32_t dim,
+                                                  const double* spacing, double sigma,
+                                                  itkg_region* input_region) {
+  if (!output_region || !largest || !spacing || !input_region || dim < 1 || dim > kMaxDim)
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "bad argument");
+  uint64_t radii[kMaxDim] = {0, 0, 0};
+  for (int d = 0; d < dim; ++d) radii[d] = kernel_radius(sigma, spacing[d]);
+  *input_region = clipped(padded(*output_region, dim, radii), dim, *largest);
+  return ITKG_SUCCESS;
+}
+
+itkg_status itkg_split_region(const itkg_region* region, int32_t dim, uint64_t num_pieces,
+                              itkg_region* pieces, uint64_t capacity, uint64_t* count) {
+  if (!region || !count || dim < 1 || dim > kMaxDim)
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "bad argument");
+  num_pieces = num_pieces < 1 ? 1 : num_pieces;
+  *count = 0;
+  if (region_len(*region, dim) == 0) return ITKG_SUCCESS;
+  const int slow = dim - 1;
+  const uint64_t total = region->size[slow];
+  uint64_t actual = std::min(num_pieces, total);
+  actual = actual < 1 ? 1 : actual;
+  const uint64_t base = total / actual, rem = total % actual;
+  int64_t start = region->index[slow];
+  for (uint64_t i = 0; i < actual; ++i) {
+    const uint64_t sz = base + (i < rem ? 1 : 0);
+    if (pieces && i < capacity) {
+      pieces[i] = *region;
+      pieces[i].index[slow] = start;
+      pieces[i].size[slow] = sz;
+    }
+    start += (int64_t)sz;
+  }
+  *count = actual;
+  return ITKG_SUCCESS;
+}
+
+itkg_status itkg_device_count(int32_t* count) {
+  if (!count) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "count is NULL");
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    *count = 0;
+    return ITKG_SUCCESS;
+  }
+  *count = n;
+  return ITKG_SUCCESS;
+}
+
+itkg_status itkg_set_device(int32_t device) {
+  ITKG_CUDA(cudaSetDevice(device));
+  return ITKG_SUCCESS;
+}
+
+itkg_status itkg_device_alloc(size_t bytes, void** ptr) {
+  if (!ptr) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "ptr is NULL");
+  ITKG_CUDA(cudaMalloc(ptr, bytes ? bytes : 1));
+  return ITKG_SUCCESS;
+}
+
+itkg_status itkg_device_free(void* ptr) {
+  ITKG_CUDA(cudaFree(ptr));
+  return ITKG_SUCCESS;
+}
+
+itkg_status itkg_host_alloc_pinned(size_t bytes, void** ptr) {
+  if (!ptr) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "ptr is NULL");
+  ITKG_CUDA(cudaMallocHost(ptr, bytes ? bytes : 1));
+  return ITKG_SUCCESS;
+}
+
+itkg_status itkg_host_free_pinned(void* ptr) {
+  ITKG_CUDA(cudaFreeHost(ptr));
+  return ITKG_SUCCESS;
+}
+
+itkg_status itkg_memcpy(void* dst, const void* src, size_t bytes, int32_t kind, void* stream) {
+  cudaMemcpyKind k = kind == 0   ? cudaMemcpyHostToDevice
+                     : kind == 1 ? cudaMemcpyDeviceToHost
+                     : kind == 2 ? cudaMemcpyDeviceToDevice
+                                 : cudaMemcpyDefault;
+  ITKG_CUDA(cudaMemcpyAsync(dst, src, bytes, k, static_cast<cudaStream_t>(stream)));
+  return ITKG_SUCCESS;
+}
+
+itkg_status itkg_memset_device(void* dst, int32_t value, size_t bytes, void* stream) {
+  ITKG_CUDA(cudaMemsetAsync(dst, value, bytes, static_cast<cudaStream_t>(stream)));
+  return ITKG_SUCCESS;
+}
+
+itkg_status itkg_stream_synchronize(void* stream) {
+  ITKG_CUDA(cudaStreamSynchronize(static_cast<cudaStream_t>(stream)));
+  return ITKG_SUCCESS;
+}
+
+itkg_status itkg_image_alloc_device(itkg_image* img, int32_t dim, int32_t dtype, int32_t components,
+                                    const itkg_region* region, const double* spacing,
+                                    const double* origin) {
+  if (!img || !region || dim < 1 || dim > kMaxDim || dtype_size(dtype) == 0 ||
+      (components != 1 && components != 3))
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "bad argument");
+  std::memset(img, 0, sizeof *img);
+  img->dim = dim;
+  img->dtype = dtype;
+  img->components = components;
+  img->location = ITKG_DEVICE;
+  img->region = *region;
+  for (int d = 0; d < kMaxDim; ++d) {
+    img->spacing[d] = spacing ? (d < dim ? spacing[d] : 1.0) : 1.0;
+    img->origin[d] = origin ? (d < dim ? origin[d] : 0.0) : 0.0;
+  }
+  dense_layout(img, 128);
+  void* p = nullptr;
+  ITKG_CUDA(cudaMalloc(&p, std::max<size_t>(image_bytes(*img), 128)));
+  img->data = p;
+  return ITKG_SUCCESS;
+}
+
+itkg_status itkg_image_free(itkg_image* img) {
+  if (!img) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "img is NULL");
+  if (img->data) ITKG_CUDA(cudaFree(img->data));
+  img->data = nullptr;
+  return ITKG_SUCCESS;
+}
+
+itkg_status itkg_image_copy_from(itkg_image* dst, const itkg_image* src, void* stream) {
+  ITKG_TRY(validate_image(dst, "dst"));
+  ITKG_TRY(validate_image(src, "src"));
+  if (dst->dim != src->dim || dst->dtype != src->dtype || dst->components != src->components)
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "copy_from: images differ in dim, dtype or components");
+  if (!region_contains(dst->region, src->region, src->dim))
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "copy_from: dst does not contain src's region");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  ITKG_TRY(copy_region(*dst, *src, src->region, s));
+  ITKG_CUDA(cudaStreamSynchronize(s));
+  return ITKG_SUCCESS;
+}
+
+itkg_status itkg_gaussian_generate_region(const itkg_image* input, const itkg_region* largest,
+                                          const itkg_region* requested,
+                                          const itkg_gaussian_params* params, itkg_image* output,
+                                          void* stream) {
+  return generate_region(input, largest, requested, params, output,
+                         static_cast<cudaStream_t>(stream));
+}
+
+itkg_status itkg_stream_full(const itkg_image* input, const itkg_region* largest,
+                             const itkg_gaussian_params* params, uint64_t num_pieces,
+                             itkg_image* output, void* stream) {
+  ITKG_TRY(validate_image(input, "input"));
+  ITKG_TRY(validate_image(output, "output"));
+  if (!largest) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "largest is NULL");
+  const int D = input->dim;
+  if (!region_contains(output->region, *largest, D))
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "output buffer does not contain the largest region");
+  uint64_t count = 0;
+  ITKG_TRY(itkg_split_region(largest, D, num_pieces, nullptr, 0, &count));
+  std::vector<itkg_region> pieces(count);
+  ITKG_TRY(itkg_split_region(largest, D, num_pieces, pieces.data(), count, &count));
+  for (const itkg_region& p : pieces)
+    ITKG_TRY(generate_region(input, largest, &p, params, output, static_cast<cudaStream_t>(stream)));
+  return ITKG_SUCCESS;
+}
+
+}  // extern "C"

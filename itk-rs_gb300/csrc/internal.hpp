@@ -1,0 +1,109 @@
+// Internal declarations shared by the C-ABI layer (abi.cpp) and the CUDA
+// translation units.  Nothing here is part of the public ABI.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "itkg.h"
+
+namespace itkg {
+
+constexpr int kMaxDim = ITKG_MAX_DIM;
+
+// Largest tap count the per-axis kernels take by value as a launch parameter
+// (r <= 384: 769 f32 weights = 3076 bytes, under the classic 4 KB limit).
+constexpr int kMaxParamTaps = 769;
+// Largest radius the u8 pixel-arithmetic path supports (LUT of K*256 bytes
+// in shared memory, K <= 255).
+constexpr int kMaxU8Radius = 127;
+
+// ---- error reporting (thread-local) ----------------------------------------
+itkg_status set_error(itkg_status st, const char* fmt, ...);
+void set_last_kernel(const char* name);
+// Called at every kernel launch: bumps the process-wide launch counter and
+// records the kernel name for itkg_last_kernel().
+void note_launch(const char* name);
+
+// ---- dtype helpers --------------------------------------------------------
+inline int dtype_size(int dt) {
+  switch (dt) {
+    case ITKG_F32: return 4;
+    case ITKG_I16: return 2;
+    case ITKG_U8: return 1;
+    case ITKG_BF16: return 2;
+    case ITKG_F16: return 2;
+    default: return 0;
+  }
+}
+
+// ---- one separable pass over one axis --------------------------------------
+// Output voxel o (absolute index, inside out_index/out_size) gets
+//   sum_k w[k] * src[o with o[axis] := clamp(o[axis] + k - r, lo, hi)]
+// src/dst addresses: base + sum_d (idx[d] - origin[d]) * pitch[d] + c * elem.
+struct AxisArgs {
+  const void* src;
+  void* dst;
+  int64_t src_origin[kMaxDim];
+  int64_t src_pitch[kMaxDim];  // bytes
+  int64_t dst_origin[kMaxDim];
+  int64_t dst_pitch[kMaxDim];  // bytes
+  int64_t out_index[kMaxDim];
+  int64_t out_size[kMaxDim];
+  int64_t lo, hi;              // clamp bounds on `axis` (absolute)
+  int32_t axis;
+  int32_t radius;
+  int32_t comps;
+  int32_t pad_;
+};
+
+struct AxisWeightsF32 {
+  float w[kMaxParamTaps];
+};
+
+struct AxisWeightsF64 {  // u8 pixel path: exact f64 weights
+  double w[kMaxParamTaps / 2];
+};
+
+// conv_axis.cu
+itkg_status launch_conv_axis_f32(const AxisArgs& a, const float* w, int in_dtype,
+                                 int out_dtype, int rounding, void* stream);
+itkg_status launch_conv_axis_u8(const AxisArgs& a, const double* w, void* stream);
+
+// ---- fused whole-filter kernels ---------------------------------------------
+// Geometry shared by every fused launch.  All indices absolute; the clamp
+// bounds on every axis are the largest region.
+struct FusedGeom {
+  const void* src;
+  void* dst;
+  int64_t src_origin[kMaxDim];
+  int64_t src_pitch[kMaxDim];  // bytes
+  int64_t dst_origin[kMaxDim];
+  int64_t dst_pitch[kMaxDim];  // bytes
+  int64_t req_index[kMaxDim];  // requested region
+  int64_t req_size[kMaxDim];
+  int64_t lo[kMaxDim];         // largest region bounds
+  int64_t hi[kMaxDim];
+  int32_t radius[kMaxDim];
+  int32_t dim;
+  int32_t comps;
+  int32_t in_dtype;
+  int32_t out_dtype;
+  int32_t rounding;
+  int32_t pad_;
+};
+
+// fused.cu: returns ITKG_ERROR_UNSUPPORTED (without setting an error) when no
+// fused kernel covers the geometry; the caller then uses the per-axis path.
+itkg_status launch_fused(const FusedGeom& g, const float* const w[kMaxDim], void* stream,
+                         bool dry_run);
+
+// ---- device scratch ---------------------------------------------------------
+// Stream-ordered scratch from a library-owned memory pool of the current
+// device (cudaMallocAsync / cudaFreeAsync on `stream`).
+itkg_status scratch_alloc(void** p, size_t bytes, void* stream);
+void scratch_free(void* p, void* stream);
+
+}  // namespace itkg

@@ -1,0 +1,413 @@
+"""Python mirror of itk-rs's Gaussian pipeline API over the itkg C ABI.
+
+Mirrors (reference file:line):
+  Region.padded_per_axis / clipped_to   src/image.rs:28-64
+  Image (host buffer, axis 0 fastest)   src/image.rs:82-141
+  ImageSource protocol                  src/source.rs:13-29 (+ Image leaf, 32-59)
+  GaussianFilter(source, sigma)         src/filters/gaussian.rs:13-91
+  UnaryFilter casts around the filter   src/filters/mod.rs:47-81,
+                                        examples/blur_png.rs:35-37
+  stream_full(source, num_pieces)       src/source.rs:81-98
+  split_region(region, num_pieces)      src/region_splitter.rs:17-48
+
+Numpy convention: a D-dimensional image is a C-ordered array whose LAST
+spatial axis is the reference's axis 0 (shape (nz, ny, nx)), plus a trailing
+component axis of length 3 for VecPixel<_, 3>.  Every filter call goes through
+libitkg.so; there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from ._abi import (ALGO_AUTO, ALGO_FUSED, ALGO_PER_AXIS, ARITH_F32, ARITH_PIXEL_U8, BF16, DEVICE,
+                   F16, F32, HOST, I16, ROUND_FMA, ROUND_REFERENCE, U8, ItkgError, check,
+                   itkg_gaussian_params, itkg_image, itkg_region, lib)
+
+__all__ = [
+    "Region", "Image", "DeviceImage", "GaussianFilter", "CastFilter", "stream_full",
+    "split_region", "kernel_radius", "build_kernel", "ItkgError", "F32", "I16", "U8", "BF16",
+    "F16", "ROUND_REFERENCE", "ROUND_FMA", "ALGO_AUTO", "ALGO_FUSED", "ALGO_PER_AXIS",
+    "ARITH_F32", "ARITH_PIXEL_U8", "gaussian", "Stream",
+]
+
+_NP_OF = {F32: np.float32, I16: np.int16, U8: np.uint8, F16: np.float16}
+
+
+def dtype_code(np_dtype, bf16: bool = False) -> int:
+    if bf16:
+        return BF16
+    d = np.dtype(np_dtype)
+    for code, t in _NP_OF.items():
+        if d == np.dtype(t):
+            return code
+    raise TypeError(f"unsupported pixel dtype {d}")
+
+
+def _storage_np(code: int):
+    """numpy dtype used to hold a storage type on the host (bf16 as uint16 bits)."""
+    return np.uint16 if code == BF16 else _NP_OF[code]
+
+
+# ---------------------------------------------------------------------------
+# Region (image.rs:12-77)
+# ---------------------------------------------------------------------------
+@dataclass(frozen=True)
+class Region:
+    index: tuple
+    size: tuple
+
+    @property
+    def dim(self) -> int:
+        return len(self.size)
+
+    def linear_len(self) -> int:
+        n = 1
+        for s in self.size:
+            n *= int(s)
+        return n
+
+    def padded_per_axis(self, radii) -> "Region":
+        return Region(tuple(i - r for i, r in zip(self.index, radii)),
+                      tuple(s + 2 * r for s, r in zip(self.size, radii)))
+
+    def clipped_to(self, bounds: "Region") -> "Region":
+        idx, sz = [], []
+        for i, s, bi, bs in zip(self.index, self.size, bounds.index, bounds.size):
+            st, en = max(i, bi), min(i + s, bi + bs)
+            idx.append(st)
+            sz.append(max(en - st, 0))
+        return Region(tuple(idx), tuple(sz))
+
+    def contains(self, idx) -> bool:
+        return all(i <= x < i + s for i, s, x in zip(self.index, self.size, idx))
+
+    def to_c(self) -> itkg_region:
+        r = itkg_region()
+        for d in range(3):
+            r.index[d] = int(self.index[d]) if d < self.dim else 0
+            r.size[d] = int(self.size[d]) if d < self.dim else 1
+        return r
+
+    @staticmethod
+    def from_c(r: itkg_region, dim: int) -> "Region":
+        return Region(tuple(r.index[d] for d in range(dim)), tuple(r.size[d] for d in range(dim)))
+
+
+def kernel_radius(sigma: float, spacing: float) -> int:
+    """GaussianFilter::kernel_radius (gaussian.rs:24-27)."""
+    return int(lib().itkg_kernel_radius(float(sigma), float(spacing)))
+
+
+def build_kernel(sigma_px: float, radius: int) -> np.ndarray:
+    """GaussianFilter::build_kernel (gaussian.rs:29-40)."""
+    out = np.zeros(2 * radius + 1, dtype=np.float64)
+    check(lib().itkg_build_kernel(float(sigma_px), int(radius), out.ctypes.data_as(ctypes.c_void_p)))
+    return out
+
+
+def split_region(region: Region, num_pieces: int):
+    """split_region (region_splitter.rs:17-48)."""
+    c = region.to_c()
+    cnt = ctypes.c_uint64(0)
+    check(lib().itkg_split_region(ctypes.byref(c), region.dim, int(num_pieces), None, 0,
+                                  ctypes.byref(cnt)))
+    arr = (itkg_region * max(cnt.value, 1))()
+    check(lib().itkg_split_region(ctypes.byref(c), region.dim, int(num_pieces), arr, cnt.value,
+                                  ctypes.byref(cnt)))
+    return [Region.from_c(arr[i], region.dim) for i in range(cnt.value)]
+
+
+class Stream:
+    """Opaque cudaStream_t handle (an int); 0 is the legacy default stream."""
+
+    def __init__(self, handle: int = 0):
+        self.handle = int(handle)
+
+    @property
+    def ptr(self):
+        return ctypes.c_void_p(self.handle) if self.handle else None
+
+    def synchronize(self):
+        check(lib().itkg_stream_synchronize(self.ptr))
+
+
+_DEFAULT_STREAM = Stream(0)
+
+
+# ---------------------------------------------------------------------------
+# Images
+# ---------------------------------------------------------------------------
+class Image:
+    """Host image: Image<P, D> (image.rs:82-141) backed by a numpy array."""
+
+    def __init__(self, data: np.ndarray, index=None, spacing=None, origin=None, components=1,
+                 bf16: bool = False):
+        self.data = np.ascontiguousarray(data)
+        self.components = components
+        spatial = self.data.shape[:-1] if components > 1 else self.data.shape
+        D = len(spatial)
+        self.region = Region(tuple(index) if index is not None else (0,) * D,
+                             tuple(reversed(spatial)))
+        self.spacing = tuple(spacing) if spacing is not None else (1.0,) * D
+        self.origin = tuple(origin) if origin is not None else (0.0,) * D
+        self.dtype = dtype_code(self.data.dtype, bf16)
+
+    @property
+    def dim(self):
+        return self.region.dim
+
+    # Image acts as an ImageSource leaf (source.rs:32-59)
+    def largest_region(self) -> Region:
+        return self.region
+
+    def to_c(self) -> itkg_image:
+        im = itkg_image()
+        im.dim = self.dim
+        im.dtype = self.dtype
+        im.components = self.components
+        im.location = HOST
+        im.region = self.region.to_c()
+        isz = self.data.itemsize * self.components
+        pitches = [isz]
+        for d in range(1, self.dim):
+            pitches.append(pitches[-1] * self.region.size[d - 1])
+        for d in range(3):
+            im.pitch[d] = pitches[d] if d < self.dim else pitches[-1] * int(self.region.size[-1])
+            im.spacing[d] = self.spacing[d] if d < self.dim else 1.0
+            im.origin[d] = self.origin[d] if d < self.dim else 0.0
+        im.data = self.data.ctypes.data
+        return im
+
+    def get_pixel(self, idx):
+        local = tuple(i - o for i, o in zip(idx, self.region.index))
+        return self.data[tuple(reversed(local))]
+
+
+class DeviceImage:
+    """Device-resident image (pitched rows, 128-byte aligned) owned by libitkg."""
+
+    def __init__(self, region: Region, dtype: int = F32, components: int = 1, spacing=None,
+                 origin=None):
+        D = region.dim
+        self.c = itkg_image()
+        sp = (ctypes.c_double * 3)(*([float(s) for s in (spacing or (1.0,) * D)] + [1.0] * (3 - D)))
+        org = (ctypes.c_double * 3)(*([float(s) for s in (origin or (0.0,) * D)] + [0.0] * (3 - D)))
+        r = region.to_c()
+        check(lib().itkg_image_alloc_device(ctypes.byref(self.c), D, dtype, components,
+                                            ctypes.byref(r), sp, org))
+        self.region = region
+        self.components = components
+        self.dtype = dtype
+        self.spacing = tuple(spacing or (1.0,) * D)
+        self.origin = tuple(origin or (0.0,) * D)
+
+    @property
+    def dim(self):
+        return self.region.dim
+
+    def largest_region(self) -> Region:
+        return self.region
+
+    def to_c(self) -> itkg_image:
+        return self.c
+
+    def __del__(self):
+        try:
+            if self.c.data:
+                lib().itkg_image_free(ctypes.byref(self.c))
+        except Exception:
+            pass
+
+    @classmethod
+    def from_host(cls, img: Image, stream: Stream = _DEFAULT_STREAM) -> "DeviceImage":
+        dev = cls(img.region, img.dtype, img.components, img.spacing, img.origin)
+        dev.upload(img.data, stream)
+        return dev
+
+    def _host_view(self, arr):
+        arr = np.ascontiguousarray(arr)
+        h = Image.__new__(Image)
+        h.data = arr
+        h.components = self.components
+        h.region = self.region
+        h.spacing = self.spacing
+        h.origin = self.origin
+        h.dtype = self.dtype
+        return h
+
+    def upload(self, arr: np.ndarray, stream: Stream = _DEFAULT_STREAM):
+        """Copy a dense host array (same shape as the region) into the pitched buffer."""
+        self._copy(self._host_view(arr), to_device=True, stream=stream)
+
+    def download(self, stream: Stream = _DEFAULT_STREAM) -> np.ndarray:
+        shape = tuple(reversed(self.region.size)) + ((self.components,) if self.components > 1 else ())
+        out = np.empty(shape, dtype=_storage_np(self.dtype))
+        self._copy(self._host_view(out), to_device=False, stream=stream)
+        return out
+
+    def _copy(self, host: Image, to_device: bool, stream: Stream):
+        # Image::copy_from (image.rs:133-140) through the C ABI.
+        hc = host.to_c()
+        if to_device:
+            check(lib().itkg_image_copy_from(ctypes.byref(self.c), ctypes.byref(hc), stream.ptr))
+        else:
+            check(lib().itkg_image_copy_from(ctypes.byref(hc), ctypes.byref(self.c), stream.ptr))
+        stream.synchronize()
+
+
+# ---------------------------------------------------------------------------
+# Filters
+# ---------------------------------------------------------------------------
+class CastFilter:
+    """UnaryFilter(|p| p as f32) in front of the Gaussian, or the output cast
+    |p: f32| p.round().clamp(0,255) as u8 behind it (examples/blur_png.rs:35-37).
+    The GPU fuses either cast into the Gaussian's load or store, so a CastFilter
+    only records the storage type it converts to."""
+
+    def __init__(self, source, to_dtype: int):
+        self.source = source
+        self.to_dtype = to_dtype
+
+    def largest_region(self):
+        return self.source.largest_region()
+
+    @property
+    def spacing(self):
+        return self.source.spacing
+
+    @property
+    def origin(self):
+        return self.source.origin
+
+    def generate_region(self, requested: Region, stream: Stream = _DEFAULT_STREAM):
+        src = self.source
+        if isinstance(src, GaussianFilter):
+            return src.generate_region(requested, stream=stream, out_dtype=self.to_dtype)
+        raise TypeError("CastFilter output is consumed by GaussianFilter (fused load)")
+
+
+class GaussianFilter:
+    """GaussianFilter { source, sigma } (gaussian.rs:13-91) on the GPU."""
+
+    def __init__(self, source, sigma: float, rounding: int = ROUND_REFERENCE,
+                 algorithm: int = ALGO_AUTO, arithmetic: int | None = None):
+        self.source = source
+        self.sigma = float(sigma)
+        self.rounding = rounding
+        self.algorithm = algorithm
+        self.arithmetic = arithmetic
+
+    def _leaf(self):
+        src = self.source
+        if isinstance(src, CastFilter):
+            src = src.source
+        if not isinstance(src, (Image, DeviceImage)):
+            raise TypeError("GaussianFilter source must be an Image, DeviceImage or CastFilter of one")
+        return src
+
+    def largest_region(self) -> Region:
+        return self.source.largest_region()
+
+    @property
+    def spacing(self):
+        return self._leaf().spacing
+
+    @property
+    def origin(self):
+        return self._leaf().origin
+
+    def input_region_for_output(self, out: Region) -> Region:
+        radii = [kernel_radius(self.sigma, s) for s in self.spacing]
+        return out.padded_per_axis(radii).clipped_to(self.largest_region())
+
+    def params(self) -> itkg_gaussian_params:
+        p = itkg_gaussian_params()
+        p.sigma = self.sigma
+        leaf = self._leaf()
+        if self.arithmetic is not None:
+            p.arithmetic = self.arithmetic
+        else:
+            # GaussianFilter directly over Image<u8> uses u8 pixel arithmetic;
+            # through a cast node it is f32 arithmetic.
+            p.arithmetic = ARITH_PIXEL_U8 if (leaf.dtype == U8 and not isinstance(self.source, CastFilter)) else ARITH_F32
+        p.rounding = self.rounding
+        p.algorithm = self.algorithm
+        return p
+
+    def generate_region(self, requested: Region, stream: Stream = _DEFAULT_STREAM,
+                        out_dtype: int | None = None, out=None):
+        """Returns a host Image for a host source, a DeviceImage for a device source."""
+        leaf = self._leaf()
+        prm = self.params()
+        if out_dtype is None:
+            out_dtype = U8 if prm.arithmetic == ARITH_PIXEL_U8 else F32
+        largest = leaf.largest_region().to_c()
+        req = requested.to_c()
+        src = leaf.to_c()
+        if isinstance(leaf, Image):
+            shape = tuple(reversed(requested.size)) + ((leaf.components,) if leaf.components > 1 else ())
+            host = out if out is not None else np.empty(shape, dtype=_storage_np(out_dtype))
+            res = Image(host, index=requested.index, spacing=leaf.spacing, origin=leaf.origin,
+                        components=leaf.components, bf16=(out_dtype == BF16))
+            oc = res.to_c()
+            check(lib().itkg_gaussian_generate_region(ctypes.byref(src), ctypes.byref(largest),
+                                                      ctypes.byref(req), ctypes.byref(prm),
+                                                      ctypes.byref(oc), stream.ptr))
+            return res
+        dev = out if out is not None else DeviceImage(requested, out_dtype, leaf.components,
+                                                      leaf.spacing, leaf.origin)
+        check(lib().itkg_gaussian_generate_region(ctypes.byref(src), ctypes.byref(largest),
+                                                  ctypes.byref(req), ctypes.byref(prm),
+                                                  ctypes.byref(dev.c), stream.ptr))
+        return dev
+
+
+def stream_full(source: GaussianFilter, num_pieces: int, stream: Stream = _DEFAULT_STREAM,
+                out_dtype: int | None = None):
+    """stream_full (source.rs:81-98): full output filled piece by piece."""
+    leaf = source._leaf()
+    prm = source.params()
+    if out_dtype is None:
+        out_dtype = U8 if prm.arithmetic == ARITH_PIXEL_U8 else F32
+    full = leaf.largest_region()
+    lc = full.to_c()
+    src = leaf.to_c()
+    if isinstance(leaf, Image):
+        shape = tuple(reversed(full.size)) + ((leaf.components,) if leaf.components > 1 else ())
+        res = Image(np.empty(shape, dtype=_storage_np(out_dtype)), index=full.index,
+                    spacing=leaf.spacing, origin=leaf.origin, components=leaf.components,
+                    bf16=(out_dtype == BF16))
+        oc = res.to_c()
+    else:
+        res = DeviceImage(full, out_dtype, leaf.components, leaf.spacing, leaf.origin)
+        oc = res.c
+    check(lib().itkg_stream_full(ctypes.byref(src), ctypes.byref(lc), ctypes.byref(prm),
+                                 int(num_pieces), ctypes.byref(oc), stream.ptr))
+    return res
+
+
+def gaussian(arr: np.ndarray, sigma: float, spacing=None, components: int = 1,
+             rounding: int = ROUND_REFERENCE, algorithm: int = ALGO_AUTO,
+             out_dtype: int | None = None, arithmetic: int | None = None, requested=None,
+             index=None):
+    """One-call convenience: host array in, host array out (through the C ABI)."""
+    img = Image(arr, index=index, spacing=spacing, components=components)
+    if arithmetic is None:
+        arithmetic = ARITH_PIXEL_U8 if img.dtype == U8 else ARITH_F32
+    src = img if (arithmetic == ARITH_PIXEL_U8 or img.dtype == F32) else CastFilter(img, F32)
+    f = GaussianFilter(src, sigma, rounding=rounding, algorithm=algorithm, arithmetic=arithmetic)
+    req = Region(*requested) if requested is not None else img.region
+    return f.generate_region(req, out_dtype=out_dtype).data
+
+
+def last_kernel() -> str:
+    return lib().itkg_last_kernel().decode()
+
+
+def device_count() -> int:
+    n = ctypes.c_int32(0)
+    check(lib().itkg_device_count(ctypes.byref(n)))
+    return n.value

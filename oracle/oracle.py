@@ -1,0 +1,275 @@
+"""CPU oracle for the separable Gaussian path -- TEST INFRASTRUCTURE ONLY.
+
+Only tests/, the smoke check in __graft_entry__.py and bench.py's CPU-baseline
+leg import this module; the product never does.  It wraps the C restatement
+in gauss_oracle.c (reference semantics, see that file's header for the
+file:line map) and adds numpy FP64 helpers for the adjoint checks.
+
+Array convention used throughout the tests: a reference ``Image<P, D>`` with
+axis 0 fastest is a C-ordered numpy array whose LAST spatial axis is the
+reference's axis 0, i.e. shape (nz, ny, nx) for D=3 and (ny, nx) for D=2, with
+a trailing component axis for ``VecPixel<f32, 3>``.  Regions are given in the
+reference's axis order: ``index=(ix, iy, iz)``, ``size=(sx, sy, sz)``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "liborc.so")
+_lib = None
+
+
+class Region(ctypes.Structure):
+    _fields_ = [("index", ctypes.c_int64 * 3), ("size", ctypes.c_int64 * 3)]
+
+
+def build():
+    """Compile the C restatement (make -C oracle)."""
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        src = os.path.join(_HERE, "gauss_oracle.c")
+        if (not os.path.exists(_LIB_PATH)
+                or os.path.getmtime(_LIB_PATH) < os.path.getmtime(src)):
+            build()
+        L = ctypes.CDLL(_LIB_PATH)
+        P = ctypes.c_void_p
+        R = ctypes.POINTER(Region)
+        L.orc_kernel_radius.restype = ctypes.c_uint64
+        L.orc_kernel_radius.argtypes = [ctypes.c_double, ctypes.c_double]
+        L.orc_build_kernel.restype = None
+        L.orc_build_kernel.argtypes = [ctypes.c_double, ctypes.c_uint64, P]
+        for name in ("orc_gaussian_f32", "orc_gaussian_u8", "orc_gaussian_f64"):
+            f = getattr(L, name)
+            f.restype = ctypes.c_int
+            f.argtypes = [P, R, P, ctypes.c_int, ctypes.c_int, ctypes.c_double, R, P]
+        L.orc_gaussian_f32_mt.restype = ctypes.c_int
+        L.orc_gaussian_f32_mt.argtypes = [P, R, P, ctypes.c_int, ctypes.c_int,
+                                          ctypes.c_double, R, P, ctypes.c_int]
+        L.orc_stream_full_f32.restype = ctypes.c_int
+        L.orc_stream_full_f32.argtypes = [P, R, P, ctypes.c_int, ctypes.c_int,
+                                          ctypes.c_double, ctypes.c_uint64, P]
+        L.orc_split_region.restype = ctypes.c_int64
+        L.orc_split_region.argtypes = [R, ctypes.c_int, ctypes.c_uint64, R]
+        L.orc_convolve_axis.restype = ctypes.c_int
+        L.orc_convolve_axis.argtypes = [P, R, ctypes.c_int, ctypes.c_int, ctypes.c_int, P,
+                                        ctypes.c_uint64, R, P, ctypes.c_int]
+        L.orc_cast_f32_to_u8.restype = None
+        L.orc_cast_f32_to_u8.argtypes = [P, P, ctypes.c_int64]
+        _lib = L
+    return _lib
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def make_region(index, size) -> Region:
+    r = Region()
+    for d in range(3):
+        r.index[d] = int(index[d]) if d < len(index) else 0
+        r.size[d] = int(size[d]) if d < len(size) else 1
+    return r
+
+
+def region_tuple(r: Region, D: int):
+    return tuple(r.index[d] for d in range(D)), tuple(r.size[d] for d in range(D))
+
+
+def kernel_radius(sigma: float, spacing: float) -> int:
+    """gaussian.rs:24-27."""
+    return int(lib().orc_kernel_radius(sigma, spacing))
+
+
+def build_kernel(sigma_px: float, radius: int) -> np.ndarray:
+    """gaussian.rs:29-40 (f64 weights)."""
+    out = np.zeros(2 * radius + 1, dtype=np.float64)
+    lib().orc_build_kernel(sigma_px, radius, _ptr(out))
+    return out
+
+
+def _dims(img: np.ndarray, comps: int):
+    shape = img.shape[:-1] if comps > 1 else img.shape
+    D = len(shape)
+    return D, tuple(reversed(shape))  # reference axis order sizes
+
+
+def _run(fn, img, dtype, sigma, spacing, index, requested, comps, extra=()):
+    img = np.ascontiguousarray(img, dtype=dtype)
+    D, sizes = _dims(img, comps)
+    index = tuple(index) if index is not None else (0,) * D
+    spacing = np.ascontiguousarray(spacing if spacing is not None else [1.0] * D,
+                                   dtype=np.float64)
+    img_reg = make_region(index, sizes)
+    if requested is None:
+        req = make_region(index, sizes)
+    else:
+        req = make_region(*requested)
+    out_shape = tuple(reversed([req.size[d] for d in range(D)]))
+    if comps > 1:
+        out_shape = out_shape + (comps,)
+    out = np.empty(out_shape, dtype=dtype)
+    rc = fn(_ptr(img), ctypes.byref(img_reg), _ptr(spacing), D, comps, float(sigma),
+            ctypes.byref(req), _ptr(out), *extra)
+    if rc != 0:
+        raise RuntimeError("oracle: generate_region failed (allocation or radius)")
+    return out
+
+
+def gaussian_f32(img, sigma, spacing=None, index=None, requested=None, comps=1):
+    """GaussianFilter<Image<f32|VecPixel<f32,3>>>::generate_region, exact reference f32."""
+    return _run(lib().orc_gaussian_f32, img, np.float32, sigma, spacing, index, requested,
+                comps)
+
+
+def gaussian_f32_mt(img, sigma, spacing=None, index=None, requested=None, comps=1,
+                    nthreads=None):
+    """Timing port (same arithmetic as gaussian_f32) with the reference's threading shape."""
+    n = nthreads or os.cpu_count() or 1
+    return _run(lib().orc_gaussian_f32_mt, img, np.float32, sigma, spacing, index,
+                requested, comps, (n,))
+
+
+def gaussian_u8(img, sigma, spacing=None, index=None, requested=None, comps=1):
+    """GaussianFilter<Image<u8>>: per-tap f64 round+clamp, wrapping u8 adds (pixel.rs:430-435)."""
+    return _run(lib().orc_gaussian_u8, img, np.uint8, sigma, spacing, index, requested,
+                comps)
+
+
+def gaussian_f64(img, sigma, spacing=None, index=None, requested=None, comps=1):
+    """FP64 oracle: same kernel and clamp boundary, f64 arithmetic throughout."""
+    return _run(lib().orc_gaussian_f64, img, np.float64, sigma, spacing, index, requested,
+                comps)
+
+
+def stream_full_f32(img, sigma, num_pieces, spacing=None, index=None, comps=1):
+    """source.rs:81-98 over GaussianFilter<Image<f32>>."""
+    img = np.ascontiguousarray(img, dtype=np.float32)
+    D, sizes = _dims(img, comps)
+    index = tuple(index) if index is not None else (0,) * D
+    sp = np.ascontiguousarray(spacing if spacing is not None else [1.0] * D, dtype=np.float64)
+    reg = make_region(index, sizes)
+    out = np.empty_like(img)
+    rc = lib().orc_stream_full_f32(_ptr(img), ctypes.byref(reg), _ptr(sp), D, comps,
+                                   float(sigma), int(num_pieces), _ptr(out))
+    if rc != 0:
+        raise RuntimeError("oracle: stream_full failed")
+    return out
+
+
+def split_region(index, size, num_pieces):
+    """region_splitter.rs:17-48 -> list of (index, size) tuples."""
+    D = len(size)
+    reg = make_region(index, size)
+    n = max(int(num_pieces), 1)
+    arr = (Region * n)()
+    cnt = lib().orc_split_region(ctypes.byref(reg), D, n, arr)
+    return [region_tuple(arr[i], D) for i in range(cnt)]
+
+
+def cast_f32_to_u8(a):
+    """|p: f32| p.round().clamp(0.0, 255.0) as u8 (tests/blur_png.rs:40)."""
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    out = np.empty(a.shape, dtype=np.uint8)
+    lib().orc_cast_f32_to_u8(_ptr(a), _ptr(out), a.size)
+    return out
+
+
+# ---------------------------------------------------------------------------
+# FP64 numpy helpers for the adjoint (not in the reference: the reference has
+# no VJP).  Per-axis clamped convolution as an explicit linear operator.
+# ---------------------------------------------------------------------------
+
+def _np_axis(D: int, axis: int) -> int:
+    """numpy axis of reference axis `axis` for an array of D spatial dims."""
+    return D - 1 - axis
+
+
+def conv_axis_f64(x: np.ndarray, w: np.ndarray, axis: int, D: int) -> np.ndarray:
+    """y[o] = sum_k w[k] x[clamp(o+k-r)] along reference axis `axis` (whole image)."""
+    ax = _np_axis(D, axis)
+    n = x.shape[ax]
+    r = (len(w) - 1) // 2
+    y = np.zeros(x.shape, dtype=np.float64)
+    o = np.arange(n)
+    for k in range(len(w)):
+        idx = np.clip(o + k - r, 0, n - 1)
+        y += w[k] * np.take(x, idx, axis=ax)
+    return y
+
+
+def conv_axis_adjoint_f64(g: np.ndarray, w: np.ndarray, axis: int, D: int) -> np.ndarray:
+    """Transpose of conv_axis_f64: scatter-add through the same clamped index map."""
+    ax = _np_axis(D, axis)
+    n = g.shape[ax]
+    r = (len(w) - 1) // 2
+    xb = np.zeros(g.shape, dtype=np.float64)
+    o = np.arange(n)
+    gm = np.moveaxis(g, ax, 0)
+    xm = np.moveaxis(xb, ax, 0)
+    for k in range(len(w)):
+        idx = np.clip(o + k - r, 0, n - 1)
+        np.add.at(xm, idx, w[k] * gm)
+    return xb
+
+
+def kernel_and_derivative(sigma: float, spacing: float, radius: int | None = None):
+    """f64 weights w_i and dw_i/dsigma (physical sigma) at a frozen radius."""
+    sp = float(spacing)
+    s = sigma / sp
+    r = kernel_radius(sigma, sp) if radius is None else int(radius)
+    x = np.arange(-r, r + 1, dtype=np.float64)
+    g = np.exp(-0.5 * (x / s) ** 2)
+    gp = g * x * x / s ** 3          # dg/dsigma_px
+    S = g.sum()
+    Sp = gp.sum()
+    w = g / S
+    dw = (gp * S - g * Sp) / (S * S) / sp
+    return w, dw
+
+
+def gaussian_whole_f64(x: np.ndarray, sigma: float, spacing=None, radii=None):
+    """FP64 whole-image forward with optional frozen radii (scalar pixels)."""
+    D = x.ndim
+    spacing = spacing or [1.0] * D
+    y = x.astype(np.float64)
+    for a in range(D):
+        r = None if radii is None else radii[a]
+        w, _ = kernel_and_derivative(sigma, spacing[a], r)
+        y = conv_axis_f64(y, w, a, D)
+    return y
+
+
+def gaussian_adjoint_f64(g: np.ndarray, sigma: float, spacing=None, radii=None):
+    """x_bar = G_0^T ... G_{D-1}^T g (FP64)."""
+    D = g.ndim
+    spacing = spacing or [1.0] * D
+    xb = g.astype(np.float64)
+    for a in reversed(range(D)):
+        r = None if radii is None else radii[a]
+        w, _ = kernel_and_derivative(sigma, spacing[a], r)
+        xb = conv_axis_adjoint_f64(xb, w, a, D)
+    return xb
+
+
+def gaussian_dsigma_f64(x: np.ndarray, sigma: float, spacing=None, radii=None):
+    """dy/dsigma = sum_a (prod_{b!=a} G_b) dG_a x (FP64, frozen radii)."""
+    D = x.ndim
+    spacing = spacing or [1.0] * D
+    total = np.zeros(x.shape, dtype=np.float64)
+    for a in range(D):
+        y = x.astype(np.float64)
+        for b in range(D):
+            r = None if radii is None else radii[b]
+            w, dw = kernel_and_derivative(sigma, spacing[b], r)
+            y = conv_axis_f64(y, dw if b == a else w, b, D)
+        total += y
+    return total

@@ -1,0 +1,246 @@
+"""Generate tests/golden/golden.npz -- small known-answer vectors for the
+Gaussian path, from a literal pure-Python transcription of the reference.
+
+The reference (a Rust crate) cannot be built here and ships no golden vectors,
+so these vectors come from a second, independent restatement written line for
+line after the reference code, using numpy float32 *scalars* so every product
+and sum rounds to f32 separately, exactly as Rust evaluates `acc + x * (w as f32)`:
+
+  kernel_radius     src/filters/gaussian.rs:24-27
+  build_kernel      src/filters/gaussian.rs:29-40   (math.exp, f64)
+  generate_region   src/filters/gaussian.rs:59-91
+  convolve_axis     src/filters/conv.rs:11-41
+  u8 scale          src/pixel.rs:430-435
+  padded/clipped    src/image.rs:28-64
+  split_region      src/region_splitter.rs:17-48
+  stream_full       src/source.rs:81-98
+
+The C oracle (oracle/gauss_oracle.c) is checked bit-exactly against these
+vectors by tests/test_oracle.py, and the GPU path by tests/test_gpu_parity.py.
+Run: python tests/golden/make_golden.py   (about a minute; pure Python loops)
+"""
+from __future__ import annotations
+
+import math
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+# ---- Region (image.rs) ------------------------------------------------------
+def padded_per_axis(index, size, radii):
+    return ([i - r for i, r in zip(index, radii)], [s + 2 * r for s, r in zip(size, radii)])
+
+
+def clipped_to(index, size, bidx, bsize):
+    ni, ns = [], []
+    for i, s, bi, bs in zip(index, size, bidx, bsize):
+        st = max(i, bi)
+        en = min(i + s, bi + bs)
+        ni.append(st)
+        ns.append(max(en - st, 0))
+    return ni, ns
+
+
+def iter_region(index, size):
+    """Axis 0 fastest (image.rs:144-174)."""
+    D = len(size)
+    n = 1
+    for s in size:
+        n *= s
+    if n == 0:
+        return
+    idx = list(index)
+    while True:
+        yield tuple(idx)
+        carry = True
+        for d in range(D):
+            if carry:
+                idx[d] += 1
+                if idx[d] < index[d] + size[d]:
+                    carry = False
+                else:
+                    idx[d] = index[d]
+        if carry:
+            break
+
+
+def flat_index(index, size, idx):
+    off, stride = 0, 1
+    for d in range(len(size)):
+        off += (idx[d] - index[d]) * stride
+        stride *= size[d]
+    return off
+
+
+# ---- GaussianFilter (gaussian.rs) ------------------------------------------
+def kernel_radius(sigma, spacing):
+    c = math.ceil(3.0 * (sigma / spacing))
+    return max(int(c), 0)
+
+
+def build_kernel(sigma_px, radius):
+    k = []
+    for i in range(2 * radius + 1):
+        x = float(i) - float(radius)
+        t = x / sigma_px
+        k.append(math.exp(-0.5 * (t * t)))
+    s = 0.0
+    for v in k:
+        s += v
+    return [v / s for v in k]
+
+
+def scale_f32(x, w):
+    return np.float32(x) * np.float32(w)  # x * (w as f32), rounded to f32
+
+
+def scale_u8(x, w):
+    v = float(x) * w
+    a = abs(v)
+    f = math.floor(a)
+    r = (f + 1.0 if a - f >= 0.5 else f) * (1.0 if v >= 0 else -1.0)  # half away from zero
+    return int(min(max(r, 0.0), 255.0))
+
+
+def convolve_axis(src, axis, kernel, req_index, req_size, kind):
+    """src = (index, size, data list of pixels); pixel = tuple of components."""
+    s_index, s_size, s_data = src
+    radius = len(kernel) // 2
+    out = []
+    for o in iter_region(req_index, req_size):
+        comps = len(s_data[0])
+        acc = [np.float32(0.0)] * comps if kind == "f32" else [0] * comps
+        for k_i, w in enumerate(kernel):
+            s = list(o)
+            s[axis] = min(max(o[axis] + k_i - radius, s_index[axis]),
+                          s_index[axis] + s_size[axis] - 1)
+            px = s_data[flat_index(s_index, s_size, s)]
+            for c in range(comps):
+                if kind == "f32":
+                    acc[c] = np.float32(acc[c] + scale_f32(px[c], w))
+                else:
+                    acc[c] = (acc[c] + scale_u8(px[c], w)) & 0xFF
+        out.append(tuple(acc))
+    return (list(req_index), list(req_size), out)
+
+
+def generate_region(img, spacing, sigma, req_index, req_size, kind="f32"):
+    b_index, b_size, data = img
+    D = len(b_size)
+    radii = [kernel_radius(sigma, spacing[d]) for d in range(D)]
+    in_i, in_s = clipped_to(*padded_per_axis(req_index, req_size, radii), b_index, b_size)
+    # Image leaf crop (source.rs:42-58)
+    cur = (in_i, in_s, [data[flat_index(b_index, b_size, p)] for p in iter_region(in_i, in_s)])
+    for axis in range(D):
+        kernel = build_kernel(sigma / spacing[axis], radii[axis])
+        if axis + 1 < D:
+            rem = [radii[d] if d > axis else 0 for d in range(D)]
+            oi, os_ = clipped_to(*padded_per_axis(req_index, req_size, rem), b_index, b_size)
+        else:
+            oi, os_ = list(req_index), list(req_size)
+        cur = convolve_axis(cur, axis, kernel, oi, os_, kind)
+    return cur
+
+
+def split_region(index, size, n):
+    n = max(n, 1)
+    D = len(size)
+    total = size[D - 1]
+    actual = max(min(n, total), 1)
+    base, rem = divmod(total, actual)
+    start = index[D - 1]
+    out = []
+    for i in range(actual):
+        sz = base + (1 if i < rem else 0)
+        ii, ss = list(index), list(size)
+        ii[D - 1], ss[D - 1] = start, sz
+        out.append((ii, ss))
+        start += sz
+    return out
+
+
+# ---- numpy <-> reference image ----------------------------------------------
+def to_ref(arr, comps=1):
+    """numpy (…, z, y, x[, c]) -> (index, size, pixels in iteration order)."""
+    spatial = arr.shape[:-1] if comps > 1 else arr.shape
+    size = list(reversed(spatial))
+    flat = arr.reshape(-1, comps) if comps > 1 else arr.reshape(-1, 1)
+    return ([0] * len(size), size, [tuple(p) for p in flat.tolist()])
+
+
+def from_ref(res, comps, dtype):
+    idx, size, data = res
+    a = np.array([list(p) for p in data], dtype=dtype)
+    shape = tuple(reversed(size))
+    return a.reshape(shape + ((comps,) if comps > 1 else ()))
+
+
+def case(name, arr, sigma, spacing=None, requested=None, comps=1, kind="f32"):
+    D = len(arr.shape) - (1 if comps > 1 else 0)
+    spacing = spacing or [1.0] * D
+    img = to_ref(arr, comps)
+    ri, rs = requested if requested else (img[0], img[1])
+    res = generate_region(img, spacing, sigma, list(ri), list(rs), kind)
+    out = from_ref(res, comps, np.float32 if kind == "f32" else np.uint8)
+    return {f"{name}__in": arr, f"{name}__out": out,
+            f"{name}__meta": np.array([sigma] + list(spacing) + [comps] + list(ri) + list(rs),
+                                      dtype=np.float64)}
+
+
+def main():
+    rng = np.random.default_rng(20261203)
+    cases = {}
+    imp = np.zeros((21, 21), np.float32)
+    imp[10, 10] = 1.0
+    cases.update(case("impulse2d_s1p5", imp, 1.5))
+    imp3 = np.zeros((11, 11, 11), np.float32)
+    imp3[5, 5, 5] = 1.0
+    cases.update(case("impulse3d_s1", imp3, 1.0))
+    vec = np.zeros((11, 11, 3), np.float32)
+    vec[5, 5] = [1.0, 2.0, 3.0]
+    cases.update(case("vecpixel2d_s1", vec, 1.0, comps=3))
+    r2 = rng.random((17, 23), dtype=np.float32)
+    cases.update(case("rand2d_s1p5", r2, 1.5))
+    cases.update(case("rand2d_sub_s1p5", r2, 1.5, requested=([4, 3], [12, 9])))
+    r3 = (rng.standard_normal((9, 12, 14)) * 3).astype(np.float32)
+    cases.update(case("rand3d_s1p2", r3, 1.2))
+    cases.update(case("rand3d_aniso", r3, 1.5, spacing=[0.7, 0.9, 2.5]))
+    cases.update(case("rand3d_sub_s2", r3, 2.0, requested=([2, 1, 3], [9, 10, 4])))
+    # radius larger than the image (clamp on both ends)
+    small = rng.random((5, 4), dtype=np.float32)
+    cases.update(case("tiny2d_s3", small, 3.0))
+    # 1-D
+    cases.update(case("line1d_s2", rng.random((40,), dtype=np.float32), 2.0))
+    # u8 NumericPixel arithmetic (wrapping u8 adds)
+    u8 = rng.integers(0, 256, (13, 16), dtype=np.uint8)
+    cases.update(case("u8pixel2d_s1p5", u8, 1.5, kind="u8"))
+    u8w = np.full((8, 9), 255, np.uint8)
+    cases.update(case("u8pixel2d_wrap_s1", u8w, 1.0, kind="u8"))
+    # i16 -> f32 cast chain (UnaryFilter(p as f32) then Gaussian<f32>)
+    i16 = rng.integers(-1000, 1500, (6, 10, 12)).astype(np.int16)
+    c = case("i16cast3d_s1p5", i16.astype(np.float32), 1.5, spacing=[0.7, 0.7, 2.5])
+    c["i16cast3d_s1p5__in"] = i16
+    cases.update(c)
+    # stream_full with 4 pieces on the impulse (tests/pipeline.rs:106-129)
+    img = to_ref(np.pad(np.zeros((20, 20), np.float32), 0))
+    data = [list(p) for p in img[2]]
+    data[10 * 20 + 10] = [1.0]
+    img = (img[0], img[1], [tuple(p) for p in data])
+    full = np.zeros((20, 20), np.float32)
+    for pi, ps in split_region([0, 0], [20, 20], 4):
+        part = from_ref(generate_region(img, [1.0, 1.0], 1.5, pi, ps), 1, np.float32)
+        full[pi[1]:pi[1] + ps[1], pi[0]:pi[0] + ps[0]] = part
+    cases["stream4_impulse2d__out"] = full
+    # kernels
+    for s, sp in [(1.5, 1.0), (2.0, 1.0), (1.5, 0.7), (1.5, 2.5), (0.5, 1.0), (8.0, 1.0)]:
+        cases[f"kernel_{s}_{sp}"] = np.array(build_kernel(s / sp, kernel_radius(s, sp)),
+                                             dtype=np.float64)
+    np.savez_compressed(os.path.join(HERE, "golden.npz"), **cases)
+    print(f"wrote {len(cases)} arrays to golden.npz")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,215 @@
+"""GPU parity through the C ABI: every result is compared with the oracle on the
+same seeded inputs.  Reference rounding must be bit-exact; FMA rounding must be
+within 1e-5 normwise relative (max|gpu-ref| / max|ref|), the tolerance the
+path is specified to; bf16/f16 storage is checked against the FP64 oracle
+within the storage type's half-ulp bound."""
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+CASES = ["impulse2d_s1p5", "impulse3d_s1", "vecpixel2d_s1", "rand2d_s1p5", "rand2d_sub_s1p5",
+         "rand3d_s1p2", "rand3d_aniso", "rand3d_sub_s2", "tiny2d_s3", "line1d_s2"]
+ALGOS = ["auto", "per_axis"]
+
+
+def _algo(itkg, name):
+    return {"auto": itkg.ALGO_AUTO, "per_axis": itkg.ALGO_PER_AXIS, "fused": itkg.ALGO_FUSED}[name]
+
+
+def bits_equal(a, b):
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    b = np.ascontiguousarray(b, dtype=np.float32)
+    return a.shape == b.shape and np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+def normwise(a, ref):
+    ref = np.asarray(ref, dtype=np.float64)
+    return float(np.abs(np.asarray(a, np.float64) - ref).max() / max(np.abs(ref).max(), 1e-300))
+
+
+def run_device(itkg, arr, sigma, spacing=None, comps=1, requested=None, rounding=0, algo="auto",
+               out_dtype=None, index=None, cast=False, arithmetic=None):
+    """Upload, run generate_region on device buffers, download."""
+    img = itkg.Image(arr, index=index, spacing=spacing, components=comps)
+    dev = itkg.DeviceImage.from_host(img)
+    src = itkg.CastFilter(dev, itkg.F32) if cast else dev
+    f = itkg.GaussianFilter(src, sigma, rounding=rounding, algorithm=_algo(itkg, algo),
+                            arithmetic=arithmetic)
+    req = itkg.Region(*requested) if requested else img.region
+    out = f.generate_region(req, out_dtype=out_dtype)
+    return out.download()
+
+
+def meta(golden, name):
+    m = golden[f"{name}__meta"]
+    D = (len(m) - 2) // 3
+    return (float(m[0]), [float(v) for v in m[1:1 + D]], int(m[1 + D]),
+            tuple(int(v) for v in m[2 + D:2 + 2 * D]), tuple(int(v) for v in m[2 + 2 * D:]))
+
+
+@pytest.mark.parametrize("algo", ALGOS)
+@pytest.mark.parametrize("name", CASES)
+def test_golden_bit_exact(gpu, golden, name, algo):
+    sigma, spacing, comps, ri, rs = meta(golden, name)
+    got = run_device(gpu, golden[f"{name}__in"], sigma, spacing, comps, (ri, rs), algo=algo)
+    assert bits_equal(got, golden[f"{name}__out"]), gpu.last_kernel()
+
+
+@pytest.mark.parametrize("name", ["u8pixel2d_s1p5", "u8pixel2d_wrap_s1"])
+def test_golden_u8_pixel_arithmetic(gpu, golden, name):
+    sigma, spacing, comps, ri, rs = meta(golden, name)
+    got = run_device(gpu, golden[f"{name}__in"], sigma, spacing, comps, (ri, rs),
+                     arithmetic=gpu.ARITH_PIXEL_U8, out_dtype=gpu.U8)
+    assert np.array_equal(got, golden[f"{name}__out"])
+
+
+def test_golden_i16_cast(gpu, golden):
+    name = "i16cast3d_s1p5"
+    sigma, spacing, comps, ri, rs = meta(golden, name)
+    got = run_device(gpu, golden[f"{name}__in"], sigma, spacing, comps, (ri, rs), cast=True)
+    assert bits_equal(got, golden[f"{name}__out"])
+
+
+def test_golden_stream_full(gpu, golden):
+    x = np.zeros((20, 20), np.float32)
+    x[10, 10] = 1.0
+    dev = gpu.DeviceImage.from_host(gpu.Image(x))
+    out = gpu.stream_full(gpu.GaussianFilter(dev, 1.5), 4).download()
+    assert bits_equal(out, golden["stream4_impulse2d__out"])
+
+
+SHAPES = [
+    ((7,), 1, 0.8), ((300,), 1, 2.5), ((33, 45), 1, 1.5), ((64, 64), 3, 1.2), ((5, 3), 1, 4.0),
+    ((9, 17, 31), 1, 1.0), ((16, 16, 16), 1, 2.0), ((21, 13, 40), 3, 1.1), ((1, 1, 1), 1, 1.0),
+    ((2, 50, 3), 1, 2.2), ((40, 1, 40), 1, 1.5), ((12, 30, 70), 1, 3.3),
+]
+
+
+@pytest.mark.parametrize("algo", ALGOS)
+@pytest.mark.parametrize("shape,comps,sigma", SHAPES)
+def test_random_shapes_reference_rounding(gpu, shape, comps, sigma, algo):
+    rng = np.random.default_rng(hash((shape, comps)) % 2**32)
+    arr = rng.standard_normal(shape + ((comps,) if comps > 1 else ())).astype(np.float32)
+    want = oracle.gaussian_f32(arr, sigma, comps=comps)
+    got = run_device(gpu, arr, sigma, comps=comps, algo=algo)
+    assert bits_equal(got, want), gpu.last_kernel()
+
+
+@pytest.mark.parametrize("algo", ALGOS)
+@pytest.mark.parametrize("shape,comps,sigma", SHAPES)
+def test_random_shapes_fma_within_1e5(gpu, shape, comps, sigma, algo):
+    rng = np.random.default_rng(1 + hash((shape, comps)) % 2**32)
+    arr = rng.random(shape + ((comps,) if comps > 1 else ()), dtype=np.float32)
+    want = oracle.gaussian_f32(arr, sigma, comps=comps)
+    got = run_device(gpu, arr, sigma, comps=comps, algo=algo, rounding=gpu.ROUND_FMA)
+    assert normwise(got, want) <= 1e-5
+
+
+@pytest.mark.parametrize("algo", ALGOS)
+def test_subregions_with_offset_index(gpu, algo):
+    rng = np.random.default_rng(7)
+    arr = rng.random((23, 29, 31), dtype=np.float32)
+    index = (5, -3, 100)
+    spacing = (0.9, 1.1, 1.7)
+    for ri, rs in [((5, -3, 100), (31, 29, 23)), ((9, 0, 104), (20, 11, 9)),
+                   ((30, 20, 121), (6, 6, 2)), ((5, -3, 100), (1, 1, 1))]:
+        want = oracle.gaussian_f32(arr, 2.1, spacing=spacing, index=index, requested=(ri, rs))
+        got = run_device(gpu, arr, 2.1, spacing=spacing, index=index, requested=(ri, rs), algo=algo)
+        assert bits_equal(got, want), (ri, rs, gpu.last_kernel())
+
+
+@pytest.mark.parametrize("algo", ALGOS)
+def test_stream_full_equals_full_3d(gpu, algo):
+    rng = np.random.default_rng(8)
+    arr = rng.random((37, 20, 24), dtype=np.float32)
+    dev = gpu.DeviceImage.from_host(gpu.Image(arr))
+    f = gpu.GaussianFilter(dev, 2.0, algorithm=_algo(gpu, algo))
+    full = f.generate_region(dev.region).download()
+    for n in (1, 3, 8, 100):
+        piece = gpu.stream_full(f, n).download()
+        assert bits_equal(piece, full)
+    assert bits_equal(full, oracle.gaussian_f32(arr, 2.0))
+
+
+def test_sigma_edge_cases(gpu):
+    arr = (np.arange(30, dtype=np.float32).reshape(5, 6) - 10.0)
+    assert bits_equal(run_device(gpu, arr, -2.0), oracle.gaussian_f32(arr, -2.0))
+    assert np.isnan(run_device(gpu, arr, 0.0)).all()
+    assert np.isnan(run_device(gpu, arr, float("nan"))).all() == np.isnan(oracle.gaussian_f32(arr, float("nan"))).all()
+
+
+def test_nonfinite_inputs_propagate_like_reference(gpu):
+    rng = np.random.default_rng(9)
+    arr = rng.random((12, 15, 11), dtype=np.float32)
+    arr[3, 4, 5] = np.inf
+    arr[8, 1, 2] = np.nan
+    arr[0, 0, 0] = -0.0
+    want = oracle.gaussian_f32(arr, 1.3)
+    got = run_device(gpu, arr, 1.3)
+    assert bits_equal(got, want)
+
+
+@pytest.mark.parametrize("in_dtype", [np.int16, np.uint8])
+def test_cast_inputs_bit_exact(gpu, in_dtype):
+    rng = np.random.default_rng(10)
+    if in_dtype == np.int16:
+        arr = rng.integers(-1000, 1500, (10, 24, 20)).astype(np.int16)
+    else:
+        arr = rng.integers(0, 256, (10, 24, 20)).astype(np.uint8)
+    want = oracle.gaussian_f32(arr.astype(np.float32), 1.5, spacing=(0.7, 0.7, 2.5))
+    got = run_device(gpu, arr, 1.5, spacing=(0.7, 0.7, 2.5), cast=True)
+    assert bits_equal(got, want)
+
+
+def test_u8_output_round_clamp(gpu):
+    rng = np.random.default_rng(12)
+    arr = rng.integers(0, 256, (30, 40)).astype(np.uint8)
+    f32 = oracle.gaussian_f32(arr.astype(np.float32), 2.0)
+    want = oracle.cast_f32_to_u8(f32)
+    got = run_device(gpu, arr, 2.0, cast=True, out_dtype=gpu.U8)
+    assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("out", ["bf16", "f16"])
+def test_half_storage_outputs(gpu, out):
+    rng = np.random.default_rng(13)
+    arr = rng.integers(-1000, 1500, (12, 40, 36)).astype(np.int16)
+    ref64 = oracle.gaussian_f64(arr.astype(np.float64), 1.5, spacing=(0.7, 0.7, 2.5))
+    code = gpu.BF16 if out == "bf16" else gpu.F16
+    raw = run_device(gpu, arr, 1.5, spacing=(0.7, 0.7, 2.5), cast=True, out_dtype=code,
+                     rounding=gpu.ROUND_FMA)
+    if out == "bf16":
+        got = (raw.astype(np.uint32) << 16).view(np.float32).astype(np.float64)
+        ulp_rel = 2.0 ** -8
+    else:
+        got = raw.astype(np.float64)
+        ulp_rel = 2.0 ** -11
+    # storage rounding: |err| <= half an ulp of the value (plus f32 arithmetic noise)
+    err = np.abs(got - ref64)
+    assert (err <= np.abs(ref64) * ulp_rel * 0.5 * 1.0001 + 1e-4).all()
+    # bf16 output equals rounding the f32 result to nearest-even
+    f32 = oracle.gaussian_f32(arr.astype(np.float32), 1.5, spacing=(0.7, 0.7, 2.5))
+    assert normwise(got, f32) <= ulp_rel
+
+
+def test_host_buffers_through_abi(gpu):
+    rng = np.random.default_rng(14)
+    arr = rng.random((18, 22, 26), dtype=np.float32)
+    img = gpu.Image(arr)
+    f = gpu.GaussianFilter(img, 1.7)
+    got = f.generate_region(gpu.Region((2, 3, 4), (20, 15, 10))).data
+    want = oracle.gaussian_f32(arr, 1.7, requested=((2, 3, 4), (20, 15, 10)))
+    assert bits_equal(got, want)
+    got = gpu.stream_full(f, 5).data
+    assert bits_equal(got, oracle.gaussian_f32(arr, 1.7))
+
+
+def test_large_radius_per_axis(gpu):
+    rng = np.random.default_rng(15)
+    arr = rng.random((30, 40, 50), dtype=np.float32)
+    want = oracle.gaussian_f32(arr, 8.0)
+    got = run_device(gpu, arr, 8.0)
+    assert bits_equal(got, want)
