@@ -400,7 +400,9 @@ static itkg_status generate_device(const itkg_image& in, const itkg_region& larg
     origin_pitch(out, g.dst_origin, g.dst_pitch);
     const itkg_region r3 = full3(requested, D);
     const itkg_region l3 = full3(largest, D);
+    const itkg_region b3 = full3(in.region, D);
     for (int d = 0; d < kMaxDim; ++d) {
+      g.src_size[d] = (int64_t)b3.size[d];
       g.req_index[d] = r3.index[d];
       g.req_size[d] = (int64_t)r3.size[d];
       g.lo[d] = l3.index[d];

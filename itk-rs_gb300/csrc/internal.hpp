@@ -79,6 +79,7 @@ struct FusedGeom {
   const void* src;
   void* dst;
   int64_t src_origin[kMaxDim];
+  int64_t src_size[kMaxDim];   // input buffer extent (region size)
   int64_t src_pitch[kMaxDim];  // bytes
   int64_t dst_origin[kMaxDim];
   int64_t dst_pitch[kMaxDim];  // bytes

@@ -20,9 +20,17 @@ def _algo(itkg, name):
 
 
 def bits_equal(a, b):
+    """Bit-exact equality; NaNs compare equal to NaNs whatever their payload
+    (x86 and the GPU produce different NaN bit patterns for the same invalid
+    operation, and the reference attaches no meaning to them)."""
     a = np.ascontiguousarray(a, dtype=np.float32)
     b = np.ascontiguousarray(b, dtype=np.float32)
-    return a.shape == b.shape and np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    if a.shape != b.shape:
+        return False
+    na, nb = np.isnan(a), np.isnan(b)
+    if not np.array_equal(na, nb):
+        return False
+    return np.array_equal(a[~na].view(np.uint32), b[~nb].view(np.uint32))
 
 
 def normwise(a, ref):
@@ -213,3 +221,58 @@ def test_large_radius_per_axis(gpu):
     want = oracle.gaussian_f32(arr, 8.0)
     got = run_device(gpu, arr, 8.0)
     assert bits_equal(got, want)
+
+
+FUSED_CASES = [((9, 17, 31), 1.0, None), ((16, 16, 16), 2.0, None), ((40, 50, 70), 2.0, None),
+               ((5, 70, 40), 2.2, None), ((12, 30, 70), 2.6, None), ((1, 1, 1), 1.0, None),
+               ((33, 65, 97), 1.5, None), ((20, 20, 20), 0.3, None), ((3, 40, 33), 1.2, None),
+               ((24, 48, 40), 1.5, (0.7, 0.7, 2.5))]
+
+
+@pytest.mark.parametrize("shape,sigma,spacing", FUSED_CASES)
+def test_fused3d_reference_rounding_bit_exact(gpu, shape, sigma, spacing):
+    rng = np.random.default_rng(sum(shape))
+    arr = rng.standard_normal(shape).astype(np.float32)
+    want = oracle.gaussian_f32(arr, sigma, spacing=spacing)
+    got = run_device(gpu, arr, sigma, spacing=spacing, algo="fused")
+    assert gpu.last_kernel().startswith("fused3d"), gpu.last_kernel()
+    assert bits_equal(got, want)
+
+
+@pytest.mark.parametrize("shape,sigma,spacing", FUSED_CASES)
+def test_fused3d_fma_within_1e5(gpu, shape, sigma, spacing):
+    rng = np.random.default_rng(1 + sum(shape))
+    arr = rng.random(shape, dtype=np.float32)
+    want = oracle.gaussian_f32(arr, sigma, spacing=spacing)
+    got = run_device(gpu, arr, sigma, spacing=spacing, algo="fused", rounding=gpu.ROUND_FMA)
+    assert gpu.last_kernel().startswith("fused3d"), gpu.last_kernel()
+    assert normwise(got, want) <= 1e-5
+
+
+def test_fused3d_subregions_and_tight_buffers(gpu):
+    # requested sub-regions; the input buffer is exactly input_region_for_output
+    rng = np.random.default_rng(21)
+    full = rng.random((30, 41, 53), dtype=np.float32)
+    for ri, rs in [((7, 5, 4), (33, 20, 11)), ((0, 0, 0), (53, 41, 30)), ((50, 40, 29), (3, 1, 1)),
+                   ((10, 0, 12), (1, 41, 6))]:
+        want = oracle.gaussian_f32(full, 1.9, requested=(ri, rs))
+        img = gpu.Image(full)
+        f = gpu.GaussianFilter(img, 1.9)
+        need = f.input_region_for_output(gpu.Region(ri, rs))
+        (x0, y0, z0), (sx, sy, sz) = need.index, need.size
+        sub = np.ascontiguousarray(full[z0:z0 + sz, y0:y0 + sy, x0:x0 + sx])
+        dev = gpu.DeviceImage(need)
+        dev.upload(sub)
+        fd = gpu.GaussianFilter(dev, 1.9, algorithm=gpu.ALGO_FUSED)
+        # the tight buffer's largest region is still the full image
+        from itkg import _abi
+        import ctypes
+        out = gpu.DeviceImage(gpu.Region(ri, rs))
+        lg = img.region.to_c()
+        rq = gpu.Region(ri, rs).to_c()
+        prm = fd.params()
+        _abi.check(_abi.lib().itkg_gaussian_generate_region(
+            ctypes.byref(dev.c), ctypes.byref(lg), ctypes.byref(rq), ctypes.byref(prm),
+            ctypes.byref(out.c), None))
+        assert gpu.last_kernel().startswith("fused3d")
+        assert bits_equal(out.download(), want), (ri, rs)
