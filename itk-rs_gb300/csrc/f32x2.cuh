@@ -1,0 +1,57 @@
+// Packed two-lane f32 arithmetic (PTX add/mul/fma .f32x2, sm_100+).  Each lane
+// rounds exactly like the scalar instruction, so the reference-rounding form
+// (mul.rn then add.rn) stays bit-identical to scalar __fmul_rn / __fadd_rn.
+#pragma once
+
+#include <cstdint>
+
+namespace itkg {
+
+typedef unsigned long long f2_t;  // {lo, hi} f32 pair in one 64-bit register
+
+__device__ __forceinline__ f2_t pack2(float lo, float hi) {
+  f2_t r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+
+__device__ __forceinline__ void unpack2(f2_t v, float& lo, float& hi) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+
+__device__ __forceinline__ f2_t fma2(f2_t a, f2_t b, f2_t c) {
+  f2_t d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+
+__device__ __forceinline__ f2_t mul2(f2_t a, f2_t b) {
+  f2_t d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+
+__device__ __forceinline__ f2_t add2(f2_t a, f2_t b) {
+  f2_t d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+
+// acc + x * w per lane: reference rounding (two roundings) or one FMA.
+template <bool REF>
+__device__ __forceinline__ f2_t tap2(f2_t acc, f2_t x, f2_t w) {
+  if constexpr (REF) {
+    return add2(acc, mul2(x, w));
+  } else {
+    return fma2(x, w, acc);
+  }
+}
+
+// Host-side: the 64-bit pattern of the pair {w, w}.
+inline unsigned long long splat2_host(float w) {
+  unsigned int u;
+  __builtin_memcpy(&u, &w, 4);
+  return ((unsigned long long)u << 32) | u;
+}
+
+}  // namespace itkg

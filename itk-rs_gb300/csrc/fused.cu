@@ -16,12 +16,13 @@
 //      register window;
 //   4. z pass, "push" form: slice j contributes w[k] * v to the outputs
 //      z = j + RZ - k; each thread keeps a ring of KZ accumulators per owned
-//      column in registers, the ring slot being a compile-time function of
-//      j mod KZ.  The accumulator of output z receives its taps in ascending
-//      k (ascending j), starting from zero, so with reference rounding the
+//      column in registers (rows paired into f32x2 registers), the ring slot
+//      being a compile-time function of the phase j mod KZ, selected by a
+//      switch.  The accumulator of output z receives its taps in ascending k
+//      (ascending j), starting from zero, so with reference rounding the
 //      result is bit-identical to the reference's sequence
-//      acc = 0; acc = acc + x * w (conv.rs:26-36); intermediates of every pass
-//      are f32 values exactly as the reference stores them.
+//      acc = 0; acc = acc + x * w (conv.rs:26-36); the intermediates of every
+//      pass are f32 values exactly as the reference stores them.
 // Slices clamped at the z ends are filtered once and pushed repeatedly.
 //
 // Work balance.  The (tile, z) units of the request are split evenly over a
@@ -34,6 +35,7 @@
 #include <mutex>
 #include <vector>
 
+#include "f32x2.cuh"
 #include "internal.hpp"
 #include "pixel.cuh"
 
@@ -52,7 +54,7 @@ struct Fused3DArgs {
   int32_t dst_origin[3];
   int32_t req_lo[3];  // requested region, inclusive bounds
   int32_t req_hi[3];
-  int32_t lo[3];  // image (largest region) bounds, inclusive
+  int32_t lo[3];  // gather bounds (image bounds within the input buffer), inclusive
   int32_t hi[3];
   int32_t ntx, nty;  // tiles along x and y
   int64_t units;     // ntx * nty * nz_requested
@@ -60,7 +62,7 @@ struct Fused3DArgs {
   int32_t pad_;
   float wx[kMaxFusedK];
   float wy[kMaxFusedK];
-  float wz[kMaxFusedK];
+  f2_t wz2[kMaxFusedK];  // {w, w} pairs for the packed z pass
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -80,15 +82,6 @@ __device__ __forceinline__ void cp_async_wait() {
 
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
-__device__ __forceinline__ void store_out(char* p, int dt, float v) {
-  switch (dt) {
-    case ITKG_F32: __stcs(reinterpret_cast<float*>(p), v); break;
-    case ITKG_BF16: *reinterpret_cast<__nv_bfloat16*>(p) = from_f32<__nv_bfloat16>(v); break;
-    case ITKG_F16: *reinterpret_cast<__half*>(p) = from_f32<__half>(v); break;
-    default: *reinterpret_cast<uint8_t*>(p) = from_f32<uint8_t>(v); break;
-  }
-}
-
 // Tile shape per radius.
 template <int RX, int RY, int RZ>
 struct Cfg3 {
@@ -96,7 +89,8 @@ struct Cfg3 {
   static constexpr int NT = 256;                  // threads per CTA
   static constexpr int NW = NT / 32;
   static constexpr int TX = 32;                   // one lane per output column
-  static constexpr int MY = RZ <= 6 ? 4 : 2;      // rows per thread (y pass, z ring)
+  static constexpr int MY = 4;                    // rows per thread (y pass, z ring)
+  static constexpr int MY2 = MY / 2;              // packed row pairs
   static constexpr int TY = NW * MY;
   static constexpr int MX = 4;                    // x outputs per x-pass task
   static constexpr int IW = TX + 2 * RX;          // staged tile width
@@ -110,13 +104,38 @@ struct Cfg3 {
   static constexpr int MINB = 2;
 };
 
+// z pass for phase P: push the packed y-filtered values into every ring slot,
+// then hand back the completed slot (P + 1) mod KZ and clear it.
+template <int P, int KZ, int MY2, bool REF>
+__device__ __forceinline__ void push_phase(f2_t (&acc)[MY2][KZ], const f2_t (&yv)[MY2],
+                                           const Fused3DArgs& a, f2_t (&done)[MY2]) {
+#pragma unroll
+  for (int k = 0; k < KZ; ++k) {
+    const int slot = (P - k + KZ) % KZ;
+#pragma unroll
+    for (int m = 0; m < MY2; ++m) acc[m][slot] = tap2<REF>(acc[m][slot], yv[m], a.wz2[k]);
+  }
+  constexpr int D = (P + 1) % KZ;
+#pragma unroll
+  for (int m = 0; m < MY2; ++m) {
+    done[m] = acc[m][D];
+    acc[m][D] = 0ull;
+  }
+}
+
+#define ITKG_PUSH_CASE(N)                                          \
+  case N:                                                          \
+    if constexpr (N < KZ) push_phase<N, KZ, MY2, REF>(acc, yv, a, done); \
+    break;
+
 template <int RX, int RY, int RZ, bool REF>
 __global__ void __launch_bounds__(Cfg3<RX, RY, RZ>::NT, Cfg3<RX, RY, RZ>::MINB)
     k_fused3d_f32(const Fused3DArgs a) {
   using C = Cfg3<RX, RY, RZ>;
   constexpr int KX = C::KX, KY = C::KY, KZ = C::KZ, TX = C::TX, TY = C::TY, MY = C::MY,
-                MX = C::MX, IW = C::IW, IH = C::IH, IWP = C::IWP, S = C::S, NLD = C::NLD,
-                NT = C::NT;
+                MY2 = C::MY2, MX = C::MX, IW = C::IW, IH = C::IH, IWP = C::IWP, S = C::S,
+                NLD = C::NLD, NT = C::NT;
+  static_assert(KZ <= 17, "phase switch covers KZ <= 17");
   extern __shared__ __align__(16) float smem[];
   float* const stage0 = smem;
   float* const xs = smem + S * C::STAGE;
@@ -125,6 +144,7 @@ __global__ void __launch_bounds__(Cfg3<RX, RY, RZ>::NT, Cfg3<RX, RY, RZ>::MINB)
   const int nzr = a.req_hi[2] - a.req_lo[2] + 1;
   const int64_t u_begin = a.units * blockIdx.x / gridDim.x;
   const int64_t u_end = a.units * (blockIdx.x + 1) / gridDim.x;
+  const uint32_t sbase = smem_u32(stage0);
 
   for (int64_t u = u_begin; u < u_end;) {
     const int64_t tile = u / nzr;
@@ -138,7 +158,6 @@ __global__ void __launch_bounds__(Cfg3<RX, RY, RZ>::NT, Cfg3<RX, RY, RZ>::MINB)
 
     // Gather offsets of this thread's share of the staged tile (clamped x, y).
     int32_t goff[NLD];
-    uint32_t soff[NLD];
 #pragma unroll
     for (int i = 0; i < NLD; ++i) {
       const int e = tid + i * NT;
@@ -147,120 +166,136 @@ __global__ void __launch_bounds__(Cfg3<RX, RY, RZ>::NT, Cfg3<RX, RY, RZ>::MINB)
       const int gy = clampi(ty0 - RY + row, a.lo[1], a.hi[1]);
       goff[i] = (int32_t)((gx - a.src_origin[0]) * a.src_pitch[0] +
                           (gy - a.src_origin[1]) * a.src_pitch[1]);
-      soff[i] = (uint32_t)(row * IWP + col) * 4u;
     }
-    const uint32_t sbase = smem_u32(stage0);
-    auto issue = [&](int s, int st) {
-      const char* base = a.src + (int64_t)(s - a.src_origin[2]) * a.src_pitch[2];
-      const uint32_t sb = sbase + (uint32_t)(st * C::STAGE * 4);
-#pragma unroll
-      for (int i = 0; i < NLD; ++i) {
-        if (i < NLD - 1 || tid + i * NT < IH * IW) cp_async4(sb + soff[i], base + goff[i]);
-      }
-    };
 
     const int jb = z0 - RZ, je = z1 - 1 + RZ;
     const int s_first = max(jb, a.lo[2]), s_last = min(je, a.hi[2]);
+#define ITKG_ISSUE(S_, ST_)                                                               \
+  do {                                                                                    \
+    const char* base_ = a.src + (int64_t)((S_) - a.src_origin[2]) * a.src_pitch[2];       \
+    const uint32_t sb_ = sbase + (uint32_t)((ST_) * C::STAGE * 4);                        \
+    _Pragma("unroll") for (int i = 0; i < NLD; ++i) {                                     \
+      const int e_ = tid + i * NT;                                                        \
+      if (i < NLD - 1 || e_ < IH * IW)                                                    \
+        cp_async4(sb_ + (uint32_t)(((e_ / IW) * IWP + e_ % IW) * 4), base_ + goff[i]);    \
+    }                                                                                     \
+  } while (0)
 #pragma unroll
     for (int q = 0; q < S; ++q) {
-      if (s_first + q <= s_last) issue(s_first + q, q);
+      if (s_first + q <= s_last) ITKG_ISSUE(s_first + q, q);
       cp_async_commit();
     }
 
-    float acc[MY][KZ];
+    f2_t acc[MY2][KZ];
 #pragma unroll
-    for (int m = 0; m < MY; ++m)
+    for (int m = 0; m < MY2; ++m)
 #pragma unroll
-      for (int q = 0; q < KZ; ++q) acc[m][q] = 0.0f;
-    float yv[MY];
+      for (int q = 0; q < KZ; ++q) acc[m][q] = 0ull;
+    f2_t yv[MY2];
 #pragma unroll
-    for (int m = 0; m < MY; ++m) yv[m] = 0.0f;
-    int prev_s = INT_MIN;
-    int cons = 0;
+    for (int m = 0; m < MY2; ++m) yv[m] = 0ull;
+
+    // Output addressing for this thread's column and rows.
     const int col_x = tx0 + lane;
     const int row_y0 = ty0 + warp * MY;
+    const bool col_ok = col_x <= a.req_hi[0];
+    int nrows_ok = a.req_hi[1] - row_y0 + 1;
+    nrows_ok = nrows_ok < 0 ? 0 : (nrows_ok > MY ? MY : nrows_ok);
+    char* const obase = a.dst + (int64_t)(col_x - a.dst_origin[0]) * a.dst_pitch[0] +
+                        (int64_t)(row_y0 - a.dst_origin[1]) * a.dst_pitch[1];
+    const int64_t opy = a.dst_pitch[1];
 
-    for (int jj = jb; jj <= je; jj += KZ) {
+    int prev_s = INT_MIN;
+    int cons = 0;
+    int p = 0;  // phase (j - jb) mod KZ
+    for (int j = jb; j <= je; ++j) {
+      const int s = clampi(j, a.lo[2], a.hi[2]);
+      if (s != prev_s) {
+        prev_s = s;
+        const int st = cons % S;
+        cp_async_wait<S - 1>();
+        __syncthreads();
+        // ---- x pass: stage -> xs ----
+        const float* tile = stage0 + st * C::STAGE;
+        constexpr int SEGS = TX / MX;
+        for (int t = tid; t < IH * SEGS; t += NT) {
+          const int row = t / SEGS, x0 = (t % SEGS) * MX;
+          float v[C::WIN];
+          const float4* src4 = reinterpret_cast<const float4*>(tile + row * IWP + x0);
 #pragma unroll
-      for (int p = 0; p < KZ; ++p) {
-        const int j = jj + p;
-        if (j <= je) {
-          const int s = clampi(j, a.lo[2], a.hi[2]);
-          if (s != prev_s) {
-            prev_s = s;
-            const int st = cons % S;
-            cp_async_wait<S - 1>();
-            __syncthreads();
-            // ---- x pass: stage -> xs ----
-            const float* tile = stage0 + st * C::STAGE;
-            constexpr int SEGS = TX / MX;
-            for (int t = tid; t < IH * SEGS; t += NT) {
-              const int row = t / SEGS, x0 = (t % SEGS) * MX;
-              float v[C::WIN];
-              const float4* src4 = reinterpret_cast<const float4*>(tile + row * IWP + x0);
-#pragma unroll
-              for (int q = 0; q < C::WIN / 4; ++q) {
-                const float4 f = src4[q];
-                v[4 * q + 0] = f.x;
-                v[4 * q + 1] = f.y;
-                v[4 * q + 2] = f.z;
-                v[4 * q + 3] = f.w;
-              }
-              float o[MX];
-#pragma unroll
-              for (int m = 0; m < MX; ++m) {
-                float acc_x = 0.0f;
-#pragma unroll
-                for (int k = 0; k < KX; ++k) acc_x = tap<REF>(acc_x, v[m + k], a.wx[k]);
-                o[m] = acc_x;
-              }
-              *reinterpret_cast<float4*>(xs + row * TX + x0) = make_float4(o[0], o[1], o[2], o[3]);
-            }
-            __syncthreads();
-            {
-              const int sn = s_first + cons + S;
-              if (sn <= s_last) issue(sn, st);
-              cp_async_commit();
-            }
-            ++cons;
-            // ---- y pass: xs -> yv (registers) ----
-            float w[MY + 2 * RY];
-#pragma unroll
-            for (int i = 0; i < MY + 2 * RY; ++i) w[i] = xs[(warp * MY + i) * TX + lane];
-#pragma unroll
-            for (int m = 0; m < MY; ++m) {
-              float acc_y = 0.0f;
-#pragma unroll
-              for (int k = 0; k < KY; ++k) acc_y = tap<REF>(acc_y, w[m + k], a.wy[k]);
-              yv[m] = acc_y;
-            }
+          for (int q = 0; q < C::WIN / 4; ++q) {
+            const float4 f = src4[q];
+            v[4 * q + 0] = f.x;
+            v[4 * q + 1] = f.y;
+            v[4 * q + 2] = f.z;
+            v[4 * q + 3] = f.w;
           }
-          // ---- z pass: push slice j into the ring ----
+          float o[MX];
 #pragma unroll
-          for (int k = 0; k < KZ; ++k) {
-            const int slot = ((p - k) % KZ + KZ) % KZ;
+          for (int m = 0; m < MX; ++m) {
+            float ax = 0.0f;
 #pragma unroll
-            for (int m = 0; m < MY; ++m) acc[m][slot] = tap<REF>(acc[m][slot], yv[m], a.wz[k]);
+            for (int k = 0; k < KX; ++k) ax = tap<REF>(ax, v[m + k], a.wx[k]);
+            o[m] = ax;
           }
-          // output z = j - RZ received its last tap; its slot is (p + 1) mod KZ
-          const int done = (p + 1) % KZ;
-          const int z = j - RZ;
-          if (z >= z0 && col_x <= a.req_hi[0]) {
-            char* orow = a.dst + (int64_t)(z - a.dst_origin[2]) * a.dst_pitch[2] +
-                         (int64_t)(col_x - a.dst_origin[0]) * a.dst_pitch[0];
+          *reinterpret_cast<float4*>(xs + row * TX + x0) = make_float4(o[0], o[1], o[2], o[3]);
+        }
+        __syncthreads();
+        {
+          const int sn = s_first + cons + S;
+          if (sn <= s_last) ITKG_ISSUE(sn, st);
+          cp_async_commit();
+        }
+        ++cons;
+        // ---- y pass: xs -> yv (registers, packed in row pairs) ----
+        float w[MY + 2 * RY];
 #pragma unroll
-            for (int m = 0; m < MY; ++m) {
-              const int y = row_y0 + m;
-              if (y <= a.req_hi[1])
-                store_out(orow + (int64_t)(y - a.dst_origin[1]) * a.dst_pitch[1], a.out_dtype,
-                          acc[m][done]);
-            }
+        for (int i = 0; i < MY + 2 * RY; ++i) w[i] = xs[(warp * MY + i) * TX + lane];
+#pragma unroll
+        for (int m = 0; m < MY2; ++m) {
+          float y0 = 0.0f, y1 = 0.0f;
+#pragma unroll
+          for (int k = 0; k < KY; ++k) {
+            y0 = tap<REF>(y0, w[2 * m + k], a.wy[k]);
+            y1 = tap<REF>(y1, w[2 * m + 1 + k], a.wy[k]);
           }
+          yv[m] = pack2(y0, y1);
+        }
+      }
+      // ---- z pass: push slice j into the ring, pop output z = j - RZ ----
+      f2_t done[MY2];
+      switch (p) {
+        ITKG_PUSH_CASE(0) ITKG_PUSH_CASE(1) ITKG_PUSH_CASE(2) ITKG_PUSH_CASE(3)
+        ITKG_PUSH_CASE(4) ITKG_PUSH_CASE(5) ITKG_PUSH_CASE(6) ITKG_PUSH_CASE(7)
+        ITKG_PUSH_CASE(8) ITKG_PUSH_CASE(9) ITKG_PUSH_CASE(10) ITKG_PUSH_CASE(11)
+        ITKG_PUSH_CASE(12) ITKG_PUSH_CASE(13) ITKG_PUSH_CASE(14) ITKG_PUSH_CASE(15)
+        ITKG_PUSH_CASE(16)
+        default: break;
+      }
+      p = p + 1 == KZ ? 0 : p + 1;
+      const int z = j - RZ;
+      if (z >= z0 && col_ok) {
+        char* orow = obase + (int64_t)(z - a.dst_origin[2]) * a.dst_pitch[2];
+        float vals[MY];
 #pragma unroll
-          for (int m = 0; m < MY; ++m) acc[m][done] = 0.0f;
+        for (int m = 0; m < MY2; ++m) unpack2(done[m], vals[2 * m], vals[2 * m + 1]);
+        if (a.out_dtype == ITKG_F32) {
+#pragma unroll
+          for (int m = 0; m < MY; ++m)
+            if (m < nrows_ok) __stcs(reinterpret_cast<float*>(orow + m * opy), vals[m]);
+        } else {
+#pragma unroll
+          for (int m = 0; m < MY; ++m) {
+            if (m >= nrows_ok) continue;
+            char* q = orow + m * opy;
+            if (a.out_dtype == ITKG_BF16) *reinterpret_cast<__nv_bfloat16*>(q) = from_f32<__nv_bfloat16>(vals[m]);
+            else if (a.out_dtype == ITKG_F16) *reinterpret_cast<__half*>(q) = from_f32<__half>(vals[m]);
+            else *reinterpret_cast<uint8_t*>(q) = from_f32<uint8_t>(vals[m]);
+          }
         }
       }
     }
+#undef ITKG_ISSUE
     cp_async_wait<0>();
     __syncthreads();
   }
@@ -273,14 +308,14 @@ struct Entry {
   int rx, ry, rz;
   KernelFn ref, fma;
   size_t smem;
-  int tx, ty;
+  int tx, ty, nt;
 };
 
 template <int RX, int RY, int RZ>
 Entry make_entry() {
   using C = Cfg3<RX, RY, RZ>;
   return Entry{RX, RY, RZ, k_fused3d_f32<RX, RY, RZ, true>, k_fused3d_f32<RX, RY, RZ, false>,
-               C::SMEM, C::TX, C::TY};
+               C::SMEM, C::TX, C::TY, C::NT};
 }
 
 const Entry kTable[] = {
@@ -375,15 +410,15 @@ itkg_status launch_fused(const FusedGeom& g, const float* const w[kMaxDim], void
   a.out_dtype = g.out_dtype;
   for (int k = 0; k < 2 * e->rx + 1; ++k) a.wx[k] = w[0][k];
   for (int k = 0; k < 2 * e->ry + 1; ++k) a.wy[k] = w[1][k];
-  for (int k = 0; k < 2 * e->rz + 1; ++k) a.wz[k] = w[2][k];
+  for (int k = 0; k < 2 * e->rz + 1; ++k) a.wz2[k] = splat2_host(w[2][k]);
   KernelFn fn = g.rounding == ITKG_ROUND_REFERENCE ? e->ref : e->fma;
   int resident = 0;
   {
-    const itkg_status st = resident_ctas(fn, e->smem, 256, &resident);
+    const itkg_status st = resident_ctas(fn, e->smem, e->nt, &resident);
     if (st != ITKG_SUCCESS) return st;
   }
   const int64_t grid = std::min<int64_t>(a.units, resident);
-  fn<<<(unsigned)grid, 256, e->smem, static_cast<cudaStream_t>(stream)>>>(a);
+  fn<<<(unsigned)grid, e->nt, e->smem, static_cast<cudaStream_t>(stream)>>>(a);
   note_launch(g.rounding == ITKG_ROUND_REFERENCE ? "fused3d_f32_ref" : "fused3d_f32_fma");
   cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) return set_error(ITKG_ERROR_CUDA, "fused3d launch: %s", cudaGetErrorString(err));

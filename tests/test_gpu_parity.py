@@ -191,13 +191,14 @@ def test_half_storage_outputs(gpu, out):
                      rounding=gpu.ROUND_FMA)
     if out == "bf16":
         got = (raw.astype(np.uint32) << 16).view(np.float32).astype(np.float64)
-        ulp_rel = 2.0 ** -8
+        half_ulp_rel = 2.0 ** -8   # 8 significand bits: half an ulp <= 2^-8 |v|
     else:
         got = raw.astype(np.float64)
-        ulp_rel = 2.0 ** -11
+        half_ulp_rel = 2.0 ** -11  # 11 significand bits
     # storage rounding: |err| <= half an ulp of the value (plus f32 arithmetic noise)
     err = np.abs(got - ref64)
-    assert (err <= np.abs(ref64) * ulp_rel * 0.5 * 1.0001 + 1e-4).all()
+    assert (err <= np.abs(ref64) * half_ulp_rel * 1.0001 + 1e-4).all()
+    ulp_rel = 2.0 * half_ulp_rel
     # bf16 output equals rounding the f32 result to nearest-even
     f32 = oracle.gaussian_f32(arr.astype(np.float32), 1.5, spacing=(0.7, 0.7, 2.5))
     assert normwise(got, f32) <= ulp_rel
