@@ -204,6 +204,26 @@ itkg_status itkg_gaussian_generate_region(const itkg_image *input, const itkg_re
                                           const itkg_gaussian_params *params,
                                           itkg_image *output, void *stream);
 
+/* ---- derivatives (not in the reference: it has no VJP) ---------------------
+ * Vector-Jacobian product of GaussianFilter over a whole image: x is the
+ * filter input (requested region = largest region = x->region), ybar = dL/dy
+ * on the same region.  The forward y = G x is recomputed, never stored.
+ *   xbar      if non-NULL: dL/dx = G^T ybar (the exact adjoint of the clamped
+ *             separable convolution, edge voxels receiving the clamped taps);
+ *             added to xbar's contents with ITKG_VJP_ACCUMULATE_XBAR.
+ *   sigma_bar if non-NULL: dL/dsigma = <ybar, dy/dsigma>, summed in f64, the
+ *             radius frozen at ceil(3 sigma / spacing) (the derivative of the
+ *             sampled, normalised kernel of gaussian.rs:29-40 at fixed r).  A
+ *             host pointer (the call synchronises the stream) unless
+ *             ITKG_VJP_SIGMA_BAR_ON_DEVICE; added to with ITKG_VJP_ACCUMULATE_SIGMA.
+ * Scalar f32 device images; FMA rounding; sigma must be finite and > 0. */
+#define ITKG_VJP_ACCUMULATE_XBAR 1
+#define ITKG_VJP_ACCUMULATE_SIGMA 2
+#define ITKG_VJP_SIGMA_BAR_ON_DEVICE 4
+itkg_status itkg_gaussian_vjp(const itkg_image *x, const itkg_image *ybar,
+                              const itkg_gaussian_params *params, itkg_image *xbar,
+                              double *sigma_bar, int32_t flags, void *stream);
+
 /* stream_full(&GaussianFilter{input, sigma}, num_pieces) (source.rs:81-98):
  * output (region == largest) is filled piece by piece along axis D-1.  With a
  * host-resident input and output, only one halo-padded input slab and one

@@ -101,6 +101,39 @@ struct FusedGeom {
 itkg_status launch_fused(const FusedGeom& g, const float* const w[kMaxDim], void* stream,
                          bool dry_run);
 
+// ---- VJP (vjp.cu): whole-image per-axis passes on f32 buffers ---------------
+constexpr int kMaxVjpTaps = 385;  // radius <= 192
+
+struct VjpAxisArgs {
+  const float* in;   // pass input (v for dual passes)
+  const float* din;  // dual passes: incoming derivative (NULL = zero)
+  float* out;
+  float* dout;       // dual passes: outgoing derivative
+  int64_t in_pitch[kMaxDim];   // bytes (shared by in and din)
+  int64_t out_pitch[kMaxDim];  // bytes (shared by out and dout)
+  int64_t size[kMaxDim];       // image size (unused axes 1)
+  int32_t axis;
+  int32_t radius;
+  int32_t accumulate;  // adjoint pass: out += result
+  int32_t pad_;
+};
+
+struct DotArgs {  // sum over the image of p * q (two pitched f32 images)
+  const float* p;
+  const float* q;
+  int64_t p_pitch[kMaxDim];
+  int64_t q_pitch[kMaxDim];
+  int64_t size[kMaxDim];
+};
+
+itkg_status launch_adjoint_axis(const VjpAxisArgs& a, const float* w, const float* prefix,
+                                void* stream);
+itkg_status launch_dual_axis(const VjpAxisArgs& a, const float* w, const float* dw, void* stream);
+int dot_partial_blocks(int64_t n);
+// partials: nblocks doubles of scratch; *out (device) = sum, or += with accumulate.
+itkg_status launch_dot(const DotArgs& d, double* partials, int nblocks, double* out,
+                       bool accumulate, void* stream);
+
 // ---- device scratch ---------------------------------------------------------
 // Stream-ordered scratch from a library-owned memory pool of the current
 // device (cudaMallocAsync / cudaFreeAsync on `stream`).

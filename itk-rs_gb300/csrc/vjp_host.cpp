@@ -1,0 +1,236 @@
+// Host side of the Gaussian VJP (no counterpart in the reference, which has
+// no derivative): itkg_gaussian_vjp and itkg_gaussian_scale_stack_loss_vjp.
+//
+// Coefficients are computed on the host in f64 from the reference's kernel
+// formula (gaussian.rs:29-40) at a radius frozen at r(sigma):
+//   g_i = exp(-0.5 t_i^2), t_i = (i - r) / s, s = sigma / spacing,
+//   w_i = g_i / S,  S = sum g,
+//   dw_i/dsigma = (g_i' S - g_i S') / S^2 / spacing,  g_i' = g_i t_i^2 / s,
+//   P_m = w_0 + ... + w_m  (adjoint edge folds).
+// The per-axis passes run on f32 buffers from the stream-ordered scratch pool;
+// the fused whole-filter kernels (fused_vjp.cu) take over where they apply.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "geom.hpp"
+#include "internal.hpp"
+
+namespace itkg {
+namespace {
+
+struct AxisCoeffs {
+  int r = 0;
+  std::vector<float> w, dw, prefix;
+};
+
+void make_coeffs(double sigma, double spacing, int r, AxisCoeffs* c) {
+  const double s = sigma / spacing;
+  const int K = 2 * r + 1;
+  std::vector<double> g(K), gp(K);
+  double S = 0.0, Sp = 0.0;
+  for (int i = 0; i < K; ++i) {
+    const double t = ((double)i - (double)r) / s;
+    g[i] = std::exp(-0.5 * (t * t));
+    gp[i] = g[i] * t * t / s;
+  }
+  for (int i = 0; i < K; ++i) S += g[i];
+  for (int i = 0; i < K; ++i) Sp += gp[i];
+  c->r = r;
+  c->w.resize(K);
+  c->dw.resize(K);
+  c->prefix.resize(K);
+  double acc = 0.0;
+  for (int i = 0; i < K; ++i) {
+    const double w = g[i] / S;
+    c->w[i] = (float)w;
+    c->dw[i] = (float)((gp[i] * S - g[i] * Sp) / (S * S) / spacing);
+    acc += w;
+    c->prefix[i] = (float)acc;
+  }
+}
+
+itkg_status check_f32_device(const itkg_image* im, const char* name, int D) {
+  ITKG_TRY(validate_image(im, name));
+  if (im->location != ITKG_DEVICE)
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "%s: the VJP takes device buffers", name);
+  if (im->dtype != ITKG_F32 || im->components != 1)
+    return set_error(ITKG_ERROR_UNSUPPORTED, "%s: the VJP takes scalar f32 images", name);
+  if (D && im->dim != D) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "%s: dim differs", name);
+  return ITKG_SUCCESS;
+}
+
+bool same_size(const itkg_image& a, const itkg_image& b) {
+  for (int d = 0; d < a.dim; ++d)
+    if (a.region.size[d] != b.region.size[d] || a.region.index[d] != b.region.index[d]) return false;
+  return true;
+}
+
+void view3(const itkg_image& im, int64_t* pitch, int64_t* size) {
+  for (int d = 0; d < kMaxDim; ++d) {
+    pitch[d] = d < im.dim ? im.pitch[d] : 0;
+    size[d] = d < im.dim ? (int64_t)im.region.size[d] : 1;
+  }
+}
+
+// Scratch images: dense f32 of the same size.
+struct Scratch {
+  std::vector<void*> ptrs;
+  cudaStream_t s;
+  explicit Scratch(cudaStream_t st) : s(st) {}
+  ~Scratch() {
+    for (void* p : ptrs) scratch_free(p, s);
+  }
+  itkg_status image(const itkg_image& like, itkg_image* out) {
+    std::memset(out, 0, sizeof *out);
+    out->dim = like.dim;
+    out->dtype = ITKG_F32;
+    out->components = 1;
+    out->location = ITKG_DEVICE;
+    out->region = like.region;
+    dense_layout(out, 16);
+    void* p = nullptr;
+    ITKG_TRY(scratch_alloc(&p, image_bytes(*out), s));
+    ptrs.push_back(p);
+    out->data = p;
+    return ITKG_SUCCESS;
+  }
+  itkg_status raw(size_t bytes, void** p) {
+    ITKG_TRY(scratch_alloc(p, bytes, s));
+    ptrs.push_back(*p);
+    return ITKG_SUCCESS;
+  }
+};
+
+VjpAxisArgs axis_args(const itkg_image& in, const itkg_image* din, const itkg_image& out,
+                      const itkg_image* dout, int axis, int r, bool accumulate) {
+  VjpAxisArgs a;
+  std::memset(&a, 0, sizeof a);
+  a.in = static_cast<const float*>(in.data);
+  a.din = din ? static_cast<const float*>(din->data) : nullptr;
+  a.out = static_cast<float*>(out.data);
+  a.dout = dout ? static_cast<float*>(dout->data) : nullptr;
+  int64_t sz[3];
+  view3(in, a.in_pitch, sz);
+  view3(out, a.out_pitch, a.size);
+  a.axis = axis;
+  a.radius = r;
+  a.accumulate = accumulate ? 1 : 0;
+  return a;
+}
+
+// xbar (+)= G^T ybar: passes along axes D-1 .. 0.
+itkg_status adjoint_chain(const itkg_image& ybar, const AxisCoeffs* c, itkg_image* xbar,
+                          bool accumulate, Scratch& sc) {
+  const int D = ybar.dim;
+  itkg_image t[2];
+  if (D > 1) ITKG_TRY(sc.image(ybar, &t[0]));
+  if (D > 2) ITKG_TRY(sc.image(ybar, &t[1]));
+  const itkg_image* cur = &ybar;
+  int k = 0;
+  for (int a = D - 1; a >= 0; --a) {
+    const bool last = a == 0;
+    itkg_image* nxt = last ? xbar : &t[k++ & 1];
+    ITKG_TRY(launch_adjoint_axis(axis_args(*cur, nullptr, *nxt, nullptr, a, c[a].r, last && accumulate),
+                                 c[a].w.data(), c[a].prefix.data(), sc.s));
+    cur = nxt;
+  }
+  return ITKG_SUCCESS;
+}
+
+// (y, dy/dsigma) of the forward: dual passes along axes 0 .. D-1.
+itkg_status dual_chain(const itkg_image& x, const AxisCoeffs* c, itkg_image* y, itkg_image* dy,
+                       Scratch& sc) {
+  const int D = x.dim;
+  itkg_image v[2], dv[2];
+  for (int i = 0; i < 2 && i < D - 1; ++i) {
+    ITKG_TRY(sc.image(x, &v[i]));
+    ITKG_TRY(sc.image(x, &dv[i]));
+  }
+  const itkg_image* cv = &x;
+  const itkg_image* cdv = nullptr;
+  for (int a = 0; a < D; ++a) {
+    const bool last = a == D - 1;
+    itkg_image* nv = last ? y : &v[a & 1];
+    itkg_image* ndv = last ? dy : &dv[a & 1];
+    ITKG_TRY(launch_dual_axis(axis_args(*cv, cdv, *nv, ndv, a, c[a].r, false), c[a].w.data(),
+                              c[a].dw.data(), sc.s));
+    cv = nv;
+    cdv = ndv;
+  }
+  return ITKG_SUCCESS;
+}
+
+itkg_status coeffs_for(const itkg_image& x, double sigma, AxisCoeffs* c) {
+  if (!(sigma > 0.0) || !std::isfinite(sigma))
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "the VJP needs a finite sigma > 0 (got %g)", sigma);
+  for (int d = 0; d < x.dim; ++d) {
+    const uint64_t r = kernel_radius(sigma, x.spacing[d]);
+    if (2 * r + 1 > (uint64_t)kMaxVjpTaps)
+      return set_error(ITKG_ERROR_UNSUPPORTED, "VJP radius %llu exceeds %d", (unsigned long long)r,
+                       (kMaxVjpTaps - 1) / 2);
+    make_coeffs(sigma, x.spacing[d], (int)r, &c[d]);
+  }
+  return ITKG_SUCCESS;
+}
+
+DotArgs dot_args(const itkg_image& p, const itkg_image& q) {
+  DotArgs d;
+  std::memset(&d, 0, sizeof d);
+  d.p = static_cast<const float*>(p.data);
+  d.q = static_cast<const float*>(q.data);
+  view3(p, d.p_pitch, d.size);
+  int64_t sz[3];
+  view3(q, d.q_pitch, sz);
+  return d;
+}
+
+}  // namespace
+}  // namespace itkg
+
+using namespace itkg;
+
+extern "C" itkg_status itkg_gaussian_vjp(const itkg_image* x, const itkg_image* ybar,
+                                         const itkg_gaussian_params* params, itkg_image* xbar,
+                                         double* sigma_bar, int32_t flags, void* stream) {
+  ITKG_TRY(check_f32_device(x, "x", 0));
+  ITKG_TRY(check_f32_device(ybar, "ybar", x->dim));
+  if (!params) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "params is NULL");
+  if (!same_size(*x, *ybar)) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "x and ybar regions differ");
+  if (xbar) {
+    ITKG_TRY(check_f32_device(xbar, "xbar", x->dim));
+    if (!same_size(*x, *xbar)) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "x and xbar regions differ");
+  }
+  if (flags & ~(ITKG_VJP_ACCUMULATE_XBAR | ITKG_VJP_ACCUMULATE_SIGMA | ITKG_VJP_SIGMA_BAR_ON_DEVICE))
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "unknown flags 0x%x", flags);
+  AxisCoeffs c[kMaxDim];
+  ITKG_TRY(coeffs_for(*x, params->sigma, c));
+  if (region_len(x->region, x->dim) == 0) return ITKG_SUCCESS;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  Scratch sc(s);
+  if (xbar) ITKG_TRY(adjoint_chain(*ybar, c, xbar, flags & ITKG_VJP_ACCUMULATE_XBAR, sc));
+  if (sigma_bar) {
+    itkg_image y, dy;
+    ITKG_TRY(sc.image(*x, &y));
+    ITKG_TRY(sc.image(*x, &dy));
+    ITKG_TRY(dual_chain(*x, c, &y, &dy, sc));
+    const int nb = dot_partial_blocks((int64_t)region_len(x->region, x->dim));
+    void* part = nullptr;
+    ITKG_TRY(sc.raw(sizeof(double) * (nb + 1), &part));
+    double* dres = static_cast<double*>(part) + nb;
+    const bool on_dev = flags & ITKG_VJP_SIGMA_BAR_ON_DEVICE;
+    const bool acc = flags & ITKG_VJP_ACCUMULATE_SIGMA;
+    ITKG_TRY(launch_dot(dot_args(*ybar, dy), static_cast<double*>(part), nb,
+                        on_dev ? sigma_bar : dres, on_dev && acc, s));
+    if (!on_dev) {
+      double h = 0.0;
+      ITKG_CUDA(cudaMemcpyAsync(&h, dres, sizeof h, cudaMemcpyDeviceToHost, s));
+      ITKG_CUDA(cudaStreamSynchronize(s));
+      *sigma_bar = acc ? *sigma_bar + h : h;
+    }
+  }
+  set_last_kernel("vjp_per_axis_f32");
+  return ITKG_SUCCESS;
+}

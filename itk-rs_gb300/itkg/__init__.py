@@ -403,6 +403,30 @@ def gaussian(arr: np.ndarray, sigma: float, spacing=None, components: int = 1,
     return f.generate_region(req, out_dtype=out_dtype).data
 
 
+VJP_ACCUMULATE_XBAR = 1
+VJP_ACCUMULATE_SIGMA = 2
+VJP_SIGMA_BAR_ON_DEVICE = 4
+
+
+def vjp(x: DeviceImage, ybar: DeviceImage, sigma: float, xbar: DeviceImage | None = None,
+        want_sigma: bool = True, flags: int = 0, sigma_bar_init: float = 0.0,
+        stream: Stream = _DEFAULT_STREAM):
+    """GaussianFilter VJP over the whole image: returns (xbar, sigma_bar).
+
+    xbar = G^T ybar (a DeviceImage, allocated if not given); sigma_bar =
+    <ybar, dy/dsigma> as a Python float (None if not requested)."""
+    p = itkg_gaussian_params()
+    p.sigma = float(sigma)
+    p.rounding = ROUND_FMA
+    if xbar is None:
+        xbar = DeviceImage(x.region, F32, 1, x.spacing, x.origin)
+    sb = ctypes.c_double(sigma_bar_init)
+    check(lib().itkg_gaussian_vjp(ctypes.byref(x.c), ctypes.byref(ybar.c), ctypes.byref(p),
+                                  ctypes.byref(xbar.c), ctypes.byref(sb) if want_sigma else None,
+                                  int(flags), stream.ptr))
+    return xbar, (sb.value if want_sigma else None)
+
+
 def last_kernel() -> str:
     return lib().itkg_last_kernel().decode()
 

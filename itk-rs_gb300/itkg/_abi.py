@@ -91,6 +91,7 @@ SIGNATURES = {
     "itkg_image_copy_from": (st, [I, I, P]),
     "itkg_gaussian_generate_region": (st, [I, R, R, G, I, P]),
     "itkg_stream_full": (st, [I, R, G, ctypes.c_uint64, I, P]),
+    "itkg_gaussian_vjp": (st, [I, I, G, I, ctypes.POINTER(ctypes.c_double), ctypes.c_int32, P]),
 }
 
 _lib = None

@@ -1,0 +1,91 @@
+"""GPU VJP checks (the reference has no VJP; these follow the specification):
+FP64 dot-product test <Gx, y> = <x, G^T y>, the adjoint against an FP64
+numpy adjoint, dL/dsigma against the FP64 analytic derivative and against
+central finite differences (h = 1e-3, radius frozen at r(sigma))."""
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+SHAPES = [((40,), 2.0, None), ((33, 45), 1.5, None), ((17, 23, 29), 1.2, None),
+          ((24, 20, 16), 2.0, (0.7, 0.9, 2.5)), ((6, 5, 4), 3.0, None), ((1, 9, 1), 1.0, None),
+          ((48, 40, 36), 4.0, None)]
+
+
+def _dev(itkg, arr, spacing=None):
+    return itkg.DeviceImage.from_host(itkg.Image(np.ascontiguousarray(arr, np.float32), spacing=spacing))
+
+
+def _radii(sigma, spacing, D):
+    sp = spacing or [1.0] * D
+    return [oracle.kernel_radius(sigma, sp[d]) for d in range(D)]
+
+
+@pytest.mark.parametrize("shape,sigma,spacing", SHAPES)
+def test_dot_product_identity(gpu, shape, sigma, spacing):
+    rng = np.random.default_rng(len(shape) * 100 + shape[0])
+    x = rng.standard_normal(shape).astype(np.float32)
+    y = rng.standard_normal(shape).astype(np.float32)
+    dx, dy = _dev(gpu, x, spacing), _dev(gpu, y, spacing)
+    Gx = gpu.GaussianFilter(dx, sigma, rounding=gpu.ROUND_FMA).generate_region(dx.region).download()
+    GTy, _ = gpu.vjp(dx, dy, sigma, want_sigma=False)
+    GTy = GTy.download()
+    lhs = float(np.dot(Gx.astype(np.float64).ravel(), y.astype(np.float64).ravel()))
+    rhs = float(np.dot(x.astype(np.float64).ravel(), GTy.astype(np.float64).ravel()))
+    scale = float(np.abs(Gx).sum() * np.abs(y).max()) + 1e-30
+    assert abs(lhs - rhs) <= 1e-6 * scale, (lhs, rhs)
+
+
+@pytest.mark.parametrize("shape,sigma,spacing", SHAPES)
+def test_adjoint_matches_fp64(gpu, shape, sigma, spacing):
+    rng = np.random.default_rng(7 + shape[0])
+    x = rng.standard_normal(shape).astype(np.float32)
+    y = rng.standard_normal(shape).astype(np.float32)
+    got, _ = gpu.vjp(_dev(gpu, x, spacing), _dev(gpu, y, spacing), sigma, want_sigma=False)
+    want = oracle.gaussian_adjoint_f64(y.astype(np.float64), sigma, spacing=list(spacing) if spacing else None)
+    got = got.download().astype(np.float64)
+    assert np.abs(got - want).max() / np.abs(want).max() <= 1e-5
+
+
+@pytest.mark.parametrize("shape,sigma,spacing", SHAPES)
+def test_sigma_bar_matches_fp64_and_finite_differences(gpu, shape, sigma, spacing):
+    rng = np.random.default_rng(11 + shape[-1])
+    x = rng.random(shape).astype(np.float32)
+    ybar = rng.standard_normal(shape).astype(np.float32)
+    sp = list(spacing) if spacing else None
+    _, sb = gpu.vjp(_dev(gpu, x, spacing), _dev(gpu, ybar, spacing), sigma)
+    radii = _radii(sigma, sp, len(shape))
+    d64 = oracle.gaussian_dsigma_f64(x.astype(np.float64), sigma, spacing=sp, radii=radii)
+    want = float((d64 * ybar.astype(np.float64)).sum())
+    scale = float(np.abs(d64 * ybar).sum()) + 1e-30
+    assert abs(sb - want) <= 1e-5 * scale, (sb, want)
+    h = 1e-3
+    fp = oracle.gaussian_whole_f64(x.astype(np.float64), sigma + h, spacing=sp, radii=radii)
+    fm = oracle.gaussian_whole_f64(x.astype(np.float64), sigma - h, spacing=sp, radii=radii)
+    fd = float(((fp - fm) / (2 * h) * ybar.astype(np.float64)).sum())
+    assert abs(sb - fd) <= 1e-4 * scale + 1e-6 * abs(fd), (sb, fd)
+
+
+def test_accumulate_flags(gpu):
+    rng = np.random.default_rng(3)
+    x = rng.random((12, 14, 16)).astype(np.float32)
+    y = rng.standard_normal((12, 14, 16)).astype(np.float32)
+    dx, dy = _dev(gpu, x), _dev(gpu, y)
+    base, sb = gpu.vjp(dx, dy, 1.3)
+    start = rng.standard_normal((12, 14, 16)).astype(np.float32)
+    acc = _dev(gpu, start)
+    out, sb2 = gpu.vjp(dx, dy, 1.3, xbar=acc, sigma_bar_init=2.5,
+                       flags=gpu.VJP_ACCUMULATE_XBAR | gpu.VJP_ACCUMULATE_SIGMA)
+    assert np.allclose(out.download(), start + base.download(), rtol=0, atol=1e-6)
+    assert abs(sb2 - (sb + 2.5)) < 1e-9 * max(1.0, abs(sb))
+
+
+def test_vjp_rejects_bad_sigma(gpu):
+    from itkg import _abi
+    x = _dev(gpu, np.zeros((4, 5, 6), np.float32))
+    with pytest.raises(_abi.ItkgError):
+        gpu.vjp(x, x, 0.0)
+    with pytest.raises(_abi.ItkgError):
+        gpu.vjp(x, x, float("nan"))
