@@ -176,6 +176,10 @@ itkg_status itkg_host_free_pinned(void *ptr);
 itkg_status itkg_memcpy(void *dst, const void *src, size_t bytes, int32_t kind, void *stream);
 itkg_status itkg_memset_device(void *dst, int32_t value, size_t bytes, void *stream);
 itkg_status itkg_stream_synchronize(void *stream);
+/* Device-side fault word of the current device: non-zero after a fused
+ * kernel's bounded wait on a tile load gave up (the kernel then returned
+ * early and its output is incomplete).  clear != 0 resets it. */
+itkg_status itkg_device_fault(int32_t clear, uint32_t *flag);
 
 /* Fill *img for a freshly allocated device image of `region`, with rows and
  * slices padded to 128-byte multiples (TMA-friendly), and allocate it. */
@@ -223,6 +227,34 @@ itkg_status itkg_gaussian_generate_region(const itkg_image *input, const itkg_re
 itkg_status itkg_gaussian_vjp(const itkg_image *x, const itkg_image *ybar,
                               const itkg_gaussian_params *params, itkg_image *xbar,
                               double *sigma_bar, int32_t flags, void *stream);
+
+/* ---- batches (not in the reference: it filters one image per call) ---------
+ * A batch collects many forward requests (the arguments of
+ * itkg_gaussian_generate_region, device buffers only) and VJP requests (the
+ * arguments of itkg_gaussian_vjp, sigma_bar a device pointer or NULL),
+ * plans them once and replays them as one CUDA graph:
+ *   itkg_batch_plan  picks each item's kernel (an autotuner times the fused
+ *                    kernel against per-axis passes once per (dtype, size
+ *                    bucket, radius) class unless ITKG_BATCH_NO_AUTOTUNE),
+ *                    merges fused items into persistent launches and captures
+ *                    everything into a graph; it runs each item at least once
+ *                    while tuning, so outputs must be writable at plan time;
+ *   itkg_batch_run   launches the graph on `stream` (asynchronous).
+ * Buffers must stay valid, and at the same addresses, while the batch exists. */
+typedef struct itkg_batch itkg_batch;
+#define ITKG_BATCH_NO_AUTOTUNE 1
+itkg_status itkg_batch_create(itkg_batch **batch);
+itkg_status itkg_batch_destroy(itkg_batch *batch);
+itkg_status itkg_batch_add(itkg_batch *batch, const itkg_image *input, const itkg_region *largest,
+                           const itkg_region *requested, const itkg_gaussian_params *params,
+                           itkg_image *output);
+itkg_status itkg_batch_add_vjp(itkg_batch *batch, const itkg_image *x, const itkg_image *ybar,
+                               const itkg_gaussian_params *params, itkg_image *xbar,
+                               double *sigma_bar_device, int32_t flags);
+itkg_status itkg_batch_plan(itkg_batch *batch, int32_t flags, void *stream);
+itkg_status itkg_batch_run(itkg_batch *batch, void *stream);
+/* One line per planned launch (kernel chosen per item); valid until the next call. */
+const char *itkg_batch_describe(itkg_batch *batch);
 
 /* stream_full(&GaussianFilter{input, sigma}, num_pieces) (source.rs:81-98):
  * output (region == largest) is filled piece by piece along axis D-1.  With a

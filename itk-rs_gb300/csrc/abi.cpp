@@ -50,6 +50,11 @@ void note_launch(const char* name) {
   t_kernel = name;
 }
 
+void note_launches(uint64_t n, const char* name) {
+  g_launches.fetch_add(n, std::memory_order_relaxed);
+  t_kernel = name;
+}
+
 // ---- scratch: one memory pool per device, never trimmed --------------------
 namespace {
 std::mutex g_pool_mu;
@@ -249,12 +254,12 @@ static itkg_status check_params(const itkg_gaussian_params* prm) {
 }
 
 // Device-resident input and output.
-static itkg_status generate_device(const itkg_image& in, const itkg_region& largest,
-                                   const itkg_region& requested, const itkg_gaussian_params& prm,
-                                   const Plan& plan, const itkg_image& out, cudaStream_t s) {
+static void make_fused_geom(const itkg_image& in, const itkg_region& largest,
+                            const itkg_region& requested, const itkg_gaussian_params& prm,
+                            const Plan& plan, const itkg_image& out, FusedGeom* gp) {
   const int D = in.dim;
-  if (prm.arithmetic != ITKG_ARITH_PIXEL_U8 && prm.algorithm != ITKG_ALGO_PER_AXIS) {
-    FusedGeom g;
+  FusedGeom& g = *gp;
+  {
     std::memset(&g, 0, sizeof g);
     g.src = in.data;
     g.dst = out.data;
@@ -276,6 +281,16 @@ static itkg_status generate_device(const itkg_image& in, const itkg_region& larg
     g.in_dtype = in.dtype;
     g.out_dtype = out.dtype;
     g.rounding = prm.rounding;
+  }
+}
+
+static itkg_status generate_device(const itkg_image& in, const itkg_region& largest,
+                                   const itkg_region& requested, const itkg_gaussian_params& prm,
+                                   const Plan& plan, const itkg_image& out, cudaStream_t s) {
+  const int D = in.dim;
+  if (prm.arithmetic != ITKG_ARITH_PIXEL_U8 && prm.algorithm != ITKG_ALGO_PER_AXIS) {
+    FusedGeom g;
+    make_fused_geom(in, largest, requested, prm, plan, out, &g);
     const float* w[kMaxDim] = {nullptr, nullptr, nullptr};
     for (int d = 0; d < D; ++d) w[d] = plan.w32[d].data();
     itkg_status st = launch_fused(g, w, s, /*dry_run=*/true);
@@ -284,6 +299,27 @@ static itkg_status generate_device(const itkg_image& in, const itkg_region& larg
       return set_error(ITKG_ERROR_UNSUPPORTED, "no fused kernel covers this geometry");
   }
   return run_per_axis(in, largest, requested, prm, plan, out, s);
+}
+
+itkg_status fused_geom_for(const itkg_image& in, const itkg_region& largest,
+                           const itkg_region& requested, const itkg_gaussian_params& prm,
+                           const itkg_image& out, FusedGeom* g,
+                           std::vector<std::vector<float>>* weights) {
+  if (prm.arithmetic == ITKG_ARITH_PIXEL_U8 || prm.algorithm == ITKG_ALGO_PER_AXIS)
+    return ITKG_ERROR_UNSUPPORTED;
+  const int D = in.dim;
+  if (out.dim != D || out.components != in.components || region_len(requested, D) == 0 ||
+      !region_contains(largest, requested, D) || !region_contains(out.region, requested, D))
+    return ITKG_ERROR_UNSUPPORTED;
+  Plan plan;
+  if (make_plan(in, requested, largest, prm.sigma, &plan) != ITKG_SUCCESS) return ITKG_ERROR_UNSUPPORTED;
+  if (!region_contains(in.region, plan.in_reg, D)) return ITKG_ERROR_UNSUPPORTED;
+  make_fused_geom(in, largest, requested, prm, plan, out, g);
+  const float* w[kMaxDim] = {nullptr, nullptr, nullptr};
+  for (int d = 0; d < D; ++d) w[d] = plan.w32[d].data();
+  if (launch_fused(*g, w, nullptr, /*dry_run=*/true) != ITKG_SUCCESS) return ITKG_ERROR_UNSUPPORTED;
+  weights->assign(plan.w32, plan.w32 + D);
+  return ITKG_SUCCESS;
 }
 
 static itkg_status generate_region(const itkg_image* input, const itkg_region* largest,
@@ -476,6 +512,14 @@ itkg_status itkg_memcpy(void* dst, const void* src, size_t bytes, int32_t kind, 
 
 itkg_status itkg_memset_device(void* dst, int32_t value, size_t bytes, void* stream) {
   ITKG_CUDA(cudaMemsetAsync(dst, value, bytes, static_cast<cudaStream_t>(stream)));
+  return ITKG_SUCCESS;
+}
+
+itkg_status itkg_device_fault(int32_t clear, uint32_t* flag) {
+  if (!flag) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "flag is NULL");
+  unsigned int f = 0;
+  ITKG_TRY(fused_fault_flag(&f, clear != 0));
+  *flag = f;
   return ITKG_SUCCESS;
 }
 

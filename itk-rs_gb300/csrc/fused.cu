@@ -7,27 +7,31 @@
 // range of output slices [z0, z1).  It marches through the input slices
 // j = z0 - RZ .. z1 - 1 + RZ (clamped to the image on z, which is the
 // reference's clamp-to-edge on axis 2, conv.rs:31-33):
-//   1. the (TX + 2RX) x (TY + 2RY) input tile of slice j is staged in shared
-//      memory by cp.async, S slices ahead; x and y coordinates are clamped to
-//      the image bounds as the tile is gathered, so the halo already holds the
-//      reference's edge replication;
+//   1. the (TX + 2XA) x (TY + 2RY) input tile of slice j is staged in shared
+//      memory S slices ahead -- by one TMA tile load per slice (an elected
+//      thread, mbarrier completion) when the buffer's pitches are 16-byte
+//      multiples, else by a cp.async gather.  Edge tiles replicate the image's
+//      edge values into the halo after the load (TMA fills zeros outside the
+//      buffer); the gather clamps its coordinates instead.  Either way the halo
+//      holds the reference's clamp-to-edge values.
 //   2. x pass: shared tile -> shared x-filtered tile (TY + 2RY rows);
 //   3. y pass: each thread filters MY consecutive rows of one column from a
 //      register window;
 //   4. z pass, "push" form: slice j contributes w[k] * v to the outputs
 //      z = j + RZ - k; each thread keeps a ring of KZ accumulators per owned
-//      column in registers (rows paired into f32x2 registers), the ring slot
-//      being a compile-time function of the phase j mod KZ, selected by a
-//      switch.  The accumulator of output z receives its taps in ascending k
-//      (ascending j), starting from zero, so with reference rounding the
-//      result is bit-identical to the reference's sequence
-//      acc = 0; acc = acc + x * w (conv.rs:26-36); the intermediates of every
-//      pass are f32 values exactly as the reference stores them.
-// Slices clamped at the z ends are filtered once and pushed repeatedly.
+//      column in registers, the ring slot being a compile-time function of
+//      the phase j mod KZ, selected by a switch.
+// FMA rounding runs the x, y and z passes as packed two-lane f32x2 FMAs
+// (rows or columns paired).  Reference rounding runs scalar
+// acc = acc + x * w with separate roundings in ascending tap order, starting
+// from zero, on f32 intermediates -- bit-identical to conv.rs:26-36 pass by
+// pass.  Slices clamped at the z ends are filtered once and pushed again.
 //
 // Work balance.  The (tile, z) units of the request are split evenly over a
 // grid of (SMs x resident CTAs) CTAs; a CTA's share is one or two z-segments.
+#include <cuda.h>
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
 
 #include <algorithm>
 #include <climits>
@@ -42,8 +46,10 @@
 namespace itkg {
 namespace {
 
-constexpr int kMaxFusedR = 8;
+constexpr int kMaxFusedR = 12;
 constexpr int kMaxFusedK = 2 * kMaxFusedR + 1;
+
+__device__ unsigned int g_fused_fault = 0;  // set when a bounded wait gives up
 
 struct Fused3DArgs {
   const char* src;
@@ -62,7 +68,10 @@ struct Fused3DArgs {
   int32_t pad_;
   float wx[kMaxFusedK];
   float wy[kMaxFusedK];
-  f2_t wz2[kMaxFusedK];  // {w, w} pairs for the packed z pass
+  float wz[kMaxFusedK];
+  f2_t wx2[kMaxFusedK];  // {w, w} pairs for the packed passes
+  f2_t wy2[kMaxFusedK];
+  f2_t wz2[kMaxFusedK];
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -80,28 +89,66 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait: gives up after ~2^31 cycles (about a second) and reports false.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const long long t0 = clock64();
+  while (!mbar_try_wait(bar, parity))
+    if (clock64() - t0 > (1ll << 31)) return false;
+  return true;
+}
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, int x, int y, int z,
+                                            uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4}], [%5];\n" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(bar)
+      : "memory");
+}
+
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
 // Tile shape per radius.
 template <int RX, int RY, int RZ>
 struct Cfg3 {
   static constexpr int KX = 2 * RX + 1, KY = 2 * RY + 1, KZ = 2 * RZ + 1;
-  static constexpr int NT = 256;                  // threads per CTA
+  static constexpr int NT = 256;                    // threads per CTA
   static constexpr int NW = NT / 32;
-  static constexpr int TX = 32;                   // one lane per output column
-  static constexpr int MY = 4;                    // rows per thread (y pass, z ring)
-  static constexpr int MY2 = MY / 2;              // packed row pairs
+  static constexpr int TX = 32;                     // one lane per output column
+  static constexpr int MY = RZ <= 8 ? 4 : 2;        // rows per thread (y pass, z ring)
+  static constexpr int MY2 = MY / 2;                // packed row pairs
   static constexpr int TY = NW * MY;
-  static constexpr int MX = 4;                    // x outputs per x-pass task
-  static constexpr int IW = TX + 2 * RX;          // staged tile width
-  static constexpr int IH = TY + 2 * RY;          // staged tile height
-  static constexpr int WIN = ((MX + 2 * RX) + 3) / 4 * 4;  // x-pass window, float4 multiple
-  static constexpr int IWP = ((TX - MX + WIN) + 3) / 4 * 4;  // row stride (floats)
-  static constexpr int S = 4;                     // slices in flight
-  static constexpr int NLD = (IH * IW + NT - 1) / NT;
-  static constexpr int STAGE = IH * IWP;          // floats per stage
-  static constexpr size_t SMEM = sizeof(float) * (size_t)(S * STAGE + IH * TX);
+  static constexpr int MX = 8;                      // x outputs per x-pass task
+  static constexpr int XA = (RX + 3) / 4 * 4;       // x halo rounded up to 16 bytes
+  static constexpr int BW = TX + 2 * XA;            // staged tile width (floats)
+  static constexpr int IH = TY + 2 * RY;            // staged tile height
+  static constexpr int OFF = (XA - RX) % 4;         // window misalignment
+  static constexpr int WB = XA - RX - OFF;          // aligned window start (col)
+  static constexpr int WIN = (MX + 2 * RX + OFF + 3) / 4 * 4;  // x-pass window (floats)
+  static constexpr int S = 4;                       // slices in flight
+  static constexpr int STAGE = (IH * BW + 31) / 32 * 32;  // floats per stage (128-byte multiple)
+  static constexpr int NLD = (STAGE + NT - 1) / NT; // gather elements per thread
+  static constexpr size_t SMEM = sizeof(float) * (size_t)(S * STAGE + 2 * IH * TX) + 128;
   static constexpr int MINB = 2;
+  static_assert(WB + TX - MX + WIN <= BW, "x window stays inside the staged row");
+  static_assert(TX % MX == 0, "x segments");
 };
 
 // z pass for phase P: push the packed y-filtered values into every ring slot,
@@ -113,7 +160,16 @@ __device__ __forceinline__ void push_phase(f2_t (&acc)[MY2][KZ], const f2_t (&yv
   for (int k = 0; k < KZ; ++k) {
     const int slot = (P - k + KZ) % KZ;
 #pragma unroll
-    for (int m = 0; m < MY2; ++m) acc[m][slot] = tap2<REF>(acc[m][slot], yv[m], a.wz2[k]);
+    for (int m = 0; m < MY2; ++m) {
+      if constexpr (REF) {
+        float a0, a1, v0, v1;
+        unpack2(acc[m][slot], a0, a1);
+        unpack2(yv[m], v0, v1);
+        acc[m][slot] = pack2(__fadd_rn(a0, __fmul_rn(v0, a.wz[k])), __fadd_rn(a1, __fmul_rn(v1, a.wz[k])));
+      } else {
+        acc[m][slot] = fma2(yv[m], a.wz2[k], acc[m][slot]);
+      }
+    }
   }
   constexpr int D = (P + 1) % KZ;
 #pragma unroll
@@ -123,28 +179,40 @@ __device__ __forceinline__ void push_phase(f2_t (&acc)[MY2][KZ], const f2_t (&yv
   }
 }
 
-#define ITKG_PUSH_CASE(N)                                          \
-  case N:                                                          \
-    if constexpr (N < KZ) push_phase<N, KZ, MY2, REF>(acc, yv, a, done); \
+#define ITKG_PUSH_CASE(N)                                                   \
+  case N:                                                                   \
+    if constexpr (N < KZ) push_phase<N, KZ, MY2, REF>(acc, yv, a, done);    \
     break;
 
-template <int RX, int RY, int RZ, bool REF>
+template <int RX, int RY, int RZ, bool REF, bool TMA>
 __global__ void __launch_bounds__(Cfg3<RX, RY, RZ>::NT, Cfg3<RX, RY, RZ>::MINB)
-    k_fused3d_f32(const Fused3DArgs a) {
+    k_fused3d_f32(const __grid_constant__ CUtensorMap tmap, const Fused3DArgs a) {
   using C = Cfg3<RX, RY, RZ>;
   constexpr int KX = C::KX, KY = C::KY, KZ = C::KZ, TX = C::TX, TY = C::TY, MY = C::MY,
-                MY2 = C::MY2, MX = C::MX, IW = C::IW, IH = C::IH, IWP = C::IWP, S = C::S,
-                NLD = C::NLD, NT = C::NT;
-  static_assert(KZ <= 17, "phase switch covers KZ <= 17");
-  extern __shared__ __align__(16) float smem[];
-  float* const stage0 = smem;
-  float* const xs = smem + S * C::STAGE;
+                MY2 = C::MY2, MX = C::MX, BW = C::BW, IH = C::IH, XA = C::XA, S = C::S,
+                NLD = C::NLD, NT = C::NT, WIN = C::WIN, WB = C::WB, OFF = C::OFF;
+  static_assert(KZ <= 25, "phase switch covers KZ <= 25");
+  extern __shared__ __align__(128) float smem[];
+  __shared__ __align__(8) uint64_t mbar[S];
+  // TMA destinations must be 128-byte aligned: align the dynamic region.
+  // (offset by an index so the compiler keeps shared-memory addressing)
+  float* const stage0 = smem + (((128u - (smem_u32(smem) & 127u)) & 127u) >> 2);
+  float* const xs = stage0 + S * C::STAGE;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nzr = a.req_hi[2] - a.req_lo[2] + 1;
   const int64_t u_begin = a.units * blockIdx.x / gridDim.x;
   const int64_t u_end = a.units * (blockIdx.x + 1) / gridDim.x;
   const uint32_t sbase = smem_u32(stage0);
+  const uint32_t bbase = smem_u32(mbar);
+  if (TMA) {
+    if (tid == 0) {
+      for (int i = 0; i < S; ++i) mbar_init(bbase + 8 * i, 1);
+      asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();
+  }
+  uint32_t phase_bits = 0;  // TMA: parity of each stage's next completion
 
   for (int64_t u = u_begin; u < u_end;) {
     const int64_t tile = u / nzr;
@@ -155,35 +223,47 @@ __global__ void __launch_bounds__(Cfg3<RX, RY, RZ>::NT, Cfg3<RX, RY, RZ>::MINB)
     const int z0 = a.req_lo[2] + zs, z1 = a.req_lo[2] + ze;  // outputs [z0, z1)
     const int tx0 = a.req_lo[0] + (int)(tile % a.ntx) * TX;
     const int ty0 = a.req_lo[1] + (int)(tile / a.ntx) * TY;
+    const int gx0 = tx0 - XA, gy0 = ty0 - RY;  // image coords of stage element (0, 0)
+    const bool edge = gx0 < a.lo[0] || gx0 + BW - 1 > a.hi[0] || gy0 < a.lo[1] || gy0 + IH - 1 > a.hi[1];
 
-    // Gather offsets of this thread's share of the staged tile (clamped x, y).
-    int32_t goff[NLD];
+    // cp.async path: gather offsets of this thread's share (clamped x, y).
+    int32_t goff[TMA ? 1 : NLD];
+    if constexpr (!TMA) {
 #pragma unroll
-    for (int i = 0; i < NLD; ++i) {
-      const int e = tid + i * NT;
-      const int row = e / IW, col = e % IW;
-      const int gx = clampi(tx0 - RX + col, a.lo[0], a.hi[0]);
-      const int gy = clampi(ty0 - RY + row, a.lo[1], a.hi[1]);
-      goff[i] = (int32_t)((gx - a.src_origin[0]) * a.src_pitch[0] +
-                          (gy - a.src_origin[1]) * a.src_pitch[1]);
+      for (int i = 0; i < NLD; ++i) {
+        const int e = tid + i * NT;
+        const int gx = clampi(gx0 + e % BW, a.lo[0], a.hi[0]);
+        const int gy = clampi(gy0 + e / BW, a.lo[1], a.hi[1]);
+        goff[i] = (int32_t)((gx - a.src_origin[0]) * a.src_pitch[0] +
+                            (gy - a.src_origin[1]) * a.src_pitch[1]);
+      }
     }
+    auto issue = [&](int s, int st) {
+      if constexpr (TMA) {
+        if (tid == 0) {
+          asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+          const uint32_t bar = bbase + 8 * st;
+          mbar_expect_tx(bar, (uint32_t)(IH * BW * 4));  // bytes of one box
+          tma_load_3d(sbase + (uint32_t)(st * C::STAGE * 4), &tmap, gx0 - a.src_origin[0],
+                      gy0 - a.src_origin[1], s - a.src_origin[2], bar);
+        }
+      } else {
+        const char* base = a.src + (int64_t)(s - a.src_origin[2]) * a.src_pitch[2];
+        const uint32_t sb = sbase + (uint32_t)(st * C::STAGE * 4);
+#pragma unroll
+        for (int i = 0; i < NLD; ++i) {
+          const int e = tid + i * NT;
+          if (i < NLD - 1 || e < C::STAGE) cp_async4(sb + (uint32_t)e * 4u, base + goff[i]);
+        }
+        cp_async_commit();
+      }
+    };
 
     const int jb = z0 - RZ, je = z1 - 1 + RZ;
     const int s_first = max(jb, a.lo[2]), s_last = min(je, a.hi[2]);
-#define ITKG_ISSUE(S_, ST_)                                                               \
-  do {                                                                                    \
-    const char* base_ = a.src + (int64_t)((S_) - a.src_origin[2]) * a.src_pitch[2];       \
-    const uint32_t sb_ = sbase + (uint32_t)((ST_) * C::STAGE * 4);                        \
-    _Pragma("unroll") for (int i = 0; i < NLD; ++i) {                                     \
-      const int e_ = tid + i * NT;                                                        \
-      if (i < NLD - 1 || e_ < IH * IW)                                                    \
-        cp_async4(sb_ + (uint32_t)(((e_ / IW) * IWP + e_ % IW) * 4), base_ + goff[i]);    \
-    }                                                                                     \
-  } while (0)
-#pragma unroll
     for (int q = 0; q < S; ++q) {
-      if (s_first + q <= s_last) ITKG_ISSUE(s_first + q, q);
-      cp_async_commit();
+      if (s_first + q <= s_last) issue(s_first + q, q);
+      else if (!TMA) cp_async_commit();
     }
 
     f2_t acc[MY2][KZ];
@@ -205,61 +285,169 @@ __global__ void __launch_bounds__(Cfg3<RX, RY, RZ>::NT, Cfg3<RX, RY, RZ>::MINB)
                         (int64_t)(row_y0 - a.dst_origin[1]) * a.dst_pitch[1];
     const int64_t opy = a.dst_pitch[1];
 
+    // Stage slice s (already issued into stage st) and run its x pass into
+    // xbuf.  Returns false if the bounded wait on the tile load gave up.
+    auto stage_and_xpass = [&](int st, float* xbuf) -> bool {
+      float* const tile = stage0 + st * C::STAGE;
+      if constexpr (TMA) {
+        const bool ok = mbar_wait(bbase + 8 * st, (phase_bits >> st) & 1u);
+        phase_bits ^= 1u << st;
+        if (!ok) return false;
+        if (edge) {
+          // Replicate the image's edge values into the halo: first the
+          // columns left of lo / right of hi (nl, nr of them), then whole
+          // rows above / below (nt, nb of them).  Sources are in-image
+          // columns and rows, which these loops never write.
+          __syncthreads();
+          const int nl = max(0, a.lo[0] - gx0), nr = max(0, gx0 + BW - 1 - a.hi[0]);
+          const int ncol = nl + nr;
+          for (int e = tid; e < ncol * IH; e += NT) {
+            const int r = e / ncol, i = e % ncol;
+            const int c = i < nl ? i : BW - 1 - (i - nl);
+            tile[r * BW + c] = tile[r * BW + clampi(gx0 + c, a.lo[0], a.hi[0]) - gx0];
+          }
+          __syncthreads();
+          const int nt = max(0, a.lo[1] - gy0), nb = max(0, gy0 + IH - 1 - a.hi[1]);
+          for (int e = tid; e < (nt + nb) * BW; e += NT) {
+            const int i = e / BW, c = e % BW;
+            const int r = i < nt ? i : IH - 1 - (i - nt);
+            tile[r * BW + c] = tile[(clampi(gy0 + r, a.lo[1], a.hi[1]) - gy0) * BW + c];
+          }
+          __syncthreads();
+        }
+      } else {
+        cp_async_wait<S - 1>();
+        __syncthreads();
+      }
+      constexpr int SEGS = TX / MX;
+      for (int t = tid; t < IH * SEGS; t += NT) {
+        const int row = t / SEGS, x0 = (t % SEGS) * MX;
+        float v[WIN];
+        const float4* src4 = reinterpret_cast<const float4*>(tile + row * BW + x0 + WB);
+#pragma unroll
+        for (int q = 0; q < WIN / 4; ++q) {
+          const float4 f = src4[q];
+          v[4 * q + 0] = f.x;
+          v[4 * q + 1] = f.y;
+          v[4 * q + 2] = f.z;
+          v[4 * q + 3] = f.w;
+        }
+        float o[MX];
+        if constexpr (REF) {
+#pragma unroll
+          for (int m = 0; m < MX; ++m) {
+            float ax = 0.0f;
+#pragma unroll
+            for (int k = 0; k < KX; ++k) ax = tap<true>(ax, v[m + k + OFF], a.wx[k]);
+            o[m] = ax;
+          }
+        } else {
+          // even/odd aligned pairs of the window: E[i] = (v[2i], v[2i+1]), O[i] = (v[2i+1], v[2i+2])
+          f2_t E[WIN / 2], O[WIN / 2 - 1];
+#pragma unroll
+          for (int i = 0; i < WIN / 2; ++i) E[i] = pack2(v[2 * i], v[2 * i + 1]);
+#pragma unroll
+          for (int i = 0; i < WIN / 2 - 1; ++i) O[i] = pack2(v[2 * i + 1], v[2 * i + 2]);
+#pragma unroll
+          for (int m = 0; m < MX / 2; ++m) {
+            f2_t ax = 0ull;
+#pragma unroll
+            for (int k = 0; k < KX; ++k) {
+              const int q = 2 * m + k + OFF;
+              ax = fma2((q & 1) ? O[(q - 1) / 2] : E[q / 2], a.wx2[k], ax);
+            }
+            unpack2(ax, o[2 * m], o[2 * m + 1]);
+          }
+        }
+        float4* dst4 = reinterpret_cast<float4*>(xbuf + row * TX + x0);
+#pragma unroll
+        for (int q = 0; q < MX / 4; ++q)
+          dst4[q] = make_float4(o[4 * q], o[4 * q + 1], o[4 * q + 2], o[4 * q + 3]);
+      }
+      return true;
+    };
+    // A tile load never completed: record it, let every other issued load
+    // land (bounded), and leave.
+#define ITKG_ON_TIMEOUT(CONS_NOW)                                                  \
+  do {                                                                             \
+    if (tid == 0) {                                                                \
+      atomicExch(&g_fused_fault, 1u);                                              \
+      if (TMA)                                                                     \
+        for (int q_ = 1; q_ < S; ++q_) {                                           \
+          const int sq_ = ((CONS_NOW) + q_) % S;                                   \
+          if (s_first + (CONS_NOW) + q_ <= s_last)                                 \
+            mbar_wait(bbase + 8 * sq_, (phase_bits >> sq_) & 1u);                  \
+        }                                                                          \
+    }                                                                              \
+  } while (0)
+
+    // Pipeline: the x pass of slice s + 1 runs in the same barrier interval
+    // as the y pass of slice s (double-buffered x-filtered tile).
+    if (s_first <= s_last) {
+      const bool ok = stage_and_xpass(0, xs);
+      if (__syncthreads_or(!ok)) {
+        ITKG_ON_TIMEOUT(0);
+        return;
+      }
+    }
     int prev_s = INT_MIN;
-    int cons = 0;
-    int p = 0;  // phase (j - jb) mod KZ
+    int cons = 0;  // slices consumed by the y pass so far
+    int p = 0;     // phase (j - jb) mod KZ
     for (int j = jb; j <= je; ++j) {
       const int s = clampi(j, a.lo[2], a.hi[2]);
       if (s != prev_s) {
         prev_s = s;
         const int st = cons % S;
-        cp_async_wait<S - 1>();
-        __syncthreads();
-        // ---- x pass: stage -> xs ----
-        const float* tile = stage0 + st * C::STAGE;
-        constexpr int SEGS = TX / MX;
-        for (int t = tid; t < IH * SEGS; t += NT) {
-          const int row = t / SEGS, x0 = (t % SEGS) * MX;
-          float v[C::WIN];
-          const float4* src4 = reinterpret_cast<const float4*>(tile + row * IWP + x0);
-#pragma unroll
-          for (int q = 0; q < C::WIN / 4; ++q) {
-            const float4 f = src4[q];
-            v[4 * q + 0] = f.x;
-            v[4 * q + 1] = f.y;
-            v[4 * q + 2] = f.z;
-            v[4 * q + 3] = f.w;
-          }
-          float o[MX];
-#pragma unroll
-          for (int m = 0; m < MX; ++m) {
-            float ax = 0.0f;
-#pragma unroll
-            for (int k = 0; k < KX; ++k) ax = tap<REF>(ax, v[m + k], a.wx[k]);
-            o[m] = ax;
-          }
-          *reinterpret_cast<float4*>(xs + row * TX + x0) = make_float4(o[0], o[1], o[2], o[3]);
+        if (cons > 0) {
+          // x pass of s (previous interval) visible; y pass of s - 1 done
+          __syncthreads();
         }
-        __syncthreads();
         {
           const int sn = s_first + cons + S;
-          if (sn <= s_last) ITKG_ISSUE(sn, st);
-          cp_async_commit();
+          if (sn <= s_last) issue(sn, st);
+          else if (!TMA) cp_async_commit();
+        }
+        const float* xcur = xs + (cons & 1) * IH * TX;
+        if (s + 1 <= s_last) {
+          const bool ok = stage_and_xpass((cons + 1) % S, xs + ((cons + 1) & 1) * IH * TX);
+          if (__syncthreads_or(!ok)) {
+            ITKG_ON_TIMEOUT(cons + 1);
+            return;
+          }
         }
         ++cons;
-        // ---- y pass: xs -> yv (registers, packed in row pairs) ----
+        // ---- y pass: xcur -> yv (registers, packed in row pairs) ----
         float w[MY + 2 * RY];
 #pragma unroll
-        for (int i = 0; i < MY + 2 * RY; ++i) w[i] = xs[(warp * MY + i) * TX + lane];
+        for (int i = 0; i < MY + 2 * RY; ++i) w[i] = xcur[(warp * MY + i) * TX + lane];
+        if constexpr (REF) {
 #pragma unroll
-        for (int m = 0; m < MY2; ++m) {
-          float y0 = 0.0f, y1 = 0.0f;
+          for (int m = 0; m < MY2; ++m) {
+            float y0 = 0.0f, y1 = 0.0f;
 #pragma unroll
-          for (int k = 0; k < KY; ++k) {
-            y0 = tap<REF>(y0, w[2 * m + k], a.wy[k]);
-            y1 = tap<REF>(y1, w[2 * m + 1 + k], a.wy[k]);
+            for (int k = 0; k < KY; ++k) {
+              y0 = tap<true>(y0, w[2 * m + k], a.wy[k]);
+              y1 = tap<true>(y1, w[2 * m + 1 + k], a.wy[k]);
+            }
+            yv[m] = pack2(y0, y1);
           }
-          yv[m] = pack2(y0, y1);
+        } else {
+          constexpr int NWIN = MY + 2 * RY;
+          f2_t E[NWIN / 2], O[NWIN / 2];
+#pragma unroll
+          for (int i = 0; i < NWIN / 2; ++i) E[i] = pack2(w[2 * i], w[2 * i + 1]);
+#pragma unroll
+          for (int i = 0; i + 1 < NWIN / 2; ++i) O[i] = pack2(w[2 * i + 1], w[2 * i + 2]);
+#pragma unroll
+          for (int m = 0; m < MY2; ++m) {
+            f2_t ay = 0ull;
+#pragma unroll
+            for (int k = 0; k < KY; ++k) {
+              const int q = 2 * m + k;
+              ay = fma2((q & 1) ? O[(q - 1) / 2] : E[q / 2], a.wy2[k], ay);
+            }
+            yv[m] = ay;
+          }
         }
       }
       // ---- z pass: push slice j into the ring, pop output z = j - RZ ----
@@ -269,7 +457,9 @@ __global__ void __launch_bounds__(Cfg3<RX, RY, RZ>::NT, Cfg3<RX, RY, RZ>::MINB)
         ITKG_PUSH_CASE(4) ITKG_PUSH_CASE(5) ITKG_PUSH_CASE(6) ITKG_PUSH_CASE(7)
         ITKG_PUSH_CASE(8) ITKG_PUSH_CASE(9) ITKG_PUSH_CASE(10) ITKG_PUSH_CASE(11)
         ITKG_PUSH_CASE(12) ITKG_PUSH_CASE(13) ITKG_PUSH_CASE(14) ITKG_PUSH_CASE(15)
-        ITKG_PUSH_CASE(16)
+        ITKG_PUSH_CASE(16) ITKG_PUSH_CASE(17) ITKG_PUSH_CASE(18) ITKG_PUSH_CASE(19)
+        ITKG_PUSH_CASE(20) ITKG_PUSH_CASE(21) ITKG_PUSH_CASE(22) ITKG_PUSH_CASE(23)
+        ITKG_PUSH_CASE(24)
         default: break;
       }
       p = p + 1 == KZ ? 0 : p + 1;
@@ -295,27 +485,31 @@ __global__ void __launch_bounds__(Cfg3<RX, RY, RZ>::NT, Cfg3<RX, RY, RZ>::MINB)
         }
       }
     }
-#undef ITKG_ISSUE
-    cp_async_wait<0>();
+    if constexpr (!TMA) cp_async_wait<0>();
     __syncthreads();
   }
+#undef ITKG_ON_TIMEOUT
 }
 
 // ---- dispatch table -----------------------------------------------------------
-using KernelFn = void (*)(const Fused3DArgs);
+using KernelFn = void (*)(const CUtensorMap, const Fused3DArgs);
 
 struct Entry {
   int rx, ry, rz;
-  KernelFn ref, fma;
+  KernelFn fn[2][2];  // [ref][tma]
   size_t smem;
-  int tx, ty, nt;
+  int tx, ty, nt, xa, bw, ih;
 };
 
 template <int RX, int RY, int RZ>
 Entry make_entry() {
   using C = Cfg3<RX, RY, RZ>;
-  return Entry{RX, RY, RZ, k_fused3d_f32<RX, RY, RZ, true>, k_fused3d_f32<RX, RY, RZ, false>,
-               C::SMEM, C::TX, C::TY, C::NT};
+  Entry e{RX, RY, RZ, {}, C::SMEM, C::TX, C::TY, C::NT, C::XA, C::BW, C::IH};
+  e.fn[0][0] = k_fused3d_f32<RX, RY, RZ, false, false>;
+  e.fn[0][1] = k_fused3d_f32<RX, RY, RZ, false, true>;
+  e.fn[1][0] = k_fused3d_f32<RX, RY, RZ, true, false>;
+  e.fn[1][1] = k_fused3d_f32<RX, RY, RZ, true, true>;
+  return e;
 }
 
 const Entry kTable[] = {
@@ -365,6 +559,29 @@ itkg_status resident_ctas(KernelFn fn, size_t smem, int nt, int* out) {
 
 bool fits_i32(int64_t v) { return v >= INT_MIN && v <= INT_MAX; }
 
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  });
+  return fn;
+}
+
+// TMA applies when the buffer base and pitches are 16-byte multiples and every
+// tile's first column (tx0 - XA, relative to the buffer) is 4-element aligned.
+bool tma_ok(const FusedGeom& g, const Entry& e) {
+  if (((uintptr_t)g.src & 15) || (g.src_pitch[1] & 15) || (g.src_pitch[2] & 15)) return false;
+  if (((g.req_index[0] - g.src_origin[0]) % 4 + 4) % 4 != 0) return false;
+  if (g.src_pitch[1] >= (1ll << 40) || g.src_pitch[2] >= (1ll << 40)) return false;
+  return encode_fn() != nullptr;
+}
+
 }  // namespace
 
 itkg_status launch_fused(const FusedGeom& g, const float* const w[kMaxDim], void* stream,
@@ -376,7 +593,8 @@ itkg_status launch_fused(const FusedGeom& g, const float* const w[kMaxDim], void
   // 32-bit in-slice offsets and coordinates
   for (int d = 0; d < 3; ++d)
     if (!fits_i32(g.lo[d]) || !fits_i32(g.hi[d]) || !fits_i32(g.src_origin[d]) ||
-        !fits_i32(g.dst_origin[d]) || !fits_i32(g.req_index[d] + g.req_size[d]))
+        !fits_i32(g.dst_origin[d]) || !fits_i32(g.req_index[d] + g.req_size[d]) ||
+        !fits_i32(g.req_index[d] - 64))
       return ITKG_ERROR_UNSUPPORTED;
   const int64_t span = (g.hi[0] - g.src_origin[0] + 1) * g.src_pitch[0] +
                        (g.hi[1] - g.src_origin[1] + 1) * g.src_pitch[1];
@@ -408,20 +626,62 @@ itkg_status launch_fused(const FusedGeom& g, const float* const w[kMaxDim], void
   a.nty = (int32_t)((g.req_size[1] + e->ty - 1) / e->ty);
   a.units = (int64_t)a.ntx * a.nty * g.req_size[2];
   a.out_dtype = g.out_dtype;
-  for (int k = 0; k < 2 * e->rx + 1; ++k) a.wx[k] = w[0][k];
-  for (int k = 0; k < 2 * e->ry + 1; ++k) a.wy[k] = w[1][k];
-  for (int k = 0; k < 2 * e->rz + 1; ++k) a.wz2[k] = splat2_host(w[2][k]);
-  KernelFn fn = g.rounding == ITKG_ROUND_REFERENCE ? e->ref : e->fma;
+  for (int k = 0; k < 2 * e->rx + 1; ++k) a.wx[k] = w[0][k], a.wx2[k] = splat2_host(w[0][k]);
+  for (int k = 0; k < 2 * e->ry + 1; ++k) a.wy[k] = w[1][k], a.wy2[k] = splat2_host(w[1][k]);
+  for (int k = 0; k < 2 * e->rz + 1; ++k) a.wz[k] = w[2][k], a.wz2[k] = splat2_host(w[2][k]);
+
+  CUtensorMap map;
+  std::memset(&map, 0, sizeof map);
+  const bool tma = tma_ok(g, *e);
+  if (tma) {
+    const cuuint64_t dims[3] = {(cuuint64_t)g.src_size[0], (cuuint64_t)g.src_size[1],
+                                (cuuint64_t)g.src_size[2]};
+    const cuuint64_t strides[2] = {(cuuint64_t)g.src_pitch[1], (cuuint64_t)g.src_pitch[2]};
+    const cuuint32_t box[3] = {(cuuint32_t)e->bw, (cuuint32_t)e->ih, 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = encode_fn()(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<void*>(g.src), dims,
+                             strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return set_error(ITKG_ERROR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+  }
+  const bool ref = g.rounding == ITKG_ROUND_REFERENCE;
+  KernelFn fn = e->fn[ref ? 1 : 0][tma ? 1 : 0];
   int resident = 0;
   {
     const itkg_status st = resident_ctas(fn, e->smem, e->nt, &resident);
     if (st != ITKG_SUCCESS) return st;
   }
   const int64_t grid = std::min<int64_t>(a.units, resident);
-  fn<<<(unsigned)grid, e->nt, e->smem, static_cast<cudaStream_t>(stream)>>>(a);
-  note_launch(g.rounding == ITKG_ROUND_REFERENCE ? "fused3d_f32_ref" : "fused3d_f32_fma");
+  fn<<<(unsigned)grid, e->nt, e->smem, static_cast<cudaStream_t>(stream)>>>(map, a);
+  note_launch(ref ? (tma ? "fused3d_f32_ref_tma" : "fused3d_f32_ref")
+                  : (tma ? "fused3d_f32_fma_tma" : "fused3d_f32_fma"));
   cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) return set_error(ITKG_ERROR_CUDA, "fused3d launch: %s", cudaGetErrorString(err));
+  return ITKG_SUCCESS;
+}
+
+itkg_status launch_fused_multi(const std::vector<FusedGeom>& geoms,
+                               const std::vector<std::vector<std::vector<float>>>& weights,
+                               void* stream, std::vector<std::string>* plan) {
+  for (size_t i = 0; i < geoms.size(); ++i) {
+    const float* w[kMaxDim] = {nullptr, nullptr, nullptr};
+    for (int d = 0; d < geoms[i].dim; ++d) w[d] = weights[i][d].data();
+    const itkg_status st = launch_fused(geoms[i], w, stream, false);
+    if (st != ITKG_SUCCESS) return st;
+    if (plan) plan->push_back(std::string("fused item ") + std::to_string(i) + ": " + itkg_last_kernel());
+  }
+  return ITKG_SUCCESS;
+}
+
+itkg_status fused_fault_flag(unsigned int* flag, bool clear) {
+  cudaError_t e = cudaMemcpyFromSymbol(flag, g_fused_fault, sizeof(unsigned int));
+  if (e != cudaSuccess) return set_error(ITKG_ERROR_CUDA, "fault flag: %s", cudaGetErrorString(e));
+  if (clear && *flag) {
+    const unsigned int zero = 0;
+    e = cudaMemcpyToSymbol(g_fused_fault, &zero, sizeof zero);
+    if (e != cudaSuccess) return set_error(ITKG_ERROR_CUDA, "fault flag: %s", cudaGetErrorString(e));
+  }
   return ITKG_SUCCESS;
 }
 

@@ -6,6 +6,7 @@
 #include <cstdint>
 #include <string>
 #include <vector>
+#include <string>
 
 #include "itkg.h"
 
@@ -100,6 +101,26 @@ struct FusedGeom {
 // fused kernel covers the geometry; the caller then uses the per-axis path.
 itkg_status launch_fused(const FusedGeom& g, const float* const w[kMaxDim], void* stream,
                          bool dry_run);
+
+// abi.cpp: validates one request and fills its fused geometry and f32 weights;
+// ITKG_ERROR_UNSUPPORTED when no fused kernel covers it.
+itkg_status fused_geom_for(const itkg_image& in, const itkg_region& largest,
+                           const itkg_region& requested, const itkg_gaussian_params& prm,
+                           const itkg_image& out, FusedGeom* g,
+                           std::vector<std::vector<float>>* weights);
+
+// fused.cu: launches many fused requests; requests sharing a kernel run as one
+// persistent multi-item launch.  Appends one line per launch to `plan`.
+itkg_status launch_fused_multi(const std::vector<FusedGeom>& geoms,
+                               const std::vector<std::vector<std::vector<float>>>& weights,
+                               void* stream, std::vector<std::string>* plan);
+
+// Bumps the launch counter by n (graph replays).
+void note_launches(uint64_t n, const char* name);
+
+// Reads (and optionally clears) the fused kernels' device fault word, which a
+// kernel sets when a bounded wait on a tile load gives up.
+itkg_status fused_fault_flag(unsigned int* flag, bool clear);
 
 // ---- VJP (vjp.cu): whole-image per-axis passes on f32 buffers ---------------
 constexpr int kMaxVjpTaps = 385;  // radius <= 192

@@ -427,6 +427,64 @@ def vjp(x: DeviceImage, ybar: DeviceImage, sigma: float, xbar: DeviceImage | Non
     return xbar, (sb.value if want_sigma else None)
 
 
+class Batch:
+    """itkg_batch: many forward / VJP requests planned once, replayed as a CUDA graph."""
+
+    BATCH_NO_AUTOTUNE = 1
+
+    def __init__(self):
+        h = ctypes.c_void_p()
+        check(lib().itkg_batch_create(ctypes.byref(h)))
+        self.h = h
+        self._keep = []  # keep device buffers referenced while the batch lives
+
+    def add(self, src: DeviceImage, sigma: float, out: DeviceImage | None = None,
+            requested: Region | None = None, rounding: int = ROUND_FMA,
+            algorithm: int = ALGO_AUTO, largest: Region | None = None):
+        req = requested or src.region
+        if out is None:
+            out = DeviceImage(req, F32, src.components, src.spacing, src.origin)
+        p = itkg_gaussian_params()
+        p.sigma = float(sigma)
+        p.rounding = rounding
+        p.algorithm = algorithm
+        lg = (largest or src.region).to_c()
+        rq = req.to_c()
+        check(lib().itkg_batch_add(self.h, ctypes.byref(src.c), ctypes.byref(lg), ctypes.byref(rq),
+                                   ctypes.byref(p), ctypes.byref(out.c)))
+        self._keep += [src, out]
+        return out
+
+    def add_vjp(self, x: DeviceImage, ybar: DeviceImage, sigma: float,
+                xbar: DeviceImage | None = None, sigma_bar_dev: int | None = None, flags: int = 0):
+        if xbar is None:
+            xbar = DeviceImage(x.region, F32, 1, x.spacing, x.origin)
+        p = itkg_gaussian_params()
+        p.sigma = float(sigma)
+        p.rounding = ROUND_FMA
+        check(lib().itkg_batch_add_vjp(self.h, ctypes.byref(x.c), ctypes.byref(ybar.c),
+                                       ctypes.byref(p), ctypes.byref(xbar.c),
+                                       ctypes.c_void_p(sigma_bar_dev) if sigma_bar_dev else None,
+                                       int(flags)))
+        self._keep += [x, ybar, xbar]
+        return xbar
+
+    def plan(self, autotune: bool = True, stream: Stream = _DEFAULT_STREAM):
+        check(lib().itkg_batch_plan(self.h, 0 if autotune else self.BATCH_NO_AUTOTUNE, stream.ptr))
+
+    def run(self, stream: Stream = _DEFAULT_STREAM):
+        check(lib().itkg_batch_run(self.h, stream.ptr))
+
+    def describe(self) -> str:
+        return lib().itkg_batch_describe(self.h).decode()
+
+    def __del__(self):
+        try:
+            lib().itkg_batch_destroy(self.h)
+        except Exception:
+            pass
+
+
 def last_kernel() -> str:
     return lib().itkg_last_kernel().decode()
 

@@ -86,12 +86,20 @@ SIGNATURES = {
     "itkg_memcpy": (st, [P, P, ctypes.c_size_t, ctypes.c_int32, P]),
     "itkg_memset_device": (st, [P, ctypes.c_int32, ctypes.c_size_t, P]),
     "itkg_stream_synchronize": (st, [P]),
+    "itkg_device_fault": (st, [ctypes.c_int32, ctypes.POINTER(ctypes.c_uint32)]),
     "itkg_image_alloc_device": (st, [I, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, R, P, P]),
     "itkg_image_free": (st, [I]),
     "itkg_image_copy_from": (st, [I, I, P]),
     "itkg_gaussian_generate_region": (st, [I, R, R, G, I, P]),
     "itkg_stream_full": (st, [I, R, G, ctypes.c_uint64, I, P]),
     "itkg_gaussian_vjp": (st, [I, I, G, I, ctypes.POINTER(ctypes.c_double), ctypes.c_int32, P]),
+    "itkg_batch_create": (st, [ctypes.POINTER(ctypes.c_void_p)]),
+    "itkg_batch_destroy": (st, [P]),
+    "itkg_batch_add": (st, [P, I, R, R, G, I]),
+    "itkg_batch_add_vjp": (st, [P, I, I, G, I, P, ctypes.c_int32]),
+    "itkg_batch_plan": (st, [P, ctypes.c_int32, P]),
+    "itkg_batch_run": (st, [P, P]),
+    "itkg_batch_describe": (ctypes.c_char_p, [P]),
 }
 
 _lib = None

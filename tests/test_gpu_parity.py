@@ -277,3 +277,52 @@ def test_fused3d_subregions_and_tight_buffers(gpu):
             ctypes.byref(out.c), None))
         assert gpu.last_kernel().startswith("fused3d")
         assert bits_equal(out.download(), want), (ri, rs)
+
+
+def _dense_device(gpu, arr):
+    """Device image with the dense (unpadded) layout of `arr` -- rows of
+    arbitrary byte length, so the fused kernel must use its cp.async gather."""
+    import ctypes
+    from itkg import _abi
+    L = _abi.lib()
+    p = ctypes.c_void_p()
+    _abi.check(L.itkg_device_alloc(arr.nbytes, ctypes.byref(p)))
+    _abi.check(L.itkg_memcpy(p, arr.ctypes.data, arr.nbytes, 0, None))
+    _abi.check(L.itkg_stream_synchronize(None))
+    im = gpu.Image(arr).to_c()
+    im.location = gpu._abi.DEVICE
+    im.data = p.value
+    return im, p
+
+
+@pytest.mark.parametrize("rounding", ["reference", "fma"])
+def test_fused3d_tma_and_gather_paths_agree(gpu, rounding):
+    import ctypes
+    from itkg import _abi
+    L = _abi.lib()
+    rng = np.random.default_rng(31)
+    arr = rng.random((21, 27, 31), dtype=np.float32)  # 31 floats per row: not 16-byte pitched
+    want = oracle.gaussian_f32(arr, 2.0)
+    rnd = gpu.ROUND_REFERENCE if rounding == "reference" else gpu.ROUND_FMA
+    got_tma = run_device(gpu, arr, 2.0, algo="fused", rounding=rnd)
+    assert "tma" in gpu.last_kernel(), gpu.last_kernel()
+    src, p = _dense_device(gpu, arr)
+    out = gpu.DeviceImage(gpu.Image(arr).region)
+    prm = _abi.itkg_gaussian_params()
+    prm.sigma = 2.0
+    prm.rounding = rnd
+    prm.algorithm = gpu.ALGO_FUSED
+    lg = gpu.Image(arr).region.to_c()
+    _abi.check(L.itkg_gaussian_generate_region(ctypes.byref(src), ctypes.byref(lg), ctypes.byref(lg),
+                                               ctypes.byref(prm), ctypes.byref(out.c), None))
+    kern = gpu.last_kernel()
+    got_gather = out.download()
+    L.itkg_device_free(p)
+    assert kern.startswith("fused3d") and "tma" not in kern, kern
+    if rounding == "reference":
+        assert bits_equal(got_tma, want) and bits_equal(got_gather, want)
+    else:
+        assert normwise(got_tma, want) <= 1e-5 and normwise(got_gather, want) <= 1e-5
+    flag = ctypes.c_uint32(1)
+    _abi.check(L.itkg_device_fault(1, ctypes.byref(flag)))
+    assert flag.value == 0
