@@ -256,6 +256,29 @@ itkg_status itkg_batch_run(itkg_batch *batch, void *stream);
 /* One line per planned launch (kernel chosen per item); valid until the next call. */
 const char *itkg_batch_describe(itkg_batch *batch);
 
+/* No counterpart in the reference.  The same result as
+ * itkg_gaussian_generate_region with algorithm ITKG_ALGO_PER_AXIS, for callers
+ * that must not allocate device memory during the call -- for example an
+ * application that has handed all device memory to its own pool or caching
+ * allocator, or a latency-critical loop that cannot absorb an allocation.
+ * This entry point calls no cudaMalloc, cudaFree or other allocating routine:
+ * the per-axis intermediates live in one fixed 32 MiB device array inside the
+ * library (held on every GPU that loads the library until the process exits).
+ *   - input and output must be device buffers (ITKG_DEVICE);
+ *   - a request whose intermediates exceed 32 MiB (two of them for D = 3, one
+ *     for D = 2; each is the requested region padded by the radius on the axes
+ *     not yet filtered, 4 bytes per component) fails with
+ *     ITKG_ERROR_INVALID_ARGUMENT;
+ *   - all calls share the array; calls whose GPU work overlaps (e.g. on two
+ *     streams) race on it and must be serialised by the caller;
+ *   - the first call on each device looks up the array's device address, so
+ *     make that first call before any stream capture. */
+itkg_status itkg_gaussian_generate_region_noalloc(const itkg_image *input,
+                                                  const itkg_region *largest,
+                                                  const itkg_region *requested,
+                                                  const itkg_gaussian_params *params,
+                                                  itkg_image *output, void *stream);
+
 /* stream_full(&GaussianFilter{input, sigma}, num_pieces) (source.rs:81-98):
  * output (region == largest) is filled piece by piece along axis D-1.  With a
  * host-resident input and output, only one halo-padded input slab and one

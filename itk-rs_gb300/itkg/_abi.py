@@ -92,6 +92,7 @@ SIGNATURES = {
     "itkg_image_copy_from": (st, [I, I, P]),
     "itkg_gaussian_generate_region": (st, [I, R, R, G, I, P]),
     "itkg_stream_full": (st, [I, R, G, ctypes.c_uint64, I, P]),
+    "itkg_gaussian_generate_region_noalloc": (st, [I, R, R, G, I, P]),
     "itkg_gaussian_vjp": (st, [I, I, G, I, ctypes.POINTER(ctypes.c_double), ctypes.c_int32, P]),
     "itkg_batch_create": (st, [ctypes.POINTER(ctypes.c_void_p)]),
     "itkg_batch_destroy": (st, [P]),
