@@ -383,6 +383,11 @@ static itkg_status generate_region(const itkg_image* input, const itkg_region* l
   if (st == ITKG_SUCCESS) {
     cudaError_t e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return cuda_status(e, "cudaStreamSynchronize");
+    // The call synchronised anyway: surface a kernel that gave up on a
+    // bounded wait instead of returning an incomplete result as success.
+    unsigned int fault = 0;
+    ITKG_TRY(fused_fault_flag(&fault, true));
+    if (fault) return set_error(ITKG_ERROR_TIMEOUT, "a fused kernel gave up waiting for a tile load");
   }
   return st;
 }
