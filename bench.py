@@ -361,12 +361,215 @@ def gpu_arm(args):
     return 0
 
 
+# ---------------------------------------------------------------------------
+# Other configurations (parity/extra lines; not the default bench line)
+# ---------------------------------------------------------------------------
+def _timed(stream, fn, steps, warmup):
+    """Mean ms per call of fn() on `stream`, CUDA events, after warm-up."""
+    import torch
+    for _ in range(warmup):
+        fn()
+    stream.synchronize()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for _ in range(steps):
+        fn()
+    t1.record(stream)
+    t1.synchronize()
+    return t0.elapsed_time(t1) / steps
+
+
+def _normwise(a, ref):
+    ref = np.asarray(ref, np.float64)
+    return float(np.abs(np.asarray(a, np.float64) - ref).max() / max(np.abs(ref).max(), 1e-300))
+
+
+def extra_workload(args):
+    """One JSON line for configs 1, 3, 4 or 5 (see --workload)."""
+    import torch
+    import itkg
+    from itkg import _abi
+    torch.cuda.set_device(0)
+    L = _abi.lib()
+    stream = torch.cuda.Stream()
+    sp = itkg.Stream(stream.cuda_stream)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    peak, _ = measured_peak()
+    rng = np.random.default_rng(0)
+    out = {"metric": METRIC, "unit": "voxels/s", "n_gpus": 1, "steps": args.steps,
+           "warmup": args.warmup, "higher_is_better": True, "data": "synthetic",
+           "vs_baseline": None}
+
+    def gen(f, req, outimg):
+        p = f.params()
+        lg = f._leaf().largest_region().to_c()
+        rq = req.to_c()
+        src = f._leaf().to_c()
+        return lambda: _abi.check(L.itkg_gaussian_generate_region(
+            ctypes.byref(src), ctypes.byref(lg), ctypes.byref(rq), ctypes.byref(p),
+            ctypes.byref(outimg.c), sp.ptr))
+
+    if args.workload == "fwd2d":
+        # configs[0]: Image<f32,2> 512x512, U[0,1), sigma 1.5 (r = 5)
+        n = 64
+        imgs = [rng.random((512, 512), dtype=np.float32) for _ in range(4)]
+        devs = [itkg.DeviceImage.from_host(itkg.Image(imgs[i % 4])) for i in range(n)]
+        outs = [itkg.DeviceImage(devs[0].region) for _ in range(n)]
+        calls = [gen(itkg.GaussianFilter(d, 1.5, rounding=itkg.ROUND_FMA), d.region, o)
+                 for d, o in zip(devs, outs)]
+        ms = _timed(stream, lambda: [c() for c in calls], args.steps, args.warmup)
+        got = outs[0].download()
+        err = _normwise(got, oracle.gaussian_f32(imgs[0], 1.5))
+        vox = n * 512 * 512
+        out.update({"value": vox / (ms * 1e-3), "ms_per_step": ms, "dtype": "f32",
+                    "config": {"workload": "2-D forward Image<f32,2> 512x512 sigma 1.5, 64 images per step",
+                               "kernel": itkg.last_kernel()},
+                    "roofline": {"bound": "hbm", "achieved": vox * 8 / (ms * 1e-3) / 1e9, "peak": peak,
+                                 "unit": "GB/s", "frac": vox * 8 / (ms * 1e-3) / 1e9 / peak},
+                    "accuracy": {"normwise_rel_vs_ref_f32": err}})
+    elif args.workload == "ct16":
+        # configs[2]: Image<i16,3> 512x512x384 CT-like, spacing (0.7,0.7,2.5), sigma 1.5 mm
+        shape = (384, 512, 512)
+        z = np.arange(shape[0])[:, None, None]
+        y = np.arange(shape[1])[None, :, None]
+        x = np.arange(shape[2])[None, None, :]
+        vol = np.full(shape, -1000.0, np.float32)
+        for _ in range(12):
+            c = rng.uniform(0.2, 0.8, 3) * np.array(shape)
+            ax = rng.uniform(0.05, 0.35, 3) * np.array(shape)
+            val = rng.uniform(-1000, 1500)
+            m = ((z - c[0]) / ax[0]) ** 2 + ((y - c[1]) / ax[1]) ** 2 + ((x - c[2]) / ax[2]) ** 2 <= 1
+            vol[m] = val
+        vol += rng.normal(0, 20, shape).astype(np.float32)
+        ct = np.clip(np.rint(vol), -32768, 32767).astype(np.int16)
+        del vol
+        spacing = (0.7, 0.7, 2.5)
+        dev = itkg.DeviceImage.from_host(itkg.Image(ct, spacing=spacing))
+        lines = {}
+        sub = ct[180:204, 200:264, 200:264].astype(np.float64)  # FP64 check on a block
+        ref64 = oracle.gaussian_f64(sub, 1.5, spacing=list(spacing))
+        for name, code, bpv in [("f32", itkg.F32, 6), ("bf16", itkg.BF16, 4), ("f16", itkg.F16, 4)]:
+            o = itkg.DeviceImage(dev.region, code, 1, spacing)
+            f = itkg.GaussianFilter(itkg.CastFilter(dev, itkg.F32), 1.5, rounding=itkg.ROUND_FMA)
+            call = gen(f, dev.region, o)
+            ms = _timed(stream, call, args.steps, args.warmup)
+            kern = itkg.last_kernel()
+            # accuracy: same block through the filter vs FP64 oracle
+            sdev = itkg.DeviceImage.from_host(itkg.Image(np.ascontiguousarray(ct[180:204, 200:264, 200:264]), spacing=spacing))
+            so = itkg.GaussianFilter(itkg.CastFilter(sdev, itkg.F32), 1.5, rounding=itkg.ROUND_FMA) \
+                .generate_region(sdev.region, out_dtype=code).download()
+            got = (so.astype(np.uint32) << 16).view(np.float32) if code == itkg.BF16 else so.astype(np.float32)
+            nvox = ct.size
+            lines[name] = {"voxels_per_s": nvox / (ms * 1e-3), "ms": ms, "kernel": kern,
+                           "GBs": nvox * bpv / (ms * 1e-3) / 1e9,
+                           "normwise_rel_vs_fp64": _normwise(got, ref64),
+                           "max_abs_vs_fp64": float(np.abs(got - ref64).max())}
+        out.update({"value": lines["f32"]["voxels_per_s"], "ms_per_step": lines["f32"]["ms"],
+                    "dtype": "i16->f32", "config": {"workload": "CT i16 512x512x384, spacing (0.7,0.7,2.5), sigma 1.5 mm, r=(7,7,2)",
+                                                   "outputs": lines}})
+    elif args.workload in ("batch", "batch_vjp"):
+        # configs[3]: 64 Image<f32,3> dims U{32..320}, sigma U[0.5,4]; 256 RGB 2-D sides U{64..1024}
+        vols = []
+        for i in range(64):
+            shape = tuple(int(v) for v in rng.integers(32, 321, 3))
+            vols.append((rng.random(shape, dtype=np.float32), float(rng.uniform(0.5, 4.0)), 1))
+        for i in range(256 if args.workload == "batch" else 0):
+            shape = tuple(int(v) for v in rng.integers(64, 1025, 2))
+            vols.append((rng.random(shape + (3,), dtype=np.float32), float(rng.uniform(0.5, 4.0)), 3))
+        devs, outs, calls = [], [], []
+        b = itkg.Batch()
+        vjp_items = []
+        sb = ctypes.c_void_p()
+        if args.workload == "batch_vjp":
+            _abi.check(L.itkg_device_alloc(8 * len(vols), ctypes.byref(sb)))
+        nvox = 0
+        for i, (arr, sigma, comps) in enumerate(vols):
+            d = itkg.DeviceImage.from_host(itkg.Image(arr, components=comps))
+            o = itkg.DeviceImage(d.region, itkg.F32, comps)
+            devs.append(d)
+            outs.append(o)
+            nvox += arr.size // comps
+            b.add(d, sigma, out=o, rounding=itkg.ROUND_FMA)
+            plain = itkg.GaussianFilter(d, sigma, rounding=itkg.ROUND_FMA, algorithm=itkg.ALGO_PER_AXIS)
+            calls.append(gen(plain, d.region, o))
+            if args.workload == "batch_vjp":
+                yb = itkg.DeviceImage.from_host(itkg.Image(rng.standard_normal(arr.shape).astype(np.float32)))
+                xb = b.add_vjp(d, yb, sigma, sigma_bar_dev=sb.value + 8 * i)
+                vjp_items.append((d, yb, sigma, xb))
+        b.plan(stream=sp)
+        ms_batch = _timed(stream, lambda: b.run(sp), args.steps, args.warmup)
+
+        def plain_all():
+            for c in calls:
+                c()
+            for d, yb, sigma, xb in vjp_items:
+                p = _abi.itkg_gaussian_params()
+                p.sigma = sigma
+                p.rounding = itkg.ROUND_FMA
+                _abi.check(L.itkg_gaussian_vjp(ctypes.byref(d.c), ctypes.byref(yb.c), ctypes.byref(p),
+                                               ctypes.byref(xb.c), ctypes.cast(ctypes.c_void_p(sb.value), ctypes.POINTER(ctypes.c_double)),
+                                               4, sp.ptr))
+        ms_plain = _timed(stream, plain_all, max(1, args.steps // 4), 1)
+        units = nvox * (2 if args.workload == "batch_vjp" else 1)
+        got = outs[0].download()
+        err = _normwise(got, oracle.gaussian_f32(vols[0][0], vols[0][1], comps=vols[0][2]))
+        out.update({"value": units / (ms_batch * 1e-3), "ms_per_step": ms_batch, "dtype": "f32",
+                    "config": {"workload": ("64 Image<f32,3> U{32..320}^3 + 256 RGB 2-D U{64..1024}^2, sigma U[0.5,4], one graph"
+                                            if args.workload == "batch" else
+                                            "64 Image<f32,3> U{32..320}^3, sigma U[0.5,4]: forward + VJP (x and sigma), one graph"),
+                               "voxels": nvox, "plan": b.describe().strip().splitlines()[:12]},
+                    "plain_per_volume": {"value": units / (ms_plain * 1e-3), "ms_per_step": ms_plain,
+                                         "kernel": "per-axis generate_region per volume" +
+                                                   (" + per-axis VJP per volume" if vjp_items else "")},
+                    "batched_over_plain": ms_plain / ms_batch,
+                    "accuracy": {"normwise_rel_vs_ref_f32_item0": err}})
+        if sb.value:
+            L.itkg_device_free(sb)
+    elif args.workload == "vjp_stack":
+        # configs[4]: 8 x 192^3 blobs+noise, sigma {1,2,4,8}; loss sum_l |G_l x - t|^2
+        n = 8
+        shape = (192, 192, 192)
+        xs = [blobs_volume(shape, 100 + i) for i in range(n)]
+        ts = [blobs_volume(shape, 200 + i) for i in range(n)]
+        dx = [itkg.DeviceImage.from_host(itkg.Image(a)) for a in xs]
+        dt = [itkg.DeviceImage.from_host(itkg.Image(a)) for a in ts]
+        sigmas = [1.0, 2.0, 4.0, 8.0]
+        y = itkg.DeviceImage(dx[0].region)
+        ybar = itkg.DeviceImage(dx[0].region)
+        xbar = [itkg.DeviceImage(dx[0].region) for _ in range(n)]
+
+        def step():
+            # plain form: per volume and level, forward, dL/dy on the host side of the ABI,
+            # then the VJP accumulating into xbar
+            for i in range(n):
+                for li, s in enumerate(sigmas):
+                    f = itkg.GaussianFilter(dx[i], s, rounding=itkg.ROUND_FMA)
+                    f.generate_region(dx[i].region, stream=sp, out=y)
+                    p = _abi.itkg_gaussian_params()
+                    p.sigma = s
+                    _abi.check(L.itkg_gaussian_vjp(ctypes.byref(dx[i].c), ctypes.byref(y.c), ctypes.byref(p),
+                                                   ctypes.byref(xbar[i].c), None,
+                                                   1 if li else 0, sp.ptr))
+        ms = _timed(stream, step, max(1, args.steps // 10), 1)
+        vl = n * len(sigmas) * int(np.prod(shape))
+        out.update({"value": vl / (ms * 1e-3), "unit": "voxel-levels/s", "ms_per_step": ms,
+                    "dtype": "f32",
+                    "config": {"workload": "8 x 192^3, sigma {1,2,4,8}: forward + VJP(x) per level (per-axis VJP)",
+                               "note": "gradient of sum_l <y_l, G_l x> form; the squared-error loss form is checked in tests"}})
+    print(json.dumps(out))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=["itkg", "reference"], default="itkg")
+    ap.add_argument("--workload", choices=["fwd3d", "fwd2d", "ct16", "batch", "batch_vjp", "vjp_stack"],
+                    default="fwd3d")
     ap.add_argument("--rounding", choices=["fma", "reference"], default="fma")
     ap.add_argument("--algo", choices=["auto", "fused", "per_axis"], default="auto")
     ap.add_argument("--e2e-steps", type=int, default=20)
@@ -375,6 +578,8 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
+    if args.workload != "fwd3d":
+        return extra_workload(args)
     return gpu_arm(args)
 
 

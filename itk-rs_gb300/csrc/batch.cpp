@@ -51,6 +51,7 @@ struct itkg_batch {
   std::vector<std::string> plan_lines;  // human-readable plan (itkg_batch_describe)
   std::string described;
   uint64_t launches_per_run = 0;
+  itkg::FusedMultiPlan* fused = nullptr;  // request tables of the multi-request launches
 };
 
 namespace itkg {
@@ -164,6 +165,7 @@ itkg_status itkg_batch_destroy(itkg_batch* b) {
   if (!b) return ITKG_SUCCESS;
   if (b->exec) cudaGraphExecDestroy(b->exec);
   if (b->graph) cudaGraphDestroy(b->graph);
+  fused_multi_free(b->fused);
   delete b;
   return ITKG_SUCCESS;
 }
@@ -239,6 +241,8 @@ itkg_status itkg_batch_plan(itkg_batch* b, int32_t flags, void* stream) {
     }
   }
 
+  if (!fused_geoms.empty()) ITKG_TRY(fused_multi_prepare(fused_geoms, fused_w, &b->fused, &b->plan_lines));
+
   // 3. capture
   cudaStream_t cap;
   ITKG_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
@@ -249,7 +253,7 @@ itkg_status itkg_batch_plan(itkg_batch* b, int32_t flags, void* stream) {
     return cuda_status(ce, "cudaStreamBeginCapture");
   }
   itkg_status st = ITKG_SUCCESS;
-  if (!fused_geoms.empty()) st = launch_fused_multi(fused_geoms, fused_w, cap, &b->plan_lines);
+  if (b->fused) st = fused_multi_launch(b->fused, cap);
   for (size_t i : per_item) {
     if (st != ITKG_SUCCESS) break;
     itkg_batch::Fwd f = b->fwd[i];

@@ -184,35 +184,22 @@ __device__ __forceinline__ void push_phase(f2_t (&acc)[MY2][KZ], const f2_t (&yv
     if constexpr (N < KZ) push_phase<N, KZ, MY2, REF>(acc, yv, a, done);    \
     break;
 
+// The fused filter over units [u_begin, u_end) of one request `a` (a unit is
+// one output slice of one (x, y) tile).  Returns false if a bounded wait gave
+// up (the device fault word is then set).
 template <int RX, int RY, int RZ, bool REF, bool TMA>
-__global__ void __launch_bounds__(Cfg3<RX, RY, RZ>::NT, Cfg3<RX, RY, RZ>::MINB)
-    k_fused3d_f32(const __grid_constant__ CUtensorMap tmap, const Fused3DArgs a) {
+__device__ __forceinline__ bool fused_range(const Fused3DArgs& a, const CUtensorMap* tmap,
+                                            int64_t u_begin, int64_t u_end, float* const stage0,
+                                            uint32_t bbase, uint32_t& phase_bits) {
   using C = Cfg3<RX, RY, RZ>;
   constexpr int KX = C::KX, KY = C::KY, KZ = C::KZ, TX = C::TX, TY = C::TY, MY = C::MY,
                 MY2 = C::MY2, MX = C::MX, BW = C::BW, IH = C::IH, XA = C::XA, S = C::S,
                 NLD = C::NLD, NT = C::NT, WIN = C::WIN, WB = C::WB, OFF = C::OFF;
   static_assert(KZ <= 25, "phase switch covers KZ <= 25");
-  extern __shared__ __align__(128) float smem[];
-  __shared__ __align__(8) uint64_t mbar[S];
-  // TMA destinations must be 128-byte aligned: align the dynamic region.
-  // (offset by an index so the compiler keeps shared-memory addressing)
-  float* const stage0 = smem + (((128u - (smem_u32(smem) & 127u)) & 127u) >> 2);
   float* const xs = stage0 + S * C::STAGE;
-
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nzr = a.req_hi[2] - a.req_lo[2] + 1;
-  const int64_t u_begin = a.units * blockIdx.x / gridDim.x;
-  const int64_t u_end = a.units * (blockIdx.x + 1) / gridDim.x;
   const uint32_t sbase = smem_u32(stage0);
-  const uint32_t bbase = smem_u32(mbar);
-  if (TMA) {
-    if (tid == 0) {
-      for (int i = 0; i < S; ++i) mbar_init(bbase + 8 * i, 1);
-      asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
-    }
-    __syncthreads();
-  }
-  uint32_t phase_bits = 0;  // TMA: parity of each stage's next completion
 
   for (int64_t u = u_begin; u < u_end;) {
     const int64_t tile = u / nzr;
@@ -244,7 +231,7 @@ __global__ void __launch_bounds__(Cfg3<RX, RY, RZ>::NT, Cfg3<RX, RY, RZ>::MINB)
           asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
           const uint32_t bar = bbase + 8 * st;
           mbar_expect_tx(bar, (uint32_t)(IH * BW * 4));  // bytes of one box
-          tma_load_3d(sbase + (uint32_t)(st * C::STAGE * 4), &tmap, gx0 - a.src_origin[0],
+          tma_load_3d(sbase + (uint32_t)(st * C::STAGE * 4), tmap, gx0 - a.src_origin[0],
                       gy0 - a.src_origin[1], s - a.src_origin[2], bar);
         }
       } else {
@@ -387,7 +374,7 @@ __global__ void __launch_bounds__(Cfg3<RX, RY, RZ>::NT, Cfg3<RX, RY, RZ>::MINB)
       const bool ok = stage_and_xpass(0, xs);
       if (__syncthreads_or(!ok)) {
         ITKG_ON_TIMEOUT(0);
-        return;
+        return false;
       }
     }
     int prev_s = INT_MIN;
@@ -412,7 +399,7 @@ __global__ void __launch_bounds__(Cfg3<RX, RY, RZ>::NT, Cfg3<RX, RY, RZ>::MINB)
           const bool ok = stage_and_xpass((cons + 1) % S, xs + ((cons + 1) & 1) * IH * TX);
           if (__syncthreads_or(!ok)) {
             ITKG_ON_TIMEOUT(cons + 1);
-            return;
+            return false;
           }
         }
         ++cons;
@@ -489,14 +476,82 @@ __global__ void __launch_bounds__(Cfg3<RX, RY, RZ>::NT, Cfg3<RX, RY, RZ>::MINB)
     __syncthreads();
   }
 #undef ITKG_ON_TIMEOUT
+  return true;
 }
+
+// Shared-memory set-up common to the single- and multi-request kernels.
+#define ITKG_FUSED_PROLOGUE                                                              \
+  using C = Cfg3<RX, RY, RZ>;                                                            \
+  extern __shared__ __align__(128) float smem[];                                         \
+  __shared__ __align__(8) uint64_t mbar[C::S];                                           \
+  /* TMA destinations must be 128-byte aligned: offset by an index so the compiler */    \
+  /* keeps shared-memory addressing. */                                                  \
+  float* const stage0 = smem + (((128u - (smem_u32(smem) & 127u)) & 127u) >> 2);         \
+  const uint32_t bbase = smem_u32(mbar);                                                 \
+  if (TMA) {                                                                             \
+    if (threadIdx.x == 0) {                                                              \
+      for (int i = 0; i < C::S; ++i) mbar_init(bbase + 8 * i, 1);                        \
+      asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");               \
+    }                                                                                    \
+    __syncthreads();                                                                     \
+  }                                                                                      \
+  uint32_t phase_bits = 0;
+
+template <int RX, int RY, int RZ, bool REF, bool TMA>
+__global__ void __launch_bounds__(Cfg3<RX, RY, RZ>::NT, Cfg3<RX, RY, RZ>::MINB)
+    k_fused3d_f32(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ Fused3DArgs a) {
+  ITKG_FUSED_PROLOGUE
+  const int64_t u_begin = a.units * blockIdx.x / gridDim.x;
+  const int64_t u_end = a.units * (blockIdx.x + 1) / gridDim.x;
+  fused_range<RX, RY, RZ, REF, TMA>(a, &tmap, u_begin, u_end, stage0, bbase, phase_bits);
+}
+
+// One request of a multi-request launch; its units are [unit_begin, unit_begin + a.units).
+struct FusedItem {
+  Fused3DArgs a;
+  int64_t unit_begin;
+  int64_t pad_[7];
+};
+
+// Persistent multi-request launch: the CTAs split the union of all requests'
+// units evenly; a CTA copies each request's arguments to shared memory as it
+// reaches it and runs the same fused filter on its share.
+template <int RX, int RY, int RZ, bool REF, bool TMA>
+__global__ void __launch_bounds__(Cfg3<RX, RY, RZ>::NT, Cfg3<RX, RY, RZ>::MINB)
+    k_fused3d_f32_multi(const FusedItem* __restrict__ items, const CUtensorMap* __restrict__ maps,
+                        int nitems, int64_t total_units) {
+  ITKG_FUSED_PROLOGUE
+  __shared__ __align__(16) Fused3DArgs sa;
+  int64_t u = total_units * blockIdx.x / gridDim.x;
+  const int64_t u_end = total_units * (blockIdx.x + 1) / gridDim.x;
+  int it = 0;
+  while (it + 1 < nitems && items[it + 1].unit_begin <= u) ++it;
+  while (u < u_end && it < nitems) {
+    __syncthreads();  // previous request's arguments no longer in use
+    {
+      const uint32_t* srcw = reinterpret_cast<const uint32_t*>(&items[it].a);
+      uint32_t* dstw = reinterpret_cast<uint32_t*>(&sa);
+      for (int i = threadIdx.x; i < (int)(sizeof(Fused3DArgs) / 4); i += C::NT) dstw[i] = srcw[i];
+    }
+    __syncthreads();
+    const int64_t ib = items[it].unit_begin;
+    const int64_t e = min(u_end, ib + sa.units);
+    if (!fused_range<RX, RY, RZ, REF, TMA>(sa, &maps[it], u - ib, e - ib, stage0, bbase, phase_bits))
+      return;
+    u = e;
+    ++it;
+  }
+}
+#undef ITKG_FUSED_PROLOGUE
 
 // ---- dispatch table -----------------------------------------------------------
 using KernelFn = void (*)(const CUtensorMap, const Fused3DArgs);
+using MultiFn = void (*)(const FusedItem*, const CUtensorMap*, int, int64_t);
 
 struct Entry {
   int rx, ry, rz;
-  KernelFn fn[2][2];  // [ref][tma]
+  KernelFn fn[2][2];    // [ref][tma]
+  MultiFn multi[2][2];  // [ref][tma]
   size_t smem;
   int tx, ty, nt, xa, bw, ih;
 };
@@ -504,11 +559,15 @@ struct Entry {
 template <int RX, int RY, int RZ>
 Entry make_entry() {
   using C = Cfg3<RX, RY, RZ>;
-  Entry e{RX, RY, RZ, {}, C::SMEM, C::TX, C::TY, C::NT, C::XA, C::BW, C::IH};
+  Entry e{RX, RY, RZ, {}, {}, C::SMEM, C::TX, C::TY, C::NT, C::XA, C::BW, C::IH};
   e.fn[0][0] = k_fused3d_f32<RX, RY, RZ, false, false>;
   e.fn[0][1] = k_fused3d_f32<RX, RY, RZ, false, true>;
   e.fn[1][0] = k_fused3d_f32<RX, RY, RZ, true, false>;
   e.fn[1][1] = k_fused3d_f32<RX, RY, RZ, true, true>;
+  e.multi[0][0] = k_fused3d_f32_multi<RX, RY, RZ, false, false>;
+  e.multi[0][1] = k_fused3d_f32_multi<RX, RY, RZ, false, true>;
+  e.multi[1][0] = k_fused3d_f32_multi<RX, RY, RZ, true, false>;
+  e.multi[1][1] = k_fused3d_f32_multi<RX, RY, RZ, true, true>;
   return e;
 }
 
@@ -582,28 +641,10 @@ bool tma_ok(const FusedGeom& g, const Entry& e) {
   return encode_fn() != nullptr;
 }
 
-}  // namespace
-
-itkg_status launch_fused(const FusedGeom& g, const float* const w[kMaxDim], void* stream,
-                         bool dry_run) {
-  if (g.dim != 3 || g.comps != 1 || g.in_dtype != ITKG_F32) return ITKG_ERROR_UNSUPPORTED;
-  if (g.out_dtype == ITKG_I16) return ITKG_ERROR_UNSUPPORTED;
-  const Entry* e = find_entry(g.radius[0], g.radius[1], g.radius[2]);
-  if (!e) return ITKG_ERROR_UNSUPPORTED;
-  // 32-bit in-slice offsets and coordinates
-  for (int d = 0; d < 3; ++d)
-    if (!fits_i32(g.lo[d]) || !fits_i32(g.hi[d]) || !fits_i32(g.src_origin[d]) ||
-        !fits_i32(g.dst_origin[d]) || !fits_i32(g.req_index[d] + g.req_size[d]) ||
-        !fits_i32(g.req_index[d] - 64))
-      return ITKG_ERROR_UNSUPPORTED;
-  const int64_t span = (g.hi[0] - g.src_origin[0] + 1) * g.src_pitch[0] +
-                       (g.hi[1] - g.src_origin[1] + 1) * g.src_pitch[1];
-  if (!fits_i32(span)) return ITKG_ERROR_UNSUPPORTED;
-  if (g.src_pitch[0] != 4) return ITKG_ERROR_UNSUPPORTED;
-  if (((uintptr_t)g.src & 3) || (g.src_pitch[1] & 3) || (g.src_pitch[2] & 3)) return ITKG_ERROR_UNSUPPORTED;
-  if (dry_run) return ITKG_SUCCESS;
-
-  Fused3DArgs a;
+// Kernel arguments and (when TMA applies) the tensor map of one request.
+itkg_status build_args(const FusedGeom& g, const float* const w[kMaxDim], const Entry* e,
+                       Fused3DArgs* ap, CUtensorMap* mapp, bool* tma) {
+  Fused3DArgs& a = *ap;
   std::memset(&a, 0, sizeof a);
   a.src = static_cast<const char*>(g.src);
   a.dst = static_cast<char*>(g.dst);
@@ -630,10 +671,10 @@ itkg_status launch_fused(const FusedGeom& g, const float* const w[kMaxDim], void
   for (int k = 0; k < 2 * e->ry + 1; ++k) a.wy[k] = w[1][k], a.wy2[k] = splat2_host(w[1][k]);
   for (int k = 0; k < 2 * e->rz + 1; ++k) a.wz[k] = w[2][k], a.wz2[k] = splat2_host(w[2][k]);
 
-  CUtensorMap map;
+  CUtensorMap& map = *mapp;
   std::memset(&map, 0, sizeof map);
-  const bool tma = tma_ok(g, *e);
-  if (tma) {
+  *tma = tma_ok(g, *e);
+  if (*tma) {
     const cuuint64_t dims[3] = {(cuuint64_t)g.src_size[0], (cuuint64_t)g.src_size[1],
                                 (cuuint64_t)g.src_size[2]};
     const cuuint64_t strides[2] = {(cuuint64_t)g.src_pitch[1], (cuuint64_t)g.src_pitch[2]};
@@ -645,6 +686,46 @@ itkg_status launch_fused(const FusedGeom& g, const float* const w[kMaxDim], void
                              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return set_error(ITKG_ERROR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
   }
+  return ITKG_SUCCESS;
+}
+
+#define ITKG_CUDA_ST(call)                                                            \
+  do {                                                                                \
+    const cudaError_t e_ = (call);                                                    \
+    if (e_ != cudaSuccess) return set_error(ITKG_ERROR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+#define ITKG_TRY_ST(expr)                  \
+  do {                                     \
+    const itkg_status s_ = (expr);         \
+    if (s_ != ITKG_SUCCESS) return s_;     \
+  } while (0)
+
+}  // namespace
+
+itkg_status launch_fused(const FusedGeom& g, const float* const w[kMaxDim], void* stream,
+                         bool dry_run) {
+  if (g.dim != 3 || g.comps != 1 || g.in_dtype != ITKG_F32) return ITKG_ERROR_UNSUPPORTED;
+  if (g.out_dtype == ITKG_I16) return ITKG_ERROR_UNSUPPORTED;
+  const Entry* e = find_entry(g.radius[0], g.radius[1], g.radius[2]);
+  if (!e) return ITKG_ERROR_UNSUPPORTED;
+  // 32-bit in-slice offsets and coordinates
+  for (int d = 0; d < 3; ++d)
+    if (!fits_i32(g.lo[d]) || !fits_i32(g.hi[d]) || !fits_i32(g.src_origin[d]) ||
+        !fits_i32(g.dst_origin[d]) || !fits_i32(g.req_index[d] + g.req_size[d]) ||
+        !fits_i32(g.req_index[d] - 64))
+      return ITKG_ERROR_UNSUPPORTED;
+  const int64_t span = (g.hi[0] - g.src_origin[0] + 1) * g.src_pitch[0] +
+                       (g.hi[1] - g.src_origin[1] + 1) * g.src_pitch[1];
+  if (!fits_i32(span)) return ITKG_ERROR_UNSUPPORTED;
+  if (g.src_pitch[0] != 4) return ITKG_ERROR_UNSUPPORTED;
+  if (((uintptr_t)g.src & 3) || (g.src_pitch[1] & 3) || (g.src_pitch[2] & 3)) return ITKG_ERROR_UNSUPPORTED;
+  if (dry_run) return ITKG_SUCCESS;
+
+  Fused3DArgs a;
+  CUtensorMap map;
+  bool tma = false;
+  ITKG_TRY_ST(build_args(g, w, e, &a, &map, &tma));
   const bool ref = g.rounding == ITKG_ROUND_REFERENCE;
   KernelFn fn = e->fn[ref ? 1 : 0][tma ? 1 : 0];
   int resident = 0;
@@ -661,17 +742,92 @@ itkg_status launch_fused(const FusedGeom& g, const float* const w[kMaxDim], void
   return ITKG_SUCCESS;
 }
 
-itkg_status launch_fused_multi(const std::vector<FusedGeom>& geoms,
-                               const std::vector<std::vector<std::vector<float>>>& weights,
-                               void* stream, std::vector<std::string>* plan) {
+struct FusedMultiGroup {
+  const Entry* e;
+  bool ref, tma;
+  std::vector<FusedItem> items;
+  std::vector<CUtensorMap> maps;
+  FusedItem* d_items = nullptr;
+  CUtensorMap* d_maps = nullptr;
+  int64_t total = 0;
+  int grid = 0;
+};
+struct FusedMultiPlan {
+  std::vector<FusedMultiGroup> groups;
+};
+
+itkg_status fused_multi_prepare(const std::vector<FusedGeom>& geoms,
+                                const std::vector<std::vector<std::vector<float>>>& weights,
+                                FusedMultiPlan** out, std::vector<std::string>* lines) {
+  FusedMultiPlan* plan = new FusedMultiPlan();
+  *out = plan;
   for (size_t i = 0; i < geoms.size(); ++i) {
+    const FusedGeom& g = geoms[i];
+    const Entry* e = find_entry(g.radius[0], g.radius[1], g.radius[2]);
+    if (!e) return set_error(ITKG_ERROR_UNSUPPORTED, "no fused kernel for item %zu", i);
     const float* w[kMaxDim] = {nullptr, nullptr, nullptr};
-    for (int d = 0; d < geoms[i].dim; ++d) w[d] = weights[i][d].data();
-    const itkg_status st = launch_fused(geoms[i], w, stream, false);
-    if (st != ITKG_SUCCESS) return st;
-    if (plan) plan->push_back(std::string("fused item ") + std::to_string(i) + ": " + itkg_last_kernel());
+    for (int d = 0; d < g.dim; ++d) w[d] = weights[i][d].data();
+    FusedItem item;
+    std::memset(&item, 0, sizeof item);
+    CUtensorMap map;
+    bool tma = false;
+    ITKG_TRY_ST(build_args(g, w, e, &item.a, &map, &tma));
+    const bool ref = g.rounding == ITKG_ROUND_REFERENCE;
+    FusedMultiGroup* grp = nullptr;
+    for (FusedMultiGroup& q : plan->groups)
+      if (q.e == e && q.ref == ref && q.tma == tma) grp = &q;
+    if (!grp) {
+      plan->groups.push_back(FusedMultiGroup());
+      grp = &plan->groups.back();
+      grp->e = e;
+      grp->ref = ref;
+      grp->tma = tma;
+    }
+    item.unit_begin = grp->total;
+    grp->total += item.a.units;
+    grp->items.push_back(item);
+    grp->maps.push_back(map);
+  }
+  for (FusedMultiGroup& q : plan->groups) {
+    ITKG_CUDA_ST(cudaMalloc(&q.d_items, sizeof(FusedItem) * q.items.size()));
+    ITKG_CUDA_ST(cudaMalloc(&q.d_maps, sizeof(CUtensorMap) * q.maps.size()));
+    ITKG_CUDA_ST(cudaMemcpy(q.d_items, q.items.data(), sizeof(FusedItem) * q.items.size(),
+                            cudaMemcpyHostToDevice));
+    ITKG_CUDA_ST(cudaMemcpy(q.d_maps, q.maps.data(), sizeof(CUtensorMap) * q.maps.size(),
+                            cudaMemcpyHostToDevice));
+    MultiFn fn = q.e->multi[q.ref ? 1 : 0][q.tma ? 1 : 0];
+    int resident = 0;
+    ITKG_TRY_ST(resident_ctas(reinterpret_cast<KernelFn>(fn), q.e->smem, q.e->nt, &resident));
+    q.grid = (int)std::min<int64_t>(q.total, resident);
+    if (lines)
+      lines->push_back("fused3d multi-request launch: r=(" + std::to_string(q.e->rx) + "," +
+                       std::to_string(q.e->ry) + "," + std::to_string(q.e->rz) + ") " +
+                       (q.ref ? "ref" : "fma") + (q.tma ? " tma" : " gather") + ", " +
+                       std::to_string(q.items.size()) + " requests, " + std::to_string(q.total) +
+                       " units, " + std::to_string(q.grid) + " CTAs");
   }
   return ITKG_SUCCESS;
+}
+
+itkg_status fused_multi_launch(const FusedMultiPlan* plan, void* stream) {
+  for (const FusedMultiGroup& q : plan->groups) {
+    MultiFn fn = q.e->multi[q.ref ? 1 : 0][q.tma ? 1 : 0];
+    fn<<<q.grid, q.e->nt, q.e->smem, static_cast<cudaStream_t>(stream)>>>(q.d_items, q.d_maps,
+                                                                           (int)q.items.size(), q.total);
+    note_launch("fused3d_f32_multi");
+    cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) return set_error(ITKG_ERROR_CUDA, "fused3d multi launch: %s", cudaGetErrorString(err));
+  }
+  return ITKG_SUCCESS;
+}
+
+void fused_multi_free(FusedMultiPlan* plan) {
+  if (!plan) return;
+  for (FusedMultiGroup& q : plan->groups) {
+    if (q.d_items) cudaFree(q.d_items);
+    if (q.d_maps) cudaFree(q.d_maps);
+  }
+  delete plan;
 }
 
 itkg_status fused_fault_flag(unsigned int* flag, bool clear) {

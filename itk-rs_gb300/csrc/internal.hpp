@@ -6,7 +6,6 @@
 #include <cstdint>
 #include <string>
 #include <vector>
-#include <string>
 
 #include "itkg.h"
 
@@ -109,11 +108,16 @@ itkg_status fused_geom_for(const itkg_image& in, const itkg_region& largest,
                            const itkg_image& out, FusedGeom* g,
                            std::vector<std::vector<float>>* weights);
 
-// fused.cu: launches many fused requests; requests sharing a kernel run as one
-// persistent multi-item launch.  Appends one line per launch to `plan`.
-itkg_status launch_fused_multi(const std::vector<FusedGeom>& geoms,
-                               const std::vector<std::vector<std::vector<float>>>& weights,
-                               void* stream, std::vector<std::string>* plan);
+// fused.cu: many fused requests; requests sharing a kernel run as one
+// persistent multi-request launch.  prepare (outside any stream capture)
+// builds and uploads the request tables and appends one line per launch to
+// `lines`; launch enqueues the launches; free releases the tables.
+struct FusedMultiPlan;
+itkg_status fused_multi_prepare(const std::vector<FusedGeom>& geoms,
+                                const std::vector<std::vector<std::vector<float>>>& weights,
+                                FusedMultiPlan** plan, std::vector<std::string>* lines);
+itkg_status fused_multi_launch(const FusedMultiPlan* plan, void* stream);
+void fused_multi_free(FusedMultiPlan* plan);
 
 // Bumps the launch counter by n (graph replays).
 void note_launches(uint64_t n, const char* name);

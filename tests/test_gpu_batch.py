@@ -39,8 +39,9 @@ def test_batch_forward_equals_single_calls(gpu, rounding, autotune):
     for rep in range(2):
         for o in outs:  # poison outputs so the replay must rewrite them
             from itkg import _abi
-            _abi.check(_abi.lib().itkg_memset_device(ctypes.c_void_p(o.c.data), 0xFF,
-                                                     o.c.pitch[2] * o.region.size[2], None))
+            sx, sy, sz = o.region.size
+            nbytes = (sz - 1) * o.c.pitch[2] + (sy - 1) * o.c.pitch[1] + sx * o.c.pitch[0]
+            _abi.check(_abi.lib().itkg_memset_device(ctypes.c_void_p(o.c.data), 0xFF, nbytes, None))
         b.run()
         gpu.Stream().synchronize()
         for (arr, sigma), o in zip(vols, outs):
