@@ -228,6 +228,20 @@ itkg_status itkg_gaussian_vjp(const itkg_image *x, const itkg_image *ybar,
                               const itkg_gaussian_params *params, itkg_image *xbar,
                               double *sigma_bar, int32_t flags, void *stream);
 
+/* Multi-scale squared-error loss and its gradient, the scale stack recomputed
+ * level by level instead of stored:
+ *   L = sum_l sum_v (G_{sigma_l} x - target)^2
+ *   loss      (host, may be NULL): L in f64
+ *   xbar      (may be NULL): dL/dx = sum_l G_l^T 2 (G_l x - target), overwritten
+ *   sigma_bar (may be NULL): nlevels values dL/dsigma_l (radius frozen per level);
+ *             host array unless ITKG_VJP_SIGMA_BAR_ON_DEVICE.
+ * Scalar f32 device images of one region; synchronises the stream when it
+ * returns host values. */
+itkg_status itkg_gaussian_scale_stack_loss_vjp(const itkg_image *x, const itkg_image *target,
+                                               const double *sigmas, int32_t nlevels,
+                                               itkg_image *xbar, double *loss, double *sigma_bar,
+                                               int32_t flags, void *stream);
+
 /* ---- batches (not in the reference: it filters one image per call) ---------
  * A batch collects many forward requests (the arguments of
  * itkg_gaussian_generate_region, device buffers only) and VJP requests (the

@@ -1,7 +1,9 @@
 // Fused 3-D Gaussian forward: all three separable passes of
 // GaussianFilter::generate_region (src/filters/gaussian.rs:74-88) in one
 // kernel, so each input voxel is read from HBM once and each output voxel is
-// written once.
+// written once.  The kernel templates are in fused_kernel.cuh; this file holds
+// the f32 instantiations and the host-side dispatch (kernel choice, TMA
+// descriptors, launch geometry, multi-request batches, the fault word).
 //
 // Decomposition.  A CTA owns an output tile of TX x TY columns (x, y) and a
 // range of output slices [z0, z1).  It marches through the input slices
@@ -9,591 +11,93 @@
 // reference's clamp-to-edge on axis 2, conv.rs:31-33):
 //   1. the (TX + 2XA) x (TY + 2RY) input tile of slice j is staged in shared
 //      memory S slices ahead -- by one TMA tile load per slice (an elected
-//      thread, mbarrier completion) when the buffer's pitches are 16-byte
-//      multiples, else by a cp.async gather.  Edge tiles replicate the image's
-//      edge values into the halo after the load (TMA fills zeros outside the
-//      buffer); the gather clamps its coordinates instead.  Either way the halo
-//      holds the reference's clamp-to-edge values.
-//   2. x pass: shared tile -> shared x-filtered tile (TY + 2RY rows);
+//      thread, mbarrier completion) when the buffer's base and pitches are
+//      16-byte multiples, else (f32 only) by a cp.async gather.  Edge tiles
+//      replicate the image's edge values into the halo after the load (TMA
+//      fills zeros outside the buffer); the gather clamps its coordinates
+//      instead.  Either way the halo holds the reference's clamp-to-edge values.
+//      i16 / u8 / bf16 / f16 inputs are staged as loaded and converted exactly
+//      to f32 as the x pass reads them (the reference's UnaryFilter(p as f32)).
+//   2. x pass: shared tile -> shared x-filtered f32 tile (TY + 2RY rows);
 //   3. y pass: each thread filters MY consecutive rows of one column from a
 //      register window;
 //   4. z pass, "push" form: slice j contributes w[k] * v to the outputs
 //      z = j + RZ - k; each thread keeps a ring of KZ accumulators per owned
 //      column in registers, the ring slot being a compile-time function of
 //      the phase j mod KZ, selected by a switch.
-// FMA rounding runs the x, y and z passes as packed two-lane f32x2 FMAs
-// (rows or columns paired).  Reference rounding runs scalar
-// acc = acc + x * w with separate roundings in ascending tap order, starting
-// from zero, on f32 intermediates -- bit-identical to conv.rs:26-36 pass by
-// pass.  Slices clamped at the z ends are filtered once and pushed again.
+// FMA rounding runs the x, y and z passes as packed two-lane f32x2 FMAs.
+// Reference rounding runs scalar acc = acc + x * w with separate roundings in
+// ascending tap order, starting from zero, on f32 intermediates --
+// bit-identical to conv.rs:26-36 pass by pass.  Slices clamped at the z ends
+// are filtered once and pushed again.
 //
 // Work balance.  The (tile, z) units of the request are split evenly over a
 // grid of (SMs x resident CTAs) CTAs; a CTA's share is one or two z-segments.
-#include <cuda.h>
-#include <cuda_runtime.h>
-#include <cudaTypedefs.h>
-
-#include <algorithm>
-#include <climits>
-#include <cstring>
-#include <mutex>
-#include <vector>
-
-#include "f32x2.cuh"
-#include "internal.hpp"
-#include "pixel.cuh"
+#include "fused_kernel.cuh"
 
 namespace itkg {
+namespace fusedk {
+namespace {
+const Entry kTableF32[] = ITKG_FUSED_TABLE(float);
+}  // namespace
+}  // namespace fusedk
+
+const fusedk::Entry* fused_entries_f32(int* n) {
+  *n = (int)(sizeof(fusedk::kTableF32) / sizeof(fusedk::kTableF32[0]));
+  return fusedk::kTableF32;
+}
+
 namespace {
 
-constexpr int kMaxFusedR = 12;
-constexpr int kMaxFusedK = 2 * kMaxFusedR + 1;
-
-__device__ unsigned int g_fused_fault = 0;  // set when a bounded wait gives up
-
-struct Fused3DArgs {
-  const char* src;
-  char* dst;
-  int64_t src_pitch[3];  // bytes
-  int64_t dst_pitch[3];
-  int32_t src_origin[3];
-  int32_t dst_origin[3];
-  int32_t req_lo[3];  // requested region, inclusive bounds
-  int32_t req_hi[3];
-  int32_t lo[3];  // gather bounds (image bounds within the input buffer), inclusive
-  int32_t hi[3];
-  int32_t ntx, nty;  // tiles along x and y
-  int64_t units;     // ntx * nty * nz_requested
-  int32_t out_dtype;
-  int32_t pad_;
-  float wx[kMaxFusedK];
-  float wy[kMaxFusedK];
-  float wz[kMaxFusedK];
-  f2_t wx2[kMaxFusedK];  // {w, w} pairs for the packed passes
-  f2_t wy2[kMaxFusedK];
-  f2_t wz2[kMaxFusedK];
-};
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ void cp_async4(uint32_t saddr, const void* g) {
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(saddr), "l"(g) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() {
-  asm volatile("cp.async.commit_group;\n" ::: "memory");
-}
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
-}
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(bar), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-      " selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(bar), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// Bounded wait: gives up after ~2^31 cycles (about a second) and reports false.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-  if (mbar_try_wait(bar, parity)) return true;
-  const long long t0 = clock64();
-  while (!mbar_try_wait(bar, parity))
-    if (clock64() - t0 > (1ll << 31)) return false;
-  return true;
-}
-__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, int x, int y, int z,
-                                            uint32_t bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
-      " [%0], [%1, {%2, %3, %4}], [%5];\n" ::"r"(dst),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(bar)
-      : "memory");
-}
-
-__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
-
-// Tile shape per radius.
-template <int RX, int RY, int RZ>
-struct Cfg3 {
-  static constexpr int KX = 2 * RX + 1, KY = 2 * RY + 1, KZ = 2 * RZ + 1;
-  static constexpr int NT = 256;                    // threads per CTA
-  static constexpr int NW = NT / 32;
-  static constexpr int TX = 32;                     // one lane per output column
-  static constexpr int MY = RZ <= 8 ? 4 : 2;        // rows per thread (y pass, z ring)
-  static constexpr int MY2 = MY / 2;                // packed row pairs
-  static constexpr int TY = NW * MY;
-  static constexpr int MX = 8;                      // x outputs per x-pass task
-  static constexpr int XA = (RX + 3) / 4 * 4;       // x halo rounded up to 16 bytes
-  static constexpr int BW = TX + 2 * XA;            // staged tile width (floats)
-  static constexpr int IH = TY + 2 * RY;            // staged tile height
-  static constexpr int OFF = (XA - RX) % 4;         // window misalignment
-  static constexpr int WB = XA - RX - OFF;          // aligned window start (col)
-  static constexpr int WIN = (MX + 2 * RX + OFF + 3) / 4 * 4;  // x-pass window (floats)
-  static constexpr int S = 4;                       // slices in flight
-  static constexpr int STAGE = (IH * BW + 31) / 32 * 32;  // floats per stage (128-byte multiple)
-  static constexpr int NLD = (STAGE + NT - 1) / NT; // gather elements per thread
-  static constexpr size_t SMEM = sizeof(float) * (size_t)(S * STAGE + 2 * IH * TX) + 128;
-  static constexpr int MINB = 2;
-  static_assert(WB + TX - MX + WIN <= BW, "x window stays inside the staged row");
-  static_assert(TX % MX == 0, "x segments");
-};
-
-// z pass for phase P: push the packed y-filtered values into every ring slot,
-// then hand back the completed slot (P + 1) mod KZ and clear it.
-template <int P, int KZ, int MY2, bool REF>
-__device__ __forceinline__ void push_phase(f2_t (&acc)[MY2][KZ], const f2_t (&yv)[MY2],
-                                           const Fused3DArgs& a, f2_t (&done)[MY2]) {
-#pragma unroll
-  for (int k = 0; k < KZ; ++k) {
-    const int slot = (P - k + KZ) % KZ;
-#pragma unroll
-    for (int m = 0; m < MY2; ++m) {
-      if constexpr (REF) {
-        float a0, a1, v0, v1;
-        unpack2(acc[m][slot], a0, a1);
-        unpack2(yv[m], v0, v1);
-        acc[m][slot] = pack2(__fadd_rn(a0, __fmul_rn(v0, a.wz[k])), __fadd_rn(a1, __fmul_rn(v1, a.wz[k])));
-      } else {
-        acc[m][slot] = fma2(yv[m], a.wz2[k], acc[m][slot]);
-      }
-    }
-  }
-  constexpr int D = (P + 1) % KZ;
-#pragma unroll
-  for (int m = 0; m < MY2; ++m) {
-    done[m] = acc[m][D];
-    acc[m][D] = 0ull;
-  }
-}
-
-#define ITKG_PUSH_CASE(N)                                                   \
-  case N:                                                                   \
-    if constexpr (N < KZ) push_phase<N, KZ, MY2, REF>(acc, yv, a, done);    \
-    break;
-
-// The fused filter over units [u_begin, u_end) of one request `a` (a unit is
-// one output slice of one (x, y) tile).  Returns false if a bounded wait gave
-// up (the device fault word is then set).
-template <int RX, int RY, int RZ, bool REF, bool TMA>
-__device__ __forceinline__ bool fused_range(const Fused3DArgs& a, const CUtensorMap* tmap,
-                                            int64_t u_begin, int64_t u_end, float* const stage0,
-                                            uint32_t bbase, uint32_t& phase_bits) {
-  using C = Cfg3<RX, RY, RZ>;
-  constexpr int KX = C::KX, KY = C::KY, KZ = C::KZ, TX = C::TX, TY = C::TY, MY = C::MY,
-                MY2 = C::MY2, MX = C::MX, BW = C::BW, IH = C::IH, XA = C::XA, S = C::S,
-                NLD = C::NLD, NT = C::NT, WIN = C::WIN, WB = C::WB, OFF = C::OFF;
-  static_assert(KZ <= 25, "phase switch covers KZ <= 25");
-  float* const xs = stage0 + S * C::STAGE;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int nzr = a.req_hi[2] - a.req_lo[2] + 1;
-  const uint32_t sbase = smem_u32(stage0);
-
-  for (int64_t u = u_begin; u < u_end;) {
-    const int64_t tile = u / nzr;
-    const int zs = (int)(u % nzr);
-    const int64_t zrem = zs + (u_end - u);
-    const int ze = zrem < nzr ? (int)zrem : nzr;
-    u += ze - zs;
-    const int z0 = a.req_lo[2] + zs, z1 = a.req_lo[2] + ze;  // outputs [z0, z1)
-    const int tx0 = a.req_lo[0] + (int)(tile % a.ntx) * TX;
-    const int ty0 = a.req_lo[1] + (int)(tile / a.ntx) * TY;
-    const int gx0 = tx0 - XA, gy0 = ty0 - RY;  // image coords of stage element (0, 0)
-    const bool edge = gx0 < a.lo[0] || gx0 + BW - 1 > a.hi[0] || gy0 < a.lo[1] || gy0 + IH - 1 > a.hi[1];
-
-    // cp.async path: gather offsets of this thread's share (clamped x, y).
-    int32_t goff[TMA ? 1 : NLD];
-    if constexpr (!TMA) {
-#pragma unroll
-      for (int i = 0; i < NLD; ++i) {
-        const int e = tid + i * NT;
-        const int gx = clampi(gx0 + e % BW, a.lo[0], a.hi[0]);
-        const int gy = clampi(gy0 + e / BW, a.lo[1], a.hi[1]);
-        goff[i] = (int32_t)((gx - a.src_origin[0]) * a.src_pitch[0] +
-                            (gy - a.src_origin[1]) * a.src_pitch[1]);
-      }
-    }
-    auto issue = [&](int s, int st) {
-      if constexpr (TMA) {
-        if (tid == 0) {
-          asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-          const uint32_t bar = bbase + 8 * st;
-          mbar_expect_tx(bar, (uint32_t)(IH * BW * 4));  // bytes of one box
-          tma_load_3d(sbase + (uint32_t)(st * C::STAGE * 4), tmap, gx0 - a.src_origin[0],
-                      gy0 - a.src_origin[1], s - a.src_origin[2], bar);
-        }
-      } else {
-        const char* base = a.src + (int64_t)(s - a.src_origin[2]) * a.src_pitch[2];
-        const uint32_t sb = sbase + (uint32_t)(st * C::STAGE * 4);
-#pragma unroll
-        for (int i = 0; i < NLD; ++i) {
-          const int e = tid + i * NT;
-          if (i < NLD - 1 || e < C::STAGE) cp_async4(sb + (uint32_t)e * 4u, base + goff[i]);
-        }
-        cp_async_commit();
-      }
-    };
-
-    const int jb = z0 - RZ, je = z1 - 1 + RZ;
-    const int s_first = max(jb, a.lo[2]), s_last = min(je, a.hi[2]);
-    for (int q = 0; q < S; ++q) {
-      if (s_first + q <= s_last) issue(s_first + q, q);
-      else if (!TMA) cp_async_commit();
-    }
-
-    f2_t acc[MY2][KZ];
-#pragma unroll
-    for (int m = 0; m < MY2; ++m)
-#pragma unroll
-      for (int q = 0; q < KZ; ++q) acc[m][q] = 0ull;
-    f2_t yv[MY2];
-#pragma unroll
-    for (int m = 0; m < MY2; ++m) yv[m] = 0ull;
-
-    // Output addressing for this thread's column and rows.
-    const int col_x = tx0 + lane;
-    const int row_y0 = ty0 + warp * MY;
-    const bool col_ok = col_x <= a.req_hi[0];
-    int nrows_ok = a.req_hi[1] - row_y0 + 1;
-    nrows_ok = nrows_ok < 0 ? 0 : (nrows_ok > MY ? MY : nrows_ok);
-    char* const obase = a.dst + (int64_t)(col_x - a.dst_origin[0]) * a.dst_pitch[0] +
-                        (int64_t)(row_y0 - a.dst_origin[1]) * a.dst_pitch[1];
-    const int64_t opy = a.dst_pitch[1];
-
-    // Stage slice s (already issued into stage st) and run its x pass into
-    // xbuf.  Returns false if the bounded wait on the tile load gave up.
-    auto stage_and_xpass = [&](int st, float* xbuf) -> bool {
-      float* const tile = stage0 + st * C::STAGE;
-      if constexpr (TMA) {
-        const bool ok = mbar_wait(bbase + 8 * st, (phase_bits >> st) & 1u);
-        phase_bits ^= 1u << st;
-        if (!ok) return false;
-        if (edge) {
-          // Replicate the image's edge values into the halo: first the
-          // columns left of lo / right of hi (nl, nr of them), then whole
-          // rows above / below (nt, nb of them).  Sources are in-image
-          // columns and rows, which these loops never write.
-          __syncthreads();
-          const int nl = max(0, a.lo[0] - gx0), nr = max(0, gx0 + BW - 1 - a.hi[0]);
-          const int ncol = nl + nr;
-          for (int e = tid; e < ncol * IH; e += NT) {
-            const int r = e / ncol, i = e % ncol;
-            const int c = i < nl ? i : BW - 1 - (i - nl);
-            tile[r * BW + c] = tile[r * BW + clampi(gx0 + c, a.lo[0], a.hi[0]) - gx0];
-          }
-          __syncthreads();
-          const int nt = max(0, a.lo[1] - gy0), nb = max(0, gy0 + IH - 1 - a.hi[1]);
-          for (int e = tid; e < (nt + nb) * BW; e += NT) {
-            const int i = e / BW, c = e % BW;
-            const int r = i < nt ? i : IH - 1 - (i - nt);
-            tile[r * BW + c] = tile[(clampi(gy0 + r, a.lo[1], a.hi[1]) - gy0) * BW + c];
-          }
-          __syncthreads();
-        }
-      } else {
-        cp_async_wait<S - 1>();
-        __syncthreads();
-      }
-      constexpr int SEGS = TX / MX;
-      for (int t = tid; t < IH * SEGS; t += NT) {
-        const int row = t / SEGS, x0 = (t % SEGS) * MX;
-        float v[WIN];
-        const float4* src4 = reinterpret_cast<const float4*>(tile + row * BW + x0 + WB);
-#pragma unroll
-        for (int q = 0; q < WIN / 4; ++q) {
-          const float4 f = src4[q];
-          v[4 * q + 0] = f.x;
-          v[4 * q + 1] = f.y;
-          v[4 * q + 2] = f.z;
-          v[4 * q + 3] = f.w;
-        }
-        float o[MX];
-        if constexpr (REF) {
-#pragma unroll
-          for (int m = 0; m < MX; ++m) {
-            float ax = 0.0f;
-#pragma unroll
-            for (int k = 0; k < KX; ++k) ax = tap<true>(ax, v[m + k + OFF], a.wx[k]);
-            o[m] = ax;
-          }
-        } else {
-          // even/odd aligned pairs of the window: E[i] = (v[2i], v[2i+1]), O[i] = (v[2i+1], v[2i+2])
-          f2_t E[WIN / 2], O[WIN / 2 - 1];
-#pragma unroll
-          for (int i = 0; i < WIN / 2; ++i) E[i] = pack2(v[2 * i], v[2 * i + 1]);
-#pragma unroll
-          for (int i = 0; i < WIN / 2 - 1; ++i) O[i] = pack2(v[2 * i + 1], v[2 * i + 2]);
-#pragma unroll
-          for (int m = 0; m < MX / 2; ++m) {
-            f2_t ax = 0ull;
-#pragma unroll
-            for (int k = 0; k < KX; ++k) {
-              const int q = 2 * m + k + OFF;
-              ax = fma2((q & 1) ? O[(q - 1) / 2] : E[q / 2], a.wx2[k], ax);
-            }
-            unpack2(ax, o[2 * m], o[2 * m + 1]);
-          }
-        }
-        float4* dst4 = reinterpret_cast<float4*>(xbuf + row * TX + x0);
-#pragma unroll
-        for (int q = 0; q < MX / 4; ++q)
-          dst4[q] = make_float4(o[4 * q], o[4 * q + 1], o[4 * q + 2], o[4 * q + 3]);
-      }
-      return true;
-    };
-    // A tile load never completed: record it, let every other issued load
-    // land (bounded), and leave.
-#define ITKG_ON_TIMEOUT(CONS_NOW)                                                  \
-  do {                                                                             \
-    if (tid == 0) {                                                                \
-      atomicExch(&g_fused_fault, 1u);                                              \
-      if (TMA)                                                                     \
-        for (int q_ = 1; q_ < S; ++q_) {                                           \
-          const int sq_ = ((CONS_NOW) + q_) % S;                                   \
-          if (s_first + (CONS_NOW) + q_ <= s_last)                                 \
-            mbar_wait(bbase + 8 * sq_, (phase_bits >> sq_) & 1u);                  \
-        }                                                                          \
-    }                                                                              \
-  } while (0)
-
-    // Pipeline: the x pass of slice s + 1 runs in the same barrier interval
-    // as the y pass of slice s (double-buffered x-filtered tile).
-    if (s_first <= s_last) {
-      const bool ok = stage_and_xpass(0, xs);
-      if (__syncthreads_or(!ok)) {
-        ITKG_ON_TIMEOUT(0);
-        return false;
-      }
-    }
-    int prev_s = INT_MIN;
-    int cons = 0;  // slices consumed by the y pass so far
-    int p = 0;     // phase (j - jb) mod KZ
-    for (int j = jb; j <= je; ++j) {
-      const int s = clampi(j, a.lo[2], a.hi[2]);
-      if (s != prev_s) {
-        prev_s = s;
-        const int st = cons % S;
-        if (cons > 0) {
-          // x pass of s (previous interval) visible; y pass of s - 1 done
-          __syncthreads();
-        }
-        {
-          const int sn = s_first + cons + S;
-          if (sn <= s_last) issue(sn, st);
-          else if (!TMA) cp_async_commit();
-        }
-        const float* xcur = xs + (cons & 1) * IH * TX;
-        if (s + 1 <= s_last) {
-          const bool ok = stage_and_xpass((cons + 1) % S, xs + ((cons + 1) & 1) * IH * TX);
-          if (__syncthreads_or(!ok)) {
-            ITKG_ON_TIMEOUT(cons + 1);
-            return false;
-          }
-        }
-        ++cons;
-        // ---- y pass: xcur -> yv (registers, packed in row pairs) ----
-        float w[MY + 2 * RY];
-#pragma unroll
-        for (int i = 0; i < MY + 2 * RY; ++i) w[i] = xcur[(warp * MY + i) * TX + lane];
-        if constexpr (REF) {
-#pragma unroll
-          for (int m = 0; m < MY2; ++m) {
-            float y0 = 0.0f, y1 = 0.0f;
-#pragma unroll
-            for (int k = 0; k < KY; ++k) {
-              y0 = tap<true>(y0, w[2 * m + k], a.wy[k]);
-              y1 = tap<true>(y1, w[2 * m + 1 + k], a.wy[k]);
-            }
-            yv[m] = pack2(y0, y1);
-          }
-        } else {
-          constexpr int NWIN = MY + 2 * RY;
-          f2_t E[NWIN / 2], O[NWIN / 2];
-#pragma unroll
-          for (int i = 0; i < NWIN / 2; ++i) E[i] = pack2(w[2 * i], w[2 * i + 1]);
-#pragma unroll
-          for (int i = 0; i + 1 < NWIN / 2; ++i) O[i] = pack2(w[2 * i + 1], w[2 * i + 2]);
-#pragma unroll
-          for (int m = 0; m < MY2; ++m) {
-            f2_t ay = 0ull;
-#pragma unroll
-            for (int k = 0; k < KY; ++k) {
-              const int q = 2 * m + k;
-              ay = fma2((q & 1) ? O[(q - 1) / 2] : E[q / 2], a.wy2[k], ay);
-            }
-            yv[m] = ay;
-          }
-        }
-      }
-      // ---- z pass: push slice j into the ring, pop output z = j - RZ ----
-      f2_t done[MY2];
-      switch (p) {
-        ITKG_PUSH_CASE(0) ITKG_PUSH_CASE(1) ITKG_PUSH_CASE(2) ITKG_PUSH_CASE(3)
-        ITKG_PUSH_CASE(4) ITKG_PUSH_CASE(5) ITKG_PUSH_CASE(6) ITKG_PUSH_CASE(7)
-        ITKG_PUSH_CASE(8) ITKG_PUSH_CASE(9) ITKG_PUSH_CASE(10) ITKG_PUSH_CASE(11)
-        ITKG_PUSH_CASE(12) ITKG_PUSH_CASE(13) ITKG_PUSH_CASE(14) ITKG_PUSH_CASE(15)
-        ITKG_PUSH_CASE(16) ITKG_PUSH_CASE(17) ITKG_PUSH_CASE(18) ITKG_PUSH_CASE(19)
-        ITKG_PUSH_CASE(20) ITKG_PUSH_CASE(21) ITKG_PUSH_CASE(22) ITKG_PUSH_CASE(23)
-        ITKG_PUSH_CASE(24)
-        default: break;
-      }
-      p = p + 1 == KZ ? 0 : p + 1;
-      const int z = j - RZ;
-      if (z >= z0 && col_ok) {
-        char* orow = obase + (int64_t)(z - a.dst_origin[2]) * a.dst_pitch[2];
-        float vals[MY];
-#pragma unroll
-        for (int m = 0; m < MY2; ++m) unpack2(done[m], vals[2 * m], vals[2 * m + 1]);
-        if (a.out_dtype == ITKG_F32) {
-#pragma unroll
-          for (int m = 0; m < MY; ++m)
-            if (m < nrows_ok) __stcs(reinterpret_cast<float*>(orow + m * opy), vals[m]);
-        } else {
-#pragma unroll
-          for (int m = 0; m < MY; ++m) {
-            if (m >= nrows_ok) continue;
-            char* q = orow + m * opy;
-            if (a.out_dtype == ITKG_BF16) *reinterpret_cast<__nv_bfloat16*>(q) = from_f32<__nv_bfloat16>(vals[m]);
-            else if (a.out_dtype == ITKG_F16) *reinterpret_cast<__half*>(q) = from_f32<__half>(vals[m]);
-            else *reinterpret_cast<uint8_t*>(q) = from_f32<uint8_t>(vals[m]);
-          }
-        }
-      }
-    }
-    if constexpr (!TMA) cp_async_wait<0>();
-    __syncthreads();
-  }
-#undef ITKG_ON_TIMEOUT
-  return true;
-}
-
-// Shared-memory set-up common to the single- and multi-request kernels.
-#define ITKG_FUSED_PROLOGUE                                                              \
-  using C = Cfg3<RX, RY, RZ>;                                                            \
-  extern __shared__ __align__(128) float smem[];                                         \
-  __shared__ __align__(8) uint64_t mbar[C::S];                                           \
-  /* TMA destinations must be 128-byte aligned: offset by an index so the compiler */    \
-  /* keeps shared-memory addressing. */                                                  \
-  float* const stage0 = smem + (((128u - (smem_u32(smem) & 127u)) & 127u) >> 2);         \
-  const uint32_t bbase = smem_u32(mbar);                                                 \
-  if (TMA) {                                                                             \
-    if (threadIdx.x == 0) {                                                              \
-      for (int i = 0; i < C::S; ++i) mbar_init(bbase + 8 * i, 1);                        \
-      asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");               \
-    }                                                                                    \
-    __syncthreads();                                                                     \
-  }                                                                                      \
-  uint32_t phase_bits = 0;
-
-template <int RX, int RY, int RZ, bool REF, bool TMA>
-__global__ void __launch_bounds__(Cfg3<RX, RY, RZ>::NT, Cfg3<RX, RY, RZ>::MINB)
-    k_fused3d_f32(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ Fused3DArgs a) {
-  ITKG_FUSED_PROLOGUE
-  const int64_t u_begin = a.units * blockIdx.x / gridDim.x;
-  const int64_t u_end = a.units * (blockIdx.x + 1) / gridDim.x;
-  fused_range<RX, RY, RZ, REF, TMA>(a, &tmap, u_begin, u_end, stage0, bbase, phase_bits);
-}
-
-// One request of a multi-request launch; its units are [unit_begin, unit_begin + a.units).
-struct FusedItem {
-  Fused3DArgs a;
-  int64_t unit_begin;
-  int64_t pad_[7];
-};
-
-// Persistent multi-request launch: the CTAs split the union of all requests'
-// units evenly; a CTA copies each request's arguments to shared memory as it
-// reaches it and runs the same fused filter on its share.
-template <int RX, int RY, int RZ, bool REF, bool TMA>
-__global__ void __launch_bounds__(Cfg3<RX, RY, RZ>::NT, Cfg3<RX, RY, RZ>::MINB)
-    k_fused3d_f32_multi(const FusedItem* __restrict__ items, const CUtensorMap* __restrict__ maps,
-                        int nitems, int64_t total_units) {
-  ITKG_FUSED_PROLOGUE
-  __shared__ __align__(16) Fused3DArgs sa;
-  int64_t u = total_units * blockIdx.x / gridDim.x;
-  const int64_t u_end = total_units * (blockIdx.x + 1) / gridDim.x;
-  int it = 0;
-  while (it + 1 < nitems && items[it + 1].unit_begin <= u) ++it;
-  while (u < u_end && it < nitems) {
-    __syncthreads();  // previous request's arguments no longer in use
-    {
-      const uint32_t* srcw = reinterpret_cast<const uint32_t*>(&items[it].a);
-      uint32_t* dstw = reinterpret_cast<uint32_t*>(&sa);
-      for (int i = threadIdx.x; i < (int)(sizeof(Fused3DArgs) / 4); i += C::NT) dstw[i] = srcw[i];
-    }
-    __syncthreads();
-    const int64_t ib = items[it].unit_begin;
-    const int64_t e = min(u_end, ib + sa.units);
-    if (!fused_range<RX, RY, RZ, REF, TMA>(sa, &maps[it], u - ib, e - ib, stage0, bbase, phase_bits))
-      return;
-    u = e;
-    ++it;
-  }
-}
-#undef ITKG_FUSED_PROLOGUE
-
-// ---- dispatch table -----------------------------------------------------------
+using fusedk::Entry;
+using fusedk::FusedItem;
+using fusedk::Fused3DArgs;
 using KernelFn = void (*)(const CUtensorMap, const Fused3DArgs);
 using MultiFn = void (*)(const FusedItem*, const CUtensorMap*, int, int64_t);
 
-struct Entry {
-  int rx, ry, rz;
-  KernelFn fn[2][2];    // [ref][tma]
-  MultiFn multi[2][2];  // [ref][tma]
-  size_t smem;
-  int tx, ty, nt, xa, bw, ih;
-};
+__device__ unsigned int g_fused_fault_word = 0;  // set when a bounded wait gives up
 
-template <int RX, int RY, int RZ>
-Entry make_entry() {
-  using C = Cfg3<RX, RY, RZ>;
-  Entry e{RX, RY, RZ, {}, {}, C::SMEM, C::TX, C::TY, C::NT, C::XA, C::BW, C::IH};
-  e.fn[0][0] = k_fused3d_f32<RX, RY, RZ, false, false>;
-  e.fn[0][1] = k_fused3d_f32<RX, RY, RZ, false, true>;
-  e.fn[1][0] = k_fused3d_f32<RX, RY, RZ, true, false>;
-  e.fn[1][1] = k_fused3d_f32<RX, RY, RZ, true, true>;
-  e.multi[0][0] = k_fused3d_f32_multi<RX, RY, RZ, false, false>;
-  e.multi[0][1] = k_fused3d_f32_multi<RX, RY, RZ, false, true>;
-  e.multi[1][0] = k_fused3d_f32_multi<RX, RY, RZ, true, false>;
-  e.multi[1][1] = k_fused3d_f32_multi<RX, RY, RZ, true, true>;
-  return e;
-}
+#define ITKG_CUDA_ST(call)                                                            \
+  do {                                                                                \
+    const cudaError_t e_ = (call);                                                    \
+    if (e_ != cudaSuccess)                                                            \
+      return set_error(ITKG_ERROR_CUDA, "%s: %s", #call, cudaGetErrorString(e_));     \
+  } while (0)
 
-const Entry kTable[] = {
-    make_entry<1, 1, 1>(), make_entry<2, 2, 2>(), make_entry<3, 3, 3>(), make_entry<4, 4, 4>(),
-    make_entry<5, 5, 5>(), make_entry<6, 6, 6>(), make_entry<7, 7, 7>(), make_entry<8, 8, 8>(),
-    make_entry<7, 7, 2>(),
-};
+#define ITKG_TRY_ST(expr)              \
+  do {                                 \
+    const itkg_status s_ = (expr);     \
+    if (s_ != ITKG_SUCCESS) return s_; \
+  } while (0)
 
-const Entry* find_entry(int rx, int ry, int rz) {
-  for (const Entry& e : kTable)
-    if (e.rx == rx && e.ry == ry && e.rz == rz) return &e;
+const Entry* find_entry(int rx, int ry, int rz, int dtype) {
+  int n = 0;
+  const Entry* t = nullptr;
+  switch (dtype) {
+    case ITKG_F32: t = fused_entries_f32(&n); break;
+    case ITKG_I16: t = fused_entries_i16(&n); break;
+    case ITKG_U8: t = fused_entries_u8(&n); break;
+    case ITKG_BF16: t = fused_entries_bf16(&n); break;
+    case ITKG_F16: t = fused_entries_f16(&n); break;
+    default: return nullptr;
+  }
+  for (int i = 0; i < n; ++i)
+    if (t[i].rx == rx && t[i].ry == ry && t[i].rz == rz) return &t[i];
   return nullptr;
 }
 
 struct Occ {
-  KernelFn fn;
+  const void* fn;
   int dev;
   int blocks;
 };
 std::mutex g_occ_mu;
 std::vector<Occ> g_occ;
+std::vector<unsigned int*> g_fault_addr;  // per device
 
-itkg_status resident_ctas(KernelFn fn, size_t smem, int nt, int* out) {
+itkg_status resident_ctas(const void* fn, size_t smem, int nt, int* out) {
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess) return set_error(ITKG_ERROR_CUDA, "cudaGetDevice failed");
+  ITKG_CUDA_ST(cudaGetDevice(&dev));
   {
     std::lock_guard<std::mutex> lk(g_occ_mu);
     for (const Occ& o : g_occ)
@@ -602,17 +106,29 @@ itkg_status resident_ctas(KernelFn fn, size_t smem, int nt, int* out) {
         return ITKG_SUCCESS;
       }
   }
-  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return set_error(ITKG_ERROR_CUDA, "cudaFuncSetAttribute: %s", cudaGetErrorString(e));
+  ITKG_CUDA_ST(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0, sms = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, nt, smem);
-  if (e != cudaSuccess) return set_error(ITKG_ERROR_CUDA, "occupancy: %s", cudaGetErrorString(e));
-  e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  if (e != cudaSuccess) return set_error(ITKG_ERROR_CUDA, "SM count: %s", cudaGetErrorString(e));
+  ITKG_CUDA_ST(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, nt, smem));
+  ITKG_CUDA_ST(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   const int blocks = std::max(1, per_sm) * sms;
   std::lock_guard<std::mutex> lk(g_occ_mu);
   g_occ.push_back({fn, dev, blocks});
   *out = blocks;
+  return ITKG_SUCCESS;
+}
+
+// Device address of the fault word on the current device.
+itkg_status fault_address(unsigned int** out) {
+  int dev = 0;
+  ITKG_CUDA_ST(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(g_occ_mu);
+  if ((int)g_fault_addr.size() <= dev) g_fault_addr.resize(dev + 1, nullptr);
+  if (!g_fault_addr[dev]) {
+    void* p = nullptr;
+    ITKG_CUDA_ST(cudaGetSymbolAddress(&p, g_fused_fault_word));
+    g_fault_addr[dev] = static_cast<unsigned int*>(p);
+  }
+  *out = g_fault_addr[dev];
   return ITKG_SUCCESS;
 }
 
@@ -632,11 +148,21 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   return fn;
 }
 
+CUtensorMapDataType tma_type(int dtype) {
+  switch (dtype) {
+    case ITKG_I16: return CU_TENSOR_MAP_DATA_TYPE_UINT16;  // raw 16-bit copy
+    case ITKG_U8: return CU_TENSOR_MAP_DATA_TYPE_UINT8;
+    case ITKG_BF16: return CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
+    case ITKG_F16: return CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
+    default: return CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+  }
+}
+
 // TMA applies when the buffer base and pitches are 16-byte multiples and every
-// tile's first column (tx0 - XA, relative to the buffer) is 4-element aligned.
+// tile's first column (tx0 - XA, relative to the buffer) is 16-byte aligned.
 bool tma_ok(const FusedGeom& g, const Entry& e) {
   if (((uintptr_t)g.src & 15) || (g.src_pitch[1] & 15) || (g.src_pitch[2] & 15)) return false;
-  if (((g.req_index[0] - g.src_origin[0]) % 4 + 4) % 4 != 0) return false;
+  if (((g.req_index[0] - g.src_origin[0]) % e.ae + e.ae) % e.ae != 0) return false;
   if (g.src_pitch[1] >= (1ll << 40) || g.src_pitch[2] >= (1ll << 40)) return false;
   return encode_fn() != nullptr;
 }
@@ -667,6 +193,7 @@ itkg_status build_args(const FusedGeom& g, const float* const w[kMaxDim], const 
   a.nty = (int32_t)((g.req_size[1] + e->ty - 1) / e->ty);
   a.units = (int64_t)a.ntx * a.nty * g.req_size[2];
   a.out_dtype = g.out_dtype;
+  ITKG_TRY_ST(fault_address(&a.fault));
   for (int k = 0; k < 2 * e->rx + 1; ++k) a.wx[k] = w[0][k], a.wx2[k] = splat2_host(w[0][k]);
   for (int k = 0; k < 2 * e->ry + 1; ++k) a.wy[k] = w[1][k], a.wy2[k] = splat2_host(w[1][k]);
   for (int k = 0; k < 2 * e->rz + 1; ++k) a.wz[k] = w[2][k], a.wz2[k] = splat2_host(w[2][k]);
@@ -680,46 +207,51 @@ itkg_status build_args(const FusedGeom& g, const float* const w[kMaxDim], const 
     const cuuint64_t strides[2] = {(cuuint64_t)g.src_pitch[1], (cuuint64_t)g.src_pitch[2]};
     const cuuint32_t box[3] = {(cuuint32_t)e->bw, (cuuint32_t)e->ih, 1};
     const cuuint32_t estr[3] = {1, 1, 1};
-    CUresult r = encode_fn()(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<void*>(g.src), dims,
-                             strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-                             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    CUresult r = encode_fn()(&map, tma_type(e->dtype), 3, const_cast<void*>(g.src), dims, strides,
+                             box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                             CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return set_error(ITKG_ERROR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
   }
   return ITKG_SUCCESS;
 }
 
-#define ITKG_CUDA_ST(call)                                                            \
-  do {                                                                                \
-    const cudaError_t e_ = (call);                                                    \
-    if (e_ != cudaSuccess) return set_error(ITKG_ERROR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
-  } while (0)
+const char* kernel_name(int dtype, bool ref, bool tma) {
+  static const char* names[5][2][2] = {
+      {{"fused3d_f32_fma", "fused3d_f32_fma_tma"}, {"fused3d_f32_ref", "fused3d_f32_ref_tma"}},
+      {{"fused3d_i16_fma", "fused3d_i16_fma_tma"}, {"fused3d_i16_ref", "fused3d_i16_ref_tma"}},
+      {{"fused3d_u8_fma", "fused3d_u8_fma_tma"}, {"fused3d_u8_ref", "fused3d_u8_ref_tma"}},
+      {{"fused3d_bf16_fma", "fused3d_bf16_fma_tma"}, {"fused3d_bf16_ref", "fused3d_bf16_ref_tma"}},
+      {{"fused3d_f16_fma", "fused3d_f16_fma_tma"}, {"fused3d_f16_ref", "fused3d_f16_ref_tma"}}};
+  return names[dtype][ref ? 1 : 0][tma ? 1 : 0];
+}
 
-#define ITKG_TRY_ST(expr)                  \
-  do {                                     \
-    const itkg_status s_ = (expr);         \
-    if (s_ != ITKG_SUCCESS) return s_;     \
-  } while (0)
+// Shape checks common to single and multi-request launches.
+bool geometry_ok(const FusedGeom& g) {
+  if (g.dim != 3 || g.comps != 1 || g.out_dtype == ITKG_I16) return false;
+  for (int d = 0; d < 3; ++d)
+    if (!fits_i32(g.lo[d]) || !fits_i32(g.hi[d]) || !fits_i32(g.src_origin[d]) ||
+        !fits_i32(g.dst_origin[d]) || !fits_i32(g.req_index[d] + g.req_size[d]) ||
+        !fits_i32(g.req_index[d] - 64))
+      return false;
+  const int64_t span = (g.hi[0] - g.src_origin[0] + 1) * g.src_pitch[0] +
+                       (g.hi[1] - g.src_origin[1] + 1) * g.src_pitch[1];
+  if (!fits_i32(span)) return false;
+  if (g.src_pitch[0] != dtype_size(g.in_dtype)) return false;
+  return true;
+}
 
 }  // namespace
 
 itkg_status launch_fused(const FusedGeom& g, const float* const w[kMaxDim], void* stream,
                          bool dry_run) {
-  if (g.dim != 3 || g.comps != 1 || g.in_dtype != ITKG_F32) return ITKG_ERROR_UNSUPPORTED;
-  if (g.out_dtype == ITKG_I16) return ITKG_ERROR_UNSUPPORTED;
-  const Entry* e = find_entry(g.radius[0], g.radius[1], g.radius[2]);
+  if (!geometry_ok(g)) return ITKG_ERROR_UNSUPPORTED;
+  const Entry* e = find_entry(g.radius[0], g.radius[1], g.radius[2], g.in_dtype);
   if (!e) return ITKG_ERROR_UNSUPPORTED;
-  // 32-bit in-slice offsets and coordinates
-  for (int d = 0; d < 3; ++d)
-    if (!fits_i32(g.lo[d]) || !fits_i32(g.hi[d]) || !fits_i32(g.src_origin[d]) ||
-        !fits_i32(g.dst_origin[d]) || !fits_i32(g.req_index[d] + g.req_size[d]) ||
-        !fits_i32(g.req_index[d] - 64))
-      return ITKG_ERROR_UNSUPPORTED;
-  const int64_t span = (g.hi[0] - g.src_origin[0] + 1) * g.src_pitch[0] +
-                       (g.hi[1] - g.src_origin[1] + 1) * g.src_pitch[1];
-  if (!fits_i32(span)) return ITKG_ERROR_UNSUPPORTED;
-  if (g.src_pitch[0] != 4) return ITKG_ERROR_UNSUPPORTED;
-  if (((uintptr_t)g.src & 3) || (g.src_pitch[1] & 3) || (g.src_pitch[2] & 3)) return ITKG_ERROR_UNSUPPORTED;
+  if (!tma_ok(g, *e)) {
+    // the cp.async gather handles f32 with 4-byte aligned rows only
+    if (g.in_dtype != ITKG_F32) return ITKG_ERROR_UNSUPPORTED;
+    if (((uintptr_t)g.src & 3) || (g.src_pitch[1] & 3) || (g.src_pitch[2] & 3)) return ITKG_ERROR_UNSUPPORTED;
+  }
   if (dry_run) return ITKG_SUCCESS;
 
   Fused3DArgs a;
@@ -728,15 +260,12 @@ itkg_status launch_fused(const FusedGeom& g, const float* const w[kMaxDim], void
   ITKG_TRY_ST(build_args(g, w, e, &a, &map, &tma));
   const bool ref = g.rounding == ITKG_ROUND_REFERENCE;
   KernelFn fn = e->fn[ref ? 1 : 0][tma ? 1 : 0];
+  if (!fn) return set_error(ITKG_ERROR_UNSUPPORTED, "no fused kernel for this input layout");
   int resident = 0;
-  {
-    const itkg_status st = resident_ctas(fn, e->smem, e->nt, &resident);
-    if (st != ITKG_SUCCESS) return st;
-  }
+  ITKG_TRY_ST(resident_ctas(reinterpret_cast<const void*>(fn), e->smem, e->nt, &resident));
   const int64_t grid = std::min<int64_t>(a.units, resident);
   fn<<<(unsigned)grid, e->nt, e->smem, static_cast<cudaStream_t>(stream)>>>(map, a);
-  note_launch(ref ? (tma ? "fused3d_f32_ref_tma" : "fused3d_f32_ref")
-                  : (tma ? "fused3d_f32_fma_tma" : "fused3d_f32_fma"));
+  note_launch(kernel_name(g.in_dtype, ref, tma));
   cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) return set_error(ITKG_ERROR_CUDA, "fused3d launch: %s", cudaGetErrorString(err));
   return ITKG_SUCCESS;
@@ -763,7 +292,7 @@ itkg_status fused_multi_prepare(const std::vector<FusedGeom>& geoms,
   *out = plan;
   for (size_t i = 0; i < geoms.size(); ++i) {
     const FusedGeom& g = geoms[i];
-    const Entry* e = find_entry(g.radius[0], g.radius[1], g.radius[2]);
+    const Entry* e = find_entry(g.radius[0], g.radius[1], g.radius[2], g.in_dtype);
     if (!e) return set_error(ITKG_ERROR_UNSUPPORTED, "no fused kernel for item %zu", i);
     const float* w[kMaxDim] = {nullptr, nullptr, nullptr};
     for (int d = 0; d < g.dim; ++d) w[d] = weights[i][d].data();
@@ -773,6 +302,8 @@ itkg_status fused_multi_prepare(const std::vector<FusedGeom>& geoms,
     bool tma = false;
     ITKG_TRY_ST(build_args(g, w, e, &item.a, &map, &tma));
     const bool ref = g.rounding == ITKG_ROUND_REFERENCE;
+    if (!e->multi[ref ? 1 : 0][tma ? 1 : 0])
+      return set_error(ITKG_ERROR_UNSUPPORTED, "no fused kernel for item %zu's input layout", i);
     FusedMultiGroup* grp = nullptr;
     for (FusedMultiGroup& q : plan->groups)
       if (q.e == e && q.ref == ref && q.tma == tma) grp = &q;
@@ -797,12 +328,12 @@ itkg_status fused_multi_prepare(const std::vector<FusedGeom>& geoms,
                             cudaMemcpyHostToDevice));
     MultiFn fn = q.e->multi[q.ref ? 1 : 0][q.tma ? 1 : 0];
     int resident = 0;
-    ITKG_TRY_ST(resident_ctas(reinterpret_cast<KernelFn>(fn), q.e->smem, q.e->nt, &resident));
+    ITKG_TRY_ST(resident_ctas(reinterpret_cast<const void*>(fn), q.e->smem, q.e->nt, &resident));
     q.grid = (int)std::min<int64_t>(q.total, resident);
     if (lines)
-      lines->push_back("fused3d multi-request launch: r=(" + std::to_string(q.e->rx) + "," +
-                       std::to_string(q.e->ry) + "," + std::to_string(q.e->rz) + ") " +
-                       (q.ref ? "ref" : "fma") + (q.tma ? " tma" : " gather") + ", " +
+      lines->push_back(std::string(kernel_name(q.e->dtype, q.ref, q.tma)) +
+                       " multi-request launch: r=(" + std::to_string(q.e->rx) + "," +
+                       std::to_string(q.e->ry) + "," + std::to_string(q.e->rz) + "), " +
                        std::to_string(q.items.size()) + " requests, " + std::to_string(q.total) +
                        " units, " + std::to_string(q.grid) + " CTAs");
   }
@@ -814,7 +345,7 @@ itkg_status fused_multi_launch(const FusedMultiPlan* plan, void* stream) {
     MultiFn fn = q.e->multi[q.ref ? 1 : 0][q.tma ? 1 : 0];
     fn<<<q.grid, q.e->nt, q.e->smem, static_cast<cudaStream_t>(stream)>>>(q.d_items, q.d_maps,
                                                                            (int)q.items.size(), q.total);
-    note_launch("fused3d_f32_multi");
+    note_launch("fused3d_multi");
     cudaError_t err = cudaGetLastError();
     if (err != cudaSuccess) return set_error(ITKG_ERROR_CUDA, "fused3d multi launch: %s", cudaGetErrorString(err));
   }
@@ -831,11 +362,11 @@ void fused_multi_free(FusedMultiPlan* plan) {
 }
 
 itkg_status fused_fault_flag(unsigned int* flag, bool clear) {
-  cudaError_t e = cudaMemcpyFromSymbol(flag, g_fused_fault, sizeof(unsigned int));
+  cudaError_t e = cudaMemcpyFromSymbol(flag, g_fused_fault_word, sizeof(unsigned int));
   if (e != cudaSuccess) return set_error(ITKG_ERROR_CUDA, "fault flag: %s", cudaGetErrorString(e));
   if (clear && *flag) {
     const unsigned int zero = 0;
-    e = cudaMemcpyToSymbol(g_fused_fault, &zero, sizeof zero);
+    e = cudaMemcpyToSymbol(g_fused_fault_word, &zero, sizeof zero);
     if (e != cudaSuccess) return set_error(ITKG_ERROR_CUDA, "fault flag: %s", cudaGetErrorString(e));
   }
   return ITKG_SUCCESS;

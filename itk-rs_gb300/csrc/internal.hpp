@@ -158,6 +158,12 @@ int dot_partial_blocks(int64_t n);
 // partials: nblocks doubles of scratch; *out (device) = sum, or += with accumulate.
 itkg_status launch_dot(const DotArgs& d, double* partials, int nblocks, double* out,
                        bool accumulate, void* stream);
+// Squared error against t (DotArgs::q / q_pitch / size): ybar = 2 (y - t) into
+// a dense buffer; *loss_out (+)= sum (y - t)^2, *sigma_out = sum ybar * dy.
+// partials: 2 * nblocks doubles of scratch.  y, dy, ybar dense f32.
+itkg_status launch_sqerr(const float* y, const float* dy, const DotArgs& t, float* ybar,
+                         double* partials, int nblocks, double* loss_out, double* sigma_out,
+                         bool accumulate_loss, void* stream);
 
 // ---- device scratch ---------------------------------------------------------
 // Stream-ordered scratch from a library-owned memory pool of the current

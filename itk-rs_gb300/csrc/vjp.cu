@@ -114,6 +114,42 @@ __global__ void __launch_bounds__(kThreads) k_dot_partials(const DotArgs d, doub
   if (threadIdx.x == 0) partials[blockIdx.x] = red[0];
 }
 
+// Squared-error loss against a target t, per voxel: d = y - t,
+// ybar = 2 d (written densely), and per-block f64 partials of sum d^2 and of
+// sum ybar * dy (the sigma gradient).  partials: [nblocks] loss, [nblocks] sigma.
+__global__ void __launch_bounds__(kThreads) k_sqerr(const float* __restrict__ y,
+                                                     const float* __restrict__ dy, const DotArgs t,
+                                                     float* __restrict__ ybar, double* partials) {
+  const int64_t nx = t.size[0], nxy = t.size[0] * t.size[1];
+  const int64_t n = nxy * t.size[2];
+  double sl = 0.0, ss = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * kThreads + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * kThreads) {
+    const int64_t x = i % nx, yy = (i / nx) % t.size[1], z = i / nxy;
+    const float tv = *reinterpret_cast<const float*>(px(t.q, t.q_pitch, x, yy, z));
+    const float d = y[i] - tv;
+    const float g = 2.0f * d;
+    ybar[i] = g;
+    sl += (double)d * (double)d;
+    ss += (double)g * (double)dy[i];
+  }
+  __shared__ double red[2][kThreads];
+  red[0][threadIdx.x] = sl;
+  red[1][threadIdx.x] = ss;
+  __syncthreads();
+  for (int w = kThreads / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) {
+      red[0][threadIdx.x] += red[0][threadIdx.x + w];
+      red[1][threadIdx.x] += red[1][threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x] = red[0][0];
+    partials[gridDim.x + blockIdx.x] = red[1][0];
+  }
+}
+
 // Fixed-order final sum of the partials (deterministic).
 __global__ void k_sum_partials(const double* partials, int n, double* out, int accumulate) {
   __shared__ double red[kThreads];
@@ -172,6 +208,19 @@ itkg_status launch_dual_axis(const VjpAxisArgs& a, const float* w, const float* 
 int dot_partial_blocks(int64_t n) {
   const int64_t b = (n + kThreads * 8 - 1) / (kThreads * 8);
   return (int)(b < 1 ? 1 : (b > 2048 ? 2048 : b));
+}
+
+itkg_status launch_sqerr(const float* y, const float* dy, const DotArgs& t, float* ybar,
+                         double* partials, int nblocks, double* loss_out, double* sigma_out,
+                         bool accumulate_loss, void* stream) {
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  k_sqerr<<<nblocks, kThreads, 0, s>>>(y, dy, t, ybar, partials);
+  itkg_status st = launched("sqerr_partials_f64");
+  if (st != ITKG_SUCCESS) return st;
+  k_sum_partials<<<1, kThreads, 0, s>>>(partials, nblocks, loss_out, accumulate_loss ? 1 : 0);
+  if ((st = launched("sum_partials_f64")) != ITKG_SUCCESS) return st;
+  k_sum_partials<<<1, kThreads, 0, s>>>(partials + nblocks, nblocks, sigma_out, 0);
+  return launched("sum_partials_f64");
 }
 
 itkg_status launch_dot(const DotArgs& d, double* partials, int nblocks, double* out,

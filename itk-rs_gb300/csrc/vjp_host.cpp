@@ -90,7 +90,7 @@ struct Scratch {
     out->components = 1;
     out->location = ITKG_DEVICE;
     out->region = like.region;
-    dense_layout(out, 16);
+    dense_layout(out, 1);  // fully dense: the loss kernel indexes it linearly
     void* p = nullptr;
     ITKG_TRY(scratch_alloc(&p, image_bytes(*out), s));
     ptrs.push_back(p);
@@ -191,6 +191,57 @@ DotArgs dot_args(const itkg_image& p, const itkg_image& q) {
 }  // namespace itkg
 
 using namespace itkg;
+
+extern "C" itkg_status itkg_gaussian_scale_stack_loss_vjp(
+    const itkg_image* x, const itkg_image* target, const double* sigmas, int32_t nlevels,
+    itkg_image* xbar, double* loss, double* sigma_bar, int32_t flags, void* stream) {
+  ITKG_TRY(check_f32_device(x, "x", 0));
+  ITKG_TRY(check_f32_device(target, "target", x->dim));
+  if (!same_size(*x, *target)) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "x and target regions differ");
+  if (xbar) {
+    ITKG_TRY(check_f32_device(xbar, "xbar", x->dim));
+    if (!same_size(*x, *xbar)) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "x and xbar regions differ");
+  }
+  if (!sigmas || nlevels < 1) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "need nlevels >= 1 sigmas");
+  if (flags & ~ITKG_VJP_SIGMA_BAR_ON_DEVICE)
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "unknown flags 0x%x", flags);
+  std::vector<AxisCoeffs> coeffs((size_t)nlevels * kMaxDim);
+  for (int l = 0; l < nlevels; ++l) ITKG_TRY(coeffs_for(*x, sigmas[l], &coeffs[(size_t)l * kMaxDim]));
+  const int64_t n = (int64_t)region_len(x->region, x->dim);
+  if (n == 0) return ITKG_SUCCESS;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  Scratch sc(s);
+  itkg_image y, dy, yb;
+  ITKG_TRY(sc.image(*x, &y));
+  ITKG_TRY(sc.image(*x, &dy));
+  ITKG_TRY(sc.image(*x, &yb));
+  const int nb = dot_partial_blocks(n);
+  void* part = nullptr;
+  ITKG_TRY(sc.raw(sizeof(double) * (2 * nb + 1 + nlevels), &part));
+  double* partials = static_cast<double*>(part);
+  double* dloss = partials + 2 * nb;
+  double* dsig = dloss + 1;
+  const bool on_dev = flags & ITKG_VJP_SIGMA_BAR_ON_DEVICE;
+  for (int l = 0; l < nlevels; ++l) {
+    const AxisCoeffs* c = &coeffs[(size_t)l * kMaxDim];
+    ITKG_TRY(dual_chain(*x, c, &y, &dy, sc));  // y_l and dy_l/dsigma_l, recomputed
+    DotArgs t = dot_args(y, *target);          // q = target
+    ITKG_TRY(launch_sqerr(static_cast<const float*>(y.data), static_cast<const float*>(dy.data), t,
+                          static_cast<float*>(yb.data), partials, nb, dloss,
+                          on_dev && sigma_bar ? sigma_bar + l : dsig + l, l > 0, s));
+    if (xbar) ITKG_TRY(adjoint_chain(yb, c, xbar, l > 0, sc));
+  }
+  if (loss || (sigma_bar && !on_dev)) {
+    std::vector<double> h(1 + nlevels);
+    ITKG_CUDA(cudaMemcpyAsync(h.data(), dloss, sizeof(double) * (1 + nlevels), cudaMemcpyDeviceToHost, s));
+    ITKG_CUDA(cudaStreamSynchronize(s));
+    if (loss) *loss = h[0];
+    if (sigma_bar && !on_dev)
+      for (int l = 0; l < nlevels; ++l) sigma_bar[l] = h[1 + l];
+  }
+  set_last_kernel("scale_stack_loss_vjp_per_axis_f32");
+  return ITKG_SUCCESS;
+}
 
 extern "C" itkg_status itkg_gaussian_vjp(const itkg_image* x, const itkg_image* ybar,
                                          const itkg_gaussian_params* params, itkg_image* xbar,

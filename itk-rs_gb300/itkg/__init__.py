@@ -427,6 +427,21 @@ def vjp(x: DeviceImage, ybar: DeviceImage, sigma: float, xbar: DeviceImage | Non
     return xbar, (sb.value if want_sigma else None)
 
 
+def scale_stack_loss_vjp(x: DeviceImage, target: DeviceImage, sigmas, xbar: DeviceImage | None = None,
+                         stream: Stream = _DEFAULT_STREAM):
+    """L = sum_l |G_{sigma_l} x - target|^2 with dL/dx and dL/dsigma_l: (loss, xbar, [sigma_bar])."""
+    n = len(sigmas)
+    if xbar is None:
+        xbar = DeviceImage(x.region, F32, 1, x.spacing, x.origin)
+    sg = (ctypes.c_double * n)(*[float(s) for s in sigmas])
+    sb = (ctypes.c_double * n)()
+    loss = ctypes.c_double(0.0)
+    check(lib().itkg_gaussian_scale_stack_loss_vjp(ctypes.byref(x.c), ctypes.byref(target.c), sg, n,
+                                                   ctypes.byref(xbar.c), ctypes.byref(loss), sb, 0,
+                                                   stream.ptr))
+    return loss.value, xbar, list(sb)
+
+
 class Batch:
     """itkg_batch: many forward / VJP requests planned once, replayed as a CUDA graph."""
 

@@ -94,6 +94,9 @@ SIGNATURES = {
     "itkg_stream_full": (st, [I, R, G, ctypes.c_uint64, I, P]),
     "itkg_gaussian_generate_region_noalloc": (st, [I, R, R, G, I, P]),
     "itkg_gaussian_vjp": (st, [I, I, G, I, ctypes.POINTER(ctypes.c_double), ctypes.c_int32, P]),
+    "itkg_gaussian_scale_stack_loss_vjp": (st, [I, I, ctypes.POINTER(ctypes.c_double), ctypes.c_int32,
+                                                I, ctypes.POINTER(ctypes.c_double),
+                                                ctypes.POINTER(ctypes.c_double), ctypes.c_int32, P]),
     "itkg_batch_create": (st, [ctypes.POINTER(ctypes.c_void_p)]),
     "itkg_batch_destroy": (st, [P]),
     "itkg_batch_add": (st, [P, I, R, R, G, I]),

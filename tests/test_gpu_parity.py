@@ -326,3 +326,44 @@ def test_fused3d_tma_and_gather_paths_agree(gpu, rounding):
     flag = ctypes.c_uint32(1)
     _abi.check(L.itkg_device_fault(1, ctypes.byref(flag)))
     assert flag.value == 0
+
+
+def _typed_input(kind, shape, rng):
+    """Input of the given storage type and its exact f32 value."""
+    if kind == "i16":
+        a = rng.integers(-1000, 1500, shape).astype(np.int16)
+        return a, a.astype(np.float32)
+    if kind == "u8":
+        a = rng.integers(0, 256, shape).astype(np.uint8)
+        return a, a.astype(np.float32)
+    if kind == "f16":
+        a = (rng.standard_normal(shape) * 100).astype(np.float16)
+        return a, a.astype(np.float32)
+    # bf16: build from f32 with the low 16 bits cleared (exactly representable)
+    f = (rng.standard_normal(shape) * 100).astype(np.float32)
+    bits = (f.view(np.uint32) & 0xFFFF0000).astype(np.uint32)
+    return (bits >> 16).astype(np.uint16), bits.view(np.float32)
+
+
+@pytest.mark.parametrize("kind", ["i16", "u8", "bf16", "f16"])
+@pytest.mark.parametrize("sigma,spacing", [(1.5, (0.7, 0.7, 2.5)), (1.0, None), (2.0, None)])
+def test_fused3d_native_inputs(gpu, kind, sigma, spacing):
+    """Fused kernel reading i16 / u8 / bf16 / f16 directly (the cast fused into
+    the load): bit-exact in reference rounding, 1e-5 in FMA rounding."""
+    import ctypes
+    from itkg import _abi
+    rng = np.random.default_rng(41)
+    raw, f32 = _typed_input(kind, (22, 40, 56), rng)
+    want = oracle.gaussian_f32(f32, sigma, spacing=spacing)
+    code = {"i16": gpu.I16, "u8": gpu.U8, "bf16": gpu.BF16, "f16": gpu.F16}[kind]
+    img = gpu.Image(raw, spacing=spacing, bf16=(kind == "bf16"))
+    dev = gpu.DeviceImage.from_host(img)
+    for rounding in (gpu.ROUND_REFERENCE, gpu.ROUND_FMA):
+        f = gpu.GaussianFilter(gpu.CastFilter(dev, gpu.F32), sigma, rounding=rounding,
+                               algorithm=gpu.ALGO_FUSED, arithmetic=gpu.ARITH_F32)
+        got = f.generate_region(dev.region).download()
+        assert gpu.last_kernel().startswith(f"fused3d_{kind}"), gpu.last_kernel()
+        if rounding == gpu.ROUND_REFERENCE:
+            assert bits_equal(got, want)
+        else:
+            assert normwise(got, want) <= 1e-5

@@ -82,6 +82,36 @@ def test_accumulate_flags(gpu):
     assert abs(sb2 - (sb + 2.5)) < 1e-9 * max(1.0, abs(sb))
 
 
+@pytest.mark.parametrize("shape", [(20, 18, 22), (9, 30, 7)])
+def test_scale_stack_loss_vjp_matches_fp64(gpu, shape):
+    """L = sum_l |G_l x - t|^2 over sigmas {1, 2, 4}: loss, dL/dx, dL/dsigma_l
+    against FP64 numpy, and dL/dsigma_l against central differences."""
+    rng = np.random.default_rng(sum(shape))
+    x = rng.random(shape).astype(np.float32)
+    t = rng.random(shape).astype(np.float32)
+    sigmas = [1.0, 2.0, 4.0]
+    loss, xbar, sb = gpu.scale_stack_loss_vjp(_dev(gpu, x), _dev(gpu, t), sigmas)
+    x64, t64 = x.astype(np.float64), t.astype(np.float64)
+    want_loss, want_x, want_s = 0.0, np.zeros(shape), []
+    for s in sigmas:
+        radii = _radii(s, None, 3)
+        y = oracle.gaussian_whole_f64(x64, s, radii=radii)
+        d = y - t64
+        want_loss += float((d * d).sum())
+        want_x += oracle.gaussian_adjoint_f64(2 * d, s, radii=radii)
+        want_s.append(float((2 * d * oracle.gaussian_dsigma_f64(x64, s, radii=radii)).sum()))
+        h = 1e-3
+        lp = ((oracle.gaussian_whole_f64(x64, s + h, radii=radii) - t64) ** 2).sum()
+        lm = ((oracle.gaussian_whole_f64(x64, s - h, radii=radii) - t64) ** 2).sum()
+        fd = (lp - lm) / (2 * h)
+        assert abs(want_s[-1] - fd) <= 1e-5 * max(1.0, abs(fd))
+    assert abs(loss - want_loss) <= 1e-5 * want_loss
+    got_x = xbar.download().astype(np.float64)
+    assert np.abs(got_x - want_x).max() <= 1e-5 * np.abs(want_x).max()
+    for g, w in zip(sb, want_s):
+        assert abs(g - w) <= 1e-4 * max(1.0, abs(w)), (sb, want_s)
+
+
 def test_vjp_rejects_bad_sigma(gpu):
     from itkg import _abi
     x = _dev(gpu, np.zeros((4, 5, 6), np.float32))
