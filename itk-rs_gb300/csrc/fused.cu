@@ -271,6 +271,47 @@ itkg_status launch_fused(const FusedGeom& g, const float* const w[kMaxDim], void
   return ITKG_SUCCESS;
 }
 
+itkg_status launch_fused_vjp(int mode, const FusedGeom& g, const float* const w[kMaxDim],
+                             const float* const prefix[kMaxDim], const void* ybar,
+                             const int64_t* ybar_pitch, const int64_t* ybar_origin, double* partials,
+                             int* grid_out, bool accumulate, void* stream, bool dry_run) {
+  if (!geometry_ok(g) || g.in_dtype != ITKG_F32 || g.out_dtype != ITKG_F32) return ITKG_ERROR_UNSUPPORTED;
+  const Entry* e = find_entry(g.radius[0], g.radius[1], g.radius[2], ITKG_F32);
+  if (!e || !e->vjp[mode == fusedk::kAdj ? 1 : 0] || !tma_ok(g, *e)) return ITKG_ERROR_UNSUPPORTED;
+  KernelFn fn = e->vjp[mode == fusedk::kAdj ? 1 : 0];
+  int resident = 0;
+  ITKG_TRY_ST(resident_ctas(reinterpret_cast<const void*>(fn), e->smem, e->nt, &resident));
+  const int64_t units = ((g.req_size[0] + e->tx - 1) / e->tx) * ((g.req_size[1] + e->ty - 1) / e->ty) *
+                        g.req_size[2];
+  if (grid_out) *grid_out = (int)std::min<int64_t>(units, resident);
+  if (dry_run) return ITKG_SUCCESS;
+  Fused3DArgs a;
+  CUtensorMap map;
+  bool tma = false;
+  ITKG_TRY_ST(build_args(g, w, e, &a, &map, &tma));
+  if (!tma) return set_error(ITKG_ERROR_UNSUPPORTED, "fused VJP needs TMA-aligned buffers");
+  a.ybar = static_cast<const char*>(ybar);
+  for (int d = 0; d < 3; ++d) {
+    a.ybar_pitch[d] = ybar_pitch ? ybar_pitch[d] : 0;
+    a.ybar_origin[d] = ybar_origin ? (int32_t)ybar_origin[d] : 0;
+  }
+  a.accumulate = accumulate ? 1 : 0;
+  a.partials = partials;
+  if (prefix)
+    for (int d = 0; d < 3; ++d) {
+      float* P = d == 0 ? a.px : (d == 1 ? a.py : a.pz);
+      for (int k = 0; k < 2 * g.radius[d] + 1; ++k) P[k] = prefix[d][k];
+    }
+  // every CTA writes its partial, so the grid is the resident count (or fewer units)
+  const int64_t grid = std::min<int64_t>(a.units, resident);
+  if (grid_out) *grid_out = (int)grid;
+  fn<<<(unsigned)grid, e->nt, e->smem, static_cast<cudaStream_t>(stream)>>>(map, a);
+  note_launch(mode == fusedk::kAdj ? "fused3d_adjoint_f32" : "fused3d_dot_f32");
+  cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess) return set_error(ITKG_ERROR_CUDA, "fused3d VJP launch: %s", cudaGetErrorString(err));
+  return ITKG_SUCCESS;
+}
+
 struct FusedMultiGroup {
   const Entry* e;
   bool ref, tma;

@@ -24,6 +24,15 @@ namespace fusedk {
 constexpr int kMaxFusedR = 12;
 constexpr int kMaxFusedK = 2 * kMaxFusedR + 1;
 
+// What a fused launch computes.
+//   kFwd  y = G x stored (or converted) into dst;
+//   kDot  <ybar, G x> summed per CTA into partials[blockIdx.x] (nothing stored;
+//         with derivative weights on one axis this is one term of dL/dsigma);
+//   kAdj  dst (+)= G^T x for the whole image: the halo outside the image is
+//         zero (not replicated) and the edge outputs of every pass add the
+//         clamped taps back, sum_{d<r} P[r-1-d] v[edge -/+ d] (P = prefix sums
+//         of the weights).
+enum FusedMode { kFwd = 0, kDot = 1, kAdj = 2 };
 
 struct Fused3DArgs {
   const char* src;
@@ -41,12 +50,21 @@ struct Fused3DArgs {
   int32_t out_dtype;
   int32_t pad_;
   unsigned int* fault;  // device fault word, set when a bounded wait gives up
+  // kDot: ybar (f32) at the output positions, and one f64 partial per CTA
+  const char* ybar;
+  int64_t ybar_pitch[3];
+  int32_t ybar_origin[3];
+  int32_t accumulate;  // kAdj: dst += result
+  double* partials;
   float wx[kMaxFusedK];
   float wy[kMaxFusedK];
   float wz[kMaxFusedK];
   f2_t wx2[kMaxFusedK];  // {w, w} pairs for the packed passes
   f2_t wy2[kMaxFusedK];
   f2_t wz2[kMaxFusedK];
+  float px[kMaxFusedK];  // kAdj: prefix sums of the weights
+  float py[kMaxFusedK];
+  float pz[kMaxFusedK];
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -162,9 +180,9 @@ __device__ __forceinline__ void load4(const __half* p, float* v) {
 // then hand back the completed slot (P + 1) mod KZ and clear it.
 template <int P, int KZ, int MY2, bool REF>
 __device__ __forceinline__ void push_phase(f2_t (&acc)[MY2][KZ], const f2_t (&yv)[MY2],
-                                           const Fused3DArgs& a, f2_t (&done)[MY2]) {
+                                           const Fused3DArgs& a, f2_t (&done)[MY2], bool push) {
 #pragma unroll
-  for (int k = 0; k < KZ; ++k) {
+  for (int k = 0; k < KZ && push; ++k) {
     const int slot = (P - k + KZ) % KZ;
 #pragma unroll
     for (int m = 0; m < MY2; ++m) {
@@ -188,13 +206,13 @@ __device__ __forceinline__ void push_phase(f2_t (&acc)[MY2][KZ], const f2_t (&yv
 
 #define ITKG_PUSH_CASE(N)                                                   \
   case N:                                                                   \
-    if constexpr (N < KZ) push_phase<N, KZ, MY2, REF>(acc, yv, a, done);    \
+    if constexpr (N < KZ) push_phase<N, KZ, MY2, REF>(acc, yv, a, done, do_push);    \
     break;
 
 // The fused filter over units [u_begin, u_end) of one request `a` (a unit is
 // one output slice of one (x, y) tile).  Returns false if a bounded wait gave
 // up (the device fault word is then set).
-template <int RX, int RY, int RZ, bool REF, bool TMA, typename Tin>
+template <int RX, int RY, int RZ, bool REF, bool TMA, typename Tin, int MODE = kFwd>
 __device__ __forceinline__ bool fused_range(const Fused3DArgs& a, const CUtensorMap* tmap,
                                             int64_t u_begin, int64_t u_end, unsigned char* const stage0,
                                             uint32_t bbase, uint32_t& phase_bits) {
@@ -207,6 +225,7 @@ __device__ __forceinline__ bool fused_range(const Fused3DArgs& a, const CUtensor
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nzr = a.req_hi[2] - a.req_lo[2] + 1;
   const uint32_t sbase = smem_u32(stage0);
+  double dot_acc = 0.0;  // kDot: this thread's share of <ybar, G x>
 
   for (int64_t u = u_begin; u < u_end;) {
     const int64_t tile = u / nzr;
@@ -219,6 +238,11 @@ __device__ __forceinline__ bool fused_range(const Fused3DArgs& a, const CUtensor
     const int ty0 = a.req_lo[1] + (int)(tile / a.ntx) * TY;
     const int gx0 = tx0 - XA, gy0 = ty0 - RY;  // image coords of stage element (0, 0)
     const bool edge = gx0 < a.lo[0] || gx0 + BW - 1 > a.hi[0] || gy0 < a.lo[1] || gy0 + IH - 1 > a.hi[1];
+    // kAdj: does this tile hold an edge column / row of the image?
+    const bool xedge = (a.lo[0] >= tx0 && a.lo[0] < tx0 + TX) || (a.hi[0] >= tx0 && a.hi[0] < tx0 + TX);
+    const bool yedge = (a.lo[1] >= ty0 && a.lo[1] < ty0 + TY) || (a.hi[1] >= ty0 && a.hi[1] < ty0 + TY);
+    (void)xedge;
+    (void)yedge;
 
     // cp.async path: gather offsets of this thread's share (clamped x, y).
     int32_t goff[TMA ? 1 : NLD];
@@ -268,6 +292,9 @@ __device__ __forceinline__ bool fused_range(const Fused3DArgs& a, const CUtensor
     f2_t yv[MY2];
 #pragma unroll
     for (int m = 0; m < MY2; ++m) yv[m] = 0ull;
+    f2_t acc_lo[MY2], acc_hi[MY2];  // kAdj: z-edge folds of outputs lo and hi
+#pragma unroll
+    for (int m = 0; m < MY2; ++m) acc_lo[m] = acc_hi[m] = 0ull;
 
     // Output addressing for this thread's column and rows.
     const int col_x = tx0 + lane;
@@ -287,7 +314,7 @@ __device__ __forceinline__ bool fused_range(const Fused3DArgs& a, const CUtensor
         const bool ok = mbar_wait(bbase + 8 * st, (phase_bits >> st) & 1u);
         phase_bits ^= 1u << st;
         if (!ok) return false;
-        if (edge) {
+        if (MODE != kAdj && edge) {
           // Replicate the image's edge values into the halo: first the
           // columns left of lo / right of hi (nl, nr of them), then whole
           // rows above / below (nt, nb of them).  Sources are in-image
@@ -345,6 +372,20 @@ __device__ __forceinline__ bool fused_range(const Fused3DArgs& a, const CUtensor
               ax = fma2((q & 1) ? O[(q - 1) / 2] : E[q / 2], a.wx2[k], ax);
             }
             unpack2(ax, o[2 * m], o[2 * m + 1]);
+          }
+          if constexpr (MODE == kAdj) {
+            if (xedge) {  // the taps the forward clamped onto the edge columns
+#pragma unroll
+              for (int m = 0; m < MX; ++m) {
+                const int X = tx0 + x0 + m;
+                if (X == a.lo[0])
+#pragma unroll
+                  for (int d = 0; d < RX; ++d) o[m] = fmaf(a.px[RX - 1 - d], v[m + RX + d + OFF], o[m]);
+                if (X == a.hi[0])
+#pragma unroll
+                  for (int d = 0; d < RX; ++d) o[m] = fmaf(a.px[RX - 1 - d], v[m + RX - d + OFF], o[m]);
+              }
+            }
           }
         }
         float4* dst4 = reinterpret_cast<float4*>(xbuf + row * TX + x0);
@@ -436,9 +477,42 @@ __device__ __forceinline__ bool fused_range(const Fused3DArgs& a, const CUtensor
             }
             yv[m] = ay;
           }
+          if constexpr (MODE == kAdj) {
+            if (yedge) {  // the taps the forward clamped onto the edge rows
+              float yl[MY];
+#pragma unroll
+              for (int m = 0; m < MY2; ++m) unpack2(yv[m], yl[2 * m], yl[2 * m + 1]);
+#pragma unroll
+              for (int m = 0; m < MY; ++m) {
+                const int Y = ty0 + warp * MY + m;
+                if (Y == a.lo[1])
+#pragma unroll
+                  for (int d = 0; d < RY; ++d) yl[m] = fmaf(a.py[RY - 1 - d], w[m + RY + d], yl[m]);
+                if (Y == a.hi[1])
+#pragma unroll
+                  for (int d = 0; d < RY; ++d) yl[m] = fmaf(a.py[RY - 1 - d], w[m + RY - d], yl[m]);
+              }
+#pragma unroll
+              for (int m = 0; m < MY2; ++m) yv[m] = pack2(yl[2 * m], yl[2 * m + 1]);
+            }
+          }
         }
       }
       // ---- z pass: push slice j into the ring, pop output z = j - RZ ----
+      const bool do_push = MODE != kAdj || (j >= a.lo[2] && j <= a.hi[2]);
+      if constexpr (MODE == kAdj) {
+        const int dl = j - a.lo[2], dh = a.hi[2] - j;
+        if (dl >= 0 && dl < RZ) {
+          const f2_t wp = pack2(a.pz[RZ - 1 - dl], a.pz[RZ - 1 - dl]);
+#pragma unroll
+          for (int m = 0; m < MY2; ++m) acc_lo[m] = fma2(yv[m], wp, acc_lo[m]);
+        }
+        if (dh >= 0 && dh < RZ) {
+          const f2_t wp = pack2(a.pz[RZ - 1 - dh], a.pz[RZ - 1 - dh]);
+#pragma unroll
+          for (int m = 0; m < MY2; ++m) acc_hi[m] = fma2(yv[m], wp, acc_hi[m]);
+        }
+      }
       f2_t done[MY2];
       switch (p) {
         ITKG_PUSH_CASE(0) ITKG_PUSH_CASE(1) ITKG_PUSH_CASE(2) ITKG_PUSH_CASE(3)
@@ -453,10 +527,36 @@ __device__ __forceinline__ bool fused_range(const Fused3DArgs& a, const CUtensor
       p = p + 1 == KZ ? 0 : p + 1;
       const int z = j - RZ;
       if (z >= z0 && col_ok) {
-        char* orow = obase + (int64_t)(z - a.dst_origin[2]) * a.dst_pitch[2];
+        if constexpr (MODE == kAdj) {
+          if (z == a.lo[2])
+#pragma unroll
+            for (int m = 0; m < MY2; ++m) done[m] = add2(done[m], acc_lo[m]);
+          if (z == a.hi[2])
+#pragma unroll
+            for (int m = 0; m < MY2; ++m) done[m] = add2(done[m], acc_hi[m]);
+        }
         float vals[MY];
 #pragma unroll
         for (int m = 0; m < MY2; ++m) unpack2(done[m], vals[2 * m], vals[2 * m + 1]);
+        if constexpr (MODE == kDot) {
+          const char* yrow = a.ybar + (int64_t)(col_x - a.ybar_origin[0]) * a.ybar_pitch[0] +
+                             (int64_t)(row_y0 - a.ybar_origin[1]) * a.ybar_pitch[1] +
+                             (int64_t)(z - a.ybar_origin[2]) * a.ybar_pitch[2];
+          float sl = 0.0f;
+#pragma unroll
+          for (int m = 0; m < MY; ++m)
+            if (m < nrows_ok) sl = fmaf(vals[m], *reinterpret_cast<const float*>(yrow + m * a.ybar_pitch[1]), sl);
+          dot_acc += (double)sl;
+        } else if constexpr (MODE == kAdj) {
+          char* orow = obase + (int64_t)(z - a.dst_origin[2]) * a.dst_pitch[2];
+#pragma unroll
+          for (int m = 0; m < MY; ++m)
+            if (m < nrows_ok) {
+              float* q = reinterpret_cast<float*>(orow + m * opy);
+              *q = a.accumulate ? *q + vals[m] : vals[m];
+            }
+        } else {
+        char* orow = obase + (int64_t)(z - a.dst_origin[2]) * a.dst_pitch[2];
         if (a.out_dtype == ITKG_F32) {
 #pragma unroll
           for (int m = 0; m < MY; ++m)
@@ -471,12 +571,25 @@ __device__ __forceinline__ bool fused_range(const Fused3DArgs& a, const CUtensor
             else *reinterpret_cast<uint8_t*>(q) = from_f32<uint8_t>(vals[m]);
           }
         }
+        }
       }
     }
     if constexpr (!TMA) cp_async_wait<0>();
     __syncthreads();
   }
 #undef ITKG_ON_TIMEOUT
+  if constexpr (MODE == kDot) {
+    // block sum of dot_acc -> partials[blockIdx.x] (fixed order)
+    __shared__ double red[NT / 32];
+    for (int off = 16; off > 0; off >>= 1) dot_acc += __shfl_down_sync(0xffffffffu, dot_acc, off);
+    if (lane == 0) red[warp] = dot_acc;
+    __syncthreads();
+    if (tid == 0) {
+      double t = 0.0;
+      for (int w = 0; w < NT / 32; ++w) t += red[w];
+      a.partials[blockIdx.x] = t;
+    }
+  }
   return true;
 }
 
@@ -507,6 +620,18 @@ __global__ void __launch_bounds__(Cfg3<RX, RY, RZ, Tin>::NT, Cfg3<RX, RY, RZ, Ti
   fused_range<RX, RY, RZ, REF, TMA, Tin>(a, &tmap, u_begin, u_end, stage0, bbase, phase_bits);
 }
 
+// VJP launches (f32 input, TMA tile loads, FMA rounding): kDot or kAdj.
+template <int RX, int RY, int RZ, int MODE>
+__global__ void __launch_bounds__(Cfg3<RX, RY, RZ, float>::NT, Cfg3<RX, RY, RZ, float>::MINB)
+    k_fused3d_vjp(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ Fused3DArgs a) {
+  using Tin = float;
+  constexpr bool TMA = true;
+  ITKG_FUSED_PROLOGUE
+  const int64_t u_begin = a.units * blockIdx.x / gridDim.x;
+  const int64_t u_end = a.units * (blockIdx.x + 1) / gridDim.x;
+  fused_range<RX, RY, RZ, false, true, float, MODE>(a, &tmap, u_begin, u_end, stage0, bbase, phase_bits);
+}
+
 // One request of a multi-request launch; its units are [unit_begin, unit_begin + a.units).
 struct FusedItem {
   Fused3DArgs a;
@@ -518,6 +643,7 @@ struct Entry {
   int rx, ry, rz, dtype;
   void (*fn[2][2])(const CUtensorMap, const Fused3DArgs);  // [ref][tma]
   void (*multi[2][2])(const FusedItem*, const CUtensorMap*, int, int64_t);
+  void (*vjp[2])(const CUtensorMap, const Fused3DArgs);  // [0] kDot, [1] kAdj (f32 only)
   size_t smem;
   int tx, ty, nt, xa, bw, ih, ae;
 };
@@ -569,7 +695,7 @@ template <> constexpr int dtype_of<__half>() { return ITKG_F16; }
 template <int RX, int RY, int RZ, typename Tin>
 Entry make_entry() {
   using C = Cfg3<RX, RY, RZ, Tin>;
-  Entry e{RX, RY, RZ, dtype_of<Tin>(), {}, {}, C::SMEM, C::TX, C::TY, C::NT, C::XA, C::BW, C::IH, C::AE};
+  Entry e{RX, RY, RZ, dtype_of<Tin>(), {}, {}, {}, C::SMEM, C::TX, C::TY, C::NT, C::XA, C::BW, C::IH, C::AE};
   e.fn[0][1] = k_fused3d<RX, RY, RZ, false, true, Tin>;
   e.fn[1][1] = k_fused3d<RX, RY, RZ, true, true, Tin>;
   e.multi[0][1] = k_fused3d_multi<RX, RY, RZ, false, true, Tin>;
@@ -579,6 +705,9 @@ Entry make_entry() {
     e.fn[1][0] = k_fused3d<RX, RY, RZ, true, false, Tin>;
     e.multi[0][0] = k_fused3d_multi<RX, RY, RZ, false, false, Tin>;
     e.multi[1][0] = k_fused3d_multi<RX, RY, RZ, true, false, Tin>;
+    e.vjp[0] = k_fused3d_vjp<RX, RY, RZ, kDot>;
+    // the adjoint's edge-fold registers spill beyond radius 6: per-axis there
+    if constexpr (RX <= 6 && RY <= 6 && RZ <= 6) e.vjp[1] = k_fused3d_vjp<RX, RY, RZ, kAdj>;
   }
   return e;
 }

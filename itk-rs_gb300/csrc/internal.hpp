@@ -119,6 +119,18 @@ itkg_status fused_multi_prepare(const std::vector<FusedGeom>& geoms,
 itkg_status fused_multi_launch(const FusedMultiPlan* plan, void* stream);
 void fused_multi_free(FusedMultiPlan* plan);
 
+// fused.cu: VJP launches over a whole 3-D f32 image (FMA rounding, TMA only).
+//   mode 1 (dot): partials[cta] = per-CTA sums of <ybar, G x> with the weights
+//                 given (derivative weights on one axis give one term of
+//                 dL/dsigma); *grid_out = number of partials written;
+//   mode 2 (adjoint): dst (+)= G^T src with prefix sums `prefix` for the folds.
+// ITKG_ERROR_UNSUPPORTED (no error set) when no fused kernel applies; dry_run
+// only checks (and reports the grid).
+itkg_status launch_fused_vjp(int mode, const FusedGeom& g, const float* const w[kMaxDim],
+                             const float* const prefix[kMaxDim], const void* ybar,
+                             const int64_t* ybar_pitch, const int64_t* ybar_origin, double* partials,
+                             int* grid_out, bool accumulate, void* stream, bool dry_run);
+
 // Bumps the launch counter by n (graph replays).
 void note_launches(uint64_t n, const char* name);
 
@@ -158,6 +170,9 @@ int dot_partial_blocks(int64_t n);
 // partials: nblocks doubles of scratch; *out (device) = sum, or += with accumulate.
 itkg_status launch_dot(const DotArgs& d, double* partials, int nblocks, double* out,
                        bool accumulate, void* stream);
+// *out (+)= sum of n f64 partials, in a fixed order.
+itkg_status launch_sum_partials(const double* partials, int n, double* out, bool accumulate,
+                                void* stream);
 // Squared error against t (DotArgs::q / q_pitch / size): ybar = 2 (y - t) into
 // a dense buffer; *loss_out (+)= sum (y - t)^2, *sigma_out = sum ybar * dy.
 // partials: 2 * nblocks doubles of scratch.  y, dy, ybar dense f32.

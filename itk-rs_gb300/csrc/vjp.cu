@@ -223,6 +223,13 @@ itkg_status launch_sqerr(const float* y, const float* dy, const DotArgs& t, floa
   return launched("sum_partials_f64");
 }
 
+itkg_status launch_sum_partials(const double* partials, int n, double* out, bool accumulate,
+                                void* stream) {
+  k_sum_partials<<<1, kThreads, 0, static_cast<cudaStream_t>(stream)>>>(partials, n, out,
+                                                                        accumulate ? 1 : 0);
+  return launched("sum_partials_f64");
+}
+
 itkg_status launch_dot(const DotArgs& d, double* partials, int nblocks, double* out,
                        bool accumulate, void* stream) {
   cudaStream_t s = static_cast<cudaStream_t>(stream);

@@ -7,8 +7,10 @@
 //   w_i = g_i / S,  S = sum g,
 //   dw_i/dsigma = (g_i' S - g_i S') / S^2 / spacing,  g_i' = g_i t_i^2 / s,
 //   P_m = w_0 + ... + w_m  (adjoint edge folds).
-// The per-axis passes run on f32 buffers from the stream-ordered scratch pool;
-// the fused whole-filter kernels (fused_vjp.cu) take over where they apply.
+// 3-D requests run as fused whole-filter launches where a kernel applies
+// (fused.cu: one adjoint launch for dL/dx, three launches dotting D_a x with
+// ybar for dL/dsigma); everything else runs per axis on f32 buffers from the
+// stream-ordered scratch pool.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -187,6 +189,35 @@ DotArgs dot_args(const itkg_image& p, const itkg_image& q) {
   return d;
 }
 
+// Fused geometry of a whole-image VJP launch: src over its own region, the
+// request and the clamp bounds both the whole image.
+FusedGeom whole_geom(const itkg_image& src, const itkg_image* dst, const AxisCoeffs* c) {
+  FusedGeom g;
+  std::memset(&g, 0, sizeof g);
+  g.src = src.data;
+  g.dst = dst ? dst->data : const_cast<void*>(src.data);
+  const itkg_image& o = dst ? *dst : src;
+  for (int d = 0; d < kMaxDim; ++d) {
+    const bool in = d < src.dim;
+    g.src_origin[d] = in ? src.region.index[d] : 0;
+    g.src_size[d] = in ? (int64_t)src.region.size[d] : 1;
+    g.src_pitch[d] = in ? src.pitch[d] : 0;
+    g.dst_origin[d] = in ? o.region.index[d] : 0;
+    g.dst_pitch[d] = in ? o.pitch[d] : 0;
+    g.req_index[d] = g.src_origin[d];
+    g.req_size[d] = g.src_size[d];
+    g.lo[d] = g.src_origin[d];
+    g.hi[d] = g.src_origin[d] + g.src_size[d] - 1;
+    g.radius[d] = in ? c[d].r : 0;
+  }
+  g.dim = src.dim;
+  g.comps = 1;
+  g.in_dtype = ITKG_F32;
+  g.out_dtype = ITKG_F32;
+  g.rounding = ITKG_ROUND_FMA;
+  return g;
+}
+
 }  // namespace
 }  // namespace itkg
 
@@ -261,20 +292,58 @@ extern "C" itkg_status itkg_gaussian_vjp(const itkg_image* x, const itkg_image* 
   if (region_len(x->region, x->dim) == 0) return ITKG_SUCCESS;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   Scratch sc(s);
-  if (xbar) ITKG_TRY(adjoint_chain(*ybar, c, xbar, flags & ITKG_VJP_ACCUMULATE_XBAR, sc));
+  const int D = x->dim;
+  const float* w[kMaxDim] = {nullptr, nullptr, nullptr};
+  const float* P[kMaxDim] = {nullptr, nullptr, nullptr};
+  for (int d = 0; d < D; ++d) w[d] = c[d].w.data(), P[d] = c[d].prefix.data();
+  bool fused_x = false, fused_s = false;
+  if (xbar) {
+    // fused adjoint (one pass) where a kernel applies, else D per-axis passes
+    const FusedGeom g = whole_geom(*ybar, xbar, c);
+    if (D == 3 && launch_fused_vjp(2, g, w, P, nullptr, nullptr, nullptr, nullptr, nullptr, false, s,
+                                   true) == ITKG_SUCCESS) {
+      ITKG_TRY(launch_fused_vjp(2, g, w, P, nullptr, nullptr, nullptr, nullptr, nullptr,
+                                flags & ITKG_VJP_ACCUMULATE_XBAR, s, false));
+      fused_x = true;
+    } else {
+      ITKG_TRY(adjoint_chain(*ybar, c, xbar, flags & ITKG_VJP_ACCUMULATE_XBAR, sc));
+    }
+  }
   if (sigma_bar) {
-    itkg_image y, dy;
-    ITKG_TRY(sc.image(*x, &y));
-    ITKG_TRY(sc.image(*x, &dy));
-    ITKG_TRY(dual_chain(*x, c, &y, &dy, sc));
-    const int nb = dot_partial_blocks((int64_t)region_len(x->region, x->dim));
-    void* part = nullptr;
-    ITKG_TRY(sc.raw(sizeof(double) * (nb + 1), &part));
-    double* dres = static_cast<double*>(part) + nb;
     const bool on_dev = flags & ITKG_VJP_SIGMA_BAR_ON_DEVICE;
     const bool acc = flags & ITKG_VJP_ACCUMULATE_SIGMA;
-    ITKG_TRY(launch_dot(dot_args(*ybar, dy), static_cast<double*>(part), nb,
-                        on_dev ? sigma_bar : dres, on_dev && acc, s));
+    void* res = nullptr;
+    ITKG_TRY(sc.raw(sizeof(double), &res));
+    double* dres = static_cast<double*>(res);
+    // dy/dsigma = sum_a D_a x, D_a the separable filter with dw/dsigma on axis a:
+    // three fused launches that dot their output with ybar, or dual per-axis passes
+    const FusedGeom g = whole_geom(*x, nullptr, c);
+    int grid = 0;
+    if (D == 3 && launch_fused_vjp(1, g, w, nullptr, ybar->data, ybar->pitch, ybar->region.index, nullptr,
+                                   &grid, false, s, true) == ITKG_SUCCESS) {
+      void* part = nullptr;
+      ITKG_TRY(sc.raw(sizeof(double) * 3 * grid, &part));
+      double* partials = static_cast<double*>(part);
+      for (int a = 0; a < 3; ++a) {
+        const float* wa[kMaxDim] = {w[0], w[1], w[2]};
+        wa[a] = c[a].dw.data();
+        int g2 = 0;
+        ITKG_TRY(launch_fused_vjp(1, g, wa, nullptr, ybar->data, ybar->pitch, ybar->region.index,
+                                  partials + a * grid, &g2, false, s, false));
+      }
+      ITKG_TRY(launch_sum_partials(partials, 3 * grid, on_dev ? sigma_bar : dres, on_dev && acc, s));
+      fused_s = true;
+    } else {
+      itkg_image y, dy;
+      ITKG_TRY(sc.image(*x, &y));
+      ITKG_TRY(sc.image(*x, &dy));
+      ITKG_TRY(dual_chain(*x, c, &y, &dy, sc));
+      const int nb = dot_partial_blocks((int64_t)region_len(x->region, x->dim));
+      void* part = nullptr;
+      ITKG_TRY(sc.raw(sizeof(double) * nb, &part));
+      ITKG_TRY(launch_dot(dot_args(*ybar, dy), static_cast<double*>(part), nb,
+                          on_dev ? sigma_bar : dres, on_dev && acc, s));
+    }
     if (!on_dev) {
       double h = 0.0;
       ITKG_CUDA(cudaMemcpyAsync(&h, dres, sizeof h, cudaMemcpyDeviceToHost, s));
@@ -282,6 +351,7 @@ extern "C" itkg_status itkg_gaussian_vjp(const itkg_image* x, const itkg_image* 
       *sigma_bar = acc ? *sigma_bar + h : h;
     }
   }
-  set_last_kernel("vjp_per_axis_f32");
+  set_last_kernel(fused_x || fused_s ? (fused_x && (fused_s || !sigma_bar) ? "vjp_fused_f32" : "vjp_mixed_f32")
+                                     : "vjp_per_axis_f32");
   return ITKG_SUCCESS;
 }

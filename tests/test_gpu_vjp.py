@@ -68,6 +68,30 @@ def test_sigma_bar_matches_fp64_and_finite_differences(gpu, shape, sigma, spacin
     assert abs(sb - fd) <= 1e-4 * scale + 1e-6 * abs(fd), (sb, fd)
 
 
+@pytest.mark.parametrize("shape,sigma", [((40, 50, 60), 2.0), ((17, 23, 29), 1.2), ((5, 70, 40), 0.9),
+                                         ((33, 8, 41), 1.7)])
+def test_fused_vjp_matches_fp64_and_is_used(gpu, shape, sigma):
+    """3-D radii <= 6 run the fused adjoint and dot kernels; check them against
+    FP64 and against the dot-product identity."""
+    rng = np.random.default_rng(shape[0] * 7 + shape[2])
+    x = rng.standard_normal(shape).astype(np.float32)
+    y = rng.standard_normal(shape).astype(np.float32)
+    dx, dy = _dev(gpu, x), _dev(gpu, y)
+    xb, sb = gpu.vjp(dx, dy, sigma)
+    assert gpu.last_kernel() == "vjp_fused_f32", gpu.last_kernel()
+    want_x = oracle.gaussian_adjoint_f64(y.astype(np.float64), sigma)
+    got_x = xb.download().astype(np.float64)
+    assert np.abs(got_x - want_x).max() / np.abs(want_x).max() <= 1e-5
+    radii = _radii(sigma, None, 3)
+    d64 = oracle.gaussian_dsigma_f64(x.astype(np.float64), sigma, radii=radii)
+    want_s = float((d64 * y.astype(np.float64)).sum())
+    assert abs(sb - want_s) <= 1e-5 * float(np.abs(d64 * y).sum())
+    Gx = gpu.GaussianFilter(dx, sigma, rounding=gpu.ROUND_FMA).generate_region(dx.region).download()
+    lhs = float(np.dot(Gx.astype(np.float64).ravel(), y.astype(np.float64).ravel()))
+    rhs = float(np.dot(x.astype(np.float64).ravel(), got_x.ravel()))
+    assert abs(lhs - rhs) <= 1e-6 * float(np.abs(Gx).sum() * np.abs(y).max())
+
+
 def test_accumulate_flags(gpu):
     rng = np.random.default_rng(3)
     x = rng.random((12, 14, 16)).astype(np.float32)
