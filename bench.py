@@ -221,7 +221,7 @@ def gpu_arm(args):
     prm.sigma = SIGMA
     prm.rounding = rounding
     prm.algorithm = {"auto": itkg.ALGO_AUTO, "fused": itkg.ALGO_FUSED,
-                     "per_axis": itkg.ALGO_PER_AXIS}[args.algo]
+                     "per_axis": itkg.ALGO_PER_AXIS, "two_pass": itkg.ALGO_TWO_PASS}[args.algo]
     lg = region.to_c()
     req = region.to_c()
     in_c = [ctypes.byref(d.c) for d in ins]
@@ -571,7 +571,7 @@ def main():
     ap.add_argument("--workload", choices=["fwd3d", "fwd2d", "ct16", "batch", "batch_vjp", "vjp_stack"],
                     default="fwd3d")
     ap.add_argument("--rounding", choices=["fma", "reference"], default="fma")
-    ap.add_argument("--algo", choices=["auto", "fused", "per_axis"], default="auto")
+    ap.add_argument("--algo", choices=["auto", "fused", "per_axis", "two_pass"], default="auto")
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-check", dest="check", action="store_false")

@@ -247,7 +247,7 @@ static itkg_status check_params(const itkg_gaussian_params* prm) {
     return set_error(ITKG_ERROR_INVALID_ARGUMENT, "unknown arithmetic %d", prm->arithmetic);
   if (prm->rounding != ITKG_ROUND_REFERENCE && prm->rounding != ITKG_ROUND_FMA)
     return set_error(ITKG_ERROR_INVALID_ARGUMENT, "unknown rounding %d", prm->rounding);
-  if (prm->algorithm < ITKG_ALGO_AUTO || prm->algorithm > ITKG_ALGO_PER_AXIS)
+  if (prm->algorithm < ITKG_ALGO_AUTO || prm->algorithm > ITKG_ALGO_TWO_PASS)
     return set_error(ITKG_ERROR_INVALID_ARGUMENT, "unknown algorithm %d", prm->algorithm);
   if (prm->reserved != 0) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "reserved must be 0");
   return ITKG_SUCCESS;
@@ -293,6 +293,11 @@ static itkg_status generate_device(const itkg_image& in, const itkg_region& larg
     make_fused_geom(in, largest, requested, prm, plan, out, &g);
     const float* w[kMaxDim] = {nullptr, nullptr, nullptr};
     for (int d = 0; d < D; ++d) w[d] = plan.w32[d].data();
+    if (prm.algorithm == ITKG_ALGO_AUTO || prm.algorithm == ITKG_ALGO_TWO_PASS) {
+      if (launch_two_pass(g, w, s, /*dry_run=*/true) == ITKG_SUCCESS) return launch_two_pass(g, w, s, false);
+      if (prm.algorithm == ITKG_ALGO_TWO_PASS)
+        return set_error(ITKG_ERROR_UNSUPPORTED, "the two-pass kernels do not cover this geometry");
+    }
     itkg_status st = launch_fused(g, w, s, /*dry_run=*/true);
     if (st == ITKG_SUCCESS) return launch_fused(g, w, s, false);
     if (prm.algorithm == ITKG_ALGO_FUSED)
@@ -308,6 +313,7 @@ itkg_status fused_geom_for(const itkg_image& in, const itkg_region& largest,
   if (prm.arithmetic == ITKG_ARITH_PIXEL_U8 || prm.algorithm == ITKG_ALGO_PER_AXIS)
     return ITKG_ERROR_UNSUPPORTED;
   const int D = in.dim;
+  if (D != 3) return ITKG_ERROR_UNSUPPORTED;  // the multi-request kernels are 3-D
   if (out.dim != D || out.components != in.components || region_len(requested, D) == 0 ||
       !region_contains(largest, requested, D) || !region_contains(out.region, requested, D))
     return ITKG_ERROR_UNSUPPORTED;

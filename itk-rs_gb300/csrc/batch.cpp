@@ -130,11 +130,17 @@ itkg_status choose_algorithm(const itkg_batch::Fwd& f, bool tune, cudaStream_t s
     *algo = ITKG_ALGO_AUTO;  // the per-call dispatcher decides
     return ITKG_SUCCESS;
   }
-  float t_fused = 1e30f, t_axis = 1e30f;
+  float t_fused = 1e30f, t_axis = 1e30f, t_two = 1e30f;
   const itkg_status sf = time_item(probe, ITKG_ALGO_FUSED, s, &t_fused);
   if (sf != ITKG_SUCCESS && sf != ITKG_ERROR_UNSUPPORTED) return sf;
+  const itkg_status s2 = time_item(f, ITKG_ALGO_TWO_PASS, s, &t_two);
+  if (s2 != ITKG_SUCCESS && s2 != ITKG_ERROR_UNSUPPORTED) return s2;
   ITKG_TRY(time_item(f, ITKG_ALGO_PER_AXIS, s, &t_axis));
-  const int pick = (sf == ITKG_SUCCESS && t_fused <= t_axis) ? ITKG_ALGO_FUSED : ITKG_ALGO_PER_AXIS;
+  if (sf != ITKG_SUCCESS) t_fused = 1e30f;
+  if (s2 != ITKG_SUCCESS) t_two = 1e30f;
+  int pick = ITKG_ALGO_PER_AXIS;
+  if (t_fused <= t_axis && t_fused <= t_two) pick = ITKG_ALGO_FUSED;
+  else if (t_two < t_axis) pick = ITKG_ALGO_TWO_PASS;
   std::lock_guard<std::mutex> lk(g_tune_mu);
   g_tune[k] = pick;
   *algo = pick;
@@ -225,7 +231,7 @@ itkg_status itkg_batch_plan(itkg_batch* b, int32_t flags, void* stream) {
   std::vector<std::vector<std::vector<float>>> fused_w;
   std::vector<size_t> per_item;
   for (size_t i = 0; i < b->fwd.size(); ++i) {
-    if (algo[i] == ITKG_ALGO_PER_AXIS) {
+    if (algo[i] == ITKG_ALGO_PER_AXIS || algo[i] == ITKG_ALGO_TWO_PASS) {
       per_item.push_back(i);
       continue;
     }
@@ -257,7 +263,8 @@ itkg_status itkg_batch_plan(itkg_batch* b, int32_t flags, void* stream) {
   for (size_t i : per_item) {
     if (st != ITKG_SUCCESS) break;
     itkg_batch::Fwd f = b->fwd[i];
-    f.prm.algorithm = algo[i] == ITKG_ALGO_AUTO ? ITKG_ALGO_AUTO : ITKG_ALGO_PER_AXIS;
+    // items without a multi-request kernel (2-D) still take their single fused kernel
+    f.prm.algorithm = (algo[i] == ITKG_ALGO_PER_AXIS || algo[i] == ITKG_ALGO_TWO_PASS) ? algo[i] : ITKG_ALGO_AUTO;
     st = itkg_gaussian_generate_region(&f.in, &f.largest, &f.requested, &f.prm, &f.out, cap);
     b->plan_lines.push_back(std::string("item ") + std::to_string(i) + ": " + itkg_last_kernel());
   }

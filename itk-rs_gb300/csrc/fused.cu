@@ -242,8 +242,30 @@ bool geometry_ok(const FusedGeom& g) {
 
 }  // namespace
 
+itkg_status max_resident_ctas(const void* fn, size_t smem, int nt, int* out) {
+  return resident_ctas(fn, smem, nt, out);
+}
+
+itkg_status device_fault_word(unsigned int** out) { return fault_address(out); }
+
+itkg_status encode_input_map(const FusedGeom& g, int box_w, int box_h, void* map_out) {
+  if (!encode_fn()) return set_error(ITKG_ERROR_UNSUPPORTED, "cuTensorMapEncodeTiled unavailable");
+  CUtensorMap& map = *static_cast<CUtensorMap*>(map_out);
+  std::memset(&map, 0, sizeof map);
+  const cuuint64_t dims[3] = {(cuuint64_t)g.src_size[0], (cuuint64_t)g.src_size[1], (cuuint64_t)g.src_size[2]};
+  const cuuint64_t strides[2] = {(cuuint64_t)g.src_pitch[1], (cuuint64_t)g.src_pitch[2]};
+  const cuuint32_t box[3] = {(cuuint32_t)box_w, (cuuint32_t)box_h, 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = encode_fn()(&map, tma_type(g.in_dtype), 3, const_cast<void*>(g.src), dims, strides, box, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return set_error(ITKG_ERROR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+  return ITKG_SUCCESS;
+}
+
 itkg_status launch_fused(const FusedGeom& g, const float* const w[kMaxDim], void* stream,
                          bool dry_run) {
+  if (g.dim == 2) return launch_fused2d(g, w, stream, dry_run);
   if (!geometry_ok(g)) return ITKG_ERROR_UNSUPPORTED;
   const Entry* e = find_entry(g.radius[0], g.radius[1], g.radius[2], g.in_dtype);
   if (!e) return ITKG_ERROR_UNSUPPORTED;

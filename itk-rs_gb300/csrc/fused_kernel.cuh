@@ -501,13 +501,15 @@ __device__ __forceinline__ bool fused_range(const Fused3DArgs& a, const CUtensor
       // ---- z pass: push slice j into the ring, pop output z = j - RZ ----
       const bool do_push = MODE != kAdj || (j >= a.lo[2] && j <= a.hi[2]);
       if constexpr (MODE == kAdj) {
+        // only in-image slices fold (j outside the image carries the clamped
+        // slice's values, which the adjoint must not count again)
         const int dl = j - a.lo[2], dh = a.hi[2] - j;
-        if (dl >= 0 && dl < RZ) {
+        if (do_push && dl < RZ) {
           const f2_t wp = pack2(a.pz[RZ - 1 - dl], a.pz[RZ - 1 - dl]);
 #pragma unroll
           for (int m = 0; m < MY2; ++m) acc_lo[m] = fma2(yv[m], wp, acc_lo[m]);
         }
-        if (dh >= 0 && dh < RZ) {
+        if (do_push && dh < RZ) {
           const f2_t wp = pack2(a.pz[RZ - 1 - dh], a.pz[RZ - 1 - dh]);
 #pragma unroll
           for (int m = 0; m < MY2; ++m) acc_hi[m] = fma2(yv[m], wp, acc_hi[m]);

@@ -101,8 +101,12 @@ struct FusedGeom {
 itkg_status launch_fused(const FusedGeom& g, const float* const w[kMaxDim], void* stream,
                          bool dry_run);
 
-// abi.cpp: validates one request and fills its fused geometry and f32 weights;
-// ITKG_ERROR_UNSUPPORTED when no fused kernel covers it.
+// fused2d.cu: the 2-D counterpart (f32 input, 1 or 3 components, radius <= 8).
+itkg_status launch_fused2d(const FusedGeom& g, const float* const w[kMaxDim], void* stream,
+                           bool dry_run);
+
+// abi.cpp: validates one 3-D request and fills its fused geometry and f32
+// weights; ITKG_ERROR_UNSUPPORTED when no multi-request fused kernel covers it.
 itkg_status fused_geom_for(const itkg_image& in, const itkg_region& largest,
                            const itkg_region& requested, const itkg_gaussian_params& prm,
                            const itkg_image& out, FusedGeom* g,
@@ -130,6 +134,21 @@ itkg_status launch_fused_vjp(int mode, const FusedGeom& g, const float* const w[
                              const float* const prefix[kMaxDim], const void* ybar,
                              const int64_t* ybar_pitch, const int64_t* ybar_origin, double* partials,
                              int* grid_out, bool accumulate, void* stream, bool dry_run);
+
+// fused.cu helpers shared by the fused kernels' launchers:
+//   max_resident_ctas: SMs x resident CTAs of `fn` (cached per device);
+//   device_fault_word: address of the fault word on the current device;
+//   encode_input_map: 3-D TMA tensor map (CUtensorMap, 128 bytes) over the
+//   input buffer of `g` with a box_w x box_h x 1 box.
+itkg_status max_resident_ctas(const void* fn, size_t smem, int nt, int* out);
+itkg_status device_fault_word(unsigned int** out);
+itkg_status encode_input_map(const FusedGeom& g, int box_w, int box_h, void* map_out);
+
+// two_pass.cu: the 3-D forward as an x-y slice kernel plus a z kernel through
+// an L2-sized f32 intermediate (rx == ry <= 8, rz <= 8, TMA-aligned input).
+// ITKG_ERROR_UNSUPPORTED (no error set) when it does not apply.
+itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], void* stream,
+                            bool dry_run);
 
 // Bumps the launch counter by n (graph replays).
 void note_launches(uint64_t n, const char* name);

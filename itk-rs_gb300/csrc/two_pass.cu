@@ -1,0 +1,207 @@
+// Host side of the two-kernel 3-D forward (kernels in two_pass.cuh): kernel
+// choice, the intermediate's layout and its z-chunking, and the launches.
+// This file holds the f32 x-y pass table and every z-pass instantiation; the
+// i16 / u8 / bf16 / f16 x-y pass tables are in two_pass_in.cu.
+#include <algorithm>
+#include <climits>
+
+#include "two_pass.cuh"
+
+namespace itkg {
+namespace twopass {
+namespace {
+const XYEntry kXYF32[] = ITKG_XY_TABLE(float, ITKG_F32);
+
+struct ZEntry {
+  int r;
+  ZFn fn[2];  // [ref]
+};
+template <int R>
+ZEntry make_z() {
+  return ZEntry{R, {k_z_pass<R, false>, k_z_pass<R, true>}};
+}
+const ZEntry kZ[] = {make_z<1>(), make_z<2>(), make_z<3>(), make_z<4>(),
+                     make_z<5>(), make_z<6>(), make_z<7>(), make_z<8>()};
+}  // namespace
+
+ZFn z_fn(int r, bool ref) {
+  for (const ZEntry& z : kZ)
+    if (z.r == r) return z.fn[ref ? 1 : 0];
+  return nullptr;
+}
+
+const XYEntry* xy_entries_f32(int* n) {
+  *n = (int)(sizeof(kXYF32) / sizeof(kXYF32[0]));
+  return kXYF32;
+}
+}  // namespace twopass
+
+namespace {
+
+using twopass::XYArgs;
+using twopass::XYEntry;
+using twopass::ZArgs;
+
+// L2 share the intermediate may take; longer z ranges are processed in chunks.
+constexpr int64_t kChunkBytes = 72ll << 20;
+
+const XYEntry* find_xy(int r, int dtype) {
+  int n = 0;
+  const XYEntry* t = nullptr;
+  switch (dtype) {
+    case ITKG_F32: t = twopass::xy_entries_f32(&n); break;
+    case ITKG_I16: t = twopass::xy_entries_i16(&n); break;
+    case ITKG_U8: t = twopass::xy_entries_u8(&n); break;
+    case ITKG_BF16: t = twopass::xy_entries_bf16(&n); break;
+    case ITKG_F16: t = twopass::xy_entries_f16(&n); break;
+    default: return nullptr;
+  }
+  for (int i = 0; i < n; ++i)
+    if (t[i].r == r) return &t[i];
+  return nullptr;
+}
+
+bool fits_i32(int64_t v) { return v >= INT_MIN && v <= INT_MAX; }
+
+const char* xy_name(int dtype, bool ref) {
+  static const char* names[5][2] = {{"xy_pass_f32_fma", "xy_pass_f32_ref"},
+                                    {"xy_pass_i16_fma", "xy_pass_i16_ref"},
+                                    {"xy_pass_u8_fma", "xy_pass_u8_ref"},
+                                    {"xy_pass_bf16_fma", "xy_pass_bf16_ref"},
+                                    {"xy_pass_f16_fma", "xy_pass_f16_ref"}};
+  return names[dtype][ref ? 1 : 0];
+}
+
+}  // namespace
+
+itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], void* stream, bool dry_run) {
+  if (g.dim != 3 || g.comps != 1 || g.out_dtype == ITKG_I16) return ITKG_ERROR_UNSUPPORTED;
+  if (g.radius[0] != g.radius[1] || g.radius[2] < 1 || g.radius[2] > twopass::kMaxR)
+    return ITKG_ERROR_UNSUPPORTED;
+  const XYEntry* e = find_xy(g.radius[0], g.in_dtype);
+  if (!e) return ITKG_ERROR_UNSUPPORTED;
+  const int esz = dtype_size(g.in_dtype);
+  if (g.src_pitch[0] != esz) return ITKG_ERROR_UNSUPPORTED;
+  // TMA: 16-byte base and pitches, 16-byte aligned first tile column
+  const int ae = 16 / esz;
+  if (((uintptr_t)g.src & 15) || (g.src_pitch[1] & 15) || (g.src_pitch[2] & 15)) return ITKG_ERROR_UNSUPPORTED;
+  if (g.src_pitch[1] >= (1ll << 40) || g.src_pitch[2] >= (1ll << 40)) return ITKG_ERROR_UNSUPPORTED;
+  if ((((g.req_index[0] - g.src_origin[0]) % ae) + ae) % ae != 0) return ITKG_ERROR_UNSUPPORTED;
+  for (int d = 0; d < 3; ++d)
+    if (!fits_i32(g.lo[d]) || !fits_i32(g.hi[d]) || !fits_i32(g.src_origin[d]) || !fits_i32(g.dst_origin[d]) ||
+        !fits_i32(g.req_index[d] + g.req_size[d] + 64) || !fits_i32(g.req_index[d] - 64))
+      return ITKG_ERROR_UNSUPPORTED;
+  const int64_t nx = g.req_size[0], ny = g.req_size[1], nz = g.req_size[2];
+  const int64_t nxp = (nx + 3) / 4 * 4;
+  if (!fits_i32(nxp) || !fits_i32(ny)) return ITKG_ERROR_UNSUPPORTED;
+  if (dry_run) return ITKG_SUCCESS;
+
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const bool ref = g.rounding == ITKG_ROUND_REFERENCE;
+  const int rz = g.radius[2];
+  // clamp bounds on z: the image within the input buffer
+  const int64_t zlo = std::max<int64_t>(g.lo[2], g.src_origin[2]);
+  const int64_t zhi = std::min<int64_t>(g.hi[2], g.src_origin[2] + g.src_size[2] - 1);
+  const int64_t slice_floats = nxp * ny;
+  // outputs per chunk: as many as keep the chunk's intermediate within kChunkBytes
+  int64_t chunk = nz;
+  {
+    const int64_t fit = kChunkBytes / (slice_floats * 4) - 2 * rz;
+    if (fit >= 2 * rz + 1) chunk = std::min<int64_t>(nz, fit);
+  }
+  const int64_t t_slices = std::min<int64_t>(chunk + 2 * rz, zhi - zlo + 1);
+  float* t = nullptr;
+  {
+    const itkg_status sa = scratch_alloc(reinterpret_cast<void**>(&t), (size_t)(t_slices * slice_floats * 4), stream);
+    if (sa != ITKG_SUCCESS) return sa;
+  }
+
+  CUtensorMap map;
+  itkg_status st = encode_input_map(g, e->bw, e->ih, &map);
+  XYArgs xa;
+  ZArgs za;
+  std::memset(&xa, 0, sizeof xa);
+  std::memset(&za, 0, sizeof za);
+  if (st == ITKG_SUCCESS) st = device_fault_word(&xa.fault);
+  int res_xy = 0, res_z = 0;
+  const twopass::ZFn zfn = twopass::z_fn(rz, ref);
+  const twopass::XYFn xyfn = e->fn[ref ? 1 : 0];
+  if (st == ITKG_SUCCESS) st = max_resident_ctas(reinterpret_cast<const void*>(xyfn), e->smem, 256, &res_xy);
+  if (st == ITKG_SUCCESS)
+    st = max_resident_ctas(reinterpret_cast<const void*>(zfn), twopass::CfgZ<1>::SMEM, 256, &res_z);
+  if (st != ITKG_SUCCESS) {
+    scratch_free(t, stream);
+    return st;
+  }
+
+  xa.t = t;
+  xa.t_row = nxp;
+  xa.t_slice = slice_floats;
+  for (int d = 0; d < 3; ++d) {
+    xa.src_origin[d] = (int32_t)g.src_origin[d];
+    xa.lo[d] = (int32_t)std::max<int64_t>(g.lo[d], g.src_origin[d]);
+    xa.hi[d] = (int32_t)std::min<int64_t>(g.hi[d], g.src_origin[d] + g.src_size[d] - 1);
+  }
+  xa.x0 = (int32_t)g.req_index[0];
+  xa.y0 = (int32_t)g.req_index[1];
+  xa.nxp = (int32_t)nxp;
+  xa.ny = (int32_t)ny;
+  xa.ntx = (int32_t)((nx + e->tx - 1) / e->tx);
+  const int64_t nty = (ny + e->ty - 1) / e->ty;
+  const int K = 2 * g.radius[0] + 1;
+  for (int k = 0; k < K; ++k) {
+    xa.wx[k] = w[0][k], xa.wx2[k] = splat2_host(w[0][k]);
+    xa.wy[k] = w[1][k], xa.wy2[k] = splat2_host(w[1][k]);
+  }
+  za.t = t;
+  za.t_row = nxp;
+  za.t_slice = slice_floats;
+  za.nx = (int32_t)nx;
+  za.ny = (int32_t)ny;
+  za.nqx = (int32_t)(nxp / 4);
+  za.out_dtype = g.out_dtype;
+  za.dst_pitch[0] = g.dst_pitch[0];
+  za.dst_pitch[1] = g.dst_pitch[1];
+  za.dst_pitch[2] = g.dst_pitch[2];
+  char* const dst0 = static_cast<char*>(g.dst) + (g.req_index[0] - g.dst_origin[0]) * g.dst_pitch[0] +
+                     (g.req_index[1] - g.dst_origin[1]) * g.dst_pitch[1];
+  za.vec_store = (g.out_dtype == ITKG_F32 && g.dst_pitch[0] == 4 && ((uintptr_t)dst0 & 15) == 0 &&
+                  (g.dst_pitch[1] & 15) == 0 && (g.dst_pitch[2] & 15) == 0)
+                     ? 1
+                     : 0;
+  for (int k = 0; k < 2 * rz + 1; ++k) za.wz[k] = w[2][k], za.wz2[k] = splat2_host(w[2][k]);
+  const int64_t qblocks = (nxp / 4 * ny + 255) / 256;
+
+  for (int64_t c0 = 0; c0 < nz && st == ITKG_SUCCESS; c0 += chunk) {
+    const int64_t c1 = std::min<int64_t>(nz, c0 + chunk);  // outputs [z0 + c0, z0 + c1)
+    const int64_t oz0 = g.req_index[2] + c0, oz1 = g.req_index[2] + c1 - 1;
+    const int64_t s0 = std::max<int64_t>(zlo, oz0 - rz), s1 = std::min<int64_t>(zhi, oz1 + rz);
+    xa.s0 = (int32_t)s0;
+    xa.ns = (int32_t)(s1 - s0 + 1);
+    xa.t_s0 = (int32_t)s0;
+    xa.units = xa.ntx * nty * xa.ns;
+    const int64_t gxy = std::min<int64_t>(xa.units, res_xy);
+    xyfn<<<(unsigned)gxy, 256, e->smem, s>>>(map, xa);
+    note_launch(xy_name(g.in_dtype, ref));
+    cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) {
+      st = set_error(ITKG_ERROR_CUDA, "xy pass launch: %s", cudaGetErrorString(err));
+      break;
+    }
+    za.t_s0 = (int32_t)s0;
+    za.t_s1 = (int32_t)s1;
+    za.z0 = (int32_t)oz0;
+    za.nz = (int32_t)(c1 - c0);
+    za.units = qblocks * za.nz;
+    za.dst = dst0 + (oz0 - g.dst_origin[2]) * g.dst_pitch[2];
+    const int64_t gz = std::min<int64_t>(za.units, res_z);
+    zfn<<<(unsigned)gz, 256, twopass::CfgZ<1>::SMEM, s>>>(za);
+    note_launch(ref ? "z_pass_f32_ref" : "z_pass_f32_fma");
+    err = cudaGetLastError();
+    if (err != cudaSuccess) st = set_error(ITKG_ERROR_CUDA, "z pass launch: %s", cudaGetErrorString(err));
+  }
+  scratch_free(t, stream);
+  return st;
+}
+
+}  // namespace itkg

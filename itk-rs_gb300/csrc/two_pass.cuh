@@ -1,0 +1,485 @@
+// Two-kernel 3-D Gaussian forward: GaussianFilter::generate_region
+// (src/filters/gaussian.rs:74-88) as
+//   xy pass: per slice, the x pass and then the y pass of a TX x TY tile,
+//            written to an f32 intermediate T (the reference's intermediate
+//            after its second pass, restricted to the requested x-y range);
+//   z pass:  the third pass, streaming T along z.
+// Neither kernel recomputes anything along z, and the z pass needs no shared
+// tile and no block barrier, so both stay close to the memory system's rate.
+// T is sized to stay in L2 (the launcher splits long z ranges into chunks),
+// so it costs little HBM traffic.
+//
+// xy pass.  A CTA runs a contiguous range of (tile, slice) units.  The
+// (TX + 2XA) x (TY + 2RY) input tile of each unit lands in shared memory by one
+// TMA tile load (S units in flight, mbarrier completion, bounded waits); edge
+// tiles replicate the image's edge values into the halo (clamp-to-edge,
+// conv.rs:31-33).  The x pass writes a double-buffered f32 tile, so the x pass
+// of unit i + 1 and the y pass of unit i share one barrier interval.  The y
+// pass gives each thread two adjacent columns (one packed f32x2 register per
+// row) and MY consecutive rows, read from a register window.
+//
+// z pass.  A thread owns four consecutive columns of one row of T and marches
+// a z-segment: slice j is copied by cp.async into the thread's own shared
+// memory ring (S slices ahead; no other thread reads it, so no barrier), then
+// pushed into a ring of KZ packed accumulators (output z = j + RZ - k gets
+// w[k] * v); output j - RZ is complete and stored.  The loop is unrolled over
+// the KZ phases so every ring slot is a compile-time register.
+//
+// Reference rounding: scalar acc = acc + x * w with separate roundings, in
+// ascending tap order from zero, on f32 intermediates -- bit-identical to the
+// reference pass by pass.  FMA rounding: packed fma.rn.f32x2.
+#pragma once
+
+#include "fused_kernel.cuh"
+
+namespace itkg {
+namespace twopass {
+
+using fusedk::clampi;
+using fusedk::load4;
+using fusedk::mbar_expect_tx;
+using fusedk::mbar_init;
+using fusedk::mbar_wait;
+using fusedk::smem_u32;
+using fusedk::tma_load_3d;
+
+constexpr int kMaxR = 8;
+constexpr int kMaxK = 2 * kMaxR + 1;
+
+struct XYArgs {
+  float* t;            // intermediate, [slice][row][col]
+  int64_t t_row;       // floats between rows of T
+  int64_t t_slice;     // floats between slices of T
+  int32_t src_origin[3];
+  int32_t lo[3], hi[3];  // gather bounds (image within the input buffer), inclusive
+  int32_t x0, y0;        // first requested column / row (absolute)
+  int32_t nxp, ny;       // T row length (floats, multiple of 4) and rows
+  int32_t s0, ns;        // first slice of this launch (absolute z) and slice count
+  int32_t t_s0;          // absolute z of T's slice 0
+  int32_t ntx;           // tiles along x
+  int64_t units;         // ntx * nty * ns
+  unsigned int* fault;
+  float wx[kMaxK], wy[kMaxK];
+  f2_t wx2[kMaxK], wy2[kMaxK];
+};
+
+struct ZArgs {
+  const float* t;
+  int64_t t_row, t_slice;  // floats
+  int32_t t_s0, t_s1;      // absolute z of T's first / last slice (the clamp bounds)
+  int32_t nx, ny;          // requested columns / rows
+  int32_t nqx;             // quads per row (nxp / 4)
+  int32_t z0, nz;          // output slices of this launch (absolute) and count
+  int64_t units;           // quad blocks * nz
+  char* dst;               // output voxel (x0, y0, z0)
+  int64_t dst_pitch[3];    // bytes
+  int32_t out_dtype;
+  int32_t vec_store;       // 1: f32 output rows allow 16-byte stores
+  float wz[kMaxK];
+  f2_t wz2[kMaxK];
+};
+
+template <int R, typename Tin>
+struct CfgXY {
+  static constexpr int K = 2 * R + 1;
+  static constexpr int ESZ = (int)sizeof(Tin);
+  static constexpr int NT = 256;
+  static constexpr int TX = 32;                 // 16 lanes x 2 columns
+  static constexpr int MY = 4;                  // rows per thread in the y pass
+  static constexpr int TY = (NT / 16) * MY;     // 64
+  static constexpr int MX = 8;                  // x outputs per x-pass task
+  static constexpr int AE = 16 / ESZ;
+  static constexpr int XA = (R + AE - 1) / AE * AE;
+  static constexpr int BW = TX + 2 * XA;
+  static constexpr int IH = TY + 2 * R;
+  static constexpr int OFF = (XA - R) % 4;
+  static constexpr int WB = XA - R - OFF;
+  static constexpr int WIN = (MX + 2 * R + OFF + 3) / 4 * 4;
+  static constexpr int S = 3;                   // units in flight
+  static constexpr int BOX = IH * BW * ESZ;
+  static constexpr int STAGE = (BOX + 127) / 128 * 128;
+  static constexpr int XBUF = IH * TX;          // floats per x-filtered tile
+  static constexpr size_t SMEM = (size_t)S * STAGE + sizeof(float) * 2 * XBUF + 128;
+  static_assert(WB + TX - MX + WIN <= BW, "x window stays inside the staged row");
+  static_assert(TX % MX == 0, "x segments");
+};
+
+template <int RZ>
+struct CfgZ {
+  static constexpr int KZ = 2 * RZ + 1;
+  static constexpr int NT = 256;
+  static constexpr int S = 8;  // slices in flight per thread
+  static constexpr size_t SMEM = (size_t)S * NT * 16;
+};
+
+// ---------------------------------------------------------------------------
+// L2 policies (createpolicy) for the cache hints of the loads and stores.
+__device__ __forceinline__ uint64_t policy_evict_first() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;\n" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ uint64_t policy_evict_last() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;\n" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ void tma_load_3d_hint(uint32_t dst, const CUtensorMap* map, int x, int y, int z,
+                                                 uint32_t bar, uint64_t pol) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint"
+      " [%0], [%1, {%2, %3, %4}], [%5], %6;\n" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(bar), "l"(pol)
+      : "memory");
+}
+__device__ __forceinline__ void st_f2_hint(float* p, f2_t v, uint64_t pol) {
+  asm volatile("st.global.L2::cache_hint.b64 [%0], %1, %2;\n" ::"l"(p), "l"(v), "l"(pol) : "memory");
+}
+__device__ __forceinline__ void cp_async16_hint(uint32_t s, const void* g, uint64_t pol) {
+  asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, %2;\n" ::"r"(s), "l"(g), "l"(pol)
+               : "memory");
+}
+
+// One staged element -> f32 (exact).
+__device__ __forceinline__ float ld1(const float* p) { return *p; }
+__device__ __forceinline__ float ld1(const int16_t* p) { return (float)*p; }
+__device__ __forceinline__ float ld1(const uint8_t* p) { return (float)*p; }
+__device__ __forceinline__ float ld1(const __nv_bfloat16* p) { return __bfloat162float(*p); }
+__device__ __forceinline__ float ld1(const __half* p) { return __half2float(*p); }
+
+// Position of one (tile, slice) unit; advanced one unit at a time without
+// divisions (slices fastest, then tiles along x, then along y).
+struct UnitCursor {
+  int tx0, ty0, s;
+  __device__ __forceinline__ void advance(const XYArgs& a, int tx, int ty) {
+    if (++s == a.s0 + a.ns) {
+      s = a.s0;
+      tx0 += tx;
+      if (tx0 >= a.x0 + a.ntx * tx) {
+        tx0 = a.x0;
+        ty0 += ty;
+      }
+    }
+  }
+};
+
+// ---------------------------------------------------------------------------
+// xy pass
+template <int R, bool REF, typename Tin>
+__global__ void __launch_bounds__(256, 3)
+    k_xy_pass(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ XYArgs a) {
+  using C = CfgXY<R, Tin>;
+  constexpr int K = C::K, TX = C::TX, TY = C::TY, MY = C::MY, MX = C::MX, BW = C::BW, IH = C::IH,
+                XA = C::XA, S = C::S, WIN = C::WIN, WB = C::WB, OFF = C::OFF, NT = C::NT;
+  constexpr int SEGS = TX / MX;
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ __align__(8) uint64_t mbar[S];
+  unsigned char* const stage0 = smem + ((128u - (smem_u32(smem) & 127u)) & 127u);
+  float* const xbuf0 = reinterpret_cast<float*>(stage0 + S * C::STAGE);
+  const uint32_t sbase = smem_u32(stage0);
+  const uint32_t bbase = smem_u32(mbar);
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    for (int i = 0; i < S; ++i) mbar_init(bbase + 8 * i, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  __syncthreads();
+  uint32_t phase_bits = 0;
+
+  const int64_t u_begin = a.units * blockIdx.x / gridDim.x;
+  const int64_t u_end = a.units * (blockIdx.x + 1) / gridDim.x;
+  const int n = (int)(u_end - u_begin);
+  if (n <= 0) return;
+
+  UnitCursor cy;  // unit of the y pass
+  {
+    const int64_t tile = u_begin / a.ns;
+    cy.s = a.s0 + (int)(u_begin - tile * a.ns);
+    const int64_t tyi = tile / a.ntx;
+    cy.tx0 = a.x0 + (int)(tile - tyi * a.ntx) * TX;
+    cy.ty0 = a.y0 + (int)tyi * TY;
+  }
+  UnitCursor cx = cy, ci = cy;  // units of the x pass and of the next tile load
+  const uint64_t pol_in = policy_evict_first();
+  const uint64_t pol_t = policy_evict_last();
+
+  int issued = 0, consumed = 0;  // units whose load was issued / waited for (uniform)
+  auto issue_next = [&]() {      // tile load of unit `issued` (cursor ci)
+    if (issued >= n) return;
+    if (tid == 0) {
+      const int st = issued % S;
+      asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+      const uint32_t bar = bbase + 8 * st;
+      mbar_expect_tx(bar, (uint32_t)C::BOX);
+      tma_load_3d_hint(sbase + (uint32_t)(st * C::STAGE), &tmap, ci.tx0 - XA - a.src_origin[0],
+                       ci.ty0 - R - a.src_origin[1], ci.s - a.src_origin[2], bar, pol_in);
+    }
+    ++issued;
+    ci.advance(a, TX, TY);
+  };
+  // Waits for the tile of unit `consumed` (cursor cx) and runs its x pass
+  // into xb.  Halo rows outside the image read the clamped row and halo
+  // columns outside it take the edge column's value (clamp-to-edge).
+  auto xpass_next = [&](float* xb) -> bool {
+    const int st = consumed % S;
+    const Tin* const tile = reinterpret_cast<const Tin*>(stage0 + st * C::STAGE);
+    const bool ok = mbar_wait(bbase + 8 * st, (phase_bits >> st) & 1u);
+    phase_bits ^= 1u << st;
+    ++consumed;
+    const int gx0 = cx.tx0 - XA, gy0 = cx.ty0 - R;
+    cx.advance(a, TX, TY);
+    if (!ok) return false;
+    const int nl = max(0, a.lo[0] - gx0);            // first in-image column of the tile
+    const int cr = min(BW - 1, a.hi[0] - gx0);       // last in-image column of the tile
+    const int rlo = a.lo[1] - gy0, rhi = a.hi[1] - gy0;
+    for (int t = tid; t < IH * SEGS; t += NT) {
+      const int row = t / SEGS, x0 = (t % SEGS) * MX;
+      const int srow = min(max(row, rlo), rhi);
+      const Tin* const src = tile + srow * BW;
+      float v[WIN];
+#pragma unroll
+      for (int q = 0; q < WIN / 4; ++q) load4(src + x0 + WB + 4 * q, v + 4 * q);
+      if (x0 + WB < nl || x0 + WB + WIN - 1 > cr) {
+        const float vl = ld1(src + nl), vr = ld1(src + cr);
+#pragma unroll
+        for (int q = 0; q < WIN; ++q) {
+          const int c = x0 + WB + q;
+          v[q] = c < nl ? vl : (c > cr ? vr : v[q]);
+        }
+      }
+      float o[MX];
+      if constexpr (REF) {
+#pragma unroll
+        for (int m = 0; m < MX; ++m) {
+          float ax = 0.0f;
+#pragma unroll
+          for (int k = 0; k < K; ++k) ax = tap<true>(ax, v[m + k + OFF], a.wx[k]);
+          o[m] = ax;
+        }
+      } else {
+        f2_t E[WIN / 2], O[WIN / 2 - 1];
+#pragma unroll
+        for (int q = 0; q < WIN / 2; ++q) E[q] = pack2(v[2 * q], v[2 * q + 1]);
+#pragma unroll
+        for (int q = 0; q < WIN / 2 - 1; ++q) O[q] = pack2(v[2 * q + 1], v[2 * q + 2]);
+#pragma unroll
+        for (int m = 0; m < MX / 2; ++m) {
+          f2_t ax = 0ull;
+#pragma unroll
+          for (int k = 0; k < K; ++k) {
+            const int q = 2 * m + k + OFF;
+            ax = fma2((q & 1) ? O[(q - 1) / 2] : E[q / 2], a.wx2[k], ax);
+          }
+          unpack2(ax, o[2 * m], o[2 * m + 1]);
+        }
+      }
+      float4* d4 = reinterpret_cast<float4*>(xb + row * TX + x0);
+#pragma unroll
+      for (int q = 0; q < MX / 4; ++q) d4[q] = make_float4(o[4 * q], o[4 * q + 1], o[4 * q + 2], o[4 * q + 3]);
+    }
+    return true;
+  };
+
+  const int lane16 = tid & 15, grp = tid >> 4;
+  const float* const ywin0 = xbuf0 + grp * MY * TX + 2 * lane16;  // this thread's y window
+  for (int q = 0; q < S; ++q) issue_next();
+  bool ok = xpass_next(xbuf0);
+  if (__syncthreads_or(!ok)) goto timeout;
+  for (int i = 0; i < n; ++i) {
+    if (i > 0) {
+      // x pass of unit i visible; y pass of unit i - 1 done with the other buffer
+      __syncthreads();
+    }
+    issue_next();  // into the stage unit i's x pass has finished reading
+    if (i + 1 < n) {
+      ok = xpass_next(xbuf0 + ((i + 1) & 1) * C::XBUF);
+      if (__syncthreads_or(!ok)) goto timeout;
+    }
+    {
+      // y pass: columns 2*lane16, +1; rows grp*MY .. +MY-1 of the tile
+      const float* const yw = ywin0 + (i & 1) * C::XBUF;
+      f2_t win[MY + 2 * R];
+#pragma unroll
+      for (int q = 0; q < MY + 2 * R; ++q) win[q] = *reinterpret_cast<const f2_t*>(yw + q * TX);
+      f2_t yv[MY];
+#pragma unroll
+      for (int m = 0; m < MY; ++m) {
+        if constexpr (REF) {
+          float y0 = 0.0f, y1 = 0.0f;
+#pragma unroll
+          for (int k = 0; k < K; ++k) {
+            float v0, v1;
+            unpack2(win[m + k], v0, v1);
+            y0 = tap<true>(y0, v0, a.wy[k]);
+            y1 = tap<true>(y1, v1, a.wy[k]);
+          }
+          yv[m] = pack2(y0, y1);
+        } else {
+          f2_t ay = 0ull;
+#pragma unroll
+          for (int k = 0; k < K; ++k) ay = fma2(win[m + k], a.wy2[k], ay);
+          yv[m] = ay;
+        }
+      }
+      const int col = cy.tx0 - a.x0 + 2 * lane16;
+      const int row0 = cy.ty0 - a.y0 + grp * MY;
+      if (col < a.nxp) {
+        float* tp = a.t + (int64_t)(cy.s - a.t_s0) * a.t_slice + (int64_t)row0 * a.t_row + col;
+#pragma unroll
+        for (int m = 0; m < MY; ++m)
+          if (row0 + m < a.ny) st_f2_hint(tp + m * a.t_row, yv[m], pol_t);
+      }
+      cy.advance(a, TX, TY);
+    }
+  }
+  return;
+timeout:
+  if (tid == 0) {
+    atomicExch(a.fault, 1u);
+    // let this CTA's other tile loads in flight land (bounded) before it exits
+    for (int k = consumed; k < issued; ++k) {
+      const int st = k % S;
+      mbar_wait(bbase + 8 * st, (phase_bits >> st) & 1u);
+      phase_bits ^= 1u << st;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// z pass
+template <int RZ, bool REF>
+__global__ void __launch_bounds__(256) k_z_pass(const __grid_constant__ ZArgs a) {
+  using C = CfgZ<RZ>;
+  constexpr int KZ = C::KZ, S = C::S, NT = C::NT;
+  extern __shared__ __align__(16) float4 zring[];
+  const int tid = threadIdx.x;
+  const int64_t u_begin = a.units * blockIdx.x / gridDim.x;
+  const int64_t u_end = a.units * (blockIdx.x + 1) / gridDim.x;
+  const int64_t nq = (int64_t)a.nqx * a.ny;
+  const uint32_t my_slot0 = smem_u32(zring + tid);
+  const uint64_t pol_t = policy_evict_first();
+
+  for (int64_t u = u_begin; u < u_end;) {
+    const int64_t blk = u / a.nz;
+    const int zs = (int)(u - blk * a.nz);
+    const int64_t zrem = zs + (u_end - u);
+    const int ze = zrem < a.nz ? (int)zrem : a.nz;
+    u += ze - zs;
+    const int64_t q = blk * NT + tid;  // this thread's quad
+    if (q >= nq) continue;             // no barriers in this kernel: idle threads just skip
+    const int qy = (int)(q / a.nqx), qx = (int)(q - (int64_t)(q / a.nqx) * a.nqx);
+    const int z0 = a.z0 + zs, z1 = a.z0 + ze;  // outputs [z0, z1)
+    const int jb = z0 - RZ, je = z1 - 1 + RZ;
+    // prefetch cursor: slice jn (clamped to T) at pn
+    const float* const tq = a.t + (int64_t)qy * a.t_row + 4 * qx;
+    int jn = jb;
+    const float* pn = tq + (int64_t)(clampi(jn, a.t_s0, a.t_s1) - a.t_s0) * a.t_slice;
+    auto prefetch = [&](uint32_t slot) {
+      cp_async16_hint(slot, pn, pol_t);
+      fusedk::cp_async_commit();
+      ++jn;
+      if (jn > a.t_s0 && jn <= a.t_s1) pn += a.t_slice;
+    };
+#pragma unroll
+    for (int i = 0; i < S; ++i) prefetch(my_slot0 + (uint32_t)(i * NT * 16));
+    f2_t acc[2][KZ];
+#pragma unroll
+    for (int m = 0; m < 2; ++m)
+#pragma unroll
+      for (int k = 0; k < KZ; ++k) acc[m][k] = 0ull;
+    const int ncols = min(4, a.nx - 4 * qx);
+    const bool vec = a.vec_store && ncols == 4;
+    char* dz = a.dst + (int64_t)(4 * qx) * a.dst_pitch[0] + (int64_t)qy * a.dst_pitch[1] +
+               (int64_t)(z0 - a.z0) * a.dst_pitch[2];
+    int cur = 0;
+    for (int jbase = jb; jbase <= je; jbase += KZ) {
+#pragma unroll
+      for (int p = 0; p < KZ; ++p) {
+        const int j = jbase + p;
+        if (j > je) break;
+        fusedk::cp_async_wait<S - 1>();
+        const float4 f = zring[cur * NT + tid];
+        const f2_t v0 = pack2(f.x, f.y), v1 = pack2(f.z, f.w);
+#pragma unroll
+        for (int k = 0; k < KZ; ++k) {
+          const int slot = (p - k + KZ) % KZ;
+          if constexpr (REF) {
+            float a0, a1;
+            unpack2(acc[0][slot], a0, a1);
+            acc[0][slot] = pack2(__fadd_rn(a0, __fmul_rn(f.x, a.wz[k])), __fadd_rn(a1, __fmul_rn(f.y, a.wz[k])));
+            unpack2(acc[1][slot], a0, a1);
+            acc[1][slot] = pack2(__fadd_rn(a0, __fmul_rn(f.z, a.wz[k])), __fadd_rn(a1, __fmul_rn(f.w, a.wz[k])));
+          } else {
+            acc[0][slot] = fma2(v0, a.wz2[k], acc[0][slot]);
+            acc[1][slot] = fma2(v1, a.wz2[k], acc[1][slot]);
+          }
+        }
+        // the stage has been read: refill it with slice j + S
+        prefetch(my_slot0 + (uint32_t)(cur * NT * 16));
+        cur = cur + 1 == S ? 0 : cur + 1;
+        const int D = (p + 1) % KZ;  // a constant once the phase loop is unrolled
+        const f2_t d0 = acc[0][D], d1 = acc[1][D];
+        acc[0][D] = 0ull;
+        acc[1][D] = 0ull;
+        if (j - RZ >= z0) {
+          float o[4];
+          unpack2(d0, o[0], o[1]);
+          unpack2(d1, o[2], o[3]);
+          if (vec) {
+            __stcs(reinterpret_cast<float4*>(dz), make_float4(o[0], o[1], o[2], o[3]));
+          } else {
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+              if (c >= ncols) break;
+              char* const dp = dz + c * a.dst_pitch[0];
+              switch (a.out_dtype) {
+                case ITKG_F32: *reinterpret_cast<float*>(dp) = o[c]; break;
+                case ITKG_BF16: *reinterpret_cast<__nv_bfloat16*>(dp) = from_f32<__nv_bfloat16>(o[c]); break;
+                case ITKG_F16: *reinterpret_cast<__half*>(dp) = from_f32<__half>(o[c]); break;
+                default: *reinterpret_cast<uint8_t*>(dp) = from_f32<uint8_t>(o[c]); break;
+              }
+            }
+          }
+          dz += a.dst_pitch[2];
+        }
+      }
+    }
+    fusedk::cp_async_wait<0>();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Kernel tables
+using XYFn = void (*)(const CUtensorMap, const XYArgs);
+using ZFn = void (*)(const ZArgs);
+
+struct XYEntry {
+  int r;
+  int dtype;
+  XYFn fn[2];  // [ref]
+  size_t smem;
+  int tx, ty, bw, ih;
+};
+
+template <int R, typename Tin>
+XYEntry make_xy(int dtype) {
+  using C = CfgXY<R, Tin>;
+  return XYEntry{R, dtype, {k_xy_pass<R, false, Tin>, k_xy_pass<R, true, Tin>}, C::SMEM, C::TX, C::TY, C::BW, C::IH};
+}
+
+// Tables: two_pass.cu (f32 and the z pass) and two_pass_in.cu (i16, u8, bf16, f16).
+const XYEntry* xy_entries_f32(int* n);
+const XYEntry* xy_entries_i16(int* n);
+const XYEntry* xy_entries_u8(int* n);
+const XYEntry* xy_entries_bf16(int* n);
+const XYEntry* xy_entries_f16(int* n);
+ZFn z_fn(int r, bool ref);
+
+#define ITKG_XY_TABLE(T, DT)                                                                      \
+  {                                                                                              \
+    make_xy<1, T>(DT), make_xy<2, T>(DT), make_xy<3, T>(DT), make_xy<4, T>(DT), make_xy<5, T>(DT), \
+        make_xy<6, T>(DT), make_xy<7, T>(DT), make_xy<8, T>(DT)                                   \
+  }
+
+}  // namespace twopass
+}  // namespace itkg

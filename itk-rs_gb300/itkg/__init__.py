@@ -22,15 +22,15 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from ._abi import (ALGO_AUTO, ALGO_FUSED, ALGO_PER_AXIS, ARITH_F32, ARITH_PIXEL_U8, BF16, DEVICE,
-                   F16, F32, HOST, I16, ROUND_FMA, ROUND_REFERENCE, U8, ItkgError, check,
+from ._abi import (ALGO_AUTO, ALGO_FUSED, ALGO_PER_AXIS, ALGO_TWO_PASS, ARITH_F32, ARITH_PIXEL_U8, BF16,
+                   DEVICE, F16, F32, HOST, I16, ROUND_FMA, ROUND_REFERENCE, U8, ItkgError, check,
                    itkg_gaussian_params, itkg_image, itkg_region, lib)
 
 __all__ = [
     "Region", "Image", "DeviceImage", "GaussianFilter", "CastFilter", "stream_full",
     "split_region", "kernel_radius", "build_kernel", "ItkgError", "F32", "I16", "U8", "BF16",
     "F16", "ROUND_REFERENCE", "ROUND_FMA", "ALGO_AUTO", "ALGO_FUSED", "ALGO_PER_AXIS",
-    "ARITH_F32", "ARITH_PIXEL_U8", "gaussian", "Stream",
+    "ALGO_TWO_PASS", "ARITH_F32", "ARITH_PIXEL_U8", "gaussian", "Stream",
 ]
 
 _NP_OF = {F32: np.float32, I16: np.int16, U8: np.uint8, F16: np.float16}

@@ -367,3 +367,166 @@ def test_fused3d_native_inputs(gpu, kind, sigma, spacing):
             assert bits_equal(got, want)
         else:
             assert normwise(got, want) <= 1e-5
+
+
+FUSED2D_CASES = [((1, 1), 1, 1.0), ((7, 600), 1, 1.0), ((64, 64), 1, 0.3), ((130, 1030), 1, 2.6),
+                 ((33, 517), 1, 1.5), ((5, 3), 1, 2.0), ((40, 70), 3, 1.5), ((9, 515), 3, 2.4),
+                 ((1, 40), 3, 0.9), ((200, 100), 3, 0.6)]
+
+
+@pytest.mark.parametrize("shape,comps,sigma", FUSED2D_CASES)
+def test_fused2d_reference_rounding_bit_exact(gpu, shape, comps, sigma):
+    """The fused 2-D kernel (scalar and VecPixel<f32, 3>): bit-exact with the
+    reference pass-by-pass arithmetic."""
+    rng = np.random.default_rng(sum(shape) + comps)
+    arr = rng.standard_normal(shape + ((comps,) if comps > 1 else ())).astype(np.float32)
+    want = oracle.gaussian_f32(arr, sigma, comps=comps)
+    got = run_device(gpu, arr, sigma, comps=comps, algo="fused")
+    assert gpu.last_kernel() == "fused2d_f32_ref", gpu.last_kernel()
+    assert bits_equal(got, want)
+
+
+@pytest.mark.parametrize("shape,comps,sigma", FUSED2D_CASES)
+def test_fused2d_fma_within_1e5(gpu, shape, comps, sigma):
+    rng = np.random.default_rng(3 + sum(shape) + comps)
+    arr = rng.random(shape + ((comps,) if comps > 1 else ()), dtype=np.float32)
+    want = oracle.gaussian_f32(arr, sigma, comps=comps)
+    got = run_device(gpu, arr, sigma, comps=comps, algo="fused", rounding=gpu.ROUND_FMA)
+    assert gpu.last_kernel() == "fused2d_f32_fma", gpu.last_kernel()
+    assert normwise(got, want) <= 1e-5
+
+
+@pytest.mark.parametrize("comps", [1, 3])
+def test_fused2d_subregions_offset_index_and_outputs(gpu, comps):
+    """Requested sub-regions of an image with a non-zero index, and the
+    converted output types, through the fused 2-D kernel."""
+    rng = np.random.default_rng(17 + comps)
+    arr = rng.random((45, 700) + ((comps,) if comps > 1 else ()), dtype=np.float32)
+    index = (-20, 11)
+    for ri, rs in [((-20, 11), (700, 45)), ((480, 20), (200, 9)), ((-20, 55), (1, 1)),
+                   ((0, 11), (513, 45)), ((679, 40), (1, 16))]:
+        want = oracle.gaussian_f32(arr, 1.7, comps=comps, index=index, requested=(ri, rs))
+        got = run_device(gpu, arr, 1.7, comps=comps, index=index, requested=(ri, rs), algo="fused")
+        assert gpu.last_kernel() == "fused2d_f32_ref", gpu.last_kernel()
+        assert bits_equal(got, want), (ri, rs)
+    want = oracle.gaussian_f32(arr * 255, 1.7, comps=comps)
+    got = run_device(gpu, arr * 255, 1.7, comps=comps, algo="fused", out_dtype=gpu.U8)
+    assert gpu.last_kernel() == "fused2d_f32_ref", gpu.last_kernel()
+    assert np.array_equal(got, oracle.cast_f32_to_u8(want))
+
+
+def test_fused2d_falls_back_for_unequal_radii(gpu):
+    """Anisotropic radii have no fused 2-D kernel: auto takes the per-axis
+    path (still bit-exact) and an explicit fused request is refused."""
+    from itkg import _abi
+    rng = np.random.default_rng(5)
+    arr = rng.random((30, 40), dtype=np.float32)
+    want = oracle.gaussian_f32(arr, 1.5, spacing=(0.5, 1.0))
+    got = run_device(gpu, arr, 1.5, spacing=(0.5, 1.0))
+    assert gpu.last_kernel().startswith("per_axis"), gpu.last_kernel()
+    assert bits_equal(got, want)
+    with pytest.raises(_abi.ItkgError):
+        run_device(gpu, arr, 1.5, spacing=(0.5, 1.0), algo="fused")
+
+
+TWO_PASS_CASES = [((9, 17, 31), 1.0, None), ((16, 16, 16), 2.0, None), ((40, 50, 70), 2.0, None),
+                  ((5, 70, 40), 2.2, None), ((12, 130, 70), 2.6, None), ((1, 1, 1), 1.0, None),
+                  ((33, 65, 97), 1.5, None), ((20, 20, 20), 0.3, None), ((3, 40, 33), 1.2, None),
+                  ((24, 48, 40), 1.5, (0.7, 0.7, 2.5)), ((30, 20, 10), 1.0, (1.0, 1.0, 0.5))]
+
+
+@pytest.mark.parametrize("shape,sigma,spacing", TWO_PASS_CASES)
+def test_two_pass_reference_rounding_bit_exact(gpu, shape, sigma, spacing):
+    """x-y slice kernel + z kernel: bit-exact with the reference pass by pass."""
+    rng = np.random.default_rng(5 + sum(shape))
+    arr = rng.standard_normal(shape).astype(np.float32)
+    want = oracle.gaussian_f32(arr, sigma, spacing=spacing)
+    img = gpu.Image(arr, spacing=spacing)
+    dev = gpu.DeviceImage.from_host(img)
+    got = gpu.GaussianFilter(dev, sigma, algorithm=gpu.ALGO_TWO_PASS).generate_region(img.region).download()
+    assert gpu.last_kernel() == "z_pass_f32_ref", gpu.last_kernel()
+    assert bits_equal(got, want)
+
+
+@pytest.mark.parametrize("shape,sigma,spacing", TWO_PASS_CASES)
+def test_two_pass_fma_within_1e5(gpu, shape, sigma, spacing):
+    rng = np.random.default_rng(6 + sum(shape))
+    arr = rng.random(shape, dtype=np.float32)
+    want = oracle.gaussian_f32(arr, sigma, spacing=spacing)
+    img = gpu.Image(arr, spacing=spacing)
+    dev = gpu.DeviceImage.from_host(img)
+    f = gpu.GaussianFilter(dev, sigma, rounding=gpu.ROUND_FMA, algorithm=gpu.ALGO_TWO_PASS)
+    got = f.generate_region(img.region).download()
+    assert gpu.last_kernel() == "z_pass_f32_fma", gpu.last_kernel()
+    assert normwise(got, want) <= 1e-5
+
+
+def test_two_pass_chunked_z_bit_exact(gpu):
+    """1024 x 1024 slices: the intermediate is split into several z chunks
+    (each with its own halo slices); the result must not depend on it."""
+    rng = np.random.default_rng(77)
+    arr = rng.random((23, 1024, 1024), dtype=np.float32)
+    for sigma, spacing in [(1.0, (1.0, 1.0, 1.5)), (0.5, None)]:
+        want = oracle.gaussian_f32(arr, sigma, spacing=spacing)
+        img = gpu.Image(arr, spacing=spacing)
+        dev = gpu.DeviceImage.from_host(img)
+        got = gpu.GaussianFilter(dev, sigma, algorithm=gpu.ALGO_TWO_PASS).generate_region(img.region).download()
+        assert gpu.last_kernel() == "z_pass_f32_ref"
+        assert bits_equal(got, want)
+
+
+def test_two_pass_subregions_offset_index_and_outputs(gpu):
+    rng = np.random.default_rng(31)
+    arr = rng.random((30, 41, 53), dtype=np.float32)
+    index = (8, -3, 100)
+    for ri, rs in [((8, -3, 100), (53, 41, 30)), ((12, 0, 104), (33, 20, 11)), ((60, 37, 129), (1, 1, 1)),
+                   ((16, -3, 110), (4, 41, 6)), ((8, 30, 100), (45, 8, 30))]:
+        want = oracle.gaussian_f32(arr, 1.9, index=index, requested=(ri, rs))
+        img = gpu.Image(arr, index=index)
+        dev = gpu.DeviceImage.from_host(img)
+        f = gpu.GaussianFilter(dev, 1.9, algorithm=gpu.ALGO_TWO_PASS)
+        got = f.generate_region(gpu.Region(ri, rs)).download()
+        assert gpu.last_kernel() == "z_pass_f32_ref", gpu.last_kernel()
+        assert bits_equal(got, want), (ri, rs)
+    # converted outputs
+    img = gpu.Image(arr * 255, index=index)
+    dev = gpu.DeviceImage.from_host(img)
+    want = oracle.gaussian_f32(arr * 255, 1.9, index=index)
+    got = gpu.GaussianFilter(dev, 1.9, algorithm=gpu.ALGO_TWO_PASS).generate_region(img.region, out_dtype=gpu.U8)
+    assert np.array_equal(got.download(), oracle.cast_f32_to_u8(want))
+
+
+def test_two_pass_refuses_unaligned_start_and_auto_falls_back(gpu):
+    """A requested x start that is not 16-byte aligned within the buffer has
+    no TMA tile: an explicit two-pass request is refused, auto still gives the
+    bit-exact result through another kernel."""
+    from itkg import _abi
+    rng = np.random.default_rng(32)
+    arr = rng.random((12, 20, 30), dtype=np.float32)
+    img = gpu.Image(arr)
+    dev = gpu.DeviceImage.from_host(img)
+    req = gpu.Region((3, 0, 0), (20, 20, 12))
+    with pytest.raises(_abi.ItkgError):
+        gpu.GaussianFilter(dev, 1.2, algorithm=gpu.ALGO_TWO_PASS).generate_region(req)
+    got = gpu.GaussianFilter(dev, 1.2).generate_region(req).download()
+    assert not gpu.last_kernel().startswith("z_pass"), gpu.last_kernel()
+    assert bits_equal(got, oracle.gaussian_f32(arr, 1.2, requested=((3, 0, 0), (20, 20, 12))))
+
+
+@pytest.mark.parametrize("kind", ["i16", "u8", "bf16", "f16"])
+def test_two_pass_native_inputs(gpu, kind):
+    rng = np.random.default_rng(43)
+    raw, f32 = _typed_input(kind, (22, 40, 56), rng)
+    spacing = (0.7, 0.7, 2.5)
+    want = oracle.gaussian_f32(f32, 1.5, spacing=spacing)
+    img = gpu.Image(raw, spacing=spacing, bf16=(kind == "bf16"))
+    dev = gpu.DeviceImage.from_host(img)
+    for rounding in (gpu.ROUND_REFERENCE, gpu.ROUND_FMA):
+        f = gpu.GaussianFilter(gpu.CastFilter(dev, gpu.F32), 1.5, rounding=rounding,
+                               algorithm=gpu.ALGO_TWO_PASS, arithmetic=gpu.ARITH_F32)
+        got = f.generate_region(dev.region).download()
+        assert gpu.last_kernel().startswith("z_pass_f32"), gpu.last_kernel()
+        if rounding == gpu.ROUND_REFERENCE:
+            assert bits_equal(got, want)
+        else:
+            assert normwise(got, want) <= 1e-5
