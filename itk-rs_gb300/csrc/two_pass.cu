@@ -82,6 +82,12 @@ itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], v
   if (!e) return ITKG_ERROR_UNSUPPORTED;
   const int esz = dtype_size(g.in_dtype);
   if (g.src_pitch[0] != esz) return ITKG_ERROR_UNSUPPORTED;
+  // FMA rounding reads zeros outside the input buffer as the halo and adds the
+  // clamped taps back at the image's edges: the buffer must lie inside the
+  // image on x and y.
+  if (g.rounding != ITKG_ROUND_REFERENCE)
+    for (int d = 0; d < 2; ++d)
+      if (g.src_origin[d] < g.lo[d] || g.src_origin[d] + g.src_size[d] - 1 > g.hi[d]) return ITKG_ERROR_UNSUPPORTED;
   // TMA: 16-byte base and pitches, 16-byte aligned first tile column
   const int ae = 16 / esz;
   if (((uintptr_t)g.src & 15) || (g.src_pitch[1] & 15) || (g.src_pitch[2] & 15)) return ITKG_ERROR_UNSUPPORTED;
@@ -126,7 +132,7 @@ itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], v
   int res_xy = 0, res_z = 0;
   const twopass::ZFn zfn = twopass::z_fn(rz, ref);
   const twopass::XYFn xyfn = e->fn[ref ? 1 : 0];
-  if (st == ITKG_SUCCESS) st = max_resident_ctas(reinterpret_cast<const void*>(xyfn), e->smem, 256, &res_xy);
+  if (st == ITKG_SUCCESS) st = max_resident_ctas(reinterpret_cast<const void*>(xyfn), e->smem, e->nt, &res_xy);
   if (st == ITKG_SUCCESS)
     st = max_resident_ctas(reinterpret_cast<const void*>(zfn), twopass::CfgZ<1>::SMEM, 256, &res_z);
   if (st != ITKG_SUCCESS) {
@@ -148,10 +154,37 @@ itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], v
   xa.ny = (int32_t)ny;
   xa.ntx = (int32_t)((nx + e->tx - 1) / e->tx);
   const int64_t nty = (ny + e->ty - 1) / e->ty;
-  const int K = 2 * g.radius[0] + 1;
+  const int R = g.radius[0], K = 2 * R + 1;
   for (int k = 0; k < K; ++k) {
     xa.wx[k] = w[0][k], xa.wx2[k] = splat2_host(w[0][k]);
     xa.wy[k] = w[1][k], xa.wy2[k] = splat2_host(w[1][k]);
+  }
+  xa.nty = (int32_t)nty;
+  {
+    // clamped-tap weights of the first / last tile column and row (FMA rounding)
+    double p[twopass::kMaxK + 1] = {0.0};
+    for (int k = 0; k < K; ++k) p[k + 1] = p[k] + w[0][k];
+    double q[twopass::kMaxK + 1] = {0.0};
+    for (int k = 0; k < K; ++k) q[k + 1] = q[k] + w[1][k];
+    auto coef = [&](const double* pp, int64_t d) { return (d >= 0 && d < R) ? (float)pp[R - d] : 0.0f; };
+    xa.xr0 = std::max(0, xa.ntx - 2);
+    xa.yr0 = std::max(0, (int)nty - 2);
+    const int64_t tx_r = g.req_index[0] + (int64_t)xa.xr0 * e->tx;  // first of the last two tile columns
+    const int64_t ty_r = g.req_index[1] + (int64_t)xa.yr0 * e->ty;
+    for (int t = 0; t < 32; ++t) {
+      xa.cxl[t] = coef(p, g.req_index[0] + t - xa.lo[0]);
+      if (xa.cxl[t] != 0.0f) xa.edge |= 1;
+    }
+    for (int t = 0; t < 64; ++t) {
+      xa.cxr[t] = coef(p, xa.hi[0] - (tx_r + t));
+      xa.cyt[t] = coef(q, g.req_index[1] + t - xa.lo[1]);
+      if (xa.cxr[t] != 0.0f) xa.edge |= 2;
+      if (xa.cyt[t] != 0.0f) xa.edge |= 4;
+    }
+    for (int t = 0; t < 128; ++t) {
+      xa.cyb[t] = coef(q, xa.hi[1] - (ty_r + t));
+      if (xa.cyb[t] != 0.0f) xa.edge |= 8;
+    }
   }
   za.t = t;
   za.t_row = nxp;
@@ -179,9 +212,9 @@ itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], v
     xa.s0 = (int32_t)s0;
     xa.ns = (int32_t)(s1 - s0 + 1);
     xa.t_s0 = (int32_t)s0;
-    xa.units = xa.ntx * nty * xa.ns;
+    xa.units = (int64_t)xa.ntx * nty * xa.ns;
     const int64_t gxy = std::min<int64_t>(xa.units, res_xy);
-    xyfn<<<(unsigned)gxy, 256, e->smem, s>>>(map, xa);
+    xyfn<<<(unsigned)gxy, e->nt, e->smem, s>>>(map, xa);
     note_launch(xy_name(g.in_dtype, ref));
     cudaError_t err = cudaGetLastError();
     if (err != cudaSuccess) {

@@ -5,18 +5,20 @@
 //            after its second pass, restricted to the requested x-y range);
 //   z pass:  the third pass, streaming T along z.
 // Neither kernel recomputes anything along z, and the z pass needs no shared
-// tile and no block barrier, so both stay close to the memory system's rate.
-// T is sized to stay in L2 (the launcher splits long z ranges into chunks),
-// so it costs little HBM traffic.
+// tile and no block barrier.  Long z ranges are split into chunks whose
+// intermediate fits a budget, so T stays a bounded scratch buffer.
 //
 // xy pass.  A CTA runs a contiguous range of (tile, slice) units.  The
 // (TX + 2XA) x (TY + 2RY) input tile of each unit lands in shared memory by one
-// TMA tile load (S units in flight, mbarrier completion, bounded waits); edge
-// tiles replicate the image's edge values into the halo (clamp-to-edge,
-// conv.rs:31-33).  The x pass writes a double-buffered f32 tile, so the x pass
-// of unit i + 1 and the y pass of unit i share one barrier interval.  The y
-// pass gives each thread two adjacent columns (one packed f32x2 register per
-// row) and MY consecutive rows, read from a register window.
+// TMA tile load (S units in flight, mbarrier completion, bounded waits).  The
+// x pass reads clamped rows and, on tiles at an x edge of the image, replaces
+// the halo columns outside the image by the edge column in registers
+// (clamp-to-edge, conv.rs:31-33).  It writes a double-buffered f32 tile, so the
+// x pass of unit i + 1 and the y pass of unit i share one barrier interval.
+// The y pass gives each thread two adjacent columns (one packed f32x2 register
+// per row) and MY consecutive rows, read from a register window.  Row strides
+// of the staged and x-filtered tiles are padded so that these shared-memory
+// accesses are free of bank conflicts.
 //
 // z pass.  A thread owns four consecutive columns of one row of T and marches
 // a z-segment: slice j is copied by cp.async into the thread's own shared
@@ -56,11 +58,23 @@ struct XYArgs {
   int32_t nxp, ny;       // T row length (floats, multiple of 4) and rows
   int32_t s0, ns;        // first slice of this launch (absolute z) and slice count
   int32_t t_s0;          // absolute z of T's slice 0
-  int32_t ntx;           // tiles along x
+  int32_t ntx, nty;      // tiles along x and y
   int64_t units;         // ntx * nty * ns
   unsigned int* fault;
   float wx[kMaxK], wy[kMaxK];
   f2_t wx2[kMaxK], wy2[kMaxK];
+  // FMA rounding: the weight of the clamped taps of each output column of the
+  // first tile column (cxl) and of the last two (cxr, tile columns xr0 and
+  // xr0 + 1), and of each output row of the first tile row (cyt) and of the
+  // last two (cyb, tile rows yr0 and yr0 + 1): p[R - d] for an output d < R
+  // inside an image edge (p[j] = w[0] + ... + w[j-1]; the same at both edges,
+  // the kernel being symmetric), else 0.  Only these tiles reach an edge
+  // (R < TX, TY).  edge: bit 0/1/2/3 = some coefficient of cxl/cxr/cyt/cyb is
+  // nonzero.
+  float cxl[32], cxr[64], cyt[64], cyb[128];
+  int32_t xr0, yr0;
+  int32_t edge;
+  int32_t pad2_;
 };
 
 struct ZArgs {
@@ -83,25 +97,32 @@ template <int R, typename Tin>
 struct CfgXY {
   static constexpr int K = 2 * R + 1;
   static constexpr int ESZ = (int)sizeof(Tin);
-  static constexpr int NT = 256;
+  static constexpr int NT = 320;                // one x-pass task per thread (IH * SEGS <= 320)
+  static constexpr int NTY = 256;               // threads of the y pass
   static constexpr int TX = 32;                 // 16 lanes x 2 columns
   static constexpr int MY = 4;                  // rows per thread in the y pass
-  static constexpr int TY = (NT / 16) * MY;     // 64
+  static constexpr int TY = (NTY / 16) * MY;    // 64
   static constexpr int MX = 8;                  // x outputs per x-pass task
+  static constexpr int SEGS = TX / MX;
   static constexpr int AE = 16 / ESZ;
   static constexpr int XA = (R + AE - 1) / AE * AE;
-  static constexpr int BW = TX + 2 * XA;
+  // Staged row: TX + 2XA columns; f32 rows get 4 more (loaded and unused) so
+  // that consecutive rows start 16 banks + 4 apart (conflict-free 16-byte loads).
+  static constexpr int BW = TX + 2 * XA + (ESZ == 4 ? 4 : 0);
   static constexpr int IH = TY + 2 * R;
+  static constexpr int NTASK = IH * SEGS;       // x-pass tasks per unit
   static constexpr int OFF = (XA - R) % 4;
   static constexpr int WB = XA - R - OFF;
   static constexpr int WIN = (MX + 2 * R + OFF + 3) / 4 * 4;
   static constexpr int S = 3;                   // units in flight
   static constexpr int BOX = IH * BW * ESZ;
   static constexpr int STAGE = (BOX + 127) / 128 * 128;
-  static constexpr int XBUF = IH * TX;          // floats per x-filtered tile
+  static constexpr int TXP = TX + 4;            // x-filtered row stride (floats)
+  static constexpr int XBUF = IH * TXP;         // floats per x-filtered tile
   static constexpr size_t SMEM = (size_t)S * STAGE + sizeof(float) * 2 * XBUF + 128;
   static_assert(WB + TX - MX + WIN <= BW, "x window stays inside the staged row");
   static_assert(TX % MX == 0, "x segments");
+  static_assert(NTASK <= NT, "each thread runs at most one x-pass task");
 };
 
 template <int RZ>
@@ -166,14 +187,15 @@ struct UnitCursor {
 // ---------------------------------------------------------------------------
 // xy pass
 template <int R, bool REF, typename Tin>
-__global__ void __launch_bounds__(256, 3)
+__global__ void __launch_bounds__(320, 3)
     k_xy_pass(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ XYArgs a) {
   using C = CfgXY<R, Tin>;
   constexpr int K = C::K, TX = C::TX, TY = C::TY, MY = C::MY, MX = C::MX, BW = C::BW, IH = C::IH,
-                XA = C::XA, S = C::S, WIN = C::WIN, WB = C::WB, OFF = C::OFF, NT = C::NT;
-  constexpr int SEGS = TX / MX;
+                XA = C::XA, S = C::S, WIN = C::WIN, WB = C::WB, OFF = C::OFF, NT = C::NT, SEGS = C::SEGS,
+                TXP = C::TXP, NTASK = C::NTASK;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t mbar[S];
+  __shared__ int s_fail;
   unsigned char* const stage0 = smem + ((128u - (smem_u32(smem) & 127u)) & 127u);
   float* const xbuf0 = reinterpret_cast<float*>(stage0 + S * C::STAGE);
   const uint32_t sbase = smem_u32(stage0);
@@ -182,6 +204,7 @@ __global__ void __launch_bounds__(256, 3)
   if (tid == 0) {
     for (int i = 0; i < S; ++i) mbar_init(bbase + 8 * i, 1);
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    s_fail = 0;
   }
   __syncthreads();
   uint32_t phase_bits = 0;
@@ -203,6 +226,10 @@ __global__ void __launch_bounds__(256, 3)
   const uint64_t pol_in = policy_evict_first();
   const uint64_t pol_t = policy_evict_last();
 
+  // this thread's x-pass task: (row, 8-column segment), if tid < NTASK
+  const int row_a = tid / SEGS, x0_a = (tid % SEGS) * MX;
+  const bool has_x = tid < NTASK;
+
   int issued = 0, consumed = 0;  // units whose load was issued / waited for (uniform)
   auto issue_next = [&]() {      // tile load of unit `issued` (cursor ci)
     if (issued >= n) return;
@@ -217,90 +244,119 @@ __global__ void __launch_bounds__(256, 3)
     ++issued;
     ci.advance(a, TX, TY);
   };
-  // Waits for the tile of unit `consumed` (cursor cx) and runs its x pass
-  // into xb.  Halo rows outside the image read the clamped row and halo
-  // columns outside it take the edge column's value (clamp-to-edge).
-  auto xpass_next = [&](float* xb) -> bool {
-    const int st = consumed % S;
-    const Tin* const tile = reinterpret_cast<const Tin*>(stage0 + st * C::STAGE);
-    const bool ok = mbar_wait(bbase + 8 * st, (phase_bits >> st) & 1u);
-    phase_bits ^= 1u << st;
-    ++consumed;
-    const int gx0 = cx.tx0 - XA, gy0 = cx.ty0 - R;
-    cx.advance(a, TX, TY);
-    if (!ok) return false;
-    const int nl = max(0, a.lo[0] - gx0);            // first in-image column of the tile
-    const int cr = min(BW - 1, a.hi[0] - gx0);       // last in-image column of the tile
-    const int rlo = a.lo[1] - gy0, rhi = a.hi[1] - gy0;
-    for (int t = tid; t < IH * SEGS; t += NT) {
-      const int row = t / SEGS, x0 = (t % SEGS) * MX;
-      const int srow = min(max(row, rlo), rhi);
+  // One x-pass task: staged row `row`, columns x0 .. x0 + MX - 1 of the tile,
+  // into xb.  nl / cr: staged columns of the image's first / last column;
+  // rlo / rhi: staged rows of its first / last row.
+  //   Reference rounding clamps: halo rows read the edge row, halo columns
+  //   take the edge column's value (the reference's arithmetic exactly).
+  //   FMA rounding filters the zero-filled halo (the input buffer lies inside
+  //   the image) and adds the clamped taps back, p[R - d] * x[edge], to the
+  //   outputs d < R columns inside an edge.
+  auto xtask = [&](const Tin* tile, float* xb, int row, int x0, bool yedge, int rlo, int rhi, int xedge, int nl,
+                   int cr) {
+    float o[MX];
+    if constexpr (REF) {
+      const int srow = yedge ? min(max(row, rlo), rhi) : row;
       const Tin* const src = tile + srow * BW;
       float v[WIN];
 #pragma unroll
       for (int q = 0; q < WIN / 4; ++q) load4(src + x0 + WB + 4 * q, v + 4 * q);
-      if (x0 + WB < nl || x0 + WB + WIN - 1 > cr) {
-        const float vl = ld1(src + nl), vr = ld1(src + cr);
+      if (xedge) {
+        const float vl = ld1(src + max(nl, 0)), vr = ld1(src + min(cr, BW - 1));
+        const int c0 = x0 + WB;
 #pragma unroll
         for (int q = 0; q < WIN; ++q) {
-          const int c = x0 + WB + q;
-          v[q] = c < nl ? vl : (c > cr ? vr : v[q]);
+          v[q] = c0 + q < nl ? vl : v[q];
+          v[q] = c0 + q > cr ? vr : v[q];
         }
       }
-      float o[MX];
-      if constexpr (REF) {
 #pragma unroll
-        for (int m = 0; m < MX; ++m) {
-          float ax = 0.0f;
+      for (int m = 0; m < MX; ++m) {
+        float ax = 0.0f;
 #pragma unroll
-          for (int k = 0; k < K; ++k) ax = tap<true>(ax, v[m + k + OFF], a.wx[k]);
-          o[m] = ax;
+        for (int k = 0; k < K; ++k) ax = tap<true>(ax, v[m + k + OFF], a.wx[k]);
+        o[m] = ax;
+      }
+    } else {
+      (void)yedge, (void)rlo, (void)rhi;
+      const Tin* const src = tile + row * BW;
+      float v[WIN];
+#pragma unroll
+      for (int q = 0; q < WIN / 4; ++q) load4(src + x0 + WB + 4 * q, v + 4 * q);
+      f2_t E[WIN / 2], O[WIN / 2 - 1];
+#pragma unroll
+      for (int q = 0; q < WIN / 2; ++q) E[q] = pack2(v[2 * q], v[2 * q + 1]);
+#pragma unroll
+      for (int q = 0; q < WIN / 2 - 1; ++q) O[q] = pack2(v[2 * q + 1], v[2 * q + 2]);
+#pragma unroll
+      for (int m = 0; m < MX / 2; ++m) {
+        f2_t ax = 0ull;
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+          const int q = 2 * m + k + OFF;
+          ax = fma2((q & 1) ? O[(q - 1) / 2] : E[q / 2], a.wx2[k], ax);
         }
-      } else {
-        f2_t E[WIN / 2], O[WIN / 2 - 1];
+        unpack2(ax, o[2 * m], o[2 * m + 1]);
+      }
+      if (xedge) {  // here: bit 0 = first tile column, bit 1 = last, with corrections
+        if (xedge & 1) {
+          const float xl = ld1(src + nl);
 #pragma unroll
-        for (int q = 0; q < WIN / 2; ++q) E[q] = pack2(v[2 * q], v[2 * q + 1]);
+          for (int m = 0; m < MX; ++m) o[m] = fmaf(a.cxl[x0 + m], xl, o[m]);
+        }
+        if (xedge & 2) {  // (xedge >> 2): which of the last two tile columns
+          const float xr = ld1(src + min(cr, BW - 1));
+          const float* const c = a.cxr + (xedge >> 2) * TX + x0;
 #pragma unroll
-        for (int q = 0; q < WIN / 2 - 1; ++q) O[q] = pack2(v[2 * q + 1], v[2 * q + 2]);
-#pragma unroll
-        for (int m = 0; m < MX / 2; ++m) {
-          f2_t ax = 0ull;
-#pragma unroll
-          for (int k = 0; k < K; ++k) {
-            const int q = 2 * m + k + OFF;
-            ax = fma2((q & 1) ? O[(q - 1) / 2] : E[q / 2], a.wx2[k], ax);
-          }
-          unpack2(ax, o[2 * m], o[2 * m + 1]);
+          for (int m = 0; m < MX; ++m) o[m] = fmaf(c[m], xr, o[m]);
         }
       }
-      float4* d4 = reinterpret_cast<float4*>(xb + row * TX + x0);
-#pragma unroll
-      for (int q = 0; q < MX / 4; ++q) d4[q] = make_float4(o[4 * q], o[4 * q + 1], o[4 * q + 2], o[4 * q + 3]);
     }
-    return true;
+    float4* d4 = reinterpret_cast<float4*>(xb + row * TXP + x0);
+#pragma unroll
+    for (int q = 0; q < MX / 4; ++q) d4[q] = make_float4(o[4 * q], o[4 * q + 1], o[4 * q + 2], o[4 * q + 3]);
+  };
+  // Waits for the tile of unit `consumed` (cursor cx) and runs its x pass into xb.
+  auto xpass_next = [&](float* xb) {
+    const int st = consumed % S;
+    const Tin* const tile = reinterpret_cast<const Tin*>(stage0 + st * C::STAGE);
+    if (!mbar_wait(bbase + 8 * st, (phase_bits >> st) & 1u)) s_fail = 1;  // checked after the next barrier
+    phase_bits ^= 1u << st;
+    ++consumed;
+    const int gx0 = cx.tx0 - XA, gy0 = cx.ty0 - R;
+    cx.advance(a, TX, TY);
+    const int nl = a.lo[0] - gx0;  // first in-image staged column (> 0 only at the left edge)
+    const int cr = a.hi[0] - gx0;  // last in-image staged column (< BW - 1 only at the right edge)
+    const int rlo = a.lo[1] - gy0, rhi = a.hi[1] - gy0;
+    const bool yedge = rlo > 0 || rhi < IH - 1;
+    int xedge;
+    if constexpr (REF) {
+      xedge = (nl > 0 || cr < BW - 1) ? 1 : 0;
+    } else {  // first / last tile column with clamped taps to add back
+      const int tcol = (gx0 + XA - a.x0) / TX - a.xr0;  // 0 / 1: the last two tile columns
+      xedge = ((gx0 + XA == a.x0) && (a.edge & 1) ? 1 : 0) |
+              ((tcol >= 0) && (a.edge & 2) ? 2 | (tcol << 2) : 0);
+    }
+    if (has_x) xtask(tile, xb, row_a, x0_a, yedge, rlo, rhi, xedge, nl, cr);
   };
 
   const int lane16 = tid & 15, grp = tid >> 4;
-  const float* const ywin0 = xbuf0 + grp * MY * TX + 2 * lane16;  // this thread's y window
+  const bool has_y = tid < C::NTY;
+  const float* const ywin0 = xbuf0 + (has_y ? grp : 0) * MY * TXP + 2 * lane16;  // this thread's y window
   for (int q = 0; q < S; ++q) issue_next();
-  bool ok = xpass_next(xbuf0);
-  if (__syncthreads_or(!ok)) goto timeout;
+  xpass_next(xbuf0);
   for (int i = 0; i < n; ++i) {
-    if (i > 0) {
-      // x pass of unit i visible; y pass of unit i - 1 done with the other buffer
-      __syncthreads();
-    }
+    // x pass of unit i visible; y pass of unit i - 1 done with the other buffer
+    __syncthreads();
+    if (s_fail) goto timeout;
     issue_next();  // into the stage unit i's x pass has finished reading
-    if (i + 1 < n) {
-      ok = xpass_next(xbuf0 + ((i + 1) & 1) * C::XBUF);
-      if (__syncthreads_or(!ok)) goto timeout;
-    }
-    {
+    if (i + 1 < n) xpass_next(xbuf0 + ((i + 1) & 1) * C::XBUF);
+    if (has_y) {
       // y pass: columns 2*lane16, +1; rows grp*MY .. +MY-1 of the tile
       const float* const yw = ywin0 + (i & 1) * C::XBUF;
       f2_t win[MY + 2 * R];
 #pragma unroll
-      for (int q = 0; q < MY + 2 * R; ++q) win[q] = *reinterpret_cast<const f2_t*>(yw + q * TX);
+      for (int q = 0; q < MY + 2 * R; ++q) win[q] = *reinterpret_cast<const f2_t*>(yw + q * TXP);
       f2_t yv[MY];
 #pragma unroll
       for (int m = 0; m < MY; ++m) {
@@ -321,6 +377,28 @@ __global__ void __launch_bounds__(256, 3)
           yv[m] = ay;
         }
       }
+      if constexpr (!REF) {
+        // first / last tile row: the clamped taps, c[row] * X[edge row]
+        if ((a.edge & 4) && cy.ty0 == a.y0) {
+          const f2_t xe = *reinterpret_cast<const f2_t*>(xbuf0 + (i & 1) * C::XBUF + (a.lo[1] - a.y0 + R) * TXP +
+                                                         2 * lane16);
+#pragma unroll
+          for (int m = 0; m < MY; ++m) {
+            const float c = a.cyt[grp * MY + m];
+            yv[m] = fma2(xe, pack2(c, c), yv[m]);
+          }
+        }
+        const int trow = (cy.ty0 - a.y0) / TY - a.yr0;  // 0 / 1: the last two tile rows
+        if ((a.edge & 8) && trow >= 0 && a.hi[1] - cy.ty0 + R < IH) {
+          const f2_t xe = *reinterpret_cast<const f2_t*>(xbuf0 + (i & 1) * C::XBUF +
+                                                         (a.hi[1] - cy.ty0 + R) * TXP + 2 * lane16);
+#pragma unroll
+          for (int m = 0; m < MY; ++m) {
+            const float c = a.cyb[trow * TY + grp * MY + m];
+            yv[m] = fma2(xe, pack2(c, c), yv[m]);
+          }
+        }
+      }
       const int col = cy.tx0 - a.x0 + 2 * lane16;
       const int row0 = cy.ty0 - a.y0 + grp * MY;
       if (col < a.nxp) {
@@ -329,8 +407,8 @@ __global__ void __launch_bounds__(256, 3)
         for (int m = 0; m < MY; ++m)
           if (row0 + m < a.ny) st_f2_hint(tp + m * a.t_row, yv[m], pol_t);
       }
-      cy.advance(a, TX, TY);
     }
+    cy.advance(a, TX, TY);
   }
   return;
 timeout:
@@ -409,6 +487,9 @@ __global__ void __launch_bounds__(256) k_z_pass(const __grid_constant__ ZArgs a)
             acc[0][slot] = pack2(__fadd_rn(a0, __fmul_rn(f.x, a.wz[k])), __fadd_rn(a1, __fmul_rn(f.y, a.wz[k])));
             unpack2(acc[1][slot], a0, a1);
             acc[1][slot] = pack2(__fadd_rn(a0, __fmul_rn(f.z, a.wz[k])), __fadd_rn(a1, __fmul_rn(f.w, a.wz[k])));
+          } else if (k == 0) {  // first contribution to output j + RZ: its slot was popped
+            acc[0][slot] = mul2(v0, a.wz2[0]);
+            acc[1][slot] = mul2(v1, a.wz2[0]);
           } else {
             acc[0][slot] = fma2(v0, a.wz2[k], acc[0][slot]);
             acc[1][slot] = fma2(v1, a.wz2[k], acc[1][slot]);
@@ -419,8 +500,10 @@ __global__ void __launch_bounds__(256) k_z_pass(const __grid_constant__ ZArgs a)
         cur = cur + 1 == S ? 0 : cur + 1;
         const int D = (p + 1) % KZ;  // a constant once the phase loop is unrolled
         const f2_t d0 = acc[0][D], d1 = acc[1][D];
-        acc[0][D] = 0ull;
-        acc[1][D] = 0ull;
+        if constexpr (REF) {  // reference rounding adds the first product to zero
+          acc[0][D] = 0ull;
+          acc[1][D] = 0ull;
+        }
         if (j - RZ >= z0) {
           float o[4];
           unpack2(d0, o[0], o[1]);
@@ -458,13 +541,15 @@ struct XYEntry {
   int dtype;
   XYFn fn[2];  // [ref]
   size_t smem;
-  int tx, ty, bw, ih;
+  int nt;              // threads per CTA
+  int tx, ty, bw, ih;  // tile, TMA box
 };
 
 template <int R, typename Tin>
 XYEntry make_xy(int dtype) {
   using C = CfgXY<R, Tin>;
-  return XYEntry{R, dtype, {k_xy_pass<R, false, Tin>, k_xy_pass<R, true, Tin>}, C::SMEM, C::TX, C::TY, C::BW, C::IH};
+  return XYEntry{R, dtype, {k_xy_pass<R, false, Tin>, k_xy_pass<R, true, Tin>}, C::SMEM, C::NT, C::TX, C::TY, C::BW,
+                 C::IH};
 }
 
 // Tables: two_pass.cu (f32 and the z pass) and two_pass_in.cu (i16, u8, bf16, f16).

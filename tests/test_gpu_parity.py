@@ -530,3 +530,38 @@ def test_two_pass_native_inputs(gpu, kind):
             assert bits_equal(got, want)
         else:
             assert normwise(got, want) <= 1e-5
+
+
+def test_two_pass_fma_subregions_and_tight_buffers(gpu):
+    """FMA rounding filters a zero-filled halo and adds the clamped taps back at
+    the image's edges; check it on requested sub-regions, with the input buffer
+    both the whole image and exactly input_region_for_output."""
+    import ctypes
+    from itkg import _abi
+    rng = np.random.default_rng(23)
+    full = rng.random((30, 41, 53), dtype=np.float32)
+    img = gpu.Image(full)
+    dev_full = gpu.DeviceImage.from_host(img)
+    for sigma in (0.4, 1.9, 2.5):
+        # x starts on 16-byte boundaries of the whole-image buffer (a TMA tile rule)
+        for ri, rs in [((0, 0, 0), (53, 41, 30)), ((8, 5, 4), (33, 20, 11)), ((48, 40, 29), (5, 1, 1)),
+                       ((12, 0, 12), (1, 41, 6)), ((0, 35, 0), (53, 6, 30))]:
+            want = oracle.gaussian_f32(full, sigma, requested=(ri, rs))
+            f = gpu.GaussianFilter(dev_full, sigma, rounding=gpu.ROUND_FMA, algorithm=gpu.ALGO_TWO_PASS)
+            got = f.generate_region(gpu.Region(ri, rs)).download()
+            assert gpu.last_kernel() == "z_pass_f32_fma"
+            assert normwise(got, want) <= 1e-5, (sigma, ri, rs)
+            need = gpu.GaussianFilter(img, sigma).input_region_for_output(gpu.Region(ri, rs))
+            (x0, y0, z0), (sx, sy, sz) = need.index, need.size
+            if (x0 - ri[0]) % 4:
+                continue  # no 16-byte aligned tile start in this tight buffer
+            dev = gpu.DeviceImage(need)
+            dev.upload(np.ascontiguousarray(full[z0:z0 + sz, y0:y0 + sy, x0:x0 + sx]))
+            out = gpu.DeviceImage(gpu.Region(ri, rs))
+            lg, rq = img.region.to_c(), gpu.Region(ri, rs).to_c()
+            prm = f.params()
+            _abi.check(_abi.lib().itkg_gaussian_generate_region(
+                ctypes.byref(dev.c), ctypes.byref(lg), ctypes.byref(rq), ctypes.byref(prm),
+                ctypes.byref(out.c), None))
+            assert gpu.last_kernel() == "z_pass_f32_fma"
+            assert normwise(out.download(), want) <= 1e-5, ("tight", sigma, ri, rs)
