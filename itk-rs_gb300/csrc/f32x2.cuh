@@ -54,4 +54,12 @@ inline unsigned long long splat2_host(float w) {
   return ((unsigned long long)u << 32) | u;
 }
 
+// Host-side: the 64-bit pattern of the pair {lo, hi} (lo in the low lane).
+inline unsigned long long pack2_host(float lo, float hi) {
+  unsigned int a, b;
+  __builtin_memcpy(&a, &lo, 4);
+  __builtin_memcpy(&b, &hi, 4);
+  return ((unsigned long long)b << 32) | a;
+}
+
 }  // namespace itkg

@@ -63,6 +63,8 @@ const XYEntry* find_xy(int r, int dtype) {
 
 bool fits_i32(int64_t v) { return v >= INT_MIN && v <= INT_MAX; }
 
+size_t z_smem(int rz) { return (size_t)(2 * rz + 1) * 256 * 16 * twopass::CfgZ<1>::QPT; }
+
 const char* xy_name(int dtype, bool ref) {
   static const char* names[5][2] = {{"xy_pass_f32_fma", "xy_pass_f32_ref"},
                                     {"xy_pass_i16_fma", "xy_pass_i16_ref"},
@@ -98,8 +100,9 @@ itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], v
         !fits_i32(g.req_index[d] + g.req_size[d] + 64) || !fits_i32(g.req_index[d] - 64))
       return ITKG_ERROR_UNSUPPORTED;
   const int64_t nx = g.req_size[0], ny = g.req_size[1], nz = g.req_size[2];
-  const int64_t nxp = (nx + 3) / 4 * 4;
-  if (!fits_i32(nxp) || !fits_i32(ny)) return ITKG_ERROR_UNSUPPORTED;
+  if (!fits_i32(nx) || !fits_i32(ny)) return ITKG_ERROR_UNSUPPORTED;
+  const int64_t ntx = (nx + twopass::kTileX - 1) / twopass::kTileX;
+  const int64_t nty = (ny + twopass::kTileY - 1) / twopass::kTileY;
   if (dry_run) return ITKG_SUCCESS;
 
   cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -108,7 +111,7 @@ itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], v
   // clamp bounds on z: the image within the input buffer
   const int64_t zlo = std::max<int64_t>(g.lo[2], g.src_origin[2]);
   const int64_t zhi = std::min<int64_t>(g.hi[2], g.src_origin[2] + g.src_size[2] - 1);
-  const int64_t slice_floats = nxp * ny;
+  const int64_t slice_floats = ntx * nty * twopass::kTile;  // T is tile-major
   // outputs per chunk: as many as keep the chunk's intermediate within kChunkBytes
   int64_t chunk = nz;
   {
@@ -134,14 +137,13 @@ itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], v
   const twopass::XYFn xyfn = e->fn[ref ? 1 : 0];
   if (st == ITKG_SUCCESS) st = max_resident_ctas(reinterpret_cast<const void*>(xyfn), e->smem, e->nt, &res_xy);
   if (st == ITKG_SUCCESS)
-    st = max_resident_ctas(reinterpret_cast<const void*>(zfn), twopass::CfgZ<1>::SMEM, 256, &res_z);
+    st = max_resident_ctas(reinterpret_cast<const void*>(zfn), z_smem(rz), 256, &res_z);
   if (st != ITKG_SUCCESS) {
     scratch_free(t, stream);
     return st;
   }
 
   xa.t = t;
-  xa.t_row = nxp;
   xa.t_slice = slice_floats;
   for (int d = 0; d < 3; ++d) {
     xa.src_origin[d] = (int32_t)g.src_origin[d];
@@ -150,14 +152,18 @@ itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], v
   }
   xa.x0 = (int32_t)g.req_index[0];
   xa.y0 = (int32_t)g.req_index[1];
-  xa.nxp = (int32_t)nxp;
-  xa.ny = (int32_t)ny;
-  xa.ntx = (int32_t)((nx + e->tx - 1) / e->tx);
-  const int64_t nty = (ny + e->ty - 1) / e->ty;
+  xa.ntx = (int32_t)ntx;
   const int R = g.radius[0], K = 2 * R + 1;
   for (int k = 0; k < K; ++k) {
     xa.wx[k] = w[0][k], xa.wx2[k] = splat2_host(w[0][k]);
     xa.wy[k] = w[1][k], xa.wy2[k] = splat2_host(w[1][k]);
+  }
+  {
+    auto wk = [&](int k) { return (k < 0 || k >= K) ? 0.0f : w[0][k]; };
+    for (int i = 0; i <= R; ++i) {
+      xa.we[i] = pack2_host(wk(2 * i), wk(2 * i + 1));
+      xa.wo[i] = pack2_host(wk(2 * i - 1), wk(2 * i));
+    }
   }
   xa.nty = (int32_t)nty;
   {
@@ -171,27 +177,28 @@ itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], v
     xa.yr0 = std::max(0, (int)nty - 2);
     const int64_t tx_r = g.req_index[0] + (int64_t)xa.xr0 * e->tx;  // first of the last two tile columns
     const int64_t ty_r = g.req_index[1] + (int64_t)xa.yr0 * e->ty;
-    for (int t = 0; t < 32; ++t) {
+    for (int t = 0; t < twopass::kTileX; ++t) {
       xa.cxl[t] = coef(p, g.req_index[0] + t - xa.lo[0]);
       if (xa.cxl[t] != 0.0f) xa.edge |= 1;
     }
-    for (int t = 0; t < 64; ++t) {
+    for (int t = 0; t < 2 * twopass::kTileX; ++t) {
       xa.cxr[t] = coef(p, xa.hi[0] - (tx_r + t));
-      xa.cyt[t] = coef(q, g.req_index[1] + t - xa.lo[1]);
       if (xa.cxr[t] != 0.0f) xa.edge |= 2;
+    }
+    for (int t = 0; t < twopass::kTileY; ++t) {
+      xa.cyt[t] = coef(q, g.req_index[1] + t - xa.lo[1]);
       if (xa.cyt[t] != 0.0f) xa.edge |= 4;
     }
-    for (int t = 0; t < 128; ++t) {
+    for (int t = 0; t < 2 * twopass::kTileY; ++t) {
       xa.cyb[t] = coef(q, xa.hi[1] - (ty_r + t));
       if (xa.cyb[t] != 0.0f) xa.edge |= 8;
     }
   }
   za.t = t;
-  za.t_row = nxp;
   za.t_slice = slice_floats;
   za.nx = (int32_t)nx;
   za.ny = (int32_t)ny;
-  za.nqx = (int32_t)(nxp / 4);
+  za.ntx = (int32_t)ntx;
   za.out_dtype = g.out_dtype;
   za.dst_pitch[0] = g.dst_pitch[0];
   za.dst_pitch[1] = g.dst_pitch[1];
@@ -203,7 +210,7 @@ itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], v
                      ? 1
                      : 0;
   for (int k = 0; k < 2 * rz + 1; ++k) za.wz[k] = w[2][k], za.wz2[k] = splat2_host(w[2][k]);
-  const int64_t qblocks = (nxp / 4 * ny + 255) / 256;
+  const int64_t qblocks = ntx * nty * (twopass::kTile / 4 / twopass::CfgZ<1>::QB);
 
   for (int64_t c0 = 0; c0 < nz && st == ITKG_SUCCESS; c0 += chunk) {
     const int64_t c1 = std::min<int64_t>(nz, c0 + chunk);  // outputs [z0 + c0, z0 + c1)
@@ -228,7 +235,7 @@ itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], v
     za.units = qblocks * za.nz;
     za.dst = dst0 + (oz0 - g.dst_origin[2]) * g.dst_pitch[2];
     const int64_t gz = std::min<int64_t>(za.units, res_z);
-    zfn<<<(unsigned)gz, 256, twopass::CfgZ<1>::SMEM, s>>>(za);
+    zfn<<<(unsigned)gz, 256, z_smem(rz), s>>>(za);
     note_launch(ref ? "z_pass_f32_ref" : "z_pass_f32_fma");
     err = cudaGetLastError();
     if (err != cudaSuccess) st = set_error(ITKG_ERROR_CUDA, "z pass launch: %s", cudaGetErrorString(err));

@@ -47,15 +47,17 @@ using fusedk::tma_load_3d;
 
 constexpr int kMaxR = 8;
 constexpr int kMaxK = 2 * kMaxR + 1;
+// x-y tile; T is stored tile-major: [slice][tile][kTileY rows][kTileX columns]
+constexpr int kTileX = 32;
+constexpr int kTileY = 128;
+constexpr int kTile = kTileX * kTileY;
 
 struct XYArgs {
-  float* t;            // intermediate, [slice][row][col]
-  int64_t t_row;       // floats between rows of T
-  int64_t t_slice;     // floats between slices of T
+  float* t;            // intermediate, [slice][tile][row][col] (tile-major)
+  int64_t t_slice;     // floats between slices of T (tiles * kTile)
   int32_t src_origin[3];
   int32_t lo[3], hi[3];  // gather bounds (image within the input buffer), inclusive
   int32_t x0, y0;        // first requested column / row (absolute)
-  int32_t nxp, ny;       // T row length (floats, multiple of 4) and rows
   int32_t s0, ns;        // first slice of this launch (absolute z) and slice count
   int32_t t_s0;          // absolute z of T's slice 0
   int32_t ntx, nty;      // tiles along x and y
@@ -63,6 +65,10 @@ struct XYArgs {
   unsigned int* fault;
   float wx[kMaxK], wy[kMaxK];
   f2_t wx2[kMaxK], wy2[kMaxK];
+  // FMA rounding, x pass: weight pairs for an output whose first tap is at an
+  // even (we) or odd (wo) window position, we[i] = (w[2i], w[2i+1]) and
+  // wo[i] = (w[2i-1], w[2i]) with w[-1] = w[2R+1] = 0.
+  f2_t we[kMaxR + 1], wo[kMaxR + 1];
   // FMA rounding: the weight of the clamped taps of each output column of the
   // first tile column (cxl) and of the last two (cxr, tile columns xr0 and
   // xr0 + 1), and of each output row of the first tile row (cyt) and of the
@@ -71,7 +77,7 @@ struct XYArgs {
   // the kernel being symmetric), else 0.  Only these tiles reach an edge
   // (R < TX, TY).  edge: bit 0/1/2/3 = some coefficient of cxl/cxr/cyt/cyb is
   // nonzero.
-  float cxl[32], cxr[64], cyt[64], cyb[128];
+  float cxl[kTileX], cxr[2 * kTileX], cyt[kTileY], cyb[2 * kTileY];
   int32_t xr0, yr0;
   int32_t edge;
   int32_t pad2_;
@@ -79,12 +85,12 @@ struct XYArgs {
 
 struct ZArgs {
   const float* t;
-  int64_t t_row, t_slice;  // floats
+  int64_t t_slice;         // floats
   int32_t t_s0, t_s1;      // absolute z of T's first / last slice (the clamp bounds)
   int32_t nx, ny;          // requested columns / rows
-  int32_t nqx;             // quads per row (nxp / 4)
+  int32_t ntx;             // tiles along x
   int32_t z0, nz;          // output slices of this launch (absolute) and count
-  int64_t units;           // quad blocks * nz
+  int64_t units;           // quad blocks (256 quads each) * nz
   char* dst;               // output voxel (x0, y0, z0)
   int64_t dst_pitch[3];    // bytes
   int32_t out_dtype;
@@ -97,11 +103,11 @@ template <int R, typename Tin>
 struct CfgXY {
   static constexpr int K = 2 * R + 1;
   static constexpr int ESZ = (int)sizeof(Tin);
-  static constexpr int NT = 320;                // one x-pass task per thread (IH * SEGS <= 320)
+  static constexpr int NT = 288;                // two x-pass tasks per thread (IH * SEGS <= 576)
   static constexpr int NTY = 256;               // threads of the y pass
-  static constexpr int TX = 32;                 // 16 lanes x 2 columns
-  static constexpr int MY = 4;                  // rows per thread in the y pass
-  static constexpr int TY = (NTY / 16) * MY;    // 64
+  static constexpr int TX = kTileX;             // 16 lanes x 2 columns
+  static constexpr int MY = 8;                  // rows per thread in the y pass
+  static constexpr int TY = (NTY / 16) * MY;    // 128
   static constexpr int MX = 8;                  // x outputs per x-pass task
   static constexpr int SEGS = TX / MX;
   static constexpr int AE = 16 / ESZ;
@@ -113,8 +119,10 @@ struct CfgXY {
   static constexpr int NTASK = IH * SEGS;       // x-pass tasks per unit
   static constexpr int OFF = (XA - R) % 4;
   static constexpr int WB = XA - R - OFF;
-  static constexpr int WIN = (MX + 2 * R + OFF + 3) / 4 * 4;
-  static constexpr int S = 3;                   // units in flight
+  // window: the reference form reads MX + 2R elements from OFF; the tap-pair
+  // form reads whole aligned pairs, one more when output MX - 1 starts even
+  static constexpr int WIN = (MX + 2 * R + OFF + (OFF & 1) + 3) / 4 * 4;
+  static constexpr int S = 2;                   // units in flight
   static constexpr int BOX = IH * BW * ESZ;
   static constexpr int STAGE = (BOX + 127) / 128 * 128;
   static constexpr int TXP = TX + 4;            // x-filtered row stride (floats)
@@ -122,15 +130,19 @@ struct CfgXY {
   static constexpr size_t SMEM = (size_t)S * STAGE + sizeof(float) * 2 * XBUF + 128;
   static_assert(WB + TX - MX + WIN <= BW, "x window stays inside the staged row");
   static_assert(TX % MX == 0, "x segments");
-  static_assert(NTASK <= NT, "each thread runs at most one x-pass task");
+  static_assert(NTASK > NT && NTASK <= 2 * NT, "each thread runs one or two x-pass tasks");
+  static_assert(TY == kTileY, "tile height");
 };
 
 template <int RZ>
 struct CfgZ {
   static constexpr int KZ = 2 * RZ + 1;
   static constexpr int NT = 256;
-  static constexpr int S = 8;  // slices in flight per thread
-  static constexpr size_t SMEM = (size_t)S * NT * 16;
+  static constexpr int QPT = 1;                 // quads (4 columns) per thread
+  static constexpr int QB = NT * QPT;           // quads per block of work
+  static constexpr int S = KZ;                  // slices in flight per thread: one per phase
+  static constexpr size_t SMEM = (size_t)S * NT * 16 * QPT;
+  static_assert((kTile / 4) % QB == 0, "blocks of work tile the T tiles");
 };
 
 // ---------------------------------------------------------------------------
@@ -168,26 +180,10 @@ __device__ __forceinline__ float ld1(const uint8_t* p) { return (float)*p; }
 __device__ __forceinline__ float ld1(const __nv_bfloat16* p) { return __bfloat162float(*p); }
 __device__ __forceinline__ float ld1(const __half* p) { return __half2float(*p); }
 
-// Position of one (tile, slice) unit; advanced one unit at a time without
-// divisions (slices fastest, then tiles along x, then along y).
-struct UnitCursor {
-  int tx0, ty0, s;
-  __device__ __forceinline__ void advance(const XYArgs& a, int tx, int ty) {
-    if (++s == a.s0 + a.ns) {
-      s = a.s0;
-      tx0 += tx;
-      if (tx0 >= a.x0 + a.ntx * tx) {
-        tx0 = a.x0;
-        ty0 += ty;
-      }
-    }
-  }
-};
-
 // ---------------------------------------------------------------------------
 // xy pass
 template <int R, bool REF, typename Tin>
-__global__ void __launch_bounds__(320, 3)
+__global__ void __launch_bounds__(288, 2)
     k_xy_pass(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ XYArgs a) {
   using C = CfgXY<R, Tin>;
   constexpr int K = C::K, TX = C::TX, TY = C::TY, MY = C::MY, MX = C::MX, BW = C::BW, IH = C::IH,
@@ -214,36 +210,18 @@ __global__ void __launch_bounds__(320, 3)
   const int n = (int)(u_end - u_begin);
   if (n <= 0) return;
 
-  UnitCursor cy;  // unit of the y pass
-  {
-    const int64_t tile = u_begin / a.ns;
-    cy.s = a.s0 + (int)(u_begin - tile * a.ns);
-    const int64_t tyi = tile / a.ntx;
-    cy.tx0 = a.x0 + (int)(tile - tyi * a.ntx) * TX;
-    cy.ty0 = a.y0 + (int)tyi * TY;
-  }
-  UnitCursor cx = cy, ci = cy;  // units of the x pass and of the next tile load
   const uint64_t pol_in = policy_evict_first();
   const uint64_t pol_t = policy_evict_last();
 
-  // this thread's x-pass task: (row, 8-column segment), if tid < NTASK
+  // this thread's x-pass tasks: (row, 8-column segment) tid and tid + NT (if < NTASK)
   const int row_a = tid / SEGS, x0_a = (tid % SEGS) * MX;
-  const bool has_x = tid < NTASK;
+  const int row_b = (tid + NT) / SEGS, x0_b = ((tid + NT) % SEGS) * MX;
+  const bool has_b = tid + NT < NTASK;
+  // this thread's y-pass share: columns 2*lane16, +1; rows grp*MY .. +MY-1
+  const int lane16 = tid & 15, grp = tid >> 4;
+  const bool has_y = tid < C::NTY;
+  const float* const ywin0 = xbuf0 + (has_y ? grp : 0) * MY * TXP + 2 * lane16;
 
-  int issued = 0, consumed = 0;  // units whose load was issued / waited for (uniform)
-  auto issue_next = [&]() {      // tile load of unit `issued` (cursor ci)
-    if (issued >= n) return;
-    if (tid == 0) {
-      const int st = issued % S;
-      asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-      const uint32_t bar = bbase + 8 * st;
-      mbar_expect_tx(bar, (uint32_t)C::BOX);
-      tma_load_3d_hint(sbase + (uint32_t)(st * C::STAGE), &tmap, ci.tx0 - XA - a.src_origin[0],
-                       ci.ty0 - R - a.src_origin[1], ci.s - a.src_origin[2], bar, pol_in);
-    }
-    ++issued;
-    ci.advance(a, TX, TY);
-  };
   // One x-pass task: staged row `row`, columns x0 .. x0 + MX - 1 of the tile,
   // into xb.  nl / cr: staged columns of the image's first / last column;
   // rlo / rhi: staged rows of its first / last row.
@@ -283,20 +261,20 @@ __global__ void __launch_bounds__(320, 3)
       float v[WIN];
 #pragma unroll
       for (int q = 0; q < WIN / 4; ++q) load4(src + x0 + WB + 4 * q, v + 4 * q);
-      f2_t E[WIN / 2], O[WIN / 2 - 1];
+      // tap pairs over the aligned window pairs (no pair-forming moves): output m
+      // sums E[j] * we[i] (first tap even) or * wo[i] (odd), then its two lanes
+      f2_t E[WIN / 2];
 #pragma unroll
       for (int q = 0; q < WIN / 2; ++q) E[q] = pack2(v[2 * q], v[2 * q + 1]);
 #pragma unroll
-      for (int q = 0; q < WIN / 2 - 1; ++q) O[q] = pack2(v[2 * q + 1], v[2 * q + 2]);
+      for (int m = 0; m < MX; ++m) {
+        const int q0 = m + OFF;
+        f2_t ax = mul2(E[q0 / 2], (q0 & 1) ? a.wo[0] : a.we[0]);
 #pragma unroll
-      for (int m = 0; m < MX / 2; ++m) {
-        f2_t ax = 0ull;
-#pragma unroll
-        for (int k = 0; k < K; ++k) {
-          const int q = 2 * m + k + OFF;
-          ax = fma2((q & 1) ? O[(q - 1) / 2] : E[q / 2], a.wx2[k], ax);
-        }
-        unpack2(ax, o[2 * m], o[2 * m + 1]);
+        for (int i = 1; i <= R; ++i) ax = fma2(E[q0 / 2 + i], (q0 & 1) ? a.wo[i] : a.we[i], ax);
+        float lo2, hi2;
+        unpack2(ax, lo2, hi2);
+        o[m] = lo2 + hi2;
       }
       if (xedge) {  // here: bit 0 = first tile column, bit 1 = last, with corrections
         if (xedge & 1) {
@@ -316,15 +294,22 @@ __global__ void __launch_bounds__(320, 3)
 #pragma unroll
     for (int q = 0; q < MX / 4; ++q) d4[q] = make_float4(o[4 * q], o[4 * q + 1], o[4 * q + 2], o[4 * q + 3]);
   };
-  // Waits for the tile of unit `consumed` (cursor cx) and runs its x pass into xb.
-  auto xpass_next = [&](float* xb) {
-    const int st = consumed % S;
-    const Tin* const tile = reinterpret_cast<const Tin*>(stage0 + st * C::STAGE);
-    if (!mbar_wait(bbase + 8 * st, (phase_bits >> st) & 1u)) s_fail = 1;  // checked after the next barrier
-    phase_bits ^= 1u << st;
-    ++consumed;
-    const int gx0 = cx.tx0 - XA, gy0 = cx.ty0 - R;
-    cx.advance(a, TX, TY);
+  int st_issue = 0, st_use = 0;       // stage ring positions (uniform)
+  int64_t n_issued = 0, n_consumed = 0;  // tile loads issued / waited for (uniform)
+
+  // The CTA's units are a run of slices of one tile, or the tail of one tile's
+  // slices and the head of the next: one or two segments, each marching z.
+  for (int64_t u = u_begin; u < u_end;) {
+    const int64_t tile = u / a.ns;
+    const int s_a = a.s0 + (int)(u - tile * a.ns);
+    const int64_t left_u = u_end - u;
+    const int ns_seg = (int)(a.s0 + a.ns - s_a < left_u ? a.s0 + a.ns - s_a : left_u);
+    u += ns_seg;
+    const int64_t tyi = tile / a.ntx;
+    const int tix = (int)(tile - tyi * a.ntx);
+    const int tx0 = a.x0 + tix * TX, ty0 = a.y0 + (int)tyi * TY;
+    const int gx0 = tx0 - XA, gy0 = ty0 - R;
+    // tile geometry, fixed over the segment
     const int nl = a.lo[0] - gx0;  // first in-image staged column (> 0 only at the left edge)
     const int cr = a.hi[0] - gx0;  // last in-image staged column (< BW - 1 only at the right edge)
     const int rlo = a.lo[1] - gy0, rhi = a.hi[1] - gy0;
@@ -332,93 +317,105 @@ __global__ void __launch_bounds__(320, 3)
     int xedge;
     if constexpr (REF) {
       xedge = (nl > 0 || cr < BW - 1) ? 1 : 0;
-    } else {  // first / last tile column with clamped taps to add back
-      const int tcol = (gx0 + XA - a.x0) / TX - a.xr0;  // 0 / 1: the last two tile columns
-      xedge = ((gx0 + XA == a.x0) && (a.edge & 1) ? 1 : 0) |
-              ((tcol >= 0) && (a.edge & 2) ? 2 | (tcol << 2) : 0);
+    } else {  // first / last two tile columns with clamped taps to add back
+      const int tcol = tix - a.xr0;
+      xedge = (tix == 0 && (a.edge & 1) ? 1 : 0) | ((tcol >= 0) && (a.edge & 2) ? 2 | (tcol << 2) : 0);
     }
-    if (has_x) xtask(tile, xb, row_a, x0_a, yedge, rlo, rhi, xedge, nl, cr);
-  };
+    const int trow = (int)tyi - a.yr0;
+    const bool top = !REF && (a.edge & 4) && tyi == 0;
+    const bool bot = !REF && (a.edge & 8) && trow >= 0 && rhi < IH;
+    // T block of this tile; rows and columns beyond the request are stored too
+    float* tp = a.t + (int64_t)(s_a - a.t_s0) * a.t_slice + tile * kTile + grp * MY * TX + 2 * lane16;
 
-  const int lane16 = tid & 15, grp = tid >> 4;
-  const bool has_y = tid < C::NTY;
-  const float* const ywin0 = xbuf0 + (has_y ? grp : 0) * MY * TXP + 2 * lane16;  // this thread's y window
-  for (int q = 0; q < S; ++q) issue_next();
-  xpass_next(xbuf0);
-  for (int i = 0; i < n; ++i) {
-    // x pass of unit i visible; y pass of unit i - 1 done with the other buffer
-    __syncthreads();
-    if (s_fail) goto timeout;
-    issue_next();  // into the stage unit i's x pass has finished reading
-    if (i + 1 < n) xpass_next(xbuf0 + ((i + 1) & 1) * C::XBUF);
-    if (has_y) {
-      // y pass: columns 2*lane16, +1; rows grp*MY .. +MY-1 of the tile
-      const float* const yw = ywin0 + (i & 1) * C::XBUF;
-      f2_t win[MY + 2 * R];
-#pragma unroll
-      for (int q = 0; q < MY + 2 * R; ++q) win[q] = *reinterpret_cast<const f2_t*>(yw + q * TXP);
-      f2_t yv[MY];
-#pragma unroll
-      for (int m = 0; m < MY; ++m) {
-        if constexpr (REF) {
-          float y0 = 0.0f, y1 = 0.0f;
-#pragma unroll
-          for (int k = 0; k < K; ++k) {
-            float v0, v1;
-            unpack2(win[m + k], v0, v1);
-            y0 = tap<true>(y0, v0, a.wy[k]);
-            y1 = tap<true>(y1, v1, a.wy[k]);
-          }
-          yv[m] = pack2(y0, y1);
-        } else {
-          f2_t ay = 0ull;
-#pragma unroll
-          for (int k = 0; k < K; ++k) ay = fma2(win[m + k], a.wy2[k], ay);
-          yv[m] = ay;
-        }
+    auto issue = [&](int sl) {  // tile load of slice sl into the next stage
+      if (tid == 0) {
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        const uint32_t bar = bbase + 8 * st_issue;
+        mbar_expect_tx(bar, (uint32_t)C::BOX);
+        tma_load_3d_hint(sbase + (uint32_t)(st_issue * C::STAGE), &tmap, gx0 - a.src_origin[0],
+                         gy0 - a.src_origin[1], sl - a.src_origin[2], bar, pol_in);
       }
-      if constexpr (!REF) {
-        // first / last tile row: the clamped taps, c[row] * X[edge row]
-        if ((a.edge & 4) && cy.ty0 == a.y0) {
-          const f2_t xe = *reinterpret_cast<const f2_t*>(xbuf0 + (i & 1) * C::XBUF + (a.lo[1] - a.y0 + R) * TXP +
-                                                         2 * lane16);
+      st_issue = st_issue + 1 == S ? 0 : st_issue + 1;
+      ++n_issued;
+    };
+    auto xpass = [&](float* xb) {  // waits for the oldest load, x pass into xb
+      const Tin* const tile_s = reinterpret_cast<const Tin*>(stage0 + st_use * C::STAGE);
+      if (!mbar_wait(bbase + 8 * st_use, (phase_bits >> st_use) & 1u)) s_fail = 1;  // checked after the next barrier
+      phase_bits ^= 1u << st_use;
+      st_use = st_use + 1 == S ? 0 : st_use + 1;
+      ++n_consumed;
+      xtask(tile_s, xb, row_a, x0_a, yedge, rlo, rhi, xedge, nl, cr);
+      if (has_b) xtask(tile_s, xb, row_b, x0_b, yedge, rlo, rhi, xedge, nl, cr);
+    };
+
+    for (int q = 0; q < S && q < ns_seg; ++q) issue(s_a + q);
+    xpass(xbuf0);
+    for (int i = 0; i < ns_seg; ++i) {
+      // x pass of slice i visible; y pass of slice i - 1 done with the other buffer
+      __syncthreads();
+      if (s_fail) goto timeout;
+      if (i + S < ns_seg) issue(s_a + i + S);  // into the stage slice i's x pass has finished reading
+      if (i + 1 < ns_seg) xpass(xbuf0 + ((i + 1) & 1) * C::XBUF);
+      if (has_y) {
+        const float* const yw = ywin0 + (i & 1) * C::XBUF;
+        f2_t win[MY + 2 * R];
 #pragma unroll
-          for (int m = 0; m < MY; ++m) {
-            const float c = a.cyt[grp * MY + m];
-            yv[m] = fma2(xe, pack2(c, c), yv[m]);
-          }
-        }
-        const int trow = (cy.ty0 - a.y0) / TY - a.yr0;  // 0 / 1: the last two tile rows
-        if ((a.edge & 8) && trow >= 0 && a.hi[1] - cy.ty0 + R < IH) {
-          const f2_t xe = *reinterpret_cast<const f2_t*>(xbuf0 + (i & 1) * C::XBUF +
-                                                         (a.hi[1] - cy.ty0 + R) * TXP + 2 * lane16);
+        for (int q = 0; q < MY + 2 * R; ++q) win[q] = *reinterpret_cast<const f2_t*>(yw + q * TXP);
+        f2_t yv[MY];
 #pragma unroll
-          for (int m = 0; m < MY; ++m) {
-            const float c = a.cyb[trow * TY + grp * MY + m];
-            yv[m] = fma2(xe, pack2(c, c), yv[m]);
+        for (int m = 0; m < MY; ++m) {
+          if constexpr (REF) {
+            float y0 = 0.0f, y1 = 0.0f;
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+              float v0, v1;
+              unpack2(win[m + k], v0, v1);
+              y0 = tap<true>(y0, v0, a.wy[k]);
+              y1 = tap<true>(y1, v1, a.wy[k]);
+            }
+            yv[m] = pack2(y0, y1);
+          } else {
+            f2_t ay = 0ull;
+#pragma unroll
+            for (int k = 0; k < K; ++k) ay = fma2(win[m + k], a.wy2[k <= R ? k : 2 * R - k], ay);
+            yv[m] = ay;
           }
         }
-      }
-      const int col = cy.tx0 - a.x0 + 2 * lane16;
-      const int row0 = cy.ty0 - a.y0 + grp * MY;
-      if (col < a.nxp) {
-        float* tp = a.t + (int64_t)(cy.s - a.t_s0) * a.t_slice + (int64_t)row0 * a.t_row + col;
+        if constexpr (!REF) {
+          // first / last two tile rows: the clamped taps, c[row] * X[edge row]
+          if (top) {
+            const f2_t xe = *reinterpret_cast<const f2_t*>(xbuf0 + (i & 1) * C::XBUF + rlo * TXP + 2 * lane16);
 #pragma unroll
-        for (int m = 0; m < MY; ++m)
-          if (row0 + m < a.ny) st_f2_hint(tp + m * a.t_row, yv[m], pol_t);
+            for (int m = 0; m < MY; ++m) {
+              const float c = a.cyt[grp * MY + m];
+              yv[m] = fma2(xe, pack2(c, c), yv[m]);
+            }
+          }
+          if (bot) {
+            const f2_t xe = *reinterpret_cast<const f2_t*>(xbuf0 + (i & 1) * C::XBUF + rhi * TXP + 2 * lane16);
+#pragma unroll
+            for (int m = 0; m < MY; ++m) {
+              const float c = a.cyb[trow * TY + grp * MY + m];
+              yv[m] = fma2(xe, pack2(c, c), yv[m]);
+            }
+          }
+        }
+#pragma unroll
+        for (int m = 0; m < MY; ++m) st_f2_hint(tp + m * TX, yv[m], pol_t);
       }
+      tp += a.t_slice;
     }
-    cy.advance(a, TX, TY);
+    __syncthreads();  // the next segment reuses both x-filtered buffers
   }
   return;
 timeout:
   if (tid == 0) {
     atomicExch(a.fault, 1u);
     // let this CTA's other tile loads in flight land (bounded) before it exits
-    for (int k = consumed; k < issued; ++k) {
-      const int st = k % S;
-      mbar_wait(bbase + 8 * st, (phase_bits >> st) & 1u);
-      phase_bits ^= 1u << st;
+    for (int64_t k = n_consumed; k < n_issued; ++k) {
+      mbar_wait(bbase + 8 * st_use, (phase_bits >> st_use) & 1u);
+      phase_bits ^= 1u << st_use;
+      st_use = st_use + 1 == S ? 0 : st_use + 1;
     }
   }
 }
@@ -426,15 +423,14 @@ timeout:
 // ---------------------------------------------------------------------------
 // z pass
 template <int RZ, bool REF>
-__global__ void __launch_bounds__(256) k_z_pass(const __grid_constant__ ZArgs a) {
+__global__ void __launch_bounds__(256, 2) k_z_pass(const __grid_constant__ ZArgs a) {
   using C = CfgZ<RZ>;
-  constexpr int KZ = C::KZ, S = C::S, NT = C::NT;
-  extern __shared__ __align__(16) float4 zring[];
+  constexpr int KZ = C::KZ, S = C::S, NT = C::NT, QPT = C::QPT, NP = 2 * QPT;  // NP packed pairs
+  extern __shared__ __align__(16) float4 zring[];  // [S][NT][QPT]
   const int tid = threadIdx.x;
   const int64_t u_begin = a.units * blockIdx.x / gridDim.x;
   const int64_t u_end = a.units * (blockIdx.x + 1) / gridDim.x;
-  const int64_t nq = (int64_t)a.nqx * a.ny;
-  const uint32_t my_slot0 = smem_u32(zring + tid);
+  const uint32_t my_slot0 = smem_u32(zring + tid * QPT);
   const uint64_t pol_t = policy_evict_first();
 
   for (int64_t u = u_begin; u < u_end;) {
@@ -443,76 +439,87 @@ __global__ void __launch_bounds__(256) k_z_pass(const __grid_constant__ ZArgs a)
     const int64_t zrem = zs + (u_end - u);
     const int ze = zrem < a.nz ? (int)zrem : a.nz;
     u += ze - zs;
-    const int64_t q = blk * NT + tid;  // this thread's quad
-    if (q >= nq) continue;             // no barriers in this kernel: idle threads just skip
-    const int qy = (int)(q / a.nqx), qx = (int)(q - (int64_t)(q / a.nqx) * a.nqx);
+    // this thread's quads: T tile `tl`, quads w .. w + QPT - 1 (row w / 8, from column 4 (w % 8))
+    const int64_t q = blk * C::QB + (int64_t)tid * QPT;
+    const int64_t tl = q / (kTile / 4);
+    const int w = (int)(q - tl * (kTile / 4));
+    const int64_t tly = tl / a.ntx;
+    const int cx = (int)(tl - tly * a.ntx) * kTileX + 4 * (w & (kTileX / 4 - 1));  // first column
+    const int cy = (int)tly * kTileY + w / (kTileX / 4);                           // row
+    if (cy >= a.ny || cx >= a.nx) continue;  // no barriers in this kernel: idle threads just skip
     const int z0 = a.z0 + zs, z1 = a.z0 + ze;  // outputs [z0, z1)
     const int jb = z0 - RZ, je = z1 - 1 + RZ;
     // prefetch cursor: slice jn (clamped to T) at pn
-    const float* const tq = a.t + (int64_t)qy * a.t_row + 4 * qx;
+    const float* const tq = a.t + tl * kTile + 4 * w;
     int jn = jb;
     const float* pn = tq + (int64_t)(clampi(jn, a.t_s0, a.t_s1) - a.t_s0) * a.t_slice;
-    auto prefetch = [&](uint32_t slot) {
-      cp_async16_hint(slot, pn, pol_t);
+    auto prefetch = [&](int stage) {
+#pragma unroll
+      for (int c = 0; c < QPT; ++c) cp_async16_hint(my_slot0 + (uint32_t)((stage * NT * QPT + c) * 16), pn + 4 * c, pol_t);
       fusedk::cp_async_commit();
       ++jn;
       if (jn > a.t_s0 && jn <= a.t_s1) pn += a.t_slice;
     };
 #pragma unroll
-    for (int i = 0; i < S; ++i) prefetch(my_slot0 + (uint32_t)(i * NT * 16));
-    f2_t acc[2][KZ];
+    for (int i = 0; i < S; ++i) prefetch(i);
+    f2_t acc[NP][KZ];
 #pragma unroll
-    for (int m = 0; m < 2; ++m)
+    for (int m = 0; m < NP; ++m)
 #pragma unroll
       for (int k = 0; k < KZ; ++k) acc[m][k] = 0ull;
-    const int ncols = min(4, a.nx - 4 * qx);
-    const bool vec = a.vec_store && ncols == 4;
-    char* dz = a.dst + (int64_t)(4 * qx) * a.dst_pitch[0] + (int64_t)qy * a.dst_pitch[1] +
+    const int ncols = min(4 * QPT, a.nx - cx);
+    const bool vec = a.vec_store && ncols == 4 * QPT;
+    char* dz = a.dst + (int64_t)cx * a.dst_pitch[0] + (int64_t)cy * a.dst_pitch[1] +
                (int64_t)(z0 - a.z0) * a.dst_pitch[2];
-    int cur = 0;
     for (int jbase = jb; jbase <= je; jbase += KZ) {
 #pragma unroll
-      for (int p = 0; p < KZ; ++p) {
+      for (int p = 0; p < KZ; ++p) {  // phase p: slice j in stage p
         const int j = jbase + p;
         if (j > je) break;
         fusedk::cp_async_wait<S - 1>();
-        const float4 f = zring[cur * NT + tid];
-        const f2_t v0 = pack2(f.x, f.y), v1 = pack2(f.z, f.w);
+        f2_t v[NP];
+#pragma unroll
+        for (int c = 0; c < QPT; ++c) {
+          const float4 f = zring[(p * NT + tid) * QPT + c];
+          v[2 * c] = pack2(f.x, f.y);
+          v[2 * c + 1] = pack2(f.z, f.w);
+        }
+        prefetch(p);  // the stage has been read: refill it with slice j + S
 #pragma unroll
         for (int k = 0; k < KZ; ++k) {
           const int slot = (p - k + KZ) % KZ;
-          if constexpr (REF) {
-            float a0, a1;
-            unpack2(acc[0][slot], a0, a1);
-            acc[0][slot] = pack2(__fadd_rn(a0, __fmul_rn(f.x, a.wz[k])), __fadd_rn(a1, __fmul_rn(f.y, a.wz[k])));
-            unpack2(acc[1][slot], a0, a1);
-            acc[1][slot] = pack2(__fadd_rn(a0, __fmul_rn(f.z, a.wz[k])), __fadd_rn(a1, __fmul_rn(f.w, a.wz[k])));
-          } else if (k == 0) {  // first contribution to output j + RZ: its slot was popped
-            acc[0][slot] = mul2(v0, a.wz2[0]);
-            acc[1][slot] = mul2(v1, a.wz2[0]);
-          } else {
-            acc[0][slot] = fma2(v0, a.wz2[k], acc[0][slot]);
-            acc[1][slot] = fma2(v1, a.wz2[k], acc[1][slot]);
+#pragma unroll
+          for (int m = 0; m < NP; ++m) {
+            if constexpr (REF) {
+              float a0, a1, v0, v1;
+              unpack2(acc[m][slot], a0, a1);
+              unpack2(v[m], v0, v1);
+              acc[m][slot] = pack2(__fadd_rn(a0, __fmul_rn(v0, a.wz[k])), __fadd_rn(a1, __fmul_rn(v1, a.wz[k])));
+            } else if (k == 0) {  // first contribution to output j + RZ: its slot was popped
+              acc[m][slot] = mul2(v[m], a.wz2[0]);
+            } else {
+              acc[m][slot] = fma2(v[m], a.wz2[k <= RZ ? k : 2 * RZ - k], acc[m][slot]);
+            }
           }
         }
-        // the stage has been read: refill it with slice j + S
-        prefetch(my_slot0 + (uint32_t)(cur * NT * 16));
-        cur = cur + 1 == S ? 0 : cur + 1;
         const int D = (p + 1) % KZ;  // a constant once the phase loop is unrolled
-        const f2_t d0 = acc[0][D], d1 = acc[1][D];
-        if constexpr (REF) {  // reference rounding adds the first product to zero
-          acc[0][D] = 0ull;
-          acc[1][D] = 0ull;
+        f2_t d[NP];
+#pragma unroll
+        for (int m = 0; m < NP; ++m) {
+          d[m] = acc[m][D];
+          if constexpr (REF) acc[m][D] = 0ull;  // reference rounding adds the first product to zero
         }
         if (j - RZ >= z0) {
-          float o[4];
-          unpack2(d0, o[0], o[1]);
-          unpack2(d1, o[2], o[3]);
+          float o[4 * QPT];
+#pragma unroll
+          for (int m = 0; m < NP; ++m) unpack2(d[m], o[2 * m], o[2 * m + 1]);
           if (vec) {
-            __stcs(reinterpret_cast<float4*>(dz), make_float4(o[0], o[1], o[2], o[3]));
+#pragma unroll
+            for (int c = 0; c < QPT; ++c)
+              __stcs(reinterpret_cast<float4*>(dz) + c, make_float4(o[4 * c], o[4 * c + 1], o[4 * c + 2], o[4 * c + 3]));
           } else {
 #pragma unroll
-            for (int c = 0; c < 4; ++c) {
+            for (int c = 0; c < 4 * QPT; ++c) {
               if (c >= ncols) break;
               char* const dp = dz + c * a.dst_pitch[0];
               switch (a.out_dtype) {
