@@ -349,6 +349,8 @@ def gpu_arm(args):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind,
                          "traffic": ncu_traffic(kernel),
+                         "per": ("call: xy_pass + z_pass kernels" if kernel.startswith("z_pass")
+                                 else "call: one kernel"),
                          "algorithmic_bytes_per_launch": nvox * BYTES_PER_VOXEL,
                          "avg_launch_us": avg_launch_s * 1e6,
                          "frac_of_8TBs": achieved / 8000.0},

@@ -11,6 +11,7 @@
 //   stream_full              src/source.rs:81-98
 #include <cuda_runtime.h>
 
+#include <array>
 #include <atomic>
 #include <cmath>
 #include <cstdarg>
@@ -328,6 +329,122 @@ itkg_status fused_geom_for(const itkg_image& in, const itkg_region& largest,
   return ITKG_SUCCESS;
 }
 
+// ---- host buffers: pipelined staging ---------------------------------------
+// Helper streams of the current device for the staged host-buffer path (created
+// once, never destroyed).
+static itkg_status staging_streams(cudaStream_t out[3]) {
+  static std::mutex mu;
+  static std::vector<std::array<cudaStream_t, 3>> per_dev;
+  int dev = 0;
+  ITKG_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(mu);
+  if ((int)per_dev.size() <= dev) per_dev.resize(dev + 1, {nullptr, nullptr, nullptr});
+  for (int i = 0; i < 3; ++i) {
+    if (!per_dev[dev][i]) ITKG_CUDA(cudaStreamCreateWithFlags(&per_dev[dev][i], cudaStreamNonBlocking));
+    out[i] = per_dev[dev][i];
+  }
+  return ITKG_SUCCESS;
+}
+
+// Slabs along axis D-1 for a host-buffer call: about 4 MiB of output each, at
+// most 8, and at least 2 kernel lengths thick (1 = no pipelining).
+static int staging_pieces(const itkg_image& out, const itkg_region& requested, int D) {
+  const uint64_t n_last = requested.size[D - 1];
+  const uint64_t bytes = region_len(requested, D) * (uint64_t)out.pitch[0];
+  uint64_t p = bytes / (4ull << 20);
+  if (p > 8) p = 8;
+  if (p > n_last / 8) p = n_last / 8;
+  return p < 2 ? 1 : (int)p;
+}
+
+// Host-buffer call in `pieces` slabs along axis D-1 (the split of stream_full,
+// source.rs:81-98): slab k's new input slices are copied to the device on
+// copy stream A, the slab is filtered on stream B once they have landed, and
+// its output is copied back on stream C -- so host-to-device copies, filtering
+// and device-to-host copies of different slabs overlap.  The result is the
+// whole-request result (every slab clamps to the largest region).
+static itkg_status generate_staged(const itkg_image* input, const itkg_region* largest,
+                                   const itkg_region* requested, const itkg_gaussian_params* prm,
+                                   const Plan& plan, const itkg_image* output, int pieces, cudaStream_t s) {
+  const int D = input->dim, L = D - 1;
+  const bool host_in = input->location == ITKG_HOST;
+  const bool host_out = output->location == ITKG_HOST;
+  cudaStream_t hs[3];
+  ITKG_TRY(staging_streams(hs));
+  itkg_image din = *input, dout = *output;
+  void* pin = nullptr;
+  void* pout = nullptr;
+  itkg_status st = ITKG_SUCCESS;
+  if (host_in) {
+    din.location = ITKG_DEVICE;
+    din.region = plan.in_reg;
+    dense_layout(&din, 16);
+    st = scratch_alloc(&pin, image_bytes(din), s);
+    din.data = pin;
+  }
+  if (st == ITKG_SUCCESS && host_out) {
+    dout.location = ITKG_DEVICE;
+    dout.region = *requested;
+    dense_layout(&dout, 16);
+    st = scratch_alloc(&pout, image_bytes(dout), s);
+    dout.data = pout;
+  }
+  std::vector<cudaEvent_t> ev;
+  auto event = [&](cudaStream_t on, cudaEvent_t* e) -> itkg_status {
+    ITKG_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    ev.push_back(*e);
+    ITKG_CUDA(cudaEventRecord(*e, on));
+    return ITKG_SUCCESS;
+  };
+  cudaEvent_t e0 = nullptr;
+  if (st == ITKG_SUCCESS) st = event(s, &e0);  // prior work on s, and the scratch
+  for (int i = 0; i < 3 && st == ITKG_SUCCESS; ++i) st = cuda_status(cudaStreamWaitEvent(hs[i], e0, 0), "wait");
+  const uint64_t n_last = requested->size[L];
+  int64_t copied_to = plan.in_reg.index[L];  // input slices below this are on the device
+  for (int k = 0; k < pieces && st == ITKG_SUCCESS; ++k) {
+    itkg_region rk = *requested;
+    rk.index[L] = requested->index[L] + (int64_t)(n_last * k / pieces);
+    rk.size[L] = n_last * (k + 1) / pieces - n_last * k / pieces;
+    Plan pk;
+    st = make_plan(din, rk, *largest, prm->sigma, &pk);
+    if (st != ITKG_SUCCESS) break;
+    cudaEvent_t ein = nullptr, eout = nullptr;
+    if (host_in) {
+      const int64_t end = pk.in_reg.index[L] + (int64_t)pk.in_reg.size[L];
+      if (end > copied_to) {
+        itkg_region cr = plan.in_reg;
+        cr.index[L] = copied_to;
+        cr.size[L] = (uint64_t)(end - copied_to);
+        st = copy_region(din, *input, cr, hs[0]);
+        copied_to = end;
+      }
+      if (st == ITKG_SUCCESS) st = event(hs[0], &ein);
+      if (st == ITKG_SUCCESS) st = cuda_status(cudaStreamWaitEvent(hs[1], ein, 0), "wait");
+    }
+    if (st == ITKG_SUCCESS) st = generate_device(din, *largest, rk, *prm, pk, dout, hs[1]);
+    if (st == ITKG_SUCCESS && host_out) {
+      st = event(hs[1], &eout);
+      if (st == ITKG_SUCCESS) st = cuda_status(cudaStreamWaitEvent(hs[2], eout, 0), "wait");
+      if (st == ITKG_SUCCESS) st = copy_region(*output, dout, rk, hs[2]);
+    }
+  }
+  // join: s waits for all three helper streams, then frees the scratch
+  for (int i = 0; i < 3; ++i) {
+    cudaEvent_t ej = nullptr;
+    if (event(hs[i], &ej) == ITKG_SUCCESS) cudaStreamWaitEvent(s, ej, 0);
+  }
+  scratch_free(pin, s);
+  scratch_free(pout, s);
+  const cudaError_t es = cudaStreamSynchronize(s);
+  for (cudaEvent_t e : ev) cudaEventDestroy(e);
+  if (st != ITKG_SUCCESS) return st;
+  if (es != cudaSuccess) return cuda_status(es, "cudaStreamSynchronize");
+  unsigned int fault = 0;
+  ITKG_TRY(fused_fault_flag(&fault, true));
+  if (fault) return set_error(ITKG_ERROR_TIMEOUT, "a fused kernel gave up waiting for a tile load");
+  return ITKG_SUCCESS;
+}
+
 static itkg_status generate_region(const itkg_image* input, const itkg_region* largest,
                                    const itkg_region* requested, const itkg_gaussian_params* prm,
                                    const itkg_image* output, cudaStream_t s) {
@@ -359,6 +476,8 @@ static itkg_status generate_region(const itkg_image* input, const itkg_region* l
   const bool host_in = input->location == ITKG_HOST;
   const bool host_out = output->location == ITKG_HOST;
   if (!host_in && !host_out) return generate_device(*input, *largest, *requested, *prm, plan, *output, s);
+  const int pieces = staging_pieces(*output, *requested, D);
+  if (pieces > 1) return generate_staged(input, largest, requested, prm, plan, output, pieces, s);
 
   // Stage host buffers through stream-ordered scratch.
   itkg_image din = *input, dout = *output;

@@ -565,3 +565,25 @@ def test_two_pass_fma_subregions_and_tight_buffers(gpu):
                 ctypes.byref(out.c), None))
             assert gpu.last_kernel() == "z_pass_f32_fma"
             assert normwise(out.download(), want) <= 1e-5, ("tight", sigma, ri, rs)
+
+
+@pytest.mark.parametrize("rounding", ["reference", "fma"])
+def test_host_buffers_pipelined_staging(gpu, rounding):
+    """Host buffers large enough to be staged in overlapping slabs along the
+    last axis: the result is the device-path result (bit-exact in reference
+    rounding), for whole and sub-region requests, 3-D and 2-D."""
+    rnd = gpu.ROUND_REFERENCE if rounding == "reference" else gpu.ROUND_FMA
+    rng = np.random.default_rng(51)
+    for arr, sigma, req in [(rng.random((96, 200, 256), dtype=np.float32), 2.0, None),
+                            (rng.random((96, 200, 256), dtype=np.float32), 1.3, ((8, 5, 3), (240, 190, 90))),
+                            (rng.random((2100, 2304), dtype=np.float32), 1.5, None),
+                            (rng.random((2100, 2304), dtype=np.float32), 0.8, ((0, 17), (2300, 2050)))]:
+        img = gpu.Image(arr)
+        region = gpu.Region(*req) if req else img.region
+        host = gpu.GaussianFilter(img, sigma, rounding=rnd).generate_region(region).data
+        dev = gpu.DeviceImage.from_host(img)
+        on_dev = gpu.GaussianFilter(dev, sigma, rounding=rnd).generate_region(region).download()
+        assert bits_equal(host, on_dev), (arr.shape, sigma, req)
+        if rounding == "reference":
+            want = oracle.gaussian_f32(arr, sigma, requested=req) if req else oracle.gaussian_f32(arr, sigma)
+            assert bits_equal(host, want)
