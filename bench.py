@@ -510,6 +510,7 @@ def extra_workload(args):
                 p = _abi.itkg_gaussian_params()
                 p.sigma = sigma
                 p.rounding = itkg.ROUND_FMA
+                p.algorithm = itkg.ALGO_PER_AXIS  # plain: per-axis adjoint and dual passes
                 _abi.check(L.itkg_gaussian_vjp(ctypes.byref(d.c), ctypes.byref(yb.c), ctypes.byref(p),
                                                ctypes.byref(xb.c), ctypes.cast(ctypes.c_void_p(sb.value), ctypes.POINTER(ctypes.c_double)),
                                                4, sp.ptr))

@@ -224,7 +224,9 @@ itkg_status itkg_gaussian_generate_region(const itkg_image *input, const itkg_re
  *             sampled, normalised kernel of gaussian.rs:29-40 at fixed r).  A
  *             host pointer (the call synchronises the stream) unless
  *             ITKG_VJP_SIGMA_BAR_ON_DEVICE; added to with ITKG_VJP_ACCUMULATE_SIGMA.
- * Scalar f32 device images; FMA rounding; sigma must be finite and > 0. */
+ * Scalar f32 device images; FMA rounding; sigma must be finite and > 0.
+ * params->algorithm ITKG_ALGO_PER_AXIS keeps to the per-axis passes; any other
+ * value uses the fused 3-D VJP kernels where they apply. */
 #define ITKG_VJP_ACCUMULATE_XBAR 1
 #define ITKG_VJP_ACCUMULATE_SIGMA 2
 #define ITKG_VJP_SIGMA_BAR_ON_DEVICE 4

@@ -20,8 +20,8 @@ template <int R>
 ZEntry make_z() {
   return ZEntry{R, {k_z_pass<R, false>, k_z_pass<R, true>}};
 }
-const ZEntry kZ[] = {make_z<1>(), make_z<2>(), make_z<3>(), make_z<4>(),
-                     make_z<5>(), make_z<6>(), make_z<7>(), make_z<8>()};
+const ZEntry kZ[] = {make_z<1>(), make_z<2>(), make_z<3>(),  make_z<4>(),  make_z<5>(),  make_z<6>(),
+                     make_z<7>(), make_z<8>(), make_z<9>(),  make_z<10>(), make_z<11>(), make_z<12>()};
 }  // namespace
 
 ZFn z_fn(int r, bool ref) {
@@ -102,7 +102,7 @@ itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], v
   const int64_t nx = g.req_size[0], ny = g.req_size[1], nz = g.req_size[2];
   if (!fits_i32(nx) || !fits_i32(ny)) return ITKG_ERROR_UNSUPPORTED;
   const int64_t ntx = (nx + twopass::kTileX - 1) / twopass::kTileX;
-  const int64_t nty = (ny + twopass::kTileY - 1) / twopass::kTileY;
+  const int64_t nty = (ny + e->ty - 1) / e->ty;
   if (dry_run) return ITKG_SUCCESS;
 
   cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -111,7 +111,8 @@ itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], v
   // clamp bounds on z: the image within the input buffer
   const int64_t zlo = std::max<int64_t>(g.lo[2], g.src_origin[2]);
   const int64_t zhi = std::min<int64_t>(g.hi[2], g.src_origin[2] + g.src_size[2] - 1);
-  const int64_t slice_floats = ntx * nty * twopass::kTile;  // T is tile-major
+  const int64_t tile_floats = (int64_t)twopass::kTileX * e->ty;
+  const int64_t slice_floats = ntx * nty * tile_floats;  // T is tile-major
   // outputs per chunk: as many as keep the chunk's intermediate within kChunkBytes
   int64_t chunk = nz;
   {
@@ -185,11 +186,11 @@ itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], v
       xa.cxr[t] = coef(p, xa.hi[0] - (tx_r + t));
       if (xa.cxr[t] != 0.0f) xa.edge |= 2;
     }
-    for (int t = 0; t < twopass::kTileY; ++t) {
+    for (int t = 0; t < e->ty; ++t) {
       xa.cyt[t] = coef(q, g.req_index[1] + t - xa.lo[1]);
       if (xa.cyt[t] != 0.0f) xa.edge |= 4;
     }
-    for (int t = 0; t < 2 * twopass::kTileY; ++t) {
+    for (int t = 0; t < 2 * e->ty; ++t) {
       xa.cyb[t] = coef(q, xa.hi[1] - (ty_r + t));
       if (xa.cyb[t] != 0.0f) xa.edge |= 8;
     }
@@ -210,7 +211,8 @@ itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], v
                      ? 1
                      : 0;
   for (int k = 0; k < 2 * rz + 1; ++k) za.wz[k] = w[2][k], za.wz2[k] = splat2_host(w[2][k]);
-  const int64_t qblocks = ntx * nty * (twopass::kTile / 4 / twopass::CfgZ<1>::QB);
+  const int64_t qblocks = ntx * nty * (tile_floats / 4 / twopass::CfgZ<1>::QB);
+  za.tile_rows = e->ty;
 
   for (int64_t c0 = 0; c0 < nz && st == ITKG_SUCCESS; c0 += chunk) {
     const int64_t c1 = std::min<int64_t>(nz, c0 + chunk);  // outputs [z0 + c0, z0 + c1)

@@ -45,16 +45,16 @@ using fusedk::mbar_wait;
 using fusedk::smem_u32;
 using fusedk::tma_load_3d;
 
-constexpr int kMaxR = 8;
+constexpr int kMaxR = 12;
 constexpr int kMaxK = 2 * kMaxR + 1;
-// x-y tile; T is stored tile-major: [slice][tile][kTileY rows][kTileX columns]
+// x-y tile: kTileX columns and 128 rows (64 for R > 8); T is stored
+// tile-major: [slice][tile][tile rows][kTileX columns]
 constexpr int kTileX = 32;
-constexpr int kTileY = 128;
-constexpr int kTile = kTileX * kTileY;
+constexpr int kTileY = 128;  // the tallest tile
 
 struct XYArgs {
   float* t;            // intermediate, [slice][tile][row][col] (tile-major)
-  int64_t t_slice;     // floats between slices of T (tiles * kTile)
+  int64_t t_slice;     // floats between slices of T (tiles * tile floats)
   int32_t src_origin[3];
   int32_t lo[3], hi[3];  // gather bounds (image within the input buffer), inclusive
   int32_t x0, y0;        // first requested column / row (absolute)
@@ -89,6 +89,7 @@ struct ZArgs {
   int32_t t_s0, t_s1;      // absolute z of T's first / last slice (the clamp bounds)
   int32_t nx, ny;          // requested columns / rows
   int32_t ntx;             // tiles along x
+  int32_t tile_rows;       // rows of a T tile (64 or 128)
   int32_t z0, nz;          // output slices of this launch (absolute) and count
   int64_t units;           // quad blocks (256 quads each) * nz
   char* dst;               // output voxel (x0, y0, z0)
@@ -106,8 +107,8 @@ struct CfgXY {
   static constexpr int NT = 288;                // two x-pass tasks per thread (IH * SEGS <= 576)
   static constexpr int NTY = 256;               // threads of the y pass
   static constexpr int TX = kTileX;             // 16 lanes x 2 columns
-  static constexpr int MY = 8;                  // rows per thread in the y pass
-  static constexpr int TY = (NTY / 16) * MY;    // 128
+  static constexpr int MY = R <= 8 ? 8 : 4;     // rows per thread in the y pass
+  static constexpr int TY = (NTY / 16) * MY;    // 128 (64 for R > 8)
   static constexpr int MX = 8;                  // x outputs per x-pass task
   static constexpr int SEGS = TX / MX;
   static constexpr int AE = 16 / ESZ;
@@ -131,7 +132,7 @@ struct CfgXY {
   static_assert(WB + TX - MX + WIN <= BW, "x window stays inside the staged row");
   static_assert(TX % MX == 0, "x segments");
   static_assert(NTASK > NT && NTASK <= 2 * NT, "each thread runs one or two x-pass tasks");
-  static_assert(TY == kTileY, "tile height");
+  static_assert(TY <= kTileY, "tile height");
 };
 
 template <int RZ>
@@ -142,7 +143,7 @@ struct CfgZ {
   static constexpr int QB = NT * QPT;           // quads per block of work
   static constexpr int S = KZ;                  // slices in flight per thread: one per phase
   static constexpr size_t SMEM = (size_t)S * NT * 16 * QPT;
-  static_assert((kTile / 4) % QB == 0, "blocks of work tile the T tiles");
+  static_assert((kTileX / 4 * 64) % QB == 0, "blocks of work tile the T tiles (64 or 128 rows)");
 };
 
 // ---------------------------------------------------------------------------
@@ -325,7 +326,7 @@ __global__ void __launch_bounds__(288, 2)
     const bool top = !REF && (a.edge & 4) && tyi == 0;
     const bool bot = !REF && (a.edge & 8) && trow >= 0 && rhi < IH;
     // T block of this tile; rows and columns beyond the request are stored too
-    float* tp = a.t + (int64_t)(s_a - a.t_s0) * a.t_slice + tile * kTile + grp * MY * TX + 2 * lane16;
+    float* tp = a.t + (int64_t)(s_a - a.t_s0) * a.t_slice + tile * (TX * TY) + grp * MY * TX + 2 * lane16;
 
     auto issue = [&](int sl) {  // tile load of slice sl into the next stage
       if (tid == 0) {
@@ -423,7 +424,7 @@ timeout:
 // ---------------------------------------------------------------------------
 // z pass
 template <int RZ, bool REF>
-__global__ void __launch_bounds__(256, 2) k_z_pass(const __grid_constant__ ZArgs a) {
+__global__ void __launch_bounds__(256, RZ <= 8 ? 2 : 1) k_z_pass(const __grid_constant__ ZArgs a) {
   using C = CfgZ<RZ>;
   constexpr int KZ = C::KZ, S = C::S, NT = C::NT, QPT = C::QPT, NP = 2 * QPT;  // NP packed pairs
   extern __shared__ __align__(16) float4 zring[];  // [S][NT][QPT]
@@ -441,16 +442,17 @@ __global__ void __launch_bounds__(256, 2) k_z_pass(const __grid_constant__ ZArgs
     u += ze - zs;
     // this thread's quads: T tile `tl`, quads w .. w + QPT - 1 (row w / 8, from column 4 (w % 8))
     const int64_t q = blk * C::QB + (int64_t)tid * QPT;
-    const int64_t tl = q / (kTile / 4);
-    const int w = (int)(q - tl * (kTile / 4));
+    const int tile_q = a.tile_rows * (kTileX / 4);  // quads per tile
+    const int64_t tl = q / tile_q;
+    const int w = (int)(q - tl * tile_q);
     const int64_t tly = tl / a.ntx;
     const int cx = (int)(tl - tly * a.ntx) * kTileX + 4 * (w & (kTileX / 4 - 1));  // first column
-    const int cy = (int)tly * kTileY + w / (kTileX / 4);                           // row
+    const int cy = (int)tly * a.tile_rows + w / (kTileX / 4);                      // row
     if (cy >= a.ny || cx >= a.nx) continue;  // no barriers in this kernel: idle threads just skip
     const int z0 = a.z0 + zs, z1 = a.z0 + ze;  // outputs [z0, z1)
     const int jb = z0 - RZ, je = z1 - 1 + RZ;
     // prefetch cursor: slice jn (clamped to T) at pn
-    const float* const tq = a.t + tl * kTile + 4 * w;
+    const float* const tq = a.t + tl * (4 * tile_q) + 4 * w;
     int jn = jb;
     const float* pn = tq + (int64_t)(clampi(jn, a.t_s0, a.t_s1) - a.t_s0) * a.t_slice;
     auto prefetch = [&](int stage) {
@@ -570,7 +572,8 @@ ZFn z_fn(int r, bool ref);
 #define ITKG_XY_TABLE(T, DT)                                                                      \
   {                                                                                              \
     make_xy<1, T>(DT), make_xy<2, T>(DT), make_xy<3, T>(DT), make_xy<4, T>(DT), make_xy<5, T>(DT), \
-        make_xy<6, T>(DT), make_xy<7, T>(DT), make_xy<8, T>(DT)                                   \
+        make_xy<6, T>(DT), make_xy<7, T>(DT), make_xy<8, T>(DT), make_xy<9, T>(DT),               \
+        make_xy<10, T>(DT), make_xy<11, T>(DT), make_xy<12, T>(DT)                                \
   }
 
 }  // namespace twopass

@@ -297,11 +297,13 @@ extern "C" itkg_status itkg_gaussian_vjp(const itkg_image* x, const itkg_image* 
   const float* P[kMaxDim] = {nullptr, nullptr, nullptr};
   for (int d = 0; d < D; ++d) w[d] = c[d].w.data(), P[d] = c[d].prefix.data();
   bool fused_x = false, fused_s = false;
+  // ITKG_ALGO_PER_AXIS: the per-axis passes only (the plain form, for comparisons)
+  const bool try_fused = D == 3 && params->algorithm != ITKG_ALGO_PER_AXIS;
   if (xbar) {
     // fused adjoint (one pass) where a kernel applies, else D per-axis passes
     const FusedGeom g = whole_geom(*ybar, xbar, c);
-    if (D == 3 && launch_fused_vjp(2, g, w, P, nullptr, nullptr, nullptr, nullptr, nullptr, false, s,
-                                   true) == ITKG_SUCCESS) {
+    if (try_fused && launch_fused_vjp(2, g, w, P, nullptr, nullptr, nullptr, nullptr, nullptr, false, s,
+                                      true) == ITKG_SUCCESS) {
       ITKG_TRY(launch_fused_vjp(2, g, w, P, nullptr, nullptr, nullptr, nullptr, nullptr,
                                 flags & ITKG_VJP_ACCUMULATE_XBAR, s, false));
       fused_x = true;
@@ -319,8 +321,8 @@ extern "C" itkg_status itkg_gaussian_vjp(const itkg_image* x, const itkg_image* 
     // three fused launches that dot their output with ybar, or dual per-axis passes
     const FusedGeom g = whole_geom(*x, nullptr, c);
     int grid = 0;
-    if (D == 3 && launch_fused_vjp(1, g, w, nullptr, ybar->data, ybar->pitch, ybar->region.index, nullptr,
-                                   &grid, false, s, true) == ITKG_SUCCESS) {
+    if (try_fused && launch_fused_vjp(1, g, w, nullptr, ybar->data, ybar->pitch, ybar->region.index, nullptr,
+                                      &grid, false, s, true) == ITKG_SUCCESS) {
       void* part = nullptr;
       ITKG_TRY(sc.raw(sizeof(double) * 3 * grid, &part));
       double* partials = static_cast<double*>(part);

@@ -432,7 +432,10 @@ def test_fused2d_falls_back_for_unequal_radii(gpu):
 TWO_PASS_CASES = [((9, 17, 31), 1.0, None), ((16, 16, 16), 2.0, None), ((40, 50, 70), 2.0, None),
                   ((5, 70, 40), 2.2, None), ((12, 130, 70), 2.6, None), ((1, 1, 1), 1.0, None),
                   ((33, 65, 97), 1.5, None), ((20, 20, 20), 0.3, None), ((3, 40, 33), 1.2, None),
-                  ((24, 48, 40), 1.5, (0.7, 0.7, 2.5)), ((30, 20, 10), 1.0, (1.0, 1.0, 0.5))]
+                  ((24, 48, 40), 1.5, (0.7, 0.7, 2.5)), ((30, 20, 10), 1.0, (1.0, 1.0, 0.5)),
+                  # radii 9..12: 32 x 64 tiles, z pass up to rz = 12
+                  ((40, 70, 90), 3.0, None), ((33, 130, 45), 3.4, None), ((26, 30, 70), 4.0, None),
+                  ((50, 20, 36), 4.0, (1.0, 1.0, 2.0)), ((12, 64, 64), 1.2, (0.3, 0.3, 1.0))]
 
 
 @pytest.mark.parametrize("shape,sigma,spacing", TWO_PASS_CASES)

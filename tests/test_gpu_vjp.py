@@ -143,3 +143,26 @@ def test_vjp_rejects_bad_sigma(gpu):
         gpu.vjp(x, x, 0.0)
     with pytest.raises(_abi.ItkgError):
         gpu.vjp(x, x, float("nan"))
+
+
+def test_per_axis_algorithm_forces_per_axis_vjp(gpu):
+    """params.algorithm = per-axis keeps the VJP to the per-axis passes; both
+    forms agree within the FMA tolerance."""
+    from itkg import _abi
+    import ctypes
+    rng = np.random.default_rng(61)
+    x = rng.standard_normal((30, 34, 38)).astype(np.float32)
+    y = rng.standard_normal((30, 34, 38)).astype(np.float32)
+    dx, dy = _dev(gpu, x), _dev(gpu, y)
+    xb_f, sb_f = gpu.vjp(dx, dy, 1.4)
+    assert gpu.last_kernel() == "vjp_fused_f32", gpu.last_kernel()
+    xb = gpu.DeviceImage(dx.region)
+    p = _abi.itkg_gaussian_params()
+    p.sigma, p.rounding, p.algorithm = 1.4, gpu.ROUND_FMA, gpu.ALGO_PER_AXIS
+    sb = ctypes.c_double(0.0)
+    _abi.check(_abi.lib().itkg_gaussian_vjp(ctypes.byref(dx.c), ctypes.byref(dy.c), ctypes.byref(p),
+                                           ctypes.byref(xb.c), ctypes.byref(sb), 0, None))
+    assert gpu.last_kernel() == "vjp_per_axis_f32", gpu.last_kernel()
+    a, b = xb.download().astype(np.float64), xb_f.download().astype(np.float64)
+    assert np.abs(a - b).max() <= 1e-5 * np.abs(b).max()
+    assert abs(sb.value - sb_f) <= 1e-5 * max(1.0, abs(sb_f))
