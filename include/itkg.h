@@ -225,8 +225,10 @@ itkg_status itkg_gaussian_generate_region(const itkg_image *input, const itkg_re
  *             host pointer (the call synchronises the stream) unless
  *             ITKG_VJP_SIGMA_BAR_ON_DEVICE; added to with ITKG_VJP_ACCUMULATE_SIGMA.
  * Scalar f32 device images; FMA rounding; sigma must be finite and > 0.
- * params->algorithm ITKG_ALGO_PER_AXIS keeps to the per-axis passes; any other
- * value uses the fused 3-D VJP kernels where they apply. */
+ * params->algorithm selects the kernels (3-D): ITKG_ALGO_AUTO / _TWO_PASS: a
+ * z-adjoint kernel and x-y kernels (rx == ry <= 12, rz <= 12, 16-byte aligned
+ * rows), else as ITKG_ALGO_FUSED: the fused VJP kernels (radii <= 8, the
+ * adjoint <= 6), else the per-axis passes; ITKG_ALGO_PER_AXIS: per-axis only. */
 #define ITKG_VJP_ACCUMULATE_XBAR 1
 #define ITKG_VJP_ACCUMULATE_SIGMA 2
 #define ITKG_VJP_SIGMA_BAR_ON_DEVICE 4

@@ -150,6 +150,21 @@ itkg_status encode_input_map(const FusedGeom& g, int box_w, int box_h, void* map
 itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], void* stream,
                             bool dry_run);
 
+// vjp2.cu: the 3-D VJP as z-adjoint and x-y kernels (rx == ry <= 12, rz <= 12,
+// f32, whole image, 16-byte aligned rows of x and ybar).  sigma_out is a
+// device double (added to with acc_sigma); xbar may be NULL, sigma_out too.
+struct VjpTwoPass {
+  const itkg_image* x;
+  const itkg_image* ybar;
+  itkg_image* xbar;
+  double* sigma_out;
+  bool acc_x, acc_sigma;
+  const float* w[kMaxDim];   // weights per axis
+  const float* dw[kMaxDim];  // their sigma derivatives
+  int radius[kMaxDim];
+};
+itkg_status launch_vjp_two_pass(const VjpTwoPass& v, void* stream, bool dry_run);
+
 // Bumps the launch counter by n (graph replays).
 void note_launches(uint64_t n, const char* name);
 

@@ -299,6 +299,40 @@ extern "C" itkg_status itkg_gaussian_vjp(const itkg_image* x, const itkg_image* 
   bool fused_x = false, fused_s = false;
   // ITKG_ALGO_PER_AXIS: the per-axis passes only (the plain form, for comparisons)
   const bool try_fused = D == 3 && params->algorithm != ITKG_ALGO_PER_AXIS;
+  if (try_fused && params->algorithm != ITKG_ALGO_FUSED) {
+    // z-adjoint and x-y kernels: xbar and sigma_bar in four launches
+    VjpTwoPass v;
+    v.x = x;
+    v.ybar = ybar;
+    v.xbar = xbar;
+    v.acc_x = flags & ITKG_VJP_ACCUMULATE_XBAR;
+    v.acc_sigma = (flags & ITKG_VJP_ACCUMULATE_SIGMA) && (flags & ITKG_VJP_SIGMA_BAR_ON_DEVICE);
+    v.sigma_out = nullptr;
+    for (int d = 0; d < D; ++d) v.w[d] = c[d].w.data(), v.dw[d] = c[d].dw.data(), v.radius[d] = (int)c[d].r;
+    if (launch_vjp_two_pass(v, s, true) == ITKG_SUCCESS) {
+      const bool on_dev = flags & ITKG_VJP_SIGMA_BAR_ON_DEVICE;
+      double* dres = nullptr;
+      if (sigma_bar) {
+        if (on_dev) {
+          v.sigma_out = sigma_bar;
+        } else {
+          void* res = nullptr;
+          ITKG_TRY(sc.raw(sizeof(double), &res));
+          dres = static_cast<double*>(res);
+          v.sigma_out = dres;
+        }
+      }
+      ITKG_TRY(launch_vjp_two_pass(v, s, false));
+      if (sigma_bar && !on_dev) {
+        double h = 0.0;
+        ITKG_CUDA(cudaMemcpyAsync(&h, dres, sizeof h, cudaMemcpyDeviceToHost, s));
+        ITKG_CUDA(cudaStreamSynchronize(s));
+        *sigma_bar = (flags & ITKG_VJP_ACCUMULATE_SIGMA) ? *sigma_bar + h : h;
+      }
+      set_last_kernel("vjp_two_pass_f32");
+      return ITKG_SUCCESS;
+    }
+  }
   if (xbar) {
     // fused adjoint (one pass) where a kernel applies, else D per-axis passes
     const FusedGeom g = whole_geom(*ybar, xbar, c);

@@ -410,7 +410,7 @@ VJP_SIGMA_BAR_ON_DEVICE = 4
 
 def vjp(x: DeviceImage, ybar: DeviceImage, sigma: float, xbar: DeviceImage | None = None,
         want_sigma: bool = True, flags: int = 0, sigma_bar_init: float = 0.0,
-        stream: Stream = _DEFAULT_STREAM):
+        stream: Stream = _DEFAULT_STREAM, algorithm: int = ALGO_AUTO):
     """GaussianFilter VJP over the whole image: returns (xbar, sigma_bar).
 
     xbar = G^T ybar (a DeviceImage, allocated if not given); sigma_bar =
@@ -418,6 +418,7 @@ def vjp(x: DeviceImage, ybar: DeviceImage, sigma: float, xbar: DeviceImage | Non
     p = itkg_gaussian_params()
     p.sigma = float(sigma)
     p.rounding = ROUND_FMA
+    p.algorithm = algorithm
     if xbar is None:
         xbar = DeviceImage(x.region, F32, 1, x.spacing, x.origin)
     sb = ctypes.c_double(sigma_bar_init)

@@ -77,7 +77,7 @@ def test_fused_vjp_matches_fp64_and_is_used(gpu, shape, sigma):
     x = rng.standard_normal(shape).astype(np.float32)
     y = rng.standard_normal(shape).astype(np.float32)
     dx, dy = _dev(gpu, x), _dev(gpu, y)
-    xb, sb = gpu.vjp(dx, dy, sigma)
+    xb, sb = gpu.vjp(dx, dy, sigma, algorithm=gpu.ALGO_FUSED)
     assert gpu.last_kernel() == "vjp_fused_f32", gpu.last_kernel()
     want_x = oracle.gaussian_adjoint_f64(y.astype(np.float64), sigma)
     got_x = xb.download().astype(np.float64)
@@ -154,7 +154,7 @@ def test_per_axis_algorithm_forces_per_axis_vjp(gpu):
     x = rng.standard_normal((30, 34, 38)).astype(np.float32)
     y = rng.standard_normal((30, 34, 38)).astype(np.float32)
     dx, dy = _dev(gpu, x), _dev(gpu, y)
-    xb_f, sb_f = gpu.vjp(dx, dy, 1.4)
+    xb_f, sb_f = gpu.vjp(dx, dy, 1.4, algorithm=gpu.ALGO_FUSED)
     assert gpu.last_kernel() == "vjp_fused_f32", gpu.last_kernel()
     xb = gpu.DeviceImage(dx.region)
     p = _abi.itkg_gaussian_params()
@@ -166,3 +166,53 @@ def test_per_axis_algorithm_forces_per_axis_vjp(gpu):
     a, b = xb.download().astype(np.float64), xb_f.download().astype(np.float64)
     assert np.abs(a - b).max() <= 1e-5 * np.abs(b).max()
     assert abs(sb.value - sb_f) <= 1e-5 * max(1.0, abs(sb_f))
+
+
+TWO_PASS_VJP = [((40, 50, 60), 2.0, None), ((17, 23, 29), 1.2, None), ((5, 70, 40), 0.9, None),
+                ((33, 8, 41), 1.7, None), ((6, 5, 4), 3.0, None), ((1, 9, 1), 1.0, None),
+                ((48, 40, 36), 4.0, None), ((30, 70, 90), 3.4, None), ((20, 30, 40), 2.0, (1.0, 1.0, 2.0)),
+                ((64, 130, 33), 1.5, (0.8, 0.8, 1.0))]
+
+
+@pytest.mark.parametrize("shape,sigma,spacing", TWO_PASS_VJP)
+def test_two_pass_vjp_matches_fp64(gpu, shape, sigma, spacing):
+    """z-adjoint + x-y kernels (radii up to 12, thin images, anisotropic z):
+    dL/dx against the FP64 adjoint, dL/dsigma against the FP64 analytic
+    derivative, and the dot-product identity against the GPU forward."""
+    rng = np.random.default_rng(shape[1] * 3 + shape[2])
+    x = rng.standard_normal(shape).astype(np.float32)
+    y = rng.standard_normal(shape).astype(np.float32)
+    sp = list(spacing) if spacing else None
+    dx, dy = _dev(gpu, x, spacing), _dev(gpu, y, spacing)
+    xb, sb = gpu.vjp(dx, dy, sigma)
+    assert gpu.last_kernel() == "vjp_two_pass_f32", gpu.last_kernel()
+    radii = _radii(sigma, sp, 3)
+    want_x = oracle.gaussian_adjoint_f64(y.astype(np.float64), sigma, spacing=sp)
+    got_x = xb.download().astype(np.float64)
+    assert np.abs(got_x - want_x).max() <= 1e-5 * np.abs(want_x).max()
+    d64 = oracle.gaussian_dsigma_f64(x.astype(np.float64), sigma, spacing=sp, radii=radii)
+    want_s = float((d64 * y.astype(np.float64)).sum())
+    assert abs(sb - want_s) <= 1e-5 * float(np.abs(d64 * y).sum()), (sb, want_s)
+    Gx = gpu.GaussianFilter(dx, sigma, rounding=gpu.ROUND_FMA).generate_region(dx.region).download()
+    lhs = float(np.dot(Gx.astype(np.float64).ravel(), y.astype(np.float64).ravel()))
+    rhs = float(np.dot(x.astype(np.float64).ravel(), got_x.ravel()))
+    assert abs(lhs - rhs) <= 1e-6 * float(np.abs(Gx).sum() * np.abs(y).max())
+
+
+def test_two_pass_vjp_accumulate_and_partial_requests(gpu):
+    rng = np.random.default_rng(9)
+    shape = (21, 35, 44)
+    x = rng.random(shape).astype(np.float32)
+    y = rng.standard_normal(shape).astype(np.float32)
+    dx, dy = _dev(gpu, x), _dev(gpu, y)
+    base, sb = gpu.vjp(dx, dy, 2.2)
+    assert gpu.last_kernel() == "vjp_two_pass_f32"
+    start = rng.standard_normal(shape).astype(np.float32)
+    acc = _dev(gpu, start)
+    out, sb2 = gpu.vjp(dx, dy, 2.2, xbar=acc, sigma_bar_init=-1.5,
+                       flags=gpu.VJP_ACCUMULATE_XBAR | gpu.VJP_ACCUMULATE_SIGMA)
+    assert np.allclose(out.download(), start + base.download(), rtol=0, atol=1e-6)
+    assert abs(sb2 - (sb - 1.5)) < 1e-9 * max(1.0, abs(sb))
+    # the same request again into a fresh buffer: the same dL/dsigma (a fixed reduction order)
+    _, sb3 = gpu.vjp(dx, dy, 2.2, xbar=gpu.DeviceImage(dx.region))
+    assert abs(sb3 - sb) <= 1e-12 * max(1.0, abs(sb))
