@@ -208,7 +208,8 @@ itkg_status launch_dot(const DotArgs& d, double* partials, int nblocks, double* 
 itkg_status launch_sum_partials(const double* partials, int n, double* out, bool accumulate,
                                 void* stream);
 // Squared error against t (DotArgs::q / q_pitch / size): ybar = 2 (y - t) into
-// a dense buffer; *loss_out (+)= sum (y - t)^2, *sigma_out = sum ybar * dy.
+// a dense buffer; *loss_out (+)= sum (y - t)^2, *sigma_out = sum ybar * dy
+// (dy and sigma_out may be NULL: no sigma term).
 // partials: 2 * nblocks doubles of scratch.  y, dy, ybar dense f32.
 itkg_status launch_sqerr(const float* y, const float* dy, const DotArgs& t, float* ybar,
                          double* partials, int nblocks, double* loss_out, double* sigma_out,

@@ -131,7 +131,7 @@ __global__ void __launch_bounds__(kThreads) k_sqerr(const float* __restrict__ y,
     const float g = 2.0f * d;
     ybar[i] = g;
     sl += (double)d * (double)d;
-    ss += (double)g * (double)dy[i];
+    if (dy) ss += (double)g * (double)dy[i];
   }
   __shared__ double red[2][kThreads];
   red[0][threadIdx.x] = sl;
@@ -219,6 +219,7 @@ itkg_status launch_sqerr(const float* y, const float* dy, const DotArgs& t, floa
   if (st != ITKG_SUCCESS) return st;
   k_sum_partials<<<1, kThreads, 0, s>>>(partials, nblocks, loss_out, accumulate_loss ? 1 : 0);
   if ((st = launched("sum_partials_f64")) != ITKG_SUCCESS) return st;
+  if (!sigma_out) return ITKG_SUCCESS;
   k_sum_partials<<<1, kThreads, 0, s>>>(partials + nblocks, nblocks, sigma_out, 0);
   return launched("sum_partials_f64");
 }

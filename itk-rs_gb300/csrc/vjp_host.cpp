@@ -253,13 +253,40 @@ extern "C" itkg_status itkg_gaussian_scale_stack_loss_vjp(
   double* dloss = partials + 2 * nb;
   double* dsig = dloss + 1;
   const bool on_dev = flags & ITKG_VJP_SIGMA_BAR_ON_DEVICE;
+  int fast_levels = 0;
   for (int l = 0; l < nlevels; ++l) {
     const AxisCoeffs* c = &coeffs[(size_t)l * kMaxDim];
+    double* const sig_l = on_dev && sigma_bar ? sigma_bar + l : dsig + l;
+    DotArgs t = dot_args(y, *target);  // q = target
+    // Two-pass forward and VJP kernels where they apply (3-D, the dense scratch
+    // rows 16-byte aligned): y_l, then ybar_l = 2 (y_l - t), then xbar and
+    // dL/dsigma_l from the VJP kernels.
+    VjpTwoPass v;
+    v.x = x;
+    v.ybar = &yb;
+    v.xbar = xbar;
+    v.sigma_out = sig_l;
+    v.acc_x = l > 0;
+    v.acc_sigma = false;
+    for (int d = 0; d < x->dim; ++d) v.w[d] = c[d].w.data(), v.dw[d] = c[d].dw.data(), v.radius[d] = (int)c[d].r;
+    if (x->dim == 3 && x->region.size[0] % 4 == 0 && launch_vjp_two_pass(v, s, true) == ITKG_SUCCESS) {
+      itkg_gaussian_params p;
+      std::memset(&p, 0, sizeof p);
+      p.sigma = sigmas[l];
+      p.arithmetic = ITKG_ARITH_F32;
+      p.rounding = ITKG_ROUND_FMA;
+      p.algorithm = ITKG_ALGO_AUTO;
+      const itkg_region reg = x->region;
+      ITKG_TRY(itkg_gaussian_generate_region(x, &reg, &reg, &p, &y, s));
+      ITKG_TRY(launch_sqerr(static_cast<const float*>(y.data), nullptr, t, static_cast<float*>(yb.data),
+                            partials, nb, dloss, nullptr, l > 0, s));
+      ITKG_TRY(launch_vjp_two_pass(v, s, false));
+      ++fast_levels;
+      continue;
+    }
     ITKG_TRY(dual_chain(*x, c, &y, &dy, sc));  // y_l and dy_l/dsigma_l, recomputed
-    DotArgs t = dot_args(y, *target);          // q = target
     ITKG_TRY(launch_sqerr(static_cast<const float*>(y.data), static_cast<const float*>(dy.data), t,
-                          static_cast<float*>(yb.data), partials, nb, dloss,
-                          on_dev && sigma_bar ? sigma_bar + l : dsig + l, l > 0, s));
+                          static_cast<float*>(yb.data), partials, nb, dloss, sig_l, l > 0, s));
     if (xbar) ITKG_TRY(adjoint_chain(yb, c, xbar, l > 0, sc));
   }
   if (loss || (sigma_bar && !on_dev)) {
@@ -270,7 +297,9 @@ extern "C" itkg_status itkg_gaussian_scale_stack_loss_vjp(
     if (sigma_bar && !on_dev)
       for (int l = 0; l < nlevels; ++l) sigma_bar[l] = h[1 + l];
   }
-  set_last_kernel("scale_stack_loss_vjp_per_axis_f32");
+  set_last_kernel(fast_levels == nlevels ? "scale_stack_loss_vjp_two_pass_f32"
+                  : fast_levels ? "scale_stack_loss_vjp_mixed_f32"
+                                : "scale_stack_loss_vjp_per_axis_f32");
   return ITKG_SUCCESS;
 }
 

@@ -106,7 +106,7 @@ def test_accumulate_flags(gpu):
     assert abs(sb2 - (sb + 2.5)) < 1e-9 * max(1.0, abs(sb))
 
 
-@pytest.mark.parametrize("shape", [(20, 18, 22), (9, 30, 7)])
+@pytest.mark.parametrize("shape", [(20, 18, 22), (9, 30, 7), (20, 18, 24), (12, 40, 32)])
 def test_scale_stack_loss_vjp_matches_fp64(gpu, shape):
     """L = sum_l |G_l x - t|^2 over sigmas {1, 2, 4}: loss, dL/dx, dL/dsigma_l
     against FP64 numpy, and dL/dsigma_l against central differences."""
@@ -115,6 +115,9 @@ def test_scale_stack_loss_vjp_matches_fp64(gpu, shape):
     t = rng.random(shape).astype(np.float32)
     sigmas = [1.0, 2.0, 4.0]
     loss, xbar, sb = gpu.scale_stack_loss_vjp(_dev(gpu, x), _dev(gpu, t), sigmas)
+    # rows of a multiple of 4 floats take the two-pass kernels at every level
+    assert gpu.last_kernel() == ("scale_stack_loss_vjp_two_pass_f32" if shape[2] % 4 == 0
+                                 else "scale_stack_loss_vjp_per_axis_f32"), gpu.last_kernel()
     x64, t64 = x.astype(np.float64), t.astype(np.float64)
     want_loss, want_x, want_s = 0.0, np.zeros(shape), []
     for s in sigmas:
