@@ -33,7 +33,7 @@
 namespace itkg {
 namespace {
 
-constexpr int kMax2DR = 8;
+constexpr int kMax2DR = 12;
 constexpr int kMax2DK = 2 * kMax2DR + 1;
 
 struct Fused2DArgs {
@@ -232,7 +232,9 @@ __global__ void __launch_bounds__(Cfg2<RX, RY, C>::NT) k_fused2d(const Fused2DAr
       switch (p) {
         ITKG_PUSH2(0) ITKG_PUSH2(1) ITKG_PUSH2(2) ITKG_PUSH2(3) ITKG_PUSH2(4) ITKG_PUSH2(5)
         ITKG_PUSH2(6) ITKG_PUSH2(7) ITKG_PUSH2(8) ITKG_PUSH2(9) ITKG_PUSH2(10) ITKG_PUSH2(11)
-        ITKG_PUSH2(12) ITKG_PUSH2(13) ITKG_PUSH2(14) ITKG_PUSH2(15) ITKG_PUSH2(16)
+        ITKG_PUSH2(12) ITKG_PUSH2(13) ITKG_PUSH2(14) ITKG_PUSH2(15) ITKG_PUSH2(16) ITKG_PUSH2(17)
+        ITKG_PUSH2(18) ITKG_PUSH2(19) ITKG_PUSH2(20) ITKG_PUSH2(21) ITKG_PUSH2(22) ITKG_PUSH2(23)
+        ITKG_PUSH2(24)
         default: break;
       }
       p = p + 1 == KY ? 0 : p + 1;
@@ -277,7 +279,8 @@ Entry2 make2() {
 const Entry2 kTable2[] = {
     make2<1, 1>(), make2<2, 1>(), make2<3, 1>(), make2<4, 1>(), make2<5, 1>(), make2<6, 1>(),
     make2<7, 1>(), make2<8, 1>(), make2<1, 3>(), make2<2, 3>(), make2<3, 3>(), make2<4, 3>(),
-    make2<5, 3>(), make2<6, 3>(), make2<7, 3>(), make2<8, 3>(),
+    make2<5, 3>(), make2<6, 3>(), make2<7, 3>(), make2<8, 3>(), make2<9, 1>(), make2<10, 1>(),
+    make2<11, 1>(), make2<12, 1>(), make2<9, 3>(), make2<10, 3>(), make2<11, 3>(), make2<12, 3>(),
 };
 
 struct Occ2 {

@@ -101,7 +101,7 @@ struct FusedGeom {
 itkg_status launch_fused(const FusedGeom& g, const float* const w[kMaxDim], void* stream,
                          bool dry_run);
 
-// fused2d.cu: the 2-D counterpart (f32 input, 1 or 3 components, radius <= 8).
+// fused2d.cu: the 2-D counterpart (f32 input, 1 or 3 components, radius <= 12).
 itkg_status launch_fused2d(const FusedGeom& g, const float* const w[kMaxDim], void* stream,
                            bool dry_run);
 

@@ -371,7 +371,8 @@ def test_fused3d_native_inputs(gpu, kind, sigma, spacing):
 
 FUSED2D_CASES = [((1, 1), 1, 1.0), ((7, 600), 1, 1.0), ((64, 64), 1, 0.3), ((130, 1030), 1, 2.6),
                  ((33, 517), 1, 1.5), ((5, 3), 1, 2.0), ((40, 70), 3, 1.5), ((9, 515), 3, 2.4),
-                 ((1, 40), 3, 0.9), ((200, 100), 3, 0.6)]
+                 ((1, 40), 3, 0.9), ((200, 100), 3, 0.6), ((90, 300), 1, 3.2), ((41, 77), 3, 4.0),
+                 ((130, 20), 3, 3.5), ((9, 600), 1, 4.0)]
 
 
 @pytest.mark.parametrize("shape,comps,sigma", FUSED2D_CASES)
