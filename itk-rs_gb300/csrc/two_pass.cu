@@ -14,19 +14,20 @@ const XYEntry kXYF32[] = ITKG_XY_TABLE(float, ITKG_F32);
 
 struct ZEntry {
   int r;
-  ZFn fn[2];  // [ref]
+  ZFn fn[2][2];  // [ref][vec]
 };
 template <int R>
 ZEntry make_z() {
-  return ZEntry{R, {k_z_pass<R, false>, k_z_pass<R, true>}};
+  return ZEntry{R, {{k_z_pass<R, false, false>, k_z_pass<R, false, true>},
+                    {k_z_pass<R, true, false>, k_z_pass<R, true, true>}}};
 }
 const ZEntry kZ[] = {make_z<1>(), make_z<2>(), make_z<3>(),  make_z<4>(),  make_z<5>(),  make_z<6>(),
                      make_z<7>(), make_z<8>(), make_z<9>(),  make_z<10>(), make_z<11>(), make_z<12>()};
 }  // namespace
 
-ZFn z_fn(int r, bool ref) {
+ZFn z_fn(int r, bool ref, bool vec) {
   for (const ZEntry& z : kZ)
-    if (z.r == r) return z.fn[ref ? 1 : 0];
+    if (z.r == r) return z.fn[ref ? 1 : 0][vec ? 1 : 0];
   return nullptr;
 }
 
@@ -134,7 +135,12 @@ itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], v
   std::memset(&za, 0, sizeof za);
   if (st == ITKG_SUCCESS) st = device_fault_word(&xa.fault);
   int res_xy = 0, res_z = 0;
-  const twopass::ZFn zfn = twopass::z_fn(rz, ref);
+  // 16-byte f32 stores when every quad of the output is full and aligned
+  char* const dst0 = static_cast<char*>(g.dst) + (g.req_index[0] - g.dst_origin[0]) * g.dst_pitch[0] +
+                     (g.req_index[1] - g.dst_origin[1]) * g.dst_pitch[1];
+  const bool vec = g.out_dtype == ITKG_F32 && g.dst_pitch[0] == 4 && ((uintptr_t)dst0 & 15) == 0 &&
+                   (g.dst_pitch[1] & 15) == 0 && (g.dst_pitch[2] & 15) == 0 && nx % 4 == 0;
+  const twopass::ZFn zfn = twopass::z_fn(rz, ref, vec);
   const twopass::XYFn xyfn = e->fn[ref ? 1 : 0];
   if (st == ITKG_SUCCESS) st = max_resident_ctas(reinterpret_cast<const void*>(xyfn), e->smem, e->nt, &res_xy);
   if (st == ITKG_SUCCESS)
@@ -204,12 +210,7 @@ itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], v
   za.dst_pitch[0] = g.dst_pitch[0];
   za.dst_pitch[1] = g.dst_pitch[1];
   za.dst_pitch[2] = g.dst_pitch[2];
-  char* const dst0 = static_cast<char*>(g.dst) + (g.req_index[0] - g.dst_origin[0]) * g.dst_pitch[0] +
-                     (g.req_index[1] - g.dst_origin[1]) * g.dst_pitch[1];
-  za.vec_store = (g.out_dtype == ITKG_F32 && g.dst_pitch[0] == 4 && ((uintptr_t)dst0 & 15) == 0 &&
-                  (g.dst_pitch[1] & 15) == 0 && (g.dst_pitch[2] & 15) == 0)
-                     ? 1
-                     : 0;
+  za.vec_store = vec ? 1 : 0;
   for (int k = 0; k < 2 * rz + 1; ++k) za.wz[k] = w[2][k], za.wz2[k] = splat2_host(w[2][k]);
   const int64_t qblocks = ntx * nty * (tile_floats / 4 / twopass::CfgZ<1>::QB);
   za.tile_rows = e->ty;

@@ -95,7 +95,7 @@ struct ZArgs {
   char* dst;               // output voxel (x0, y0, z0)
   int64_t dst_pitch[3];    // bytes
   int32_t out_dtype;
-  int32_t vec_store;       // 1: f32 output rows allow 16-byte stores
+  int32_t vec_store;       // 1: the 16-byte store variant (see k_z_pass)
   float wz[kMaxK];
   f2_t wz2[kMaxK];
 };
@@ -423,15 +423,18 @@ timeout:
 
 // ---------------------------------------------------------------------------
 // z pass
-template <int RZ, bool REF>
+// VEC: f32 output whose rows allow 16-byte stores and whose width is a
+// multiple of 4 (every quad full).
+template <int RZ, bool REF, bool VEC>
 __global__ void __launch_bounds__(256, RZ <= 8 ? 2 : 1) k_z_pass(const __grid_constant__ ZArgs a) {
   using C = CfgZ<RZ>;
-  constexpr int KZ = C::KZ, S = C::S, NT = C::NT, QPT = C::QPT, NP = 2 * QPT;  // NP packed pairs
-  extern __shared__ __align__(16) float4 zring[];  // [S][NT][QPT]
+  constexpr int KZ = C::KZ, S = C::S, NT = C::NT;
+  static_assert(C::QPT == 1, "one quad per thread");
+  extern __shared__ __align__(16) float4 zring[];  // [S][NT]
   const int tid = threadIdx.x;
   const int64_t u_begin = a.units * blockIdx.x / gridDim.x;
   const int64_t u_end = a.units * (blockIdx.x + 1) / gridDim.x;
-  const uint32_t my_slot0 = smem_u32(zring + tid * QPT);
+  const uint32_t my_slot0 = smem_u32(zring + tid);
   const uint64_t pol_t = policy_evict_first();
 
   for (int64_t u = u_begin; u < u_end;) {
@@ -440,8 +443,8 @@ __global__ void __launch_bounds__(256, RZ <= 8 ? 2 : 1) k_z_pass(const __grid_co
     const int64_t zrem = zs + (u_end - u);
     const int ze = zrem < a.nz ? (int)zrem : a.nz;
     u += ze - zs;
-    // this thread's quads: T tile `tl`, quads w .. w + QPT - 1 (row w / 8, from column 4 (w % 8))
-    const int64_t q = blk * C::QB + (int64_t)tid * QPT;
+    // this thread's quad: T tile `tl`, quad w (row w / 8, columns 4 (w % 8) .. + 3)
+    const int64_t q = blk * C::QB + tid;
     const int tile_q = a.tile_rows * (kTileX / 4);  // quads per tile
     const int64_t tl = q / tile_q;
     const int w = (int)(q - tl * tile_q);
@@ -450,91 +453,93 @@ __global__ void __launch_bounds__(256, RZ <= 8 ? 2 : 1) k_z_pass(const __grid_co
     const int cy = (int)tly * a.tile_rows + w / (kTileX / 4);                      // row
     if (cy >= a.ny || cx >= a.nx) continue;  // no barriers in this kernel: idle threads just skip
     const int z0 = a.z0 + zs, z1 = a.z0 + ze;  // outputs [z0, z1)
-    const int jb = z0 - RZ, je = z1 - 1 + RZ;
+    const int jb = z0 - RZ;
     // prefetch cursor: slice jn (clamped to T) at pn
     const float* const tq = a.t + tl * (4 * tile_q) + 4 * w;
     int jn = jb;
     const float* pn = tq + (int64_t)(clampi(jn, a.t_s0, a.t_s1) - a.t_s0) * a.t_slice;
     auto prefetch = [&](int stage) {
-#pragma unroll
-      for (int c = 0; c < QPT; ++c) cp_async16_hint(my_slot0 + (uint32_t)((stage * NT * QPT + c) * 16), pn + 4 * c, pol_t);
+      cp_async16_hint(my_slot0 + (uint32_t)(stage * NT * 16), pn, pol_t);
       fusedk::cp_async_commit();
       ++jn;
-      if (jn > a.t_s0 && jn <= a.t_s1) pn += a.t_slice;
+      pn += (jn > a.t_s0 && jn <= a.t_s1) ? a.t_slice : 0;
     };
 #pragma unroll
     for (int i = 0; i < S; ++i) prefetch(i);
-    f2_t acc[NP][KZ];
+    f2_t acc[2][KZ];
 #pragma unroll
-    for (int m = 0; m < NP; ++m)
+    for (int m = 0; m < 2; ++m)
 #pragma unroll
       for (int k = 0; k < KZ; ++k) acc[m][k] = 0ull;
-    const int ncols = min(4 * QPT, a.nx - cx);
-    const bool vec = a.vec_store && ncols == 4 * QPT;
+    const int ncols = min(4, a.nx - cx);
     char* dz = a.dst + (int64_t)cx * a.dst_pitch[0] + (int64_t)cy * a.dst_pitch[1] +
                (int64_t)(z0 - a.z0) * a.dst_pitch[2];
-    for (int jbase = jb; jbase <= je; jbase += KZ) {
+    // One slice at phase p (a constant once the callers' loops are unrolled):
+    // slice j = (period start) + p sits in stage p; push it, refill the stage
+    // with slice j + S, pop output j - RZ and store it if `store`.
+    auto step = [&](int p, bool store) {
+      fusedk::cp_async_wait<S - 1>();
+      const float4 f = zring[p * NT + tid];
+      f2_t v[2] = {pack2(f.x, f.y), pack2(f.z, f.w)};
+      prefetch(p);
 #pragma unroll
-      for (int p = 0; p < KZ; ++p) {  // phase p: slice j in stage p
-        const int j = jbase + p;
-        if (j > je) break;
-        fusedk::cp_async_wait<S - 1>();
-        f2_t v[NP];
+      for (int k = 0; k < KZ; ++k) {
+        const int slot = (p - k + KZ) % KZ;
 #pragma unroll
-        for (int c = 0; c < QPT; ++c) {
-          const float4 f = zring[(p * NT + tid) * QPT + c];
-          v[2 * c] = pack2(f.x, f.y);
-          v[2 * c + 1] = pack2(f.z, f.w);
-        }
-        prefetch(p);  // the stage has been read: refill it with slice j + S
-#pragma unroll
-        for (int k = 0; k < KZ; ++k) {
-          const int slot = (p - k + KZ) % KZ;
-#pragma unroll
-          for (int m = 0; m < NP; ++m) {
-            if constexpr (REF) {
-              float a0, a1, v0, v1;
-              unpack2(acc[m][slot], a0, a1);
-              unpack2(v[m], v0, v1);
-              acc[m][slot] = pack2(__fadd_rn(a0, __fmul_rn(v0, a.wz[k])), __fadd_rn(a1, __fmul_rn(v1, a.wz[k])));
-            } else if (k == 0) {  // first contribution to output j + RZ: its slot was popped
-              acc[m][slot] = mul2(v[m], a.wz2[0]);
-            } else {
-              acc[m][slot] = fma2(v[m], a.wz2[k <= RZ ? k : 2 * RZ - k], acc[m][slot]);
-            }
-          }
-        }
-        const int D = (p + 1) % KZ;  // a constant once the phase loop is unrolled
-        f2_t d[NP];
-#pragma unroll
-        for (int m = 0; m < NP; ++m) {
-          d[m] = acc[m][D];
-          if constexpr (REF) acc[m][D] = 0ull;  // reference rounding adds the first product to zero
-        }
-        if (j - RZ >= z0) {
-          float o[4 * QPT];
-#pragma unroll
-          for (int m = 0; m < NP; ++m) unpack2(d[m], o[2 * m], o[2 * m + 1]);
-          if (vec) {
-#pragma unroll
-            for (int c = 0; c < QPT; ++c)
-              __stcs(reinterpret_cast<float4*>(dz) + c, make_float4(o[4 * c], o[4 * c + 1], o[4 * c + 2], o[4 * c + 3]));
+        for (int m = 0; m < 2; ++m) {
+          if constexpr (REF) {
+            float a0, a1, v0, v1;
+            unpack2(acc[m][slot], a0, a1);
+            unpack2(v[m], v0, v1);
+            acc[m][slot] = pack2(__fadd_rn(a0, __fmul_rn(v0, a.wz[k])), __fadd_rn(a1, __fmul_rn(v1, a.wz[k])));
+          } else if (k == 0) {  // first contribution to output j + RZ: its slot was popped
+            acc[m][slot] = mul2(v[m], a.wz2[0]);
           } else {
-#pragma unroll
-            for (int c = 0; c < 4 * QPT; ++c) {
-              if (c >= ncols) break;
-              char* const dp = dz + c * a.dst_pitch[0];
-              switch (a.out_dtype) {
-                case ITKG_F32: *reinterpret_cast<float*>(dp) = o[c]; break;
-                case ITKG_BF16: *reinterpret_cast<__nv_bfloat16*>(dp) = from_f32<__nv_bfloat16>(o[c]); break;
-                case ITKG_F16: *reinterpret_cast<__half*>(dp) = from_f32<__half>(o[c]); break;
-                default: *reinterpret_cast<uint8_t*>(dp) = from_f32<uint8_t>(o[c]); break;
-              }
-            }
+            acc[m][slot] = fma2(v[m], a.wz2[k <= RZ ? k : 2 * RZ - k], acc[m][slot]);
           }
-          dz += a.dst_pitch[2];
         }
       }
+      const int D = (p + 1) % KZ;
+      const f2_t d0 = acc[0][D], d1 = acc[1][D];
+      if constexpr (REF) {  // reference rounding adds the first product to zero
+        acc[0][D] = 0ull;
+        acc[1][D] = 0ull;
+      }
+      if (!store) return;
+      float o[4];
+      unpack2(d0, o[0], o[1]);
+      unpack2(d1, o[2], o[3]);
+      if constexpr (VEC) {
+        __stcs(reinterpret_cast<float4*>(dz), make_float4(o[0], o[1], o[2], o[3]));
+      } else {
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          if (c >= ncols) break;
+          char* const dp = dz + c * a.dst_pitch[0];
+          switch (a.out_dtype) {
+            case ITKG_F32: *reinterpret_cast<float*>(dp) = o[c]; break;
+            case ITKG_BF16: *reinterpret_cast<__nv_bfloat16*>(dp) = from_f32<__nv_bfloat16>(o[c]); break;
+            case ITKG_F16: *reinterpret_cast<__half*>(dp) = from_f32<__half>(o[c]); break;
+            default: *reinterpret_cast<uint8_t*>(dp) = from_f32<uint8_t>(o[c]); break;
+          }
+        }
+      }
+      dz += a.dst_pitch[2];
+    };
+    // first period: slices z0 - RZ .. z0 + RZ; only the last one completes an output (z0)
+#pragma unroll
+    for (int p = 0; p < KZ; ++p) step(p, p == KZ - 1);
+    // then every slice completes one: whole periods, then the tail
+    const int rest = z1 - z0 - 1;
+    const int nfull = rest / KZ, tail = rest - nfull * KZ;
+    for (int it = 0; it < nfull; ++it) {
+#pragma unroll
+      for (int p = 0; p < KZ; ++p) step(p, true);
+    }
+#pragma unroll
+    for (int p = 0; p < KZ; ++p) {
+      if (p >= tail) break;
+      step(p, true);
     }
     fusedk::cp_async_wait<0>();
   }
@@ -567,7 +572,7 @@ const XYEntry* xy_entries_i16(int* n);
 const XYEntry* xy_entries_u8(int* n);
 const XYEntry* xy_entries_bf16(int* n);
 const XYEntry* xy_entries_f16(int* n);
-ZFn z_fn(int r, bool ref);
+ZFn z_fn(int r, bool ref, bool vec);
 
 #define ITKG_XY_TABLE(T, DT)                                                                      \
   {                                                                                              \
