@@ -238,9 +238,22 @@ itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], v
     za.units = qblocks * za.nz;
     za.dst = dst0 + (oz0 - g.dst_origin[2]) * g.dst_pitch[2];
     const int64_t gz = std::min<int64_t>(za.units, res_z);
-    zfn<<<(unsigned)gz, 256, z_smem(rz), s>>>(za);
+    // programmatic dependent launch: z CTAs may start while the x-y CTAs retire;
+    // the z kernel waits on the x-y grid before it reads T
+    cudaLaunchConfig_t cfg;
+    std::memset(&cfg, 0, sizeof cfg);
+    cfg.gridDim = dim3((unsigned)gz);
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = z_smem(rz);
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    err = cudaLaunchKernelEx(&cfg, zfn, za);
     note_launch(ref ? "z_pass_f32_ref" : "z_pass_f32_fma");
-    err = cudaGetLastError();
+    if (err == cudaSuccess) err = cudaGetLastError();
     if (err != cudaSuccess) st = set_error(ITKG_ERROR_CUDA, "z pass launch: %s", cudaGetErrorString(err));
   }
   scratch_free(t, stream);

@@ -206,6 +206,8 @@ __global__ void __launch_bounds__(288, 2)
   __syncthreads();
   uint32_t phase_bits = 0;
 
+  // the dependent z pass may be scheduled now; it waits for this grid before reading T
+  asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
   const int64_t u_begin = a.units * blockIdx.x / gridDim.x;
   const int64_t u_end = a.units * (blockIdx.x + 1) / gridDim.x;
   const int n = (int)(u_end - u_begin);
@@ -436,6 +438,9 @@ __global__ void __launch_bounds__(256, RZ <= 8 ? 2 : 1) k_z_pass(const __grid_co
   const int64_t u_end = a.units * (blockIdx.x + 1) / gridDim.x;
   const uint32_t my_slot0 = smem_u32(zring + tid);
   const uint64_t pol_t = policy_evict_first();
+  // T is written by the x-y grid this launch depends on (programmatic dependent
+  // launch): wait for it to complete and its writes to be visible
+  asm volatile("griddepcontrol.wait;\n" ::: "memory");
 
   for (int64_t u = u_begin; u < u_end;) {
     const int64_t blk = u / a.nz;
