@@ -155,9 +155,34 @@ def cpu_sample_rate(vol, budget_s, threads):
     return s, run
 
 
+# ---------------------------------------------------------------------------
+# Replicas across ranks (one process per GPU, no data exchange)
+# ---------------------------------------------------------------------------
+def max_over_ranks(value, dist, device):
+    """The largest of every rank's `value` (a float), e.g. the timed region's
+    duration: the job is as slow as its slowest replica."""
+    import torch
+    if dist is None:
+        return float(value)
+    t = torch.tensor([float(value)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(world, units_per_rank, elapsed_s):
+    """Whole-job throughput of `world` replicas, each processing
+    `units_per_rank` units, timed by the slowest one (weak scaling)."""
+    return world * units_per_rank / elapsed_s
+
+
+def reports(rank):
+    """Only rank 0 prints the JSON line."""
+    return rank == 0
+
+
 def reference_arm(args):
     rank = int(os.environ.get("RANK", "0"))
-    if rank != 0:
+    if not reports(rank):  # under torchrun only rank 0 times the CPU reference
         return 0
     threads = os.cpu_count() or 1
     vol = blobs_volume(SHAPE, 0)
@@ -280,13 +305,10 @@ def gpu_arm(args):
     clk = clocks.stop()
     elapsed_ms = t0.elapsed_time(t1)
     per_launch_ms = [e[0].elapsed_time(e[1]) for row in ev for e in row]
-    if dist is not None:
-        t = torch.tensor([elapsed_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
+    elapsed_ms = max_over_ranks(elapsed_ms, dist, "cuda")
 
     nvox = SHAPE[0] * SHAPE[1] * SHAPE[2]
-    value = world * args.steps * NVOL * nvox / (elapsed_ms * 1e-3)
+    value = job_throughput(world, args.steps * NVOL * nvox, elapsed_ms * 1e-3)
     avg_launch_s = statistics.mean(per_launch_ms) * 1e-3
     peak, peak_kind = measured_peak()
     achieved = nvox * BYTES_PER_VOXEL / avg_launch_s / 1e9
@@ -312,16 +334,13 @@ def gpu_arm(args):
         for _ in range(args.e2e_steps):
             _abi.check(gen(ctypes.byref(hin), lg_r, req_r, prm_r, ctypes.byref(hout), sptr))
         te = time.perf_counter() - ts
-        if dist is not None:
-            t = torch.tensor([te], device="cuda", dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            te = float(t.item())
+        te = max_over_ranks(te, dist, "cuda")
         res = np.frombuffer((ctypes.c_char * nbytes).from_address(hp_out.value), dtype=np.float32)
         if not np.array_equal(res.reshape(SHAPE).view(np.uint32), got.view(np.uint32)):
             raise RuntimeError("e2e result differs from the device-resident result")
         L.itkg_host_free_pinned(hp_in)
         L.itkg_host_free_pinned(hp_out)
-        e2e = {"value": world * args.e2e_steps * nvox / te, "unit": "voxels/s",
+        e2e = {"value": job_throughput(world, args.e2e_steps * nvox, te), "unit": "voxels/s",
                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                "steps": args.e2e_steps}
 
@@ -335,7 +354,7 @@ def gpu_arm(args):
                "sample": f"{SHAPE[2]}x{SHAPE[1]}x{s} slab of the 256^3 volume, {t:.1f} s; "
                          "C restatement of the reference rayon path"}
 
-    if rank == 0:
+    if reports(rank):
         line = {
             "metric": METRIC, "value": value, "unit": "voxels/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup,
