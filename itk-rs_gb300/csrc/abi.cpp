@@ -346,6 +346,46 @@ static itkg_status staging_streams(cudaStream_t out[3]) {
   return ITKG_SUCCESS;
 }
 
+// Timing-free events for the staged path, per thread and device, created once
+// and reused: a call records each of its events once and ends with a stream
+// synchronize that covers every stream it recorded on.
+static itkg_status staging_event(size_t idx, cudaEvent_t* e) {
+  thread_local std::vector<std::vector<cudaEvent_t>> per_dev;
+  int dev = 0;
+  ITKG_CUDA(cudaGetDevice(&dev));
+  if ((int)per_dev.size() <= dev) per_dev.resize(dev + 1);
+  std::vector<cudaEvent_t>& pool = per_dev[dev];
+  while (pool.size() <= idx) {
+    cudaEvent_t ne = nullptr;
+    ITKG_CUDA(cudaEventCreateWithFlags(&ne, cudaEventDisableTiming));
+    pool.push_back(ne);
+  }
+  *e = pool[idx];
+  return ITKG_SUCCESS;
+}
+
+// Copies the kernels' fault word into a per-thread pinned word on stream s, so
+// that a call which synchronises s anyway reads it with no second synchronous
+// copy.  *word is valid once s has been synchronised.
+static itkg_status fault_word_async(cudaStream_t s, const unsigned int** word) {
+  thread_local unsigned int* pinned = nullptr;
+  if (!pinned) ITKG_CUDA(cudaMallocHost(reinterpret_cast<void**>(&pinned), sizeof(unsigned int)));
+  unsigned int* dev_word = nullptr;
+  ITKG_TRY(device_fault_word(&dev_word));
+  ITKG_CUDA(cudaMemcpyAsync(pinned, dev_word, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
+  *word = pinned;
+  return ITKG_SUCCESS;
+}
+
+// After the synchronize: a kernel that gave up on a bounded wait makes the call
+// fail (and the fault word is cleared) instead of returning an incomplete result.
+static itkg_status check_fault_word(const unsigned int* word) {
+  if (!word || *word == 0) return ITKG_SUCCESS;
+  unsigned int fault = 0;
+  ITKG_TRY(fused_fault_flag(&fault, true));
+  return set_error(ITKG_ERROR_TIMEOUT, "a kernel gave up waiting for a tile load");
+}
+
 // Slabs along axis D-1 for a host-buffer call: about 4 MiB of output each, at
 // most 8, and at least 2 kernel lengths thick (1 = no pipelining).
 static int staging_pieces(const itkg_image& out, const itkg_region& requested, int D) {
@@ -389,10 +429,9 @@ static itkg_status generate_staged(const itkg_image* input, const itkg_region* l
     st = scratch_alloc(&pout, image_bytes(dout), s);
     dout.data = pout;
   }
-  std::vector<cudaEvent_t> ev;
+  size_t n_events = 0;
   auto event = [&](cudaStream_t on, cudaEvent_t* e) -> itkg_status {
-    ITKG_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
-    ev.push_back(*e);
+    ITKG_TRY(staging_event(n_events++, e));
     ITKG_CUDA(cudaEventRecord(*e, on));
     return ITKG_SUCCESS;
   };
@@ -435,14 +474,12 @@ static itkg_status generate_staged(const itkg_image* input, const itkg_region* l
   }
   scratch_free(pin, s);
   scratch_free(pout, s);
+  const unsigned int* fw = nullptr;
+  if (st == ITKG_SUCCESS) st = fault_word_async(s, &fw);
   const cudaError_t es = cudaStreamSynchronize(s);
-  for (cudaEvent_t e : ev) cudaEventDestroy(e);
   if (st != ITKG_SUCCESS) return st;
   if (es != cudaSuccess) return cuda_status(es, "cudaStreamSynchronize");
-  unsigned int fault = 0;
-  ITKG_TRY(fused_fault_flag(&fault, true));
-  if (fault) return set_error(ITKG_ERROR_TIMEOUT, "a fused kernel gave up waiting for a tile load");
-  return ITKG_SUCCESS;
+  return check_fault_word(fw);
 }
 
 static itkg_status generate_region(const itkg_image* input, const itkg_region* largest,
@@ -506,13 +543,13 @@ static itkg_status generate_region(const itkg_image* input, const itkg_region* l
   scratch_free(pin, s);
   scratch_free(pout, s);
   if (st == ITKG_SUCCESS) {
+    // The call synchronises anyway: surface a kernel that gave up on a
+    // bounded wait instead of returning an incomplete result as success.
+    const unsigned int* fw = nullptr;
+    ITKG_TRY(fault_word_async(s, &fw));
     cudaError_t e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return cuda_status(e, "cudaStreamSynchronize");
-    // The call synchronised anyway: surface a kernel that gave up on a
-    // bounded wait instead of returning an incomplete result as success.
-    unsigned int fault = 0;
-    ITKG_TRY(fused_fault_flag(&fault, true));
-    if (fault) return set_error(ITKG_ERROR_TIMEOUT, "a fused kernel gave up waiting for a tile load");
+    return check_fault_word(fw);
   }
   return st;
 }

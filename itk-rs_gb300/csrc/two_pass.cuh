@@ -115,7 +115,8 @@ struct CfgXY {
   static constexpr int XA = (R + AE - 1) / AE * AE;
   // Staged row: TX + 2XA columns; f32 rows get 4 more (loaded and unused) so
   // that consecutive rows start 16 banks + 4 apart (conflict-free 16-byte loads).
-  static constexpr int BW = TX + 2 * XA + (ESZ == 4 ? 4 : 0);
+  static constexpr int PAD = 4;
+  static constexpr int BW = TX + 2 * XA + (ESZ == 4 ? PAD : 0);
   static constexpr int IH = TY + 2 * R;
   static constexpr int NTASK = IH * SEGS;       // x-pass tasks per unit
   static constexpr int OFF = (XA - R) % 4;
@@ -124,11 +125,13 @@ struct CfgXY {
   // form reads whole aligned pairs, one more when output MX - 1 starts even
   static constexpr int WIN = (MX + 2 * R + OFF + (OFF & 1) + 3) / 4 * 4;
   static constexpr int S = 2;                   // units in flight
+  static constexpr int NXB = 2;                 // x-filtered tiles (2: one block barrier per slice)
+  static constexpr int MINB = 2;                // CTAs per SM the register budget is set for
   static constexpr int BOX = IH * BW * ESZ;
   static constexpr int STAGE = (BOX + 127) / 128 * 128;
   static constexpr int TXP = TX + 4;            // x-filtered row stride (floats)
   static constexpr int XBUF = IH * TXP;         // floats per x-filtered tile
-  static constexpr size_t SMEM = (size_t)S * STAGE + sizeof(float) * 2 * XBUF + 128;
+  static constexpr size_t SMEM = (size_t)S * STAGE + sizeof(float) * NXB * XBUF + 128;
   static_assert(WB + TX - MX + WIN <= BW, "x window stays inside the staged row");
   static_assert(TX % MX == 0, "x segments");
   static_assert(NTASK > NT && NTASK <= 2 * NT, "each thread runs one or two x-pass tasks");
@@ -184,12 +187,12 @@ __device__ __forceinline__ float ld1(const __half* p) { return __half2float(*p);
 // ---------------------------------------------------------------------------
 // xy pass
 template <int R, bool REF, typename Tin>
-__global__ void __launch_bounds__(288, 2)
+__global__ void __launch_bounds__(288, CfgXY<R, Tin>::MINB)
     k_xy_pass(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ XYArgs a) {
   using C = CfgXY<R, Tin>;
   constexpr int K = C::K, TX = C::TX, TY = C::TY, MY = C::MY, MX = C::MX, BW = C::BW, IH = C::IH,
                 XA = C::XA, S = C::S, WIN = C::WIN, WB = C::WB, OFF = C::OFF, NT = C::NT, SEGS = C::SEGS,
-                TXP = C::TXP, NTASK = C::NTASK;
+                TXP = C::TXP, NTASK = C::NTASK, NXB = C::NXB;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t mbar[S];
   __shared__ int s_fail;
@@ -351,16 +354,10 @@ __global__ void __launch_bounds__(288, 2)
       if (has_b) xtask(tile_s, xb, row_b, x0_b, yedge, rlo, rhi, xedge, nl, cr);
     };
 
-    for (int q = 0; q < S && q < ns_seg; ++q) issue(s_a + q);
-    xpass(xbuf0);
-    for (int i = 0; i < ns_seg; ++i) {
-      // x pass of slice i visible; y pass of slice i - 1 done with the other buffer
-      __syncthreads();
-      if (s_fail) goto timeout;
-      if (i + S < ns_seg) issue(s_a + i + S);  // into the stage slice i's x pass has finished reading
-      if (i + 1 < ns_seg) xpass(xbuf0 + ((i + 1) & 1) * C::XBUF);
+    // y pass of the x-filtered tile xb into T
+    auto ypass = [&](const float* xb) {
       if (has_y) {
-        const float* const yw = ywin0 + (i & 1) * C::XBUF;
+        const float* const yw = ywin0 + (xb - xbuf0);
         f2_t win[MY + 2 * R];
 #pragma unroll
         for (int q = 0; q < MY + 2 * R; ++q) win[q] = *reinterpret_cast<const f2_t*>(yw + q * TXP);
@@ -387,7 +384,7 @@ __global__ void __launch_bounds__(288, 2)
         if constexpr (!REF) {
           // first / last two tile rows: the clamped taps, c[row] * X[edge row]
           if (top) {
-            const f2_t xe = *reinterpret_cast<const f2_t*>(xbuf0 + (i & 1) * C::XBUF + rlo * TXP + 2 * lane16);
+            const f2_t xe = *reinterpret_cast<const f2_t*>(xb + rlo * TXP + 2 * lane16);
 #pragma unroll
             for (int m = 0; m < MY; ++m) {
               const float c = a.cyt[grp * MY + m];
@@ -395,7 +392,7 @@ __global__ void __launch_bounds__(288, 2)
             }
           }
           if (bot) {
-            const f2_t xe = *reinterpret_cast<const f2_t*>(xbuf0 + (i & 1) * C::XBUF + rhi * TXP + 2 * lane16);
+            const f2_t xe = *reinterpret_cast<const f2_t*>(xb + rhi * TXP + 2 * lane16);
 #pragma unroll
             for (int m = 0; m < MY; ++m) {
               const float c = a.cyb[trow * TY + grp * MY + m];
@@ -406,9 +403,31 @@ __global__ void __launch_bounds__(288, 2)
 #pragma unroll
         for (int m = 0; m < MY; ++m) st_f2_hint(tp + m * TX, yv[m], pol_t);
       }
+    };
+
+    for (int q = 0; q < S && q < ns_seg; ++q) issue(s_a + q);
+    xpass(xbuf0);
+    for (int i = 0; i < ns_seg; ++i) {
+      const float* const xb = xbuf0 + (NXB == 2 ? (i & 1) * C::XBUF : 0);
+      // x pass of slice i visible (and, with two x-filtered tiles, the y pass
+      // of slice i - 1 done with the other one)
+      __syncthreads();
+      if (s_fail) goto timeout;
+      if (i + S < ns_seg) issue(s_a + i + S);  // into the stage slice i's x pass has finished reading
+      if constexpr (NXB == 2 && S >= 2) {
+        if (i + 1 < ns_seg) xpass(xbuf0 + ((i + 1) & 1) * C::XBUF);
+        ypass(xb);
+      } else if constexpr (NXB == 2) {  // one stage: slice i + 1 lands during the y pass
+        ypass(xb);
+        if (i + 1 < ns_seg) xpass(xbuf0 + ((i + 1) & 1) * C::XBUF);
+      } else {
+        ypass(xb);
+        __syncthreads();  // the y pass is done with the only x-filtered tile
+        if (i + 1 < ns_seg) xpass(xbuf0);
+      }
       tp += a.t_slice;
     }
-    __syncthreads();  // the next segment reuses both x-filtered buffers
+    __syncthreads();  // the next segment reuses the x-filtered tiles
   }
   return;
 timeout:
