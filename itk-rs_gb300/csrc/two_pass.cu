@@ -75,6 +75,44 @@ const char* xy_name(int dtype, bool ref) {
   return names[dtype][ref ? 1 : 0];
 }
 
+// Per-CTA unit ranges of the z pass.  Units are (quad block, output slice),
+// block-major; a CTA marches each column segment of its range from 2 rz slices
+// before the segment's first output, so its cost is its units plus 2 rz per
+// segment.  The ranges are cut greedily under the smallest cost budget that
+// lets at most `grid` CTAs cover all units (an even split leaves the CTAs whose
+// range straddles two blocks about 2 rz slices behind).  Returns the CTA count
+// and fills split[0 .. count]; 0 when the units do not fit the table.
+int z_split(int64_t qblocks, int64_t nz, int rz, int64_t grid, int32_t* split) {
+  if (grid < 1 || grid > twopass::kMaxZSplit || qblocks * nz > INT_MAX) return 0;
+  auto cover = [&](int64_t budget, int32_t* out) -> int64_t {
+    int64_t blk = 0, zs = 0, n = 0;
+    while (blk < qblocks) {
+      if (n == grid) return grid + 1;
+      if (out) out[n] = (int32_t)(blk * nz + zs);
+      ++n;
+      int64_t left = budget;
+      while (blk < qblocks) {
+        const int64_t take = std::min<int64_t>(nz - zs, left - 2 * rz);
+        if (take <= 0) break;
+        zs += take;
+        left -= take + 2 * rz;
+        if (zs < nz) break;
+        ++blk;
+        zs = 0;
+      }
+    }
+    if (out) out[n] = (int32_t)(qblocks * nz);
+    return n;
+  };
+  int64_t lo = 2 * rz + 1, hi = qblocks * (nz + 2 * rz);
+  while (lo < hi) {
+    const int64_t mid = lo + (hi - lo) / 2;
+    if (cover(mid, nullptr) <= grid) hi = mid;
+    else lo = mid + 1;
+  }
+  return (int)cover(lo, split);
+}
+
 }  // namespace
 
 itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], void* stream, bool dry_run) {
@@ -224,9 +262,23 @@ itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], v
     xa.t_s0 = (int32_t)s0;
     xa.units = (int64_t)xa.ntx * nty * xa.ns;
     const int64_t gxy = std::min<int64_t>(xa.units, res_xy);
-    xyfn<<<(unsigned)gxy, e->nt, e->smem, s>>>(map, xa);
+    // programmatic dependent launch on both kernels: the x-y CTAs may start
+    // while the stream's previous kernel retires (they wait for it before
+    // touching global memory), the z CTAs while the x-y CTAs retire
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg;
+    std::memset(&cfg, 0, sizeof cfg);
+    cfg.gridDim = dim3((unsigned)gxy);
+    cfg.blockDim = dim3((unsigned)e->nt);
+    cfg.dynamicSmemBytes = e->smem;
+    cfg.stream = s;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaError_t err = cudaLaunchKernelEx(&cfg, xyfn, map, xa);
     note_launch(xy_name(g.in_dtype, ref));
-    cudaError_t err = cudaGetLastError();
+    if (err == cudaSuccess) err = cudaGetLastError();
     if (err != cudaSuccess) {
       st = set_error(ITKG_ERROR_CUDA, "xy pass launch: %s", cudaGetErrorString(err));
       break;
@@ -237,20 +289,12 @@ itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], v
     za.nz = (int32_t)(c1 - c0);
     za.units = qblocks * za.nz;
     za.dst = dst0 + (oz0 - g.dst_origin[2]) * g.dst_pitch[2];
-    const int64_t gz = std::min<int64_t>(za.units, res_z);
-    // programmatic dependent launch: z CTAs may start while the x-y CTAs retire;
-    // the z kernel waits on the x-y grid before it reads T
-    cudaLaunchConfig_t cfg;
-    std::memset(&cfg, 0, sizeof cfg);
+    int64_t gz = std::min<int64_t>(za.units, res_z);
+    za.nsplit = z_split(qblocks, za.nz, rz, gz, za.split);
+    if (za.nsplit > 0) gz = za.nsplit;
     cfg.gridDim = dim3((unsigned)gz);
     cfg.blockDim = dim3(256);
     cfg.dynamicSmemBytes = z_smem(rz);
-    cfg.stream = s;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
     err = cudaLaunchKernelEx(&cfg, zfn, za);
     note_launch(ref ? "z_pass_f32_ref" : "z_pass_f32_fma");
     if (err == cudaSuccess) err = cudaGetLastError();

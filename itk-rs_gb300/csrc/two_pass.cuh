@@ -50,6 +50,7 @@ constexpr int kMaxK = 2 * kMaxR + 1;
 // x-y tile: kTileX columns and 128 rows (64 for R > 8); T is stored
 // tile-major: [slice][tile][tile rows][kTileX columns]
 constexpr int kTileX = 32;
+constexpr int kMaxZSplit = 1024;  // z-pass CTAs with a per-CTA unit range
 constexpr int kTileY = 128;  // the tallest tile
 
 struct XYArgs {
@@ -98,6 +99,8 @@ struct ZArgs {
   int32_t vec_store;       // 1: the 16-byte store variant (see k_z_pass)
   float wz[kMaxK];
   f2_t wz2[kMaxK];
+  int32_t nsplit;          // > 0: CTA b processes units [split[b], split[b + 1]); 0: an even split
+  int32_t split[kMaxZSplit + 1];
 };
 
 template <int R, typename Tin>
@@ -211,6 +214,10 @@ __global__ void __launch_bounds__(288, CfgXY<R, Tin>::MINB)
 
   // the dependent z pass may be scheduled now; it waits for this grid before reading T
   asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
+  // this grid is a programmatic dependent of the stream's previous kernel (which
+  // may have written the input, or used the memory T now takes): wait for it
+  // to complete before the first global memory access
+  asm volatile("griddepcontrol.wait;\n" ::: "memory");
   const int64_t u_begin = a.units * blockIdx.x / gridDim.x;
   const int64_t u_end = a.units * (blockIdx.x + 1) / gridDim.x;
   const int n = (int)(u_end - u_begin);
@@ -453,10 +460,13 @@ __global__ void __launch_bounds__(256, RZ <= 8 ? 2 : 1) k_z_pass(const __grid_co
   static_assert(C::QPT == 1, "one quad per thread");
   extern __shared__ __align__(16) float4 zring[];  // [S][NT]
   const int tid = threadIdx.x;
-  const int64_t u_begin = a.units * blockIdx.x / gridDim.x;
-  const int64_t u_end = a.units * (blockIdx.x + 1) / gridDim.x;
+  const int64_t u_begin = a.nsplit > 0 ? (int64_t)a.split[blockIdx.x] : a.units * blockIdx.x / gridDim.x;
+  const int64_t u_end = a.nsplit > 0 ? (int64_t)a.split[blockIdx.x + 1] : a.units * (blockIdx.x + 1) / gridDim.x;
   const uint32_t my_slot0 = smem_u32(zring + tid);
   const uint64_t pol_t = policy_evict_first();
+  // the next call's x-y grid may be scheduled now; it waits for this grid
+  // before its first global memory access
+  asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
   // T is written by the x-y grid this launch depends on (programmatic dependent
   // launch): wait for it to complete and its writes to be visible
   asm volatile("griddepcontrol.wait;\n" ::: "memory");
