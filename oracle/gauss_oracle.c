@@ -342,6 +342,92 @@ int orc_gaussian_f32_mt(const float *img, const orc_region *img_reg, const doubl
                            nthreads < 1 ? 1 : nthreads);
 }
 
+/* ---- the convolve_axis family with explicit kernels -------------------- *
+ * MeanFilter and BoxMeanFilterN (mean.rs:59-83, 116-136): one pass per axis
+ * with that axis's box kernel, each weight 1/(2r+1) (mean.rs:15-18), and the
+ * Gaussian's intermediate regions.  BinomialBlurFilter (binomial_blur.rs:
+ * 57-89): `reps` rounds of one pass per axis with [1/4, 1/2, 1/4]; the input is
+ * requested padded by reps per axis, pass (rep, axis) writes requested padded
+ * by reps - rep - 1 on every axis and one more on the axes after `axis`
+ * (clipped to the bounds), and the last pass writes requested.  Written for a
+ * kernel of radius r_d on axis d, the pads are those counts times r_d; with
+ * reps = 1 both schedules are the Gaussian's.  reps = 0 returns the crop of
+ * requested (the reference runs no pass).  kernels[d]: 2 radii[d] + 1 f64
+ * weights of axis d. */
+static int separable_region(const void *img, const orc_region *img_reg, int D, int comps,
+                            const uint64_t *radii, const double *const *kernels, uint64_t reps,
+                            const orc_region *requested, void *out, pix_kind kind, int nthreads) {
+    const orc_region bounds = *img_reg;
+    size_t pb = pix_bytes(kind, comps);
+    for (int d = 0; d < D; d++)
+        if (radii[d] > (1u << 20)) return -1;
+    uint64_t total[ORC_MAXD] = {0, 0, 0};
+    for (int d = 0; d < D; d++) total[d] = reps * radii[d];
+    orc_region in_reg = orc_clipped_to(orc_padded_per_axis(*requested, total, D), bounds, D);
+    if (reps == 0) {
+        crop(img, *img_reg, *requested, D, pb, out);
+        return 0;
+    }
+    void *cur = malloc((size_t)(region_len(&in_reg, D) * pb + 1));
+    if (!cur) return -1;
+    crop(img, *img_reg, in_reg, D, pb, cur);
+    orc_region cur_reg = in_reg;
+    for (uint64_t rep = 0; rep < reps; rep++) {
+        const uint64_t remaining = reps - rep - 1;
+        for (int axis = 0; axis < D; axis++) {
+            const int last = rep + 1 == reps && axis + 1 == D;
+            orc_region out_reg;
+            if (last) {
+                out_reg = *requested;
+            } else {
+                uint64_t pad[ORC_MAXD] = {0, 0, 0};
+                for (int d = 0; d < D; d++) pad[d] = (d > axis ? remaining + 1 : remaining) * radii[d];
+                out_reg = orc_clipped_to(orc_padded_per_axis(*requested, pad, D), bounds, D);
+            }
+            void *nxt = last ? out : malloc((size_t)(region_len(&out_reg, D) * pb + 1));
+            if (!nxt) { free(cur); return -1; }
+            convolve_axis(cur, cur_reg, D, comps, axis, kernels[axis], 2 * radii[axis] + 1, out_reg, nxt,
+                          kind, nthreads);
+            free(cur);
+            cur = last ? NULL : nxt;
+            cur_reg = out_reg;
+        }
+    }
+    return 0;
+}
+
+int orc_separable_f32(const float *img, const orc_region *img_reg, int D, int comps,
+                      const uint64_t *radii, const double *const *kernels, uint64_t reps,
+                      const orc_region *requested, float *out) {
+    return separable_region(img, img_reg, D, comps, radii, kernels, reps, requested, out, PIX_F32, 1);
+}
+
+int orc_separable_u8(const uint8_t *img, const orc_region *img_reg, int D, int comps,
+                     const uint64_t *radii, const double *const *kernels, uint64_t reps,
+                     const orc_region *requested, uint8_t *out) {
+    return separable_region(img, img_reg, D, comps, radii, kernels, reps, requested, out, PIX_U8, 1);
+}
+
+int orc_separable_f64(const double *img, const orc_region *img_reg, int D, int comps,
+                      const uint64_t *radii, const double *const *kernels, uint64_t reps,
+                      const orc_region *requested, double *out) {
+    return separable_region(img, img_reg, D, comps, radii, kernels, reps, requested, out, PIX_F64, 1);
+}
+
+/* Timing port for the family (f32, `nthreads` workers per pass). */
+int orc_separable_f32_mt(const float *img, const orc_region *img_reg, int D, int comps,
+                         const uint64_t *radii, const double *const *kernels, uint64_t reps,
+                         const orc_region *requested, float *out, int nthreads) {
+    return separable_region(img, img_reg, D, comps, radii, kernels, reps, requested, out, PIX_F32,
+                            nthreads < 1 ? 1 : nthreads);
+}
+
+/* box_kernel (mean.rs:15-18) */
+void orc_box_kernel(uint64_t radius, double *out) {
+    const uint64_t len = 2 * radius + 1;
+    for (uint64_t k = 0; k < len; k++) out[k] = 1.0 / (double)len;
+}
+
 /* ---- split_region (region_splitter.rs:17-48) ----------------------------- *
  * Writes up to num_pieces regions into `pieces`; returns the count. */
 int64_t orc_split_region(const orc_region *region, int D, uint64_t num_pieces,

@@ -62,6 +62,15 @@ def lib():
         L.orc_convolve_axis.restype = ctypes.c_int
         L.orc_convolve_axis.argtypes = [P, R, ctypes.c_int, ctypes.c_int, ctypes.c_int, P,
                                         ctypes.c_uint64, R, P, ctypes.c_int]
+        for name in ("orc_separable_f32", "orc_separable_u8", "orc_separable_f64"):
+            f = getattr(L, name)
+            f.restype = ctypes.c_int
+            f.argtypes = [P, R, ctypes.c_int, ctypes.c_int, P, P, ctypes.c_uint64, R, P]
+        L.orc_separable_f32_mt.restype = ctypes.c_int
+        L.orc_separable_f32_mt.argtypes = [P, R, ctypes.c_int, ctypes.c_int, P, P, ctypes.c_uint64,
+                                           R, P, ctypes.c_int]
+        L.orc_box_kernel.restype = None
+        L.orc_box_kernel.argtypes = [ctypes.c_uint64, P]
         L.orc_cast_f32_to_u8.restype = None
         L.orc_cast_f32_to_u8.argtypes = [P, P, ctypes.c_int64]
         _lib = L
@@ -163,6 +172,81 @@ def stream_full_f32(img, sigma, num_pieces, spacing=None, index=None, comps=1):
     if rc != 0:
         raise RuntimeError("oracle: stream_full failed")
     return out
+
+
+BINOMIAL_KERNEL = np.array([0.25, 0.5, 0.25])  # binomial_blur.rs:35
+
+
+def box_kernel(radius: int) -> np.ndarray:
+    """box_kernel (mean.rs:15-18): 2r + 1 weights of 1 / (2r + 1)."""
+    out = np.empty(2 * int(radius) + 1, dtype=np.float64)
+    lib().orc_box_kernel(int(radius), _ptr(out))
+    return out
+
+
+def _run_separable(fn, img, dtype, kernels, reps, index, requested, comps, extra=()):
+    img = np.ascontiguousarray(img, dtype=dtype)
+    D, sizes = _dims(img, comps)
+    index = tuple(index) if index is not None else (0,) * D
+    ks = [np.ascontiguousarray(k, dtype=np.float64) for k in kernels]
+    if len(ks) != D or any(len(k) % 2 != 1 for k in ks):
+        raise ValueError("one odd-length kernel per axis")
+    radii = (ctypes.c_uint64 * 3)(*([(len(k) - 1) // 2 for k in ks] + [0] * (3 - D)))
+    kp = (ctypes.c_void_p * 3)(*([k.ctypes.data for k in ks] + [None] * (3 - D)))
+    img_reg = make_region(index, sizes)
+    req = make_region(index, sizes) if requested is None else make_region(*requested)
+    out_shape = tuple(reversed([req.size[d] for d in range(D)]))
+    if comps > 1:
+        out_shape = out_shape + (comps,)
+    out = np.empty(out_shape, dtype=dtype)
+    rc = fn(_ptr(img), ctypes.byref(img_reg), D, comps, radii, kp, int(reps), ctypes.byref(req),
+            _ptr(out), *extra)
+    if rc != 0:
+        raise RuntimeError("oracle: separable generate_region failed (allocation or radius)")
+    return out
+
+
+def separable_f32(img, kernels, reps=1, index=None, requested=None, comps=1):
+    """The convolve_axis family (mean.rs, binomial_blur.rs) with one f64 kernel per axis
+    and `reps` interleaved rounds, exact reference f32."""
+    return _run_separable(lib().orc_separable_f32, img, np.float32, kernels, reps, index,
+                          requested, comps)
+
+
+def separable_u8(img, kernels, reps=1, index=None, requested=None, comps=1):
+    """The family over Image<u8>: per-tap f64 round+clamp, wrapping u8 adds."""
+    return _run_separable(lib().orc_separable_u8, img, np.uint8, kernels, reps, index,
+                          requested, comps)
+
+
+def separable_f64(img, kernels, reps=1, index=None, requested=None, comps=1):
+    """FP64 oracle of the family: same schedule and clamp boundary, f64 arithmetic."""
+    return _run_separable(lib().orc_separable_f64, img, np.float64, kernels, reps, index,
+                          requested, comps)
+
+
+def separable_f32_mt(img, kernels, reps=1, index=None, requested=None, comps=1, nthreads=None):
+    """Timing port of the family (same arithmetic as separable_f32)."""
+    n = nthreads or os.cpu_count() or 1
+    return _run_separable(lib().orc_separable_f32_mt, img, np.float32, kernels, reps, index,
+                          requested, comps, (n,))
+
+
+def mean_f32(img, radius, **kw):
+    """MeanFilter (mean.rs:27-84): the box kernel of `radius` on every axis."""
+    D = _dims(np.asarray(img), kw.get("comps", 1))[0]
+    return separable_f32(img, [box_kernel(radius)] * D, 1, **kw)
+
+
+def box_mean_f32(img, radii, **kw):
+    """BoxMeanFilterN (mean.rs:103-137): one box radius per axis (reference axis order)."""
+    return separable_f32(img, [box_kernel(r) for r in radii], 1, **kw)
+
+
+def binomial_f32(img, repetitions, **kw):
+    """BinomialBlurFilter (binomial_blur.rs:17-89)."""
+    D = _dims(np.asarray(img), kw.get("comps", 1))[0]
+    return separable_f32(img, [BINOMIAL_KERNEL] * D, repetitions, **kw)
 
 
 def split_region(index, size, num_pieces):

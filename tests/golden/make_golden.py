@@ -145,6 +145,39 @@ def generate_region(img, spacing, sigma, req_index, req_size, kind="f32"):
     return cur
 
 
+def box_kernel(radius):
+    """mean.rs:15-18"""
+    n = 2 * radius + 1
+    return [1.0 / n] * n
+
+
+BINOMIAL = [0.25, 0.5, 0.25]  # binomial_blur.rs:35
+
+
+def separable_region(img, kernels, reps, req_index, req_size, kind="f32"):
+    """MeanFilter / BoxMeanFilterN::generate_region (mean.rs:59-83, 116-136) when reps = 1,
+    BinomialBlurFilter::generate_region (binomial_blur.rs:57-89) with kernels = [BINOMIAL] * D."""
+    b_index, b_size, data = img
+    D = len(b_size)
+    radii = [len(k) // 2 for k in kernels]
+    total = [reps * r for r in radii]
+    in_i, in_s = clipped_to(*padded_per_axis(req_index, req_size, total), b_index, b_size)
+    cur = (in_i, in_s, [data[flat_index(b_index, b_size, p)] for p in iter_region(in_i, in_s)])
+    if reps == 0:
+        return (list(req_index), list(req_size),
+                [cur[2][flat_index(in_i, in_s, p)] for p in iter_region(req_index, req_size)])
+    for rep in range(reps):
+        remaining = reps - rep - 1
+        for axis in range(D):
+            if rep + 1 == reps and axis + 1 == D:
+                oi, os_ = list(req_index), list(req_size)
+            else:
+                pad = [(remaining + 1 if d > axis else remaining) * radii[d] for d in range(D)]
+                oi, os_ = clipped_to(*padded_per_axis(req_index, req_size, pad), b_index, b_size)
+            cur = convolve_axis(cur, axis, kernels[axis], oi, os_, kind)
+    return cur
+
+
 def split_region(index, size, n):
     n = max(n, 1)
     D = len(size)
@@ -234,6 +267,50 @@ def main():
         part = from_ref(generate_region(img, [1.0, 1.0], 1.5, pi, ps), 1, np.float32)
         full[pi[1]:pi[1] + ps[1], pi[0]:pi[0] + ps[0]] = part
     cases["stream4_impulse2d__out"] = full
+    # the convolve_axis family: mean, per-axis box mean, binomial blur
+    srng = np.random.default_rng(20261204)
+
+    def sep_case(name, arr, family, param, requested=None, comps=1, kind="f32"):
+        D = len(arr.shape) - (1 if comps > 1 else 0)
+        if family == "mean":
+            kernels, reps, radii = [box_kernel(param)] * D, 1, [param] * D
+        elif family == "boxmean":
+            kernels, reps, radii = [box_kernel(r) for r in param], 1, list(param)
+        else:
+            kernels, reps, radii = [BINOMIAL] * D, param, [1] * D
+        img = to_ref(arr, comps)
+        ri, rs = requested if requested else (img[0], img[1])
+        res = separable_region(img, kernels, reps, list(ri), list(rs), kind)
+        out = from_ref(res, comps, np.float32 if kind == "f32" else np.uint8)
+        fam = {"mean": 0, "boxmean": 1, "binomial": 2}[family]
+        rad3 = radii + [0] * (3 - D)
+        return {f"sep_{name}__in": arr, f"sep_{name}__out": out,
+                f"sep_{name}__meta": np.array([fam, reps, comps] + rad3 + list(ri) + list(rs),
+                                              dtype=np.int64)}
+
+    cases.update(sep_case("mean1d_const_r2", np.full((10,), 5.0, np.float32), "mean", 2))
+    cases.update(sep_case("mean1d_ramp_r2", np.arange(20, dtype=np.float32), "mean", 2))
+    cases.update(sep_case("boxmean2d_const", np.full((8, 8), 3.0, np.float32), "boxmean", (1, 2)))
+    m2 = srng.random((13, 17), dtype=np.float32)
+    cases.update(sep_case("mean2d_r3", m2, "mean", 3))
+    cases.update(sep_case("mean2d_sub_r2", m2, "mean", 2, requested=([3, 2], [9, 8])))
+    m3 = (srng.standard_normal((7, 9, 11)) * 2).astype(np.float32)
+    cases.update(sep_case("mean3d_r2", m3, "mean", 2))
+    cases.update(sep_case("boxmean3d_aniso", m3, "boxmean", (1, 3, 2)))
+    cases.update(sep_case("mean2d_r6_tiny", srng.random((4, 5), dtype=np.float32), "mean", 6))
+    cases.update(sep_case("mean_vec2d_r1", srng.random((6, 7, 3), dtype=np.float32), "mean", 1, comps=3))
+    cases.update(sep_case("mean_u8_2d_r2", srng.integers(0, 256, (9, 10), dtype=np.uint8), "mean", 2,
+                          kind="u8"))
+    cases.update(sep_case("binomial1d_const_r4", np.full((20,), 3.0, np.float32), "binomial", 4))
+    bimp = np.zeros((21,), np.float32)
+    bimp[10] = 1.0
+    cases.update(sep_case("binomial1d_impulse_r4", bimp, "binomial", 4))
+    cases.update(sep_case("binomial2d_r3", m2, "binomial", 3))
+    cases.update(sep_case("binomial2d_sub_r2", m2, "binomial", 2, requested=([2, 4], [11, 6])))
+    cases.update(sep_case("binomial3d_r2", m3, "binomial", 2))
+    cases.update(sep_case("binomial3d_r0", m3, "binomial", 0))
+    cases.update(sep_case("binomial_u8_2d_r2", srng.integers(0, 256, (8, 9), dtype=np.uint8),
+                          "binomial", 2, kind="u8"))
     # kernels
     for s, sp in [(1.5, 1.0), (2.0, 1.0), (1.5, 0.7), (1.5, 2.5), (0.5, 1.0), (8.0, 1.0)]:
         cases[f"kernel_{s}_{sp}"] = np.array(build_kernel(s / sp, kernel_radius(s, sp)),
