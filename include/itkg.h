@@ -212,6 +212,52 @@ itkg_status itkg_gaussian_generate_region(const itkg_image *input, const itkg_re
                                           const itkg_gaussian_params *params,
                                           itkg_image *output, void *stream);
 
+/* ---- the convolve_axis family ---------------------------------------------
+ * The filters that run convolve_axis (conv.rs:11-41) with their own kernels:
+ *   MeanFilter { source, radius }        mean.rs:27-84    box kernel of `radius` on every axis
+ *   BoxMeanFilterN { source, radii }     mean.rs:103-137  box kernel of radii[d] on axis d
+ *   BinomialBlurFilter { source, reps }  binomial_blur.rs:17-89  [1/4, 1/2, 1/4], `reps` rounds
+ *   the Gaussian stages of UnsharpMaskFilter (edges.rs:406-430) and
+ *   CannyEdgeDetectionFilter (edges.rs:562-577), which build their own kernels.
+ * weights[d]: 2 radius[d] + 1 f64 weights of axis d (axes >= dim ignored),
+ * each applied as x * (float)w in ascending order like the Gaussian's.
+ * repetitions: rounds of one pass per axis (1 for all but the binomial blur;
+ * 0 copies `requested`).  Pass (rep, axis) writes `requested` padded by
+ * (repetitions - rep - 1) radii on every axis and one more on the axes after
+ * `axis` (binomial_blur.rs:63-87); every pass clamps to `largest`.
+ * arithmetic, rounding, algorithm: as for the Gaussian.  The single-launch
+ * kernels (ITKG_ALGO_TWO_PASS, _FUSED) take one round of kernels that read the
+ * same backwards; other calls run per axis (AUTO) or return
+ * ITKG_ERROR_UNSUPPORTED (explicit TWO_PASS / FUSED). */
+typedef struct itkg_separable_params {
+    uint64_t radius[3];
+    const double *weights[3];
+    uint64_t repetitions;
+    int32_t arithmetic;
+    int32_t rounding;
+    int32_t algorithm;
+    int32_t reserved; /* 0 */
+} itkg_separable_params;
+
+/* box_kernel (mean.rs:15-18): 2*radius+1 weights of 1 / (2*radius+1). */
+itkg_status itkg_box_kernel(uint64_t radius, double *weights_out);
+
+/* input_region_for_output of the family: `output_region` padded by
+ * radius[d] * repetitions on axis d, clipped to `largest` (mean.rs:49-57,
+ * 120-122; binomial_blur.rs:44-53). */
+itkg_status itkg_separable_input_region_for_output(const itkg_region *output_region,
+                                                   const itkg_region *largest, int32_t dim,
+                                                   const uint64_t *radius, uint64_t repetitions,
+                                                   itkg_region *input_region);
+
+/* generate_region of the family (same buffer rules as
+ * itkg_gaussian_generate_region; the input buffer must contain
+ * itkg_separable_input_region_for_output(requested)). */
+itkg_status itkg_separable_generate_region(const itkg_image *input, const itkg_region *largest,
+                                           const itkg_region *requested,
+                                           const itkg_separable_params *params,
+                                           itkg_image *output, void *stream);
+
 /* ---- derivatives (not in the reference: it has no VJP) ---------------------
  * Vector-Jacobian product of GaussianFilter over a whole image: x is the
  * filter input (requested region = largest region = x->region), ybar = dL/dy

@@ -136,59 +136,94 @@ static itkg_status copy_region(const itkg_image& dst, const itkg_image& src, con
   return ITKG_SUCCESS;
 }
 
+// What a call convolves with: the Gaussian of sigma (radius and kernel per axis
+// from the spacing, gaussian.rs:24-40), or explicit f64 kernels per axis applied
+// in `reps` rounds of one pass per axis (the convolve_axis family: mean.rs,
+// binomial_blur.rs).
+struct KernelSpec {
+  bool gaussian = true;
+  double sigma = 0.0;
+  uint64_t radius[kMaxDim] = {0, 0, 0};
+  const double* w[kMaxDim] = {nullptr, nullptr, nullptr};
+  uint64_t reps = 1;
+};
+
 struct Plan {
   int D = 0;
   uint64_t radii[kMaxDim] = {0, 0, 0};
   std::vector<double> w64[kMaxDim];
   std::vector<float> w32[kMaxDim];
+  uint64_t reps = 1;       // rounds of one pass per axis
+  bool symmetric = true;   // every f32 kernel reads the same backwards
   itkg_region in_reg;
 };
 
 static itkg_status make_plan(const itkg_image& in, const itkg_region& requested, const itkg_region& largest,
-                             double sigma, Plan* p) {
+                             const KernelSpec& ks, Plan* p) {
   const int D = in.dim;
   p->D = D;
+  p->reps = ks.gaussian ? 1 : ks.reps;
+  uint64_t pad[kMaxDim] = {0, 0, 0};
   for (int d = 0; d < D; ++d) {
-    const uint64_t r = kernel_radius(sigma, in.spacing[d]);
+    const uint64_t r = ks.gaussian ? kernel_radius(ks.sigma, in.spacing[d]) : ks.radius[d];
     if (r > (1u << 20))
-      return set_error(ITKG_ERROR_INVALID_ARGUMENT,
-                       "kernel radius %llu on axis %d (sigma=%g, spacing=%g) is not allocatable",
-                       (unsigned long long)r, d, sigma, in.spacing[d]);
+      return ks.gaussian ? set_error(ITKG_ERROR_INVALID_ARGUMENT,
+                                     "kernel radius %llu on axis %d (sigma=%g, spacing=%g) is not allocatable",
+                                     (unsigned long long)r, d, ks.sigma, in.spacing[d])
+                         : set_error(ITKG_ERROR_INVALID_ARGUMENT, "kernel radius %llu on axis %d is not allocatable",
+                                     (unsigned long long)r, d);
     p->radii[d] = r;
     p->w64[d].resize(2 * r + 1);
-    build_kernel(sigma / in.spacing[d], r, p->w64[d].data());
+    if (ks.gaussian) build_kernel(ks.sigma / in.spacing[d], r, p->w64[d].data());
+    else std::copy(ks.w[d], ks.w[d] + 2 * r + 1, p->w64[d].begin());
     p->w32[d].resize(2 * r + 1);
     for (size_t k = 0; k < p->w64[d].size(); ++k) p->w32[d][k] = (float)p->w64[d][k];
+    for (size_t k = 0; k < p->w32[d].size(); ++k)
+      if (std::memcmp(&p->w32[d][k], &p->w32[d][2 * r - k], sizeof(float)) != 0) p->symmetric = false;
+    pad[d] = r * p->reps;
   }
-  p->in_reg = clipped(padded(requested, D, p->radii), D, largest);
+  p->in_reg = clipped(padded(requested, D, pad), D, largest);
   return ITKG_SUCCESS;
 }
 
-// ---- per-axis execution (D passes through scratch) --------------------------
+// ---- per-axis execution (one pass per axis and round, through scratch) -------
+// Pass (rep, axis) writes `requested` padded by (reps - rep - 1) kernel radii on
+// every axis and one more on the axes after `axis`, clipped to the bounds; the
+// last pass writes `requested` (binomial_blur.rs:63-87; with one round these
+// are the Gaussian's intermediate regions, gaussian.rs:79-85).  Zero rounds
+// copy `requested` (through one pass of the 1-tap kernel [1] when the output
+// type differs from the input's).
 static itkg_status run_per_axis(const itkg_image& in, const itkg_region& largest,
                                 const itkg_region& requested, const itkg_gaussian_params& prm,
                                 const Plan& plan, const itkg_image& out, cudaStream_t s) {
   const int D = in.dim;
   const bool u8pix = prm.arithmetic == ITKG_ARITH_PIXEL_U8;
   const int scratch_dtype = u8pix ? ITKG_U8 : ITKG_F32;
-  // intermediate regions (gaussian.rs:79-85)
-  itkg_region regs[kMaxDim];
-  size_t max_bytes = 0;
-  for (int a = 0; a < D; ++a) {
-    if (a + 1 < D) {
-      uint64_t rem[kMaxDim] = {0, 0, 0};
-      for (int d = a + 1; d < D; ++d) rem[d] = plan.radii[d];
-      regs[a] = clipped(padded(requested, D, rem), D, largest);
-      const size_t bytes = region_len(regs[a], D) * (size_t)in.components * dtype_size(scratch_dtype);
-      max_bytes = std::max(max_bytes, bytes);
-    } else {
-      regs[a] = requested;
-    }
+  static const double kOne64 = 1.0;
+  static const float kOne32 = 1.0f;
+  const uint64_t reps = plan.reps;
+  if (reps == 0 && in.dtype == out.dtype) {  // the reference returns the crop itself
+    ITKG_TRY(copy_region(out, in, requested, s));
+    set_last_kernel("copy");
+    return ITKG_SUCCESS;
   }
+  const int npass = reps == 0 ? 1 : (int)std::min<uint64_t>(reps * (uint64_t)D, (uint64_t)INT32_MAX);
+  auto region_of = [&](int p) {
+    if (p + 1 == npass) return requested;
+    const uint64_t rep = (uint64_t)(p / D), remaining = reps - rep - 1;
+    const int axis = p % D;
+    uint64_t pad[kMaxDim] = {0, 0, 0};
+    for (int d = 0; d < D; ++d) pad[d] = (d > axis ? remaining + 1 : remaining) * plan.radii[d];
+    return clipped(padded(requested, D, pad), D, largest);
+  };
+  size_t max_bytes = 0;
+  for (int p = 0; p + 1 < npass; ++p)
+    max_bytes = std::max(max_bytes, (size_t)region_len(region_of(p), D) * (size_t)in.components *
+                                        dtype_size(scratch_dtype));
   void* bufs[2] = {nullptr, nullptr};
-  if (D > 1) {
+  if (npass > 1) {
     ITKG_TRY(scratch_alloc(&bufs[0], max_bytes, s));
-    if (D > 2) {
+    if (npass > 2) {
       itkg_status st = scratch_alloc(&bufs[1], max_bytes, s);
       if (st != ITKG_SUCCESS) {
         scratch_free(bufs[0], s);
@@ -198,16 +233,18 @@ static itkg_status run_per_axis(const itkg_image& in, const itkg_region& largest
   }
   itkg_image cur = in;
   itkg_status st = ITKG_SUCCESS;
-  for (int a = 0; a < D && st == ITKG_SUCCESS; ++a) {
+  for (int p = 0; p < npass && st == ITKG_SUCCESS; ++p) {
+    const int a = reps == 0 ? 0 : p % D;
+    const itkg_region reg = region_of(p);
     itkg_image nxt;
-    if (a + 1 < D) {
+    if (p + 1 < npass) {
       std::memset(&nxt, 0, sizeof nxt);
       nxt.dim = D;
       nxt.dtype = scratch_dtype;
       nxt.components = in.components;
-      nxt.region = regs[a];
+      nxt.region = reg;
       dense_layout(&nxt, 1);
-      nxt.data = bufs[a & 1];
+      nxt.data = bufs[p & 1];
     } else {
       nxt = out;
     }
@@ -217,7 +254,7 @@ static itkg_status run_per_axis(const itkg_image& in, const itkg_region& largest
     args.dst = nxt.data;
     origin_pitch(cur, args.src_origin, args.src_pitch);
     origin_pitch(nxt, args.dst_origin, args.dst_pitch);
-    const itkg_region o3 = full3(regs[a], D);
+    const itkg_region o3 = full3(reg, D);
     for (int d = 0; d < kMaxDim; ++d) {
       args.out_index[d] = o3.index[d];
       args.out_size[d] = (int64_t)o3.size[d];
@@ -225,14 +262,14 @@ static itkg_status run_per_axis(const itkg_image& in, const itkg_region& largest
     args.lo = largest.index[a];
     args.hi = largest.index[a] + (int64_t)largest.size[a] - 1;
     args.axis = a;
-    args.radius = (int32_t)plan.radii[a];
+    args.radius = reps == 0 ? 0 : (int32_t)plan.radii[a];
     args.comps = in.components;
     if (u8pix) {
-      st = launch_conv_axis_u8(args, plan.w64[a].data(), s);
+      st = launch_conv_axis_u8(args, reps == 0 ? &kOne64 : plan.w64[a].data(), s);
     } else {
-      const int in_dt = a == 0 ? in.dtype : ITKG_F32;
-      const int out_dt = a + 1 < D ? ITKG_F32 : out.dtype;
-      st = launch_conv_axis_f32(args, plan.w32[a].data(), in_dt, out_dt, prm.rounding, s);
+      const int in_dt = p == 0 ? in.dtype : ITKG_F32;
+      const int out_dt = p + 1 < npass ? ITKG_F32 : out.dtype;
+      st = launch_conv_axis_f32(args, reps == 0 ? &kOne32 : plan.w32[a].data(), in_dt, out_dt, prm.rounding, s);
     }
     cur = nxt;
   }
@@ -289,6 +326,14 @@ static itkg_status generate_device(const itkg_image& in, const itkg_region& larg
                                    const itkg_region& requested, const itkg_gaussian_params& prm,
                                    const Plan& plan, const itkg_image& out, cudaStream_t s) {
   const int D = in.dim;
+  // The single-launch kernels run one round of a kernel that reads the same
+  // backwards (their y and z passes index the weights by distance from the centre).
+  if (plan.reps != 1 || !plan.symmetric) {
+    if (prm.algorithm == ITKG_ALGO_FUSED || prm.algorithm == ITKG_ALGO_TWO_PASS)
+      return set_error(ITKG_ERROR_UNSUPPORTED,
+                       "repeated rounds and asymmetric kernels run per axis only (ITKG_ALGO_PER_AXIS or AUTO)");
+    return run_per_axis(in, largest, requested, prm, plan, out, s);
+  }
   if (prm.arithmetic != ITKG_ARITH_PIXEL_U8 && prm.algorithm != ITKG_ALGO_PER_AXIS) {
     FusedGeom g;
     make_fused_geom(in, largest, requested, prm, plan, out, &g);
@@ -319,7 +364,9 @@ itkg_status fused_geom_for(const itkg_image& in, const itkg_region& largest,
       !region_contains(largest, requested, D) || !region_contains(out.region, requested, D))
     return ITKG_ERROR_UNSUPPORTED;
   Plan plan;
-  if (make_plan(in, requested, largest, prm.sigma, &plan) != ITKG_SUCCESS) return ITKG_ERROR_UNSUPPORTED;
+  KernelSpec ks;
+  ks.sigma = prm.sigma;
+  if (make_plan(in, requested, largest, ks, &plan) != ITKG_SUCCESS) return ITKG_ERROR_UNSUPPORTED;
   if (!region_contains(in.region, plan.in_reg, D)) return ITKG_ERROR_UNSUPPORTED;
   make_fused_geom(in, largest, requested, prm, plan, out, g);
   const float* w[kMaxDim] = {nullptr, nullptr, nullptr};
@@ -404,8 +451,9 @@ static int staging_pieces(const itkg_image& out, const itkg_region& requested, i
 // and device-to-host copies of different slabs overlap.  The result is the
 // whole-request result (every slab clamps to the largest region).
 static itkg_status generate_staged(const itkg_image* input, const itkg_region* largest,
-                                   const itkg_region* requested, const itkg_gaussian_params* prm,
-                                   const Plan& plan, const itkg_image* output, int pieces, cudaStream_t s) {
+                                   const itkg_region* requested, const KernelSpec& ks,
+                                   const itkg_gaussian_params* prm, const Plan& plan, const itkg_image* output,
+                                   int pieces, cudaStream_t s) {
   const int D = input->dim, L = D - 1;
   const bool host_in = input->location == ITKG_HOST;
   const bool host_out = output->location == ITKG_HOST;
@@ -445,7 +493,7 @@ static itkg_status generate_staged(const itkg_image* input, const itkg_region* l
     rk.index[L] = requested->index[L] + (int64_t)(n_last * k / pieces);
     rk.size[L] = n_last * (k + 1) / pieces - n_last * k / pieces;
     Plan pk;
-    st = make_plan(din, rk, *largest, prm->sigma, &pk);
+    st = make_plan(din, rk, *largest, ks, &pk);
     if (st != ITKG_SUCCESS) break;
     cudaEvent_t ein = nullptr, eout = nullptr;
     if (host_in) {
@@ -482,12 +530,17 @@ static itkg_status generate_staged(const itkg_image* input, const itkg_region* l
   return check_fault_word(fw);
 }
 
+// ks: the kernels (NULL: the Gaussian of prm->sigma); prm: arithmetic,
+// rounding and algorithm.
 static itkg_status generate_region(const itkg_image* input, const itkg_region* largest,
-                                   const itkg_region* requested, const itkg_gaussian_params* prm,
-                                   const itkg_image* output, cudaStream_t s) {
+                                   const itkg_region* requested, const KernelSpec* ks_in,
+                                   const itkg_gaussian_params* prm, const itkg_image* output, cudaStream_t s) {
   ITKG_TRY(validate_image(input, "input"));
   ITKG_TRY(validate_image(output, "output"));
   ITKG_TRY(check_params(prm));
+  KernelSpec gauss;
+  gauss.sigma = prm->sigma;
+  const KernelSpec& ks = ks_in ? *ks_in : gauss;
   if (!largest || !requested) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "region is NULL");
   const int D = input->dim;
   if (output->dim != D) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "input/output dim differ");
@@ -505,7 +558,7 @@ static itkg_status generate_region(const itkg_image* input, const itkg_region* l
   if (!region_contains(output->region, *requested, D))
     return set_error(ITKG_ERROR_INVALID_ARGUMENT, "output buffer does not contain the requested region");
   Plan plan;
-  ITKG_TRY(make_plan(*input, *requested, *largest, prm->sigma, &plan));
+  ITKG_TRY(make_plan(*input, *requested, *largest, ks, &plan));
   if (!region_contains(input->region, plan.in_reg, D))
     return set_error(ITKG_ERROR_INVALID_ARGUMENT,
                      "input buffer does not cover input_region_for_output(requested)");
@@ -514,7 +567,7 @@ static itkg_status generate_region(const itkg_image* input, const itkg_region* l
   const bool host_out = output->location == ITKG_HOST;
   if (!host_in && !host_out) return generate_device(*input, *largest, *requested, *prm, plan, *output, s);
   const int pieces = staging_pieces(*output, *requested, D);
-  if (pieces > 1) return generate_staged(input, largest, requested, prm, plan, output, pieces, s);
+  if (pieces > 1) return generate_staged(input, largest, requested, ks, prm, plan, output, pieces, s);
 
   // Stage host buffers through stream-ordered scratch.
   itkg_image din = *input, dout = *output;
@@ -742,8 +795,64 @@ itkg_status itkg_gaussian_generate_region(const itkg_image* input, const itkg_re
                                           const itkg_region* requested,
                                           const itkg_gaussian_params* params, itkg_image* output,
                                           void* stream) {
-  return generate_region(input, largest, requested, params, output,
+  return generate_region(input, largest, requested, nullptr, params, output,
                          static_cast<cudaStream_t>(stream));
+}
+
+itkg_status itkg_box_kernel(uint64_t radius, double* weights_out) {
+  if (!weights_out) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "weights_out is NULL");
+  if (radius > (1u << 20)) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "radius too large");
+  const uint64_t len = 2 * radius + 1;  // mean.rs:15-18
+  for (uint64_t k = 0; k < len; ++k) weights_out[k] = 1.0 / (double)len;
+  return ITKG_SUCCESS;
+}
+
+itkg_status itkg_separable_input_region_for_output(const itkg_region* output_region,
+                                                   const itkg_region* largest, int32_t dim,
+                                                   const uint64_t* radius, uint64_t repetitions,
+                                                   itkg_region* input_region) {
+  if (!output_region || !largest || !radius || !input_region || dim < 1 || dim > kMaxDim)
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "bad argument");
+  uint64_t pad[kMaxDim] = {0, 0, 0};
+  for (int d = 0; d < dim; ++d) {
+    if (radius[d] > (1u << 20) || repetitions > (1u << 20))
+      return set_error(ITKG_ERROR_INVALID_ARGUMENT, "radius or repetitions too large");
+    pad[d] = radius[d] * repetitions;
+  }
+  *input_region = clipped(padded(*output_region, dim, pad), dim, *largest);
+  return ITKG_SUCCESS;
+}
+
+itkg_status itkg_separable_generate_region(const itkg_image* input, const itkg_region* largest,
+                                           const itkg_region* requested,
+                                           const itkg_separable_params* params, itkg_image* output,
+                                           void* stream) {
+  if (!params) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "params is NULL");
+  if (!input) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "input is NULL");
+  KernelSpec ks;
+  ks.gaussian = false;
+  ks.reps = params->repetitions;
+  if (params->repetitions > (1u << 20))
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "repetitions %llu is too large",
+                     (unsigned long long)params->repetitions);
+  for (int d = 0; d < kMaxDim; ++d) {
+    if (d >= input->dim) continue;
+    if (params->radius[d] > (1u << 20))
+      return set_error(ITKG_ERROR_INVALID_ARGUMENT, "radius %llu on axis %d is too large",
+                       (unsigned long long)params->radius[d], d);
+    if (!params->weights[d]) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "weights[%d] is NULL", d);
+    if (params->radius[d] * params->repetitions > (1u << 20))
+      return set_error(ITKG_ERROR_INVALID_ARGUMENT, "radius x repetitions on axis %d is too large", d);
+    ks.radius[d] = params->radius[d];
+    ks.w[d] = params->weights[d];
+  }
+  itkg_gaussian_params opts;
+  std::memset(&opts, 0, sizeof opts);
+  opts.arithmetic = params->arithmetic;
+  opts.rounding = params->rounding;
+  opts.algorithm = params->algorithm;
+  opts.reserved = params->reserved;
+  return generate_region(input, largest, requested, &ks, &opts, output, static_cast<cudaStream_t>(stream));
 }
 
 itkg_status itkg_stream_full(const itkg_image* input, const itkg_region* largest,
@@ -760,7 +869,7 @@ itkg_status itkg_stream_full(const itkg_image* input, const itkg_region* largest
   std::vector<itkg_region> pieces(count);
   ITKG_TRY(itkg_split_region(largest, D, num_pieces, pieces.data(), count, &count));
   for (const itkg_region& p : pieces)
-    ITKG_TRY(generate_region(input, largest, &p, params, output, static_cast<cudaStream_t>(stream)));
+    ITKG_TRY(generate_region(input, largest, &p, nullptr, params, output, static_cast<cudaStream_t>(stream)));
   return ITKG_SUCCESS;
 }
 

@@ -410,6 +410,122 @@ GaussianFilter<S> make_gaussian(S s, double sigma) {
 template <typename S>
 auto spacing_of(const GaussianFilter<S>& g) { return g.spacing(); }
 
+// The convolve_axis family with explicit kernels (one f64 kernel per axis,
+// `repetitions` rounds of one pass per axis): the engine of MeanFilter
+// (mean.rs:27-84), BoxMeanFilterN (mean.rs:103-137) and BinomialBlurFilter
+// (binomial_blur.rs:17-89); make_mean / make_box_mean / make_binomial build it.
+template <typename S>
+struct SeparableFilter {
+  S source;
+  std::vector<std::vector<double>> kernels;  // per axis, odd lengths
+  uint64_t repetitions = 1;
+  int rounding = ITKG_ROUND_REFERENCE;
+  int algorithm = ITKG_ALGO_AUTO;
+
+  static constexpr int Dim = std::decay_t<S>::Dim;
+  using Pixel = typename std::decay_t<S>::Pixel;
+
+  SeparableFilter(S s, std::vector<std::vector<double>> k, uint64_t reps)
+      : source(std::forward<S>(s)), kernels(std::move(k)), repetitions(reps) {
+    if ((int)kernels.size() != Dim) throw std::runtime_error("one kernel per axis");
+    for (const auto& w : kernels)
+      if (w.size() % 2 != 1) throw std::runtime_error("kernels have odd length");
+  }
+
+  Region<Dim> largest_region() const { return source.largest_region(); }
+  std::array<double, Dim> spacing() const { return spacing_of(source); }
+
+  Region<Dim> input_region_for_output(const Region<Dim>& out) const {
+    itkg_region o = out.to_c(), l = largest_region().to_c(), in;
+    uint64_t r[3] = {0, 0, 0};
+    for (int d = 0; d < Dim; ++d) r[d] = (kernels[d].size() - 1) / 2;
+    check(itkg_separable_input_region_for_output(&o, &l, Dim, r, repetitions, &in));
+    return Region<Dim>::from_c(in);
+  }
+
+  itkg_separable_params params(int arith) const {
+    itkg_separable_params p;
+    std::memset(&p, 0, sizeof p);
+    for (int d = 0; d < Dim; ++d) {
+      p.radius[d] = (kernels[d].size() - 1) / 2;
+      p.weights[d] = kernels[d].data();
+    }
+    p.repetitions = repetitions;
+    p.arithmetic = arith;
+    p.rounding = rounding;
+    p.algorithm = algorithm;
+    return p;
+  }
+
+  auto generate_region(const Region<Dim>& requested) const {
+    using S0 = std::decay_t<S>;
+    if constexpr (is_device_image<S0>::value) {
+      DeviceImage<Pixel, Dim> out(requested, source.spacing(), source.origin());
+      run(source.c, source.largest_region(), requested, PixelTraits<Pixel>::arith, out.c);
+      return out;
+    } else if constexpr (is_host_image_t<S0>::value) {
+      auto out = Image<Pixel, Dim>::allocate(requested, source.spacing, source.origin, Pixel{});
+      run(source.desc(), source.largest_region(), requested, PixelTraits<Pixel>::arith, out.desc());
+      return out;
+    } else {
+      auto in = source.generate_region(input_region_for_output(requested));
+      auto out = Image<Pixel, Dim>::allocate(requested, in.spacing, in.origin, Pixel{});
+      run(in.desc(), largest_region(), requested, PixelTraits<Pixel>::arith, out.desc());
+      return out;
+    }
+  }
+
+ private:
+  template <typename T>
+  struct is_device_image : std::false_type {};
+  template <typename P, int D>
+  struct is_device_image<DeviceImage<P, D>> : std::true_type {};
+  template <typename T>
+  struct is_host_image_t : std::false_type {};
+  template <typename P, int D>
+  struct is_host_image_t<Image<P, D>> : std::true_type {};
+
+  void run(itkg_image in, const Region<Dim>& largest, const Region<Dim>& requested, int arith,
+           itkg_image out) const {
+    itkg_region l = largest.to_c(), r = requested.to_c();
+    itkg_separable_params p = params(arith);
+    check(itkg_separable_generate_region(&in, &l, &r, &p, &out, nullptr));
+  }
+};
+
+// box_kernel (mean.rs:15-18)
+inline std::vector<double> box_kernel(uint64_t radius) {
+  std::vector<double> w(2 * radius + 1);
+  check(itkg_box_kernel(radius, w.data()));
+  return w;
+}
+
+// MeanFilter::new(source, radius) (mean.rs:35-39)
+template <typename S>
+SeparableFilter<S> make_mean(S s, uint64_t radius) {
+  constexpr int D = std::decay_t<S>::Dim;
+  return SeparableFilter<S>(std::move(s), std::vector<std::vector<double>>(D, box_kernel(radius)), 1);
+}
+
+// BoxMeanFilterN::new(source, radii) (mean.rs:109-113)
+template <typename S, size_t N>
+SeparableFilter<S> make_box_mean(S s, const std::array<uint64_t, N>& radii) {
+  std::vector<std::vector<double>> k;
+  for (uint64_t r : radii) k.push_back(box_kernel(r));
+  return SeparableFilter<S>(std::move(s), std::move(k), 1);
+}
+
+// BinomialBlurFilter::new(source, repetitions) (binomial_blur.rs:23-26)
+template <typename S>
+SeparableFilter<S> make_binomial(S s, uint64_t repetitions) {
+  constexpr int D = std::decay_t<S>::Dim;
+  return SeparableFilter<S>(std::move(s), std::vector<std::vector<double>>(D, {0.25, 0.5, 0.25}),
+                            repetitions);
+}
+
+template <typename S>
+auto spacing_of(const SeparableFilter<S>& f) { return f.spacing(); }
+
 // stream_full (source.rs:81-98): allocate the full output once, fill it piece
 // by piece along the slowest axis.
 template <typename S>

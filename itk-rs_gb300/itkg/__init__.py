@@ -24,13 +24,14 @@ import numpy as np
 
 from ._abi import (ALGO_AUTO, ALGO_FUSED, ALGO_PER_AXIS, ALGO_TWO_PASS, ARITH_F32, ARITH_PIXEL_U8, BF16,
                    DEVICE, F16, F32, HOST, I16, ROUND_FMA, ROUND_REFERENCE, U8, ItkgError, check,
-                   itkg_gaussian_params, itkg_image, itkg_region, lib)
+                   itkg_gaussian_params, itkg_image, itkg_region, itkg_separable_params, lib)
 
 __all__ = [
     "Region", "Image", "DeviceImage", "GaussianFilter", "CastFilter", "stream_full",
     "split_region", "kernel_radius", "build_kernel", "ItkgError", "F32", "I16", "U8", "BF16",
     "F16", "ROUND_REFERENCE", "ROUND_FMA", "ALGO_AUTO", "ALGO_FUSED", "ALGO_PER_AXIS",
-    "ALGO_TWO_PASS", "ARITH_F32", "ARITH_PIXEL_U8", "gaussian", "Stream",
+    "ALGO_TWO_PASS", "ARITH_F32", "ARITH_PIXEL_U8", "gaussian", "Stream", "SeparableFilter",
+    "MeanFilter", "BoxMeanFilterN", "BinomialBlurFilter", "box_kernel", "BINOMIAL_KERNEL",
 ]
 
 _NP_OF = {F32: np.float32, I16: np.int16, U8: np.uint8, F16: np.float16}
@@ -353,16 +354,97 @@ class GaussianFilter:
             res = Image(host, index=requested.index, spacing=leaf.spacing, origin=leaf.origin,
                         components=leaf.components, bf16=(out_dtype == BF16))
             oc = res.to_c()
-            check(lib().itkg_gaussian_generate_region(ctypes.byref(src), ctypes.byref(largest),
-                                                      ctypes.byref(req), ctypes.byref(prm),
-                                                      ctypes.byref(oc), stream.ptr))
+            self._call(src, largest, req, oc, stream)
             return res
         dev = out if out is not None else DeviceImage(requested, out_dtype, leaf.components,
                                                       leaf.spacing, leaf.origin)
-        check(lib().itkg_gaussian_generate_region(ctypes.byref(src), ctypes.byref(largest),
-                                                  ctypes.byref(req), ctypes.byref(prm),
-                                                  ctypes.byref(dev.c), stream.ptr))
+        self._call(src, largest, req, dev.c, stream)
         return dev
+
+    def _call(self, src, largest, req, out_c, stream):
+        prm = self.params()
+        check(lib().itkg_gaussian_generate_region(ctypes.byref(src), ctypes.byref(largest), ctypes.byref(req),
+                                                  ctypes.byref(prm), ctypes.byref(out_c), stream.ptr))
+
+
+BINOMIAL_KERNEL = np.array([0.25, 0.5, 0.25])  # binomial_blur.rs:35
+
+
+def box_kernel(radius: int) -> np.ndarray:
+    """box_kernel (mean.rs:15-18): 2r + 1 weights of 1 / (2r + 1)."""
+    out = np.empty(2 * int(radius) + 1, dtype=np.float64)
+    check(lib().itkg_box_kernel(int(radius), out.ctypes.data))
+    return out
+
+
+class SeparableFilter(GaussianFilter):
+    """A filter of the convolve_axis family with explicit f64 kernels per axis
+    (reference axis order) and `repetitions` rounds of one pass per axis: the
+    engine of MeanFilter, BoxMeanFilterN and BinomialBlurFilter, and of the
+    Gaussian stages of UnsharpMaskFilter / CannyEdgeDetectionFilter
+    (edges.rs:406-430, 562-577), which build their own kernels."""
+
+    def __init__(self, source, kernels, repetitions: int = 1, rounding: int = ROUND_REFERENCE,
+                 algorithm: int = ALGO_AUTO, arithmetic: int | None = None):
+        super().__init__(source, 0.0, rounding, algorithm, arithmetic)
+        self.kernels = [np.ascontiguousarray(k, dtype=np.float64) for k in kernels]
+        if any(k.ndim != 1 or len(k) % 2 != 1 for k in self.kernels):
+            raise ValueError("each kernel is a 1-D array of odd length")
+        self.repetitions = int(repetitions)
+
+    @property
+    def radii(self):
+        return [(len(k) - 1) // 2 for k in self.kernels]
+
+    def input_region_for_output(self, out: Region) -> Region:
+        return out.padded_per_axis([r * self.repetitions for r in self.radii]).clipped_to(
+            self.largest_region())
+
+    def separable_params(self) -> itkg_separable_params:
+        g = self.params()
+        p = itkg_separable_params()
+        if len(self.kernels) != len(self.largest_region().size):
+            raise ValueError("one kernel per axis")
+        for d, k in enumerate(self.kernels):
+            p.radius[d] = (len(k) - 1) // 2
+            p.weights[d] = k.ctypes.data
+        p.repetitions = self.repetitions
+        p.arithmetic, p.rounding, p.algorithm = g.arithmetic, g.rounding, g.algorithm
+        return p
+
+    def _call(self, src, largest, req, out_c, stream):
+        prm = self.separable_params()
+        check(lib().itkg_separable_generate_region(ctypes.byref(src), ctypes.byref(largest), ctypes.byref(req),
+                                                   ctypes.byref(prm), ctypes.byref(out_c), stream.ptr))
+
+
+class MeanFilter(SeparableFilter):
+    """MeanFilter { source, radius } (mean.rs:27-84)."""
+
+    def __init__(self, source, radius: int, **kw):
+        D = len(source.largest_region().size)
+        super().__init__(source, [box_kernel(radius)] * D, 1, **kw)
+        self.radius = int(radius)
+
+
+class BoxMeanFilterN(SeparableFilter):
+    """BoxMeanFilterN { source, radii } (mean.rs:103-137), radii in reference axis order."""
+
+    def __init__(self, source, radii, **kw):
+        super().__init__(source, [box_kernel(r) for r in radii], 1, **kw)
+
+
+class BinomialBlurFilter(SeparableFilter):
+    """BinomialBlurFilter { source, repetitions } (binomial_blur.rs:17-89)."""
+
+    def __init__(self, source, repetitions: int, **kw):
+        D = len(source.largest_region().size)
+        super().__init__(source, [BINOMIAL_KERNEL] * D, repetitions, **kw)
+
+    @staticmethod
+    def effective_sigma_pixels(repetitions: int) -> float:
+        """binomial_blur.rs:28-30"""
+        return (repetitions / 4.0) ** 0.5
 
 
 def stream_full(source: GaussianFilter, num_pieces: int, stream: Stream = _DEFAULT_STREAM,

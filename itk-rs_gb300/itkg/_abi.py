@@ -59,6 +59,18 @@ class itkg_gaussian_params(ctypes.Structure):
     ]
 
 
+class itkg_separable_params(ctypes.Structure):
+    _fields_ = [
+        ("radius", ctypes.c_uint64 * 3),
+        ("weights", ctypes.c_void_p * 3),
+        ("repetitions", ctypes.c_uint64),
+        ("arithmetic", ctypes.c_int32),
+        ("rounding", ctypes.c_int32),
+        ("algorithm", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+    ]
+
+
 # name -> (restype, argtypes); every symbol include/itkg.h declares.
 P = ctypes.c_void_p
 R = ctypes.POINTER(itkg_region)
@@ -93,6 +105,9 @@ SIGNATURES = {
     "itkg_gaussian_generate_region": (st, [I, R, R, G, I, P]),
     "itkg_stream_full": (st, [I, R, G, ctypes.c_uint64, I, P]),
     "itkg_gaussian_generate_region_noalloc": (st, [I, R, R, G, I, P]),
+    "itkg_box_kernel": (st, [ctypes.c_uint64, P]),
+    "itkg_separable_input_region_for_output": (st, [R, R, ctypes.c_int32, P, ctypes.c_uint64, R]),
+    "itkg_separable_generate_region": (st, [I, R, R, ctypes.POINTER(itkg_separable_params), I, P]),
     "itkg_gaussian_vjp": (st, [I, I, G, I, ctypes.POINTER(ctypes.c_double), ctypes.c_int32, P]),
     "itkg_gaussian_scale_stack_loss_vjp": (st, [I, I, ctypes.POINTER(ctypes.c_double), ctypes.c_int32,
                                                 I, ctypes.POINTER(ctypes.c_double),

@@ -158,6 +158,41 @@ static void test_device_source_matches_host() {
     CHECK(want.data[i] == got.data[i], "device/host mismatch at %zu", i);
 }
 
+// mean.rs:254-292
+static void test_mean_filters() {
+  auto c = solid_image<1>({10}, 5.0f);
+  auto m = make_mean(c, 2);
+  auto out = m.generate_region(m.largest_region());
+  for (float v : out.data) CHECK(std::fabs(v - 5.0f) < 1e-5f, "constant: %g", v);
+  auto ramp = solid_image<1>({20}, 0.0f);
+  for (int64_t i = 0; i < 20; ++i) ramp.set_pixel({{i}}, (float)i);
+  auto mr = make_mean(ramp, 2);
+  auto outr = mr.generate_region(mr.largest_region());
+  for (int64_t i = 2; i < 18; ++i)
+    CHECK(std::fabs(outr.get_pixel({{i}}) - (float)i) < 1e-4f, "ramp at %lld", (long long)i);
+  auto c2 = solid_image<2>({8, 8}, 3.0f);
+  auto bm = make_box_mean(c2, std::array<uint64_t, 2>{1, 2});
+  auto out2 = bm.generate_region(bm.largest_region());
+  for (float v : out2.data) CHECK(std::fabs(v - 3.0f) < 1e-5f, "box mean constant: %g", v);
+}
+
+// binomial_blur.rs:96-121
+static void test_binomial_blur() {
+  auto c = solid_image<1>({20}, 3.0f);
+  auto b = make_binomial(c, 4);
+  auto out = b.generate_region(b.largest_region());
+  for (int64_t i = 4; i < 16; ++i) CHECK(std::fabs(out.get_pixel({{i}}) - 3.0f) < 1e-5f, "constant");
+  auto imp = solid_image<1>({21}, 0.0f);
+  imp.set_pixel({{10}}, 1.0f);
+  auto bi = make_binomial(imp, 4);
+  auto outi = bi.generate_region(bi.largest_region());
+  const float peak = outi.get_pixel({{10}});
+  float sum = 0.0f;
+  for (float v : outi.data) sum += v;
+  CHECK(peak > 0.0f && peak < 1.0f, "peak=%g", peak);
+  CHECK(std::fabs(sum - 1.0f) < 0.05f, "sum=%g", sum);
+}
+
 int main() {
   int ndev = 0;
   itkg_device_count(&ndev);
@@ -174,6 +209,8 @@ int main() {
       {"unary_filter_pipeline", test_unary_filter_pipeline},
       {"blur_u8_roundtrip", test_blur_u8_roundtrip},
       {"device_source_matches_host", test_device_source_matches_host},
+      {"mean_filters", test_mean_filters},
+      {"binomial_blur", test_binomial_blur},
   };
   for (auto& t : tests) {
     const int before = g_fail;
