@@ -10,6 +10,10 @@
 // source extent on `axis`, acc starting at zero.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <cstdint>
+#include <type_traits>
+
 #include "internal.hpp"
 #include "pixel.cuh"
 
@@ -115,6 +119,103 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
+// f32 -> f32 passes with radius <= 12 (every intermediate pass of the per-axis
+// path, and the binomial blur's rounds): the radius is a template parameter
+// (taps unrolled, weights read from the parameter bank) and each thread makes
+// kRun outputs along a marching axis -- y for passes along x and y, z for
+// passes along z.  Along y and z the kRun outputs share one register window of
+// K + kRun - 1 loads; along x each of the kRun rows takes its K taps from the
+// cache lines its warp already loaded.  Same arithmetic as k_conv_axis_f32: ascending taps from
+// zero, clamp to [lo, hi] on `axis`.
+constexpr int kRun = 4;
+constexpr int kMaxSmallR = 12;
+
+template <int R, bool REF>
+__global__ void __launch_bounds__(kThreads, 4)
+    k_conv_axis_small(const AxisArgs a, const AxisWeightsF32 W) {
+  constexpr int K = 2 * R + 1;
+  const int64_t rowlen = a.out_size[0] * a.comps;
+  const int64_t t = (int64_t)blockIdx.x * kThreads + threadIdx.x;
+  if (t >= rowlen) return;
+  const int c = (int)(t % a.comps);
+  const int64_t x = t / a.comps + a.out_index[0];
+  const int axis = a.axis;
+  const int md = axis == 2 ? 2 : 1;  // marching axis
+  const int od = axis == 2 ? 1 : 2;  // the remaining axis
+  const int64_t m0 = a.out_index[md], mn = a.out_size[md];
+  const int64_t o0 = a.out_index[od], on = a.out_size[od];
+  const char* const sx = static_cast<const char*>(a.src) + c * 4 + (x - a.src_origin[0]) * a.src_pitch[0];
+  char* const dx = static_cast<char*>(a.dst) + c * 4 + (x - a.dst_origin[0]) * a.dst_pitch[0];
+  const int64_t spm = a.src_pitch[md], spo = a.src_pitch[od];
+  const int64_t dpm = a.dst_pitch[md], dpo = a.dst_pitch[od];
+  // passes along x: the clamped tap offsets of this column
+  int32_t xo[K];  // (clamped tap - x) * pitch: within +-R pixels
+  if (axis == 0) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      int64_t s = x + k - R;
+      s = s < a.lo ? a.lo : (s > a.hi ? a.hi : s);
+      xo[k] = (int32_t)((s - x) * a.src_pitch[0]);
+    }
+  }
+  for (int64_t o = o0 + blockIdx.z; o < o0 + on; o += gridDim.z) {
+    const char* const so = sx + (o - a.src_origin[od]) * spo;
+    char* const dso = dx + (o - a.dst_origin[od]) * dpo;
+    for (int64_t mb = m0 + (int64_t)blockIdx.y * kRun; mb < m0 + mn; mb += (int64_t)gridDim.y * kRun) {
+      const int nv = (int)(m0 + mn - mb < kRun ? m0 + mn - mb : kRun);  // valid outputs of the run
+      float acc[kRun];
+      if (axis == 0) {
+#pragma unroll
+        for (int r = 0; r < kRun; ++r) {
+          acc[r] = 0.0f;
+          if (r < nv) {
+            const char* const row = so + (mb + r - a.src_origin[md]) * spm;
+#pragma unroll
+            for (int k = 0; k < K; ++k) acc[r] = tap<REF>(acc[r], __ldg(reinterpret_cast<const float*>(row + xo[k])), W.w[k]);
+          }
+        }
+      } else {
+        // window over the marching axis: positions mb - R .. mb + kRun - 1 + R, clamped
+        // to [lo, hi] and, beyond the last valid output's taps, to its last tap
+        const int64_t top = mb + nv - 1 + R < a.hi ? mb + nv - 1 + R : a.hi;
+        float v[K + kRun - 1];
+#pragma unroll
+        for (int j = 0; j < K + kRun - 1; ++j) {
+          int64_t s = mb - R + j;
+          s = s < a.lo ? a.lo : (s > top ? top : s);
+          v[j] = __ldg(reinterpret_cast<const float*>(so + (s - a.src_origin[md]) * spm));
+        }
+#pragma unroll
+        for (int r = 0; r < kRun; ++r) {
+          acc[r] = 0.0f;
+#pragma unroll
+          for (int k = 0; k < K; ++k) acc[r] = tap<REF>(acc[r], v[r + k], W.w[k]);
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < kRun; ++r)
+        if (r < nv) *reinterpret_cast<float*>(dso + (mb + r - a.dst_origin[md]) * dpm) = acc[r];
+    }
+  }
+}
+
+using SmallFn = void (*)(const AxisArgs, const AxisWeightsF32);
+template <int R>
+constexpr SmallFn small_fn(bool ref) {
+  return ref ? k_conv_axis_small<R, true> : k_conv_axis_small<R, false>;
+}
+SmallFn small_table(int r, bool ref) {
+  static const SmallFn t[kMaxSmallR + 1][2] = {
+      {nullptr, nullptr},
+      {small_fn<1>(false), small_fn<1>(true)},   {small_fn<2>(false), small_fn<2>(true)},
+      {small_fn<3>(false), small_fn<3>(true)},   {small_fn<4>(false), small_fn<4>(true)},
+      {small_fn<5>(false), small_fn<5>(true)},   {small_fn<6>(false), small_fn<6>(true)},
+      {small_fn<7>(false), small_fn<7>(true)},   {small_fn<8>(false), small_fn<8>(true)},
+      {small_fn<9>(false), small_fn<9>(true)},   {small_fn<10>(false), small_fn<10>(true)},
+      {small_fn<11>(false), small_fn<11>(true)}, {small_fn<12>(false), small_fn<12>(true)}};
+  return (r >= 1 && r <= kMaxSmallR) ? t[r][ref ? 1 : 0] : nullptr;
+}
+
 dim3 grid_for(const AxisArgs& a) {
   const int64_t rowlen = a.out_size[0] * a.comps;
   const int64_t nrows = a.out_size[1] * a.out_size[2];
@@ -126,6 +227,22 @@ dim3 grid_for(const AxisArgs& a) {
 template <typename Tin, typename Tout>
 itkg_status launch_typed(const AxisArgs& a, const AxisWeightsF32& W, int rounding,
                          cudaStream_t s) {
+  if constexpr (std::is_same<Tin, float>::value && std::is_same<Tout, float>::value) {
+    const SmallFn fn = small_table(a.radius, rounding == ITKG_ROUND_REFERENCE);
+    if (fn) {
+      const int md = a.axis == 2 ? 2 : 1, od = a.axis == 2 ? 1 : 2;
+      const int64_t gx = (a.out_size[0] * a.comps + kThreads - 1) / kThreads;
+      const int64_t gy = std::min<int64_t>((a.out_size[md] + kRun - 1) / kRun, 65535);
+      const int64_t gz = std::min<int64_t>(a.out_size[od], 65535);
+      if (gx <= INT32_MAX) {
+        fn<<<dim3((unsigned)gx, (unsigned)gy, (unsigned)gz), kThreads, 0, s>>>(a, W);
+        note_launch(rounding == ITKG_ROUND_REFERENCE ? "conv_axis_f32_ref" : "conv_axis_f32_fma");
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return set_error(ITKG_ERROR_CUDA, "conv_axis launch: %s", cudaGetErrorString(e));
+        return ITKG_SUCCESS;
+      }
+    }
+  }
   dim3 grid = grid_for(a);
   if (rounding == ITKG_ROUND_REFERENCE) {
     k_conv_axis_f32<Tin, Tout, true><<<grid, kThreads, 0, s>>>(a, W);
