@@ -324,16 +324,79 @@ static void make_fused_geom(const itkg_image& in, const itkg_region& largest,
 
 static itkg_status generate_device(const itkg_image& in, const itkg_region& largest,
                                    const itkg_region& requested, const itkg_gaussian_params& prm,
+                                   const Plan& plan, const itkg_image& out, cudaStream_t s);
+
+// Several rounds of symmetric kernels (the binomial blur): round k is one
+// single-round call -- x, y and z passes in the two-pass, fused or per-axis
+// kernels, whichever fits, as for the Gaussian -- that writes `requested`
+// padded by (reps - k - 1) radii (clipped) into f32 scratch.  Inside a round
+// those kernels write exactly the intermediate regions of passes (k, x),
+// (k, y), (k, z) of the per-axis schedule (binomial_blur.rs:63-87) and round
+// each pass to f32, so the result is the schedule's.
+static itkg_status run_rounds(const itkg_image& in, const itkg_region& largest,
+                              const itkg_region& requested, const itkg_gaussian_params& prm,
+                              const Plan& plan, const itkg_image& out, cudaStream_t s) {
+  const int D = in.dim;
+  const uint64_t reps = plan.reps;
+  Plan one = plan;
+  one.reps = 1;
+  auto round_region = [&](uint64_t k) {
+    if (k + 1 == reps) return requested;
+    uint64_t pad[kMaxDim] = {0, 0, 0};
+    for (int d = 0; d < D; ++d) pad[d] = (reps - k - 1) * plan.radii[d];
+    return clipped(padded(requested, D, pad), D, largest);
+  };
+  itkg_image bufs[2];
+  void* mem[2] = {nullptr, nullptr};
+  size_t bytes = 0;
+  for (int i = 0; i < 2; ++i) {
+    std::memset(&bufs[i], 0, sizeof bufs[i]);
+    bufs[i].dim = D;
+    bufs[i].dtype = ITKG_F32;
+    bufs[i].components = in.components;
+    bufs[i].location = ITKG_DEVICE;
+    for (int d = 0; d < D; ++d) bufs[i].spacing[d] = in.spacing[d];
+  }
+  {
+    itkg_image probe = bufs[0];
+    probe.region = round_region(0);  // the largest round region
+    dense_layout(&probe, 16);
+    bytes = image_bytes(probe);
+  }
+  itkg_status st = scratch_alloc(&mem[0], bytes, s);
+  if (st == ITKG_SUCCESS && reps > 2) st = scratch_alloc(&mem[1], bytes, s);
+  itkg_image cur = in;
+  for (uint64_t k = 0; k < reps && st == ITKG_SUCCESS; ++k) {
+    const itkg_region rk = round_region(k);
+    itkg_image nxt = out;
+    if (k + 1 < reps) {
+      nxt = bufs[k & 1];
+      nxt.region = rk;
+      dense_layout(&nxt, 16);
+      nxt.data = mem[k & 1];
+    }
+    st = generate_device(cur, largest, rk, prm, one, nxt, s);
+    cur = nxt;
+  }
+  scratch_free(mem[0], s);
+  scratch_free(mem[1], s);
+  return st;
+}
+
+static itkg_status generate_device(const itkg_image& in, const itkg_region& largest,
+                                   const itkg_region& requested, const itkg_gaussian_params& prm,
                                    const Plan& plan, const itkg_image& out, cudaStream_t s) {
   const int D = in.dim;
   // The single-launch kernels run one round of a kernel that reads the same
   // backwards (their y and z passes index the weights by distance from the centre).
-  if (plan.reps != 1 || !plan.symmetric) {
+  if (!plan.symmetric || plan.reps == 0 ||
+      (plan.reps > 1 && (prm.algorithm == ITKG_ALGO_PER_AXIS || prm.arithmetic == ITKG_ARITH_PIXEL_U8))) {
     if (prm.algorithm == ITKG_ALGO_FUSED || prm.algorithm == ITKG_ALGO_TWO_PASS)
       return set_error(ITKG_ERROR_UNSUPPORTED,
-                       "repeated rounds and asymmetric kernels run per axis only (ITKG_ALGO_PER_AXIS or AUTO)");
+                       "asymmetric kernels, zero rounds and u8 pixel arithmetic over several rounds run per axis only");
     return run_per_axis(in, largest, requested, prm, plan, out, s);
   }
+  if (plan.reps > 1) return run_rounds(in, largest, requested, prm, plan, out, s);
   if (prm.arithmetic != ITKG_ARITH_PIXEL_U8 && prm.algorithm != ITKG_ALGO_PER_AXIS) {
     FusedGeom g;
     make_fused_geom(in, largest, requested, prm, plan, out, &g);

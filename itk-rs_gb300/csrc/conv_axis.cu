@@ -127,13 +127,15 @@ __global__ void __launch_bounds__(kThreads)
 // K + kRun - 1 loads; along x each of the kRun rows takes its K taps from the
 // cache lines its warp already loaded.  Same arithmetic as k_conv_axis_f32: ascending taps from
 // zero, clamp to [lo, hi] on `axis`.
-constexpr int kRun = 4;
+template <int R>
+constexpr int run_of() { return R <= 2 ? 8 : 4; }
 constexpr int kMaxSmallR = 12;
 
 template <int R, bool REF>
-__global__ void __launch_bounds__(kThreads, 4)
+__global__ void __launch_bounds__(kThreads, R <= 4 ? 4 : 2)
     k_conv_axis_small(const AxisArgs a, const AxisWeightsF32 W) {
   constexpr int K = 2 * R + 1;
+  constexpr int kRun = run_of<R>();
   const int64_t rowlen = a.out_size[0] * a.comps;
   const int64_t t = (int64_t)blockIdx.x * kThreads + threadIdx.x;
   if (t >= rowlen) return;
@@ -232,7 +234,8 @@ itkg_status launch_typed(const AxisArgs& a, const AxisWeightsF32& W, int roundin
     if (fn) {
       const int md = a.axis == 2 ? 2 : 1, od = a.axis == 2 ? 1 : 2;
       const int64_t gx = (a.out_size[0] * a.comps + kThreads - 1) / kThreads;
-      const int64_t gy = std::min<int64_t>((a.out_size[md] + kRun - 1) / kRun, 65535);
+      const int run = a.radius <= 2 ? 8 : 4;
+      const int64_t gy = std::min<int64_t>((a.out_size[md] + run - 1) / run, 65535);
       const int64_t gz = std::min<int64_t>(a.out_size[od], 65535);
       if (gx <= INT32_MAX) {
         fn<<<dim3((unsigned)gx, (unsigned)gy, (unsigned)gz), kThreads, 0, s>>>(a, W);

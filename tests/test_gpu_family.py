@@ -151,10 +151,25 @@ def test_asymmetric_kernel_runs_per_axis(gpu):
     assert "per_axis" in k and bits_equal(got, want), k
 
 
-def test_explicit_single_launch_kernels_refuse_rounds(gpu):
+@pytest.mark.parametrize("algo,kernel", [("two_pass", "z_pass"), ("fused", "fused3d"), ("per_axis", "per_axis")])
+@pytest.mark.parametrize("rounding", [0, 1])
+def test_binomial_rounds_through_single_round_kernels(gpu, algo, kernel, rounding):
+    """Each round is one single-round call (x, y, z) in the chosen kernels."""
+    x = vol((24, 28, 32), 61)
+    want = oracle.binomial_f32(x, 3)
+    got, k = run(gpu, lambda s, **kw: gpu.BinomialBlurFilter(s, 3, **kw), x, algo=algo, rounding=rounding)
+    assert kernel in k, k
+    if rounding == 0:
+        assert bits_equal(got, want), k
+    else:
+        assert normwise(got, want) <= TOL_FMA, k
+
+
+def test_explicit_single_launch_kernels_refuse_asymmetric(gpu):
     x = vol((10, 12, 16), 61)
+    ks = [np.array([0.1, 0.2, 0.7])] * 3
     with pytest.raises(gpu.ItkgError) as e:
-        run(gpu, lambda s, **kw: gpu.BinomialBlurFilter(s, 2, **kw), x, algo="two_pass")
+        run(gpu, lambda s, **kw: gpu.SeparableFilter(s, ks, 1, **kw), x, algo="fused")
     assert e.value.status == 2  # ITKG_ERROR_UNSUPPORTED
 
 
