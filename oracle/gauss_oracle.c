@@ -422,6 +422,70 @@ int orc_separable_f32_mt(const float *img, const orc_region *img_reg, int D, int
                             nthreads < 1 ? 1 : nthreads);
 }
 
+/* ---- RecursiveGaussianFilter (recursive_gaussian.rs) --------------------- *
+ * Young & van Vliet 3rd-order coefficients (recursive_gaussian.rs:33-49),
+ * every product and sum rounded separately in the order written there. */
+void orc_yvv_coeffs(double sigma, double *out4) {
+    if (!(sigma > 0.5)) sigma = 0.5; /* sigma.max(0.5); f64::max takes 0.5 over NaN */
+    double q = sigma >= 2.5 ? 0.98711 * sigma - 0.96330 : 3.97156 - 4.14554 * sqrt(1.0 - 0.26891 * sigma);
+    double q2 = q * q;
+    double q3 = q2 * q;
+    double b0 = 1.57825 + 2.44413 * q + 1.4281 * q2 + 0.422205 * q3;
+    double b1 = 2.44413 * q + 2.85619 * q2 + 1.26661 * q3;
+    double b2 = -(1.4281 * q2 + 1.26661 * q3);
+    double b3 = 0.422205 * q3;
+    double big_b = 1.0 - (b1 + b2 + b3) / b0;
+    out4[0] = big_b;
+    out4[1] = b1 / b0;
+    out4[2] = b2 / b0;
+    out4[3] = b3 / b0;
+}
+
+/* filter_axis (recursive_gaussian.rs:93-130) on a dense f64 image of `size`
+ * (axis 0 fastest): every line along `axis` gets the causal pass
+ * (recursive_gaussian.rs:56-71), then the anticausal pass (73-88), in place;
+ * lines of length <= 1 are left alone. */
+static void iir_axis(double *data, const int64_t *size, int D, int axis, double sigma_px) {
+    const int64_t n = size[axis];
+    if (n <= 1) return;
+    double c[4];
+    orc_yvv_coeffs(sigma_px, c);
+    const double B = c[0], a1 = c[1], a2 = c[2], a3 = c[3];
+    int64_t stride[ORC_MAXD] = {1, 1, 1};
+    for (int d = 1; d < D; d++) stride[d] = stride[d - 1] * size[d - 1];
+    int64_t total = 1;
+    for (int d = 0; d < D; d++) total *= size[d];
+    const int64_t s = stride[axis];
+    for (int64_t lin = 0; lin < total; lin++) {
+        /* line starts: the voxels whose coordinate on `axis` is 0 */
+        if ((lin / s) % n != 0) continue;
+        double *p = data + lin;
+        double ym1 = p[0], ym2 = p[0], ym3 = p[0];
+        for (int64_t i = 0; i < n; i++) {
+            double v = B * p[i * s] + a1 * ym1 + a2 * ym2 + a3 * ym3;
+            ym3 = ym2; ym2 = ym1; ym1 = v;
+            p[i * s] = v;
+        }
+        ym1 = ym2 = ym3 = p[(n - 1) * s];
+        for (int64_t i = n - 1; i >= 0; i--) {
+            double v = B * p[i * s] + a1 * ym1 + a2 * ym2 + a3 * ym3;
+            ym3 = ym2; ym2 = ym1; ym1 = v;
+            p[i * s] = v;
+        }
+    }
+}
+
+/* RecursiveGaussianFilter::generate_region (recursive_gaussian.rs:154-180) and
+ * RecursiveGaussianAxisFilter (218-238, axis >= 0): `img` is the whole largest
+ * region already converted to f64 (P::to_f64), filtered in place; sigma is in
+ * physical units (sigma / spacing per axis).  The caller crops and converts
+ * (P::from_f64). */
+void orc_recursive_gaussian_f64(double *img, const int64_t *size, const double *spacing, int D,
+                                double sigma, int axis) {
+    for (int a = 0; a < D; a++)
+        if (axis < 0 || axis == a) iir_axis(img, size, D, a, sigma / spacing[a]);
+}
+
 /* box_kernel (mean.rs:15-18) */
 void orc_box_kernel(uint64_t radius, double *out) {
     const uint64_t len = 2 * radius + 1;

@@ -69,6 +69,10 @@ def lib():
         L.orc_separable_f32_mt.restype = ctypes.c_int
         L.orc_separable_f32_mt.argtypes = [P, R, ctypes.c_int, ctypes.c_int, P, P, ctypes.c_uint64,
                                            R, P, ctypes.c_int]
+        L.orc_yvv_coeffs.restype = None
+        L.orc_yvv_coeffs.argtypes = [ctypes.c_double, P]
+        L.orc_recursive_gaussian_f64.restype = None
+        L.orc_recursive_gaussian_f64.argtypes = [P, P, P, ctypes.c_int, ctypes.c_double, ctypes.c_int]
         L.orc_box_kernel.restype = None
         L.orc_box_kernel.argtypes = [ctypes.c_uint64, P]
         L.orc_cast_f32_to_u8.restype = None
@@ -247,6 +251,51 @@ def binomial_f32(img, repetitions, **kw):
     """BinomialBlurFilter (binomial_blur.rs:17-89)."""
     D = _dims(np.asarray(img), kw.get("comps", 1))[0]
     return separable_f32(img, [BINOMIAL_KERNEL] * D, repetitions, **kw)
+
+
+def yvv_coeffs(sigma: float) -> np.ndarray:
+    """(B, a1, a2, a3) of recursive_gaussian.rs:33-49."""
+    out = np.empty(4, dtype=np.float64)
+    lib().orc_yvv_coeffs(float(sigma), _ptr(out))
+    return out
+
+
+def recursive_gaussian_f64(img, sigma, spacing=None, axis=-1):
+    """RecursiveGaussianFilter (axis = -1) or RecursiveGaussianAxisFilter (axis >= 0,
+    reference axis order) over the whole image, before the output conversion:
+    the f64 image after every causal / anticausal line pass."""
+    a = np.array(img, dtype=np.float64, order="C", copy=True)  # P::to_f64 (exact for f32, i16, u8)
+    D = a.ndim
+    size = np.ascontiguousarray(list(reversed(a.shape)), dtype=np.int64)
+    sp = np.ascontiguousarray(spacing if spacing is not None else [1.0] * D, dtype=np.float64)
+    lib().orc_recursive_gaussian_f64(_ptr(a), _ptr(size), _ptr(sp), D, float(sigma), int(axis))
+    return a
+
+
+def from_f64_u8(v: np.ndarray) -> np.ndarray:
+    """u8::from_f64 (pixel.rs:36): round half away from zero, clamp to [0, 255], NaN -> 0."""
+    v = np.asarray(v, dtype=np.float64)
+    a = np.abs(v)
+    f = np.floor(a)
+    r = np.copysign(f + (a - f >= 0.5), v)  # a - f is exact
+    r = np.clip(np.nan_to_num(r, nan=0.0), 0.0, 255.0)
+    return r.astype(np.uint8)
+
+
+def recursive_gaussian_f32(img, sigma, spacing=None, axis=-1, requested=None, index=None):
+    """RecursiveGaussianFilter<Image<f32>>::generate_region: f64 filtering, crop, `as f32`."""
+    full = recursive_gaussian_f64(img, sigma, spacing, axis)
+    return _crop(full, requested, index).astype(np.float32)
+
+
+def _crop(full, requested, index):
+    if requested is None:
+        return full
+    D = full.ndim
+    index = tuple(index) if index is not None else (0,) * D
+    (ri, rs) = requested
+    sl = tuple(slice(ri[d] - index[d], ri[d] - index[d] + rs[d]) for d in reversed(range(D)))
+    return full[sl]
 
 
 def split_region(index, size, num_pieces):

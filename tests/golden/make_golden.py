@@ -178,6 +178,58 @@ def separable_region(img, kernels, reps, req_index, req_size, kind="f32"):
     return cur
 
 
+def yvv_coeffs(sigma):
+    """recursive_gaussian.rs:33-49"""
+    sigma = 0.5 if not (sigma > 0.5) else sigma
+    if sigma >= 2.5:
+        q = 0.98711 * sigma - 0.96330
+    else:
+        q = 3.97156 - 4.14554 * math.sqrt(1.0 - 0.26891 * sigma)
+    q2 = q * q
+    q3 = q2 * q
+    b0 = 1.57825 + 2.44413 * q + 1.4281 * q2 + 0.422205 * q3
+    b1 = 2.44413 * q + 2.85619 * q2 + 1.26661 * q3
+    b2 = -(1.4281 * q2 + 1.26661 * q3)
+    b3 = 0.422205 * q3
+    big_b = 1.0 - (b1 + b2 + b3) / b0
+    return big_b, b1 / b0, b2 / b0, b3 / b0
+
+
+def recursive_region(img, spacing, sigma, axis_only=None):
+    """RecursiveGaussianFilter (recursive_gaussian.rs:154-180) / RecursiveGaussianAxisFilter
+    (218-238) over the whole image: f64 pixels, per axis causal then anticausal line passes
+    (56-88, 93-130).  Returns the f64 image (index, size, flat list)."""
+    b_index, b_size, data = img
+    D = len(b_size)
+    vals = [float(p[0]) for p in data]
+    for axis in range(D):
+        if axis_only is not None and axis != axis_only:
+            continue
+        n = b_size[axis]
+        if n <= 1:
+            continue
+        big_b, a1, a2, a3 = yvv_coeffs(sigma / spacing[axis])
+        stripe = list(b_size)
+        stripe[axis] = 1
+        for start in iter_region(b_index, stripe):
+            line = []
+            for k in range(n):
+                idx = list(start)
+                idx[axis] += k
+                line.append(flat_index(b_index, b_size, idx))
+            ym1 = ym2 = ym3 = vals[line[0]]
+            for i in range(n):
+                v = big_b * vals[line[i]] + a1 * ym1 + a2 * ym2 + a3 * ym3
+                ym3, ym2, ym1 = ym2, ym1, v
+                vals[line[i]] = v
+            ym1 = ym2 = ym3 = vals[line[n - 1]]
+            for i in range(n - 1, -1, -1):
+                v = big_b * vals[line[i]] + a1 * ym1 + a2 * ym2 + a3 * ym3
+                ym3, ym2, ym1 = ym2, ym1, v
+                vals[line[i]] = v
+    return vals
+
+
 def split_region(index, size, n):
     n = max(n, 1)
     D = len(size)
@@ -311,6 +363,28 @@ def main():
     cases.update(sep_case("binomial3d_r0", m3, "binomial", 0))
     cases.update(sep_case("binomial_u8_2d_r2", srng.integers(0, 256, (8, 9), dtype=np.uint8),
                           "binomial", 2, kind="u8"))
+    # RecursiveGaussianFilter: f64 result before the output conversion, and the f32 output
+    rrng = np.random.default_rng(20261205)
+
+    def rec_case(name, arr, sigma, spacing=None, axis=None):
+        D = arr.ndim
+        spacing = spacing or [1.0] * D
+        img = to_ref(arr)
+        vals = recursive_region(img, spacing, sigma, axis)
+        f64 = np.array(vals, dtype=np.float64).reshape(arr.shape)
+        return {f"rec_{name}__in": arr, f"rec_{name}__f64": f64,
+                f"rec_{name}__meta": np.array([sigma, -1 if axis is None else axis] + list(spacing), dtype=np.float64)}
+
+    r1 = np.zeros((51,), np.float32)
+    r1[25] = 1.0
+    cases.update(rec_case("impulse1d_s2", r1, 2.0))
+    cases.update(rec_case("const2d_s1p5", np.full((15, 15), 4.0, np.float32), 1.5))
+    cases.update(rec_case("rand2d_s3", rrng.random((12, 17), dtype=np.float32), 3.0))
+    cases.update(rec_case("rand3d_s1p2_aniso", (rrng.standard_normal((6, 8, 9)) * 2).astype(np.float32), 1.2,
+                          spacing=[0.8, 1.0, 2.0]))
+    cases.update(rec_case("rand3d_axis1_s0p3", rrng.random((5, 7, 6), dtype=np.float32), 0.3, axis=1))
+    cases.update(rec_case("u8_2d_s2", rrng.integers(0, 256, (9, 11), dtype=np.uint8), 2.0))
+    cases.update(rec_case("thin3d_s2", rrng.random((1, 6, 7), dtype=np.float32), 2.0))
     # kernels
     for s, sp in [(1.5, 1.0), (2.0, 1.0), (1.5, 0.7), (1.5, 2.5), (0.5, 1.0), (8.0, 1.0)]:
         cases[f"kernel_{s}_{sp}"] = np.array(build_kernel(s / sp, kernel_radius(s, sp)),
