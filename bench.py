@@ -641,6 +641,43 @@ def extra_workload(args):
                                  "note": "8 B per voxel per call; per-axis passes each move ~8 B per voxel"},
                     "cpu_baseline": cpu,
                     "accuracy": {"normwise_rel_vs_ref_f32": err}})
+    elif args.workload == "recursive3d":
+        # RecursiveGaussianFilter sigma 2 on the 256^3 blobs volume: f64 bit-exact and f64 with FMA
+        vol = blobs_volume(SHAPE, 0)
+        nvox = int(np.prod(SHAPE))
+        n = 4
+        devs = [itkg.DeviceImage.from_host(itkg.Image(vol)) for _ in range(n)]
+        outs = [itkg.DeviceImage(devs[0].region) for _ in range(n)]
+        lg = devs[0].region.to_c()
+        rq = devs[0].region.to_c()
+        lines = {}
+        want = oracle.recursive_gaussian_f32(vol, SIGMA)
+        for name, rnd in (("f64_reference", itkg.ROUND_REFERENCE), ("f64_fma", itkg.ROUND_FMA)):
+            p = _abi.itkg_recursive_params()
+            p.sigma, p.axis, p.rounding = SIGMA, -1, rnd
+
+            def step(p=p):
+                for d, o in zip(devs, outs):
+                    _abi.check(L.itkg_recursive_gaussian_generate_region(
+                        ctypes.byref(d.c), ctypes.byref(lg), ctypes.byref(rq), ctypes.byref(p),
+                        ctypes.byref(o.c), sp.ptr))
+            ms = _timed(stream, step, max(2, args.steps // 8), args.warmup)
+            got = outs[0].download()
+            lines[name] = {"voxels_per_s": n * nvox / (ms * 1e-3), "ms_per_call": ms / n,
+                           "kernel": itkg.last_kernel(), "normwise_rel_vs_ref": _normwise(got, want),
+                           "bit_exact": bool(np.array_equal(got.view(np.uint32), want.view(np.uint32)))}
+        cpu = None
+        if args.cpu_seconds > 0:
+            sub = vol[:, :64, :64]  # the recursion is sequential per line: time a 256 x 64 x 64 block
+            t = time.perf_counter()
+            oracle.recursive_gaussian_f32(sub, SIGMA)
+            dt = time.perf_counter() - t
+            cpu = {"value": sub.size / dt, "unit": "voxels/s", "cores": 1, "kind": "port",
+                   "sample": "256x64x64 block, C restatement (the reference runs its lines sequentially)"}
+        out.update({"value": lines["f64_reference"]["voxels_per_s"], "ms_per_step": lines["f64_reference"]["ms_per_call"] * n,
+                    "dtype": "f64", "config": {"workload": "RecursiveGaussianFilter sigma 2, Image<f32,3> 256^3 blobs+noise, 4 volumes per step",
+                                               "variants": lines},
+                    "cpu_baseline": cpu})
     print(json.dumps(out))
     return 0
 
@@ -652,7 +689,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=["itkg", "reference"], default="itkg")
     ap.add_argument("--workload", choices=["fwd3d", "fwd2d", "ct16", "batch", "batch_vjp", "vjp_stack",
-                                           "mean3d", "binomial3d"],
+                                           "mean3d", "binomial3d", "recursive3d"],
                     default="fwd3d")
     ap.add_argument("--rounding", choices=["fma", "reference"], default="fma")
     ap.add_argument("--algo", choices=["auto", "fused", "per_axis", "two_pass"], default="auto")

@@ -93,7 +93,7 @@ typedef enum itkg_algorithm {
     ITKG_ALGO_PER_AXIS = 2, /* D separate passes through an f32 scratch buffer */
     ITKG_ALGO_TWO_PASS = 3  /* 3-D: an x-y slice kernel and a z kernel through an f32
                                intermediate sized for L2; ITKG_ERROR_UNSUPPORTED if it
-                               does not fit (needs rx == ry <= 8, rz <= 8, one component,
+                               does not fit (needs rx == ry <= 12, rz <= 12, one component,
                                16-byte aligned input rows) */
 } itkg_algorithm;
 
@@ -257,6 +257,33 @@ itkg_status itkg_separable_generate_region(const itkg_image *input, const itkg_r
                                            const itkg_region *requested,
                                            const itkg_separable_params *params,
                                            itkg_image *output, void *stream);
+
+/* ---- RecursiveGaussianFilter (recursive_gaussian.rs) -----------------------
+ * Young & van Vliet 3rd-order IIR Gaussian: RecursiveGaussianFilter (axis -1,
+ * every axis; recursive_gaussian.rs:133-181) and RecursiveGaussianAxisFilter
+ * (axis 0..dim-1; 183-239).  The whole largest region is filtered (the
+ * reference's input_region_for_output is the largest region), so `input` must
+ * cover `largest`; `requested` is written to `output`.
+ *   sigma     physical units; sigma / spacing per axis, at least 0.5 (:34)
+ *   rounding  f64 either way; ITKG_ROUND_REFERENCE: every product and sum
+ *             rounded in the reference's order, bit-exact; ITKG_ROUND_FMA:
+ *             fused multiply-adds
+ * Scalar input of any dtype (converted exactly); output f32 (`v as f32`) or u8
+ * (round half away from zero, clamp to [0, 255], pixel.rs:36). */
+typedef struct itkg_recursive_params {
+    double sigma;
+    int32_t axis;
+    int32_t rounding;
+    int32_t reserved[2]; /* 0 */
+} itkg_recursive_params;
+
+/* (B, a1, a2, a3) of recursive_gaussian.rs:33-49 for sigma in pixels. */
+itkg_status itkg_yvv_coeffs(double sigma, double *coeffs_out);
+
+itkg_status itkg_recursive_gaussian_generate_region(const itkg_image *input, const itkg_region *largest,
+                                                    const itkg_region *requested,
+                                                    const itkg_recursive_params *params,
+                                                    itkg_image *output, void *stream);
 
 /* ---- derivatives (not in the reference: it has no VJP) ---------------------
  * Vector-Jacobian product of GaussianFilter over a whole image: x is the

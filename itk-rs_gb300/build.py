@@ -22,8 +22,13 @@ LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libitkg.so")
 NVCC = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-COMMON = ["-std=c++17", "-O3", "-Xcompiler", "-fPIC", "-I", os.path.join(ROOT, "include"),
-          "-I", CSRC]
+# -ffp-contract=off for the host compiler: host-side coefficients (the
+# recursive Gaussian's, the kernels' f64 weights and edge tables) must round
+# every product and sum separately as the reference does; gcc on aarch64 would
+# otherwise fuse them into FMAs and the coefficients would differ by an ulp
+# between an x86 and an Arm host.
+COMMON = ["-std=c++17", "-O3", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+          "-I", os.path.join(ROOT, "include"), "-I", CSRC]
 # -fmad=false: ptxas must not contract a separate multiply and add into an FMA
 # (the reference-rounding kernels rely on two roundings per tap, including the
 # packed mul.rn.f32x2 / add.rn.f32x2 pairs); FMA-rounding code uses explicit

@@ -870,6 +870,70 @@ itkg_status itkg_box_kernel(uint64_t radius, double* weights_out) {
   return ITKG_SUCCESS;
 }
 
+itkg_status itkg_yvv_coeffs(double sigma, double* coeffs_out) {
+  if (!coeffs_out) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "coeffs_out is NULL");
+  yvv_coeffs(sigma, coeffs_out);
+  return ITKG_SUCCESS;
+}
+
+itkg_status itkg_recursive_gaussian_generate_region(const itkg_image* input, const itkg_region* largest,
+                                                    const itkg_region* requested,
+                                                    const itkg_recursive_params* params, itkg_image* output,
+                                                    void* stream) {
+  ITKG_TRY(validate_image(input, "input"));
+  ITKG_TRY(validate_image(output, "output"));
+  if (!params) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "params is NULL");
+  if (!largest || !requested) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "region is NULL");
+  const int D = input->dim;
+  if (output->dim != D) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "input/output dim differ");
+  if (input->components != 1 || output->components != 1)
+    return set_error(ITKG_ERROR_UNSUPPORTED, "the recursive Gaussian takes scalar pixels");
+  if (params->rounding != ITKG_ROUND_REFERENCE && params->rounding != ITKG_ROUND_FMA)
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "unknown rounding %d", params->rounding);
+  if (params->axis < -1 || params->axis >= D)
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "axis %d outside [-1, %d]", params->axis, D - 1);
+  if (params->reserved[0] != 0 || params->reserved[1] != 0)
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "reserved must be 0");
+  if (output->dtype != ITKG_F32 && output->dtype != ITKG_U8)
+    return set_error(ITKG_ERROR_UNSUPPORTED, "output dtype %d: f32 and u8 are provided", output->dtype);
+  if (region_len(*requested, D) == 0) return ITKG_SUCCESS;
+  if (!region_contains(*largest, *requested, D))
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "requested region lies outside the largest region");
+  if (!region_contains(output->region, *requested, D))
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "output buffer does not contain the requested region");
+  // the reference filters the whole largest region (recursive_gaussian.rs:148-150)
+  if (!region_contains(input->region, *largest, D))
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "input buffer does not cover the largest region");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const bool host_in = input->location == ITKG_HOST, host_out = output->location == ITKG_HOST;
+  itkg_image din = *input, dout = *output;
+  void* pin = nullptr;
+  void* pout = nullptr;
+  itkg_status st = ITKG_SUCCESS;
+  if (host_in) {
+    din.location = ITKG_DEVICE;
+    din.region = *largest;
+    dense_layout(&din, 16);
+    st = scratch_alloc(&pin, image_bytes(din), s);
+    din.data = pin;
+    if (st == ITKG_SUCCESS) st = copy_region(din, *input, *largest, s);
+  }
+  if (st == ITKG_SUCCESS && host_out) {
+    dout.location = ITKG_DEVICE;
+    dout.region = *requested;
+    dense_layout(&dout, 16);
+    st = scratch_alloc(&pout, image_bytes(dout), s);
+    dout.data = pout;
+  }
+  if (st == ITKG_SUCCESS)
+    st = launch_recursive(din, *largest, *requested, params->sigma, params->axis, params->rounding, dout, s);
+  if (st == ITKG_SUCCESS && host_out) st = copy_region(*output, dout, *requested, s);
+  scratch_free(pin, s);
+  scratch_free(pout, s);
+  if (st == ITKG_SUCCESS && (host_in || host_out)) ITKG_CUDA(cudaStreamSynchronize(s));
+  return st;
+}
+
 itkg_status itkg_separable_input_region_for_output(const itkg_region* output_region,
                                                    const itkg_region* largest, int32_t dim,
                                                    const uint64_t* radius, uint64_t repetitions,

@@ -165,6 +165,12 @@ struct VjpTwoPass {
 };
 itkg_status launch_vjp_two_pass(const VjpTwoPass& v, void* stream, bool dry_run);
 
+// RecursiveGaussianFilter (recursive.cu): `in` device image covering `largest`,
+// `out` device image covering `requested`; axis -1 = every axis.
+void yvv_coeffs(double sigma, double out[4]);
+itkg_status launch_recursive(const itkg_image& in, const itkg_region& largest, const itkg_region& requested,
+                             double sigma, int axis, int rounding, const itkg_image& out, void* stream);
+
 // Bumps the launch counter by n (graph replays).
 void note_launches(uint64_t n, const char* name);
 

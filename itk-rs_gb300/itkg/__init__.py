@@ -24,7 +24,8 @@ import numpy as np
 
 from ._abi import (ALGO_AUTO, ALGO_FUSED, ALGO_PER_AXIS, ALGO_TWO_PASS, ARITH_F32, ARITH_PIXEL_U8, BF16,
                    DEVICE, F16, F32, HOST, I16, ROUND_FMA, ROUND_REFERENCE, U8, ItkgError, check,
-                   itkg_gaussian_params, itkg_image, itkg_region, itkg_separable_params, lib)
+                   itkg_gaussian_params, itkg_image, itkg_recursive_params, itkg_region,
+                   itkg_separable_params, lib)
 
 __all__ = [
     "Region", "Image", "DeviceImage", "GaussianFilter", "CastFilter", "stream_full",
@@ -32,6 +33,7 @@ __all__ = [
     "F16", "ROUND_REFERENCE", "ROUND_FMA", "ALGO_AUTO", "ALGO_FUSED", "ALGO_PER_AXIS",
     "ALGO_TWO_PASS", "ARITH_F32", "ARITH_PIXEL_U8", "gaussian", "Stream", "SeparableFilter",
     "MeanFilter", "BoxMeanFilterN", "BinomialBlurFilter", "box_kernel", "BINOMIAL_KERNEL",
+    "RecursiveGaussianFilter", "RecursiveGaussianAxisFilter", "yvv_coeffs",
 ]
 
 _NP_OF = {F32: np.float32, I16: np.int16, U8: np.uint8, F16: np.float16}
@@ -445,6 +447,68 @@ class BinomialBlurFilter(SeparableFilter):
     def effective_sigma_pixels(repetitions: int) -> float:
         """binomial_blur.rs:28-30"""
         return (repetitions / 4.0) ** 0.5
+
+
+def yvv_coeffs(sigma: float) -> np.ndarray:
+    """(B, a1, a2, a3) of recursive_gaussian.rs:33-49, sigma in pixels."""
+    out = np.empty(4, dtype=np.float64)
+    check(lib().itkg_yvv_coeffs(float(sigma), out.ctypes.data))
+    return out
+
+
+class RecursiveGaussianFilter:
+    """RecursiveGaussianFilter { source, sigma } (recursive_gaussian.rs:133-181); with
+    `axis` set, RecursiveGaussianAxisFilter { source, sigma, axis } (183-239).
+    Filters the whole largest region; the source must be an Image or DeviceImage."""
+
+    def __init__(self, source, sigma: float, axis: int | None = None, rounding: int = ROUND_REFERENCE):
+        if not isinstance(source, (Image, DeviceImage)):
+            raise TypeError("source must be an Image or a DeviceImage")
+        self.source = source
+        self.sigma = float(sigma)
+        self.axis = -1 if axis is None else int(axis)
+        self.rounding = rounding
+
+    def largest_region(self) -> Region:
+        return self.source.largest_region()
+
+    def input_region_for_output(self, out: Region) -> Region:
+        return self.largest_region()
+
+    def params(self) -> itkg_recursive_params:
+        p = itkg_recursive_params()
+        p.sigma, p.axis, p.rounding = self.sigma, self.axis, self.rounding
+        return p
+
+    def generate_region(self, requested: Region, stream: Stream = _DEFAULT_STREAM, out_dtype: int | None = None):
+        """Returns a host Image for a host source, a DeviceImage for a device source."""
+        src = self.source
+        if out_dtype is None:
+            out_dtype = U8 if src.dtype == U8 else F32
+        prm = self.params()
+        largest = src.largest_region().to_c()
+        req = requested.to_c()
+        sc = src.to_c()
+        if isinstance(src, Image):
+            host = np.empty(tuple(reversed(requested.size)), dtype=_storage_np(out_dtype))
+            res = Image(host, index=requested.index, spacing=src.spacing, origin=src.origin)
+            oc = res.to_c()
+            check(lib().itkg_recursive_gaussian_generate_region(ctypes.byref(sc), ctypes.byref(largest),
+                                                                ctypes.byref(req), ctypes.byref(prm),
+                                                                ctypes.byref(oc), stream.ptr))
+            return res
+        dev = DeviceImage(requested, out_dtype, 1, src.spacing, src.origin)
+        check(lib().itkg_recursive_gaussian_generate_region(ctypes.byref(sc), ctypes.byref(largest),
+                                                            ctypes.byref(req), ctypes.byref(prm),
+                                                            ctypes.byref(dev.c), stream.ptr))
+        return dev
+
+
+class RecursiveGaussianAxisFilter(RecursiveGaussianFilter):
+    """RecursiveGaussianAxisFilter { source, sigma, axis } (recursive_gaussian.rs:183-239)."""
+
+    def __init__(self, source, sigma: float, axis: int, rounding: int = ROUND_REFERENCE):
+        super().__init__(source, sigma, axis, rounding)
 
 
 def stream_full(source: GaussianFilter, num_pieces: int, stream: Stream = _DEFAULT_STREAM,

@@ -187,3 +187,10 @@ def test_valid_call_without_gpu_reports_no_device(itkg_lib):
     st = _call(itkg_lib, a.to_c(), a.region.to_c(), a.region.to_c(), p, b.to_c())
     assert st in (itkg._abi.ERROR_NO_DEVICE, itkg._abi.ERROR_CUDA)
     assert itkg_lib.itkg_last_error().decode() != ""
+
+
+@pytest.mark.parametrize("sigma", [0.1, 0.5, 1.3, 2.5, 7.0, float("nan")])
+def test_yvv_coefficients_match_oracle(itkg_lib, sigma):
+    """The library's Young & van Vliet coefficients (recursive_gaussian.rs:33-49) are the oracle's, bit for bit."""
+    import itkg
+    assert np.array_equal(itkg.yvv_coeffs(sigma), oracle.yvv_coeffs(sigma))
