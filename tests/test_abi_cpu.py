@@ -194,3 +194,94 @@ def test_yvv_coefficients_match_oracle(itkg_lib, sigma):
     """The library's Young & van Vliet coefficients (recursive_gaussian.rs:33-49) are the oracle's, bit for bit."""
     import itkg
     assert np.array_equal(itkg.yvv_coeffs(sigma), oracle.yvv_coeffs(sigma))
+
+
+def _sep_params(radius=(1, 1, 1), reps=1, kernels=None):
+    import itkg
+    ks = kernels if kernels is not None else [itkg.box_kernel(r) for r in radius]
+    p = itkg._abi.itkg_separable_params()
+    for d, k in enumerate(ks):
+        p.radius[d] = (len(k) - 1) // 2
+        p.weights[d] = k.ctypes.data
+    p.repetitions = reps
+    return p, ks
+
+
+def test_separable_invalid_arguments_return_status(itkg_lib):
+    import itkg
+    E = itkg._abi.ERROR_INVALID_ARGUMENT
+    a, b, _ = _host_pair()
+    ac, bc = a.to_c(), b.to_c()
+    lg, rq = a.region.to_c(), a.region.to_c()
+
+    def call(p):
+        return itkg_lib.itkg_separable_generate_region(ctypes.byref(ac), ctypes.byref(lg), ctypes.byref(rq),
+                                                       ctypes.byref(p) if p is not None else None,
+                                                       ctypes.byref(bc), None)
+    assert call(None) == E
+    p, ks = _sep_params()
+    p.weights[1] = None
+    assert call(p) == E
+    p, ks = _sep_params()
+    p.radius[0] = 1 << 21
+    assert call(p) == E
+    p, ks = _sep_params(reps=1 << 21)
+    assert call(p) == E
+    p, ks = _sep_params()
+    p.rounding = 7
+    assert call(p) == E
+    # input buffer smaller than requested padded by radius x repetitions
+    p, ks = _sep_params(reps=3)
+    small = itkg.Image(np.zeros((6, 7, 4), np.float32)).to_c()
+    rq2 = itkg.Region((0, 0, 0), (4, 7, 6)).to_c()
+    st = itkg_lib.itkg_separable_generate_region(ctypes.byref(small), ctypes.byref(lg), ctypes.byref(rq2),
+                                                 ctypes.byref(p), ctypes.byref(bc), None)
+    assert st == E and "input_region_for_output" in itkg_lib.itkg_last_error().decode()
+
+
+def test_separable_input_region_and_box_kernel(itkg_lib):
+    import itkg
+    r = itkg.Region((10, 4, 2), (5, 6, 7)).to_c()
+    lg = itkg.Region((0, 0, 0), (40, 30, 20)).to_c()
+    out = itkg._abi.itkg_region()
+    radius = (ctypes.c_uint64 * 3)(1, 2, 3)
+    itkg._abi.check(itkg_lib.itkg_separable_input_region_for_output(ctypes.byref(r), ctypes.byref(lg), 3, radius, 2,
+                                                                    ctypes.byref(out)))
+    assert itkg.Region.from_c(out, 3) == itkg.Region((8, 0, 0), (9, 14, 15))  # z: [2 - 6, 8 + 6] clipped
+    assert np.array_equal(itkg.box_kernel(3), oracle.box_kernel(3))
+
+
+def test_recursive_invalid_arguments_return_status(itkg_lib):
+    import itkg
+    E = itkg._abi.ERROR_INVALID_ARGUMENT
+    a, b, _ = _host_pair()
+    ac, bc = a.to_c(), b.to_c()
+    lg, rq = a.region.to_c(), a.region.to_c()
+
+    def call(p, inp=ac, out=bc, req=rq):
+        return itkg_lib.itkg_recursive_gaussian_generate_region(
+            ctypes.byref(inp), ctypes.byref(lg), ctypes.byref(req), ctypes.byref(p) if p is not None else None,
+            ctypes.byref(out), None)
+    assert call(None) == E
+    p = itkg._abi.itkg_recursive_params()
+    p.sigma = 2.0
+    p.axis = 3
+    assert call(p) == E
+    p.axis = -2
+    assert call(p) == E
+    p.axis, p.rounding = -1, 5
+    assert call(p) == E
+    p.rounding = 0
+    p.reserved[1] = 1
+    assert call(p) == E
+    p.reserved[1] = 0
+    # the input must cover the whole largest region
+    small = itkg.Image(np.zeros((6, 7, 4), np.float32)).to_c()
+    assert call(p, inp=small) == E and "largest" in itkg_lib.itkg_last_error().decode()
+    # i16 output is not a NumericPixel of the recursive filter
+    bad = b.to_c()
+    bad.dtype = itkg.I16
+    bad.pitch[0], bad.pitch[1], bad.pitch[2] = 2, 16, 112
+    assert call(p, out=bad) == itkg._abi.ERROR_UNSUPPORTED
+    empty = itkg.Region((0, 0, 0), (8, 0, 6)).to_c()
+    assert call(p, req=empty) == 0
