@@ -92,6 +92,185 @@ __global__ void __launch_bounds__(kThreads) k_dual_axis(const VjpAxisArgs a, con
   }
 }
 
+// The same two passes with the radius a template parameter (R <= 24: taps
+// unrolled, weights read from the parameter bank) and RUN outputs per thread
+// along a marching axis -- y for passes along x and y, z for passes along z.
+// Along y and z the RUN outputs share one register window of K + RUN - 1
+// loads; along x the taps' offsets (and, for the adjoint, which taps fall
+// inside the image) are computed once per thread.
+constexpr int kMaxSmallVjpR = 24;
+
+template <int R, int RUN, bool AX0>
+__global__ void __launch_bounds__(kThreads, 2) k_adjoint_small(const VjpAxisArgs a, const Taps T) {
+  constexpr int K = 2 * R + 1;
+  const int64_t x = (int64_t)blockIdx.x * kThreads + threadIdx.x;
+  if (x >= a.size[0]) return;
+  const int axis = AX0 ? 0 : a.axis;
+  const int md = axis == 2 ? 2 : 1, od = axis == 2 ? 1 : 2;
+  const int64_t n = a.size[axis], mn = a.size[md], on = a.size[od];
+  const int64_t ap = a.in_pitch[axis];
+  const char* const ix = reinterpret_cast<const char*>(a.in) + x * a.in_pitch[0];
+  char* const ox = reinterpret_cast<char*>(a.out) + x * a.out_pitch[0];
+  for (int64_t o = blockIdx.z; o < on; o += gridDim.z) {
+    const char* const io = ix + o * a.in_pitch[od];
+    char* const oo = ox + o * a.out_pitch[od];
+    for (int64_t mb = (int64_t)blockIdx.y * RUN; mb < mn; mb += (int64_t)gridDim.y * RUN) {
+      const int nv = (int)(mn - mb < RUN ? mn - mb : RUN);
+      float acc[RUN];
+      if constexpr (AX0) {
+        // taps along x: offset and whether the tap lies in [0, n), shared by the RUN rows
+        const char* rows[RUN];
+#pragma unroll
+        for (int r = 0; r < RUN; ++r) {
+          acc[r] = 0.0f;
+          rows[r] = io + (mb + (r < nv ? r : 0)) * a.in_pitch[md];
+        }
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+          const int64_t sx = x - R + k;
+          if (sx >= 0 && sx < n) {
+            const int64_t off = (sx - x) * ap;
+#pragma unroll
+            for (int r = 0; r < RUN; ++r)
+              acc[r] = fmaf(T.w[k], __ldg(reinterpret_cast<const float*>(rows[r] + off)), acc[r]);
+          }
+        }
+      } else {
+        float v[K + RUN - 1];  // ybar at mb - R .. mb + RUN - 1 + R, zero outside the image
+#pragma unroll
+        for (int j = 0; j < K + RUN - 1; ++j) {
+          const int64_t s = mb - R + j;
+          v[j] = (s >= 0 && s < n) ? __ldg(reinterpret_cast<const float*>(io + s * ap)) : 0.0f;
+        }
+#pragma unroll
+        for (int r = 0; r < RUN; ++r) {
+          acc[r] = 0.0f;
+#pragma unroll
+          for (int k = 0; k < K; ++k) acc[r] = fmaf(T.w[k], v[r + k], acc[r]);
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < RUN; ++r) {
+        if (r >= nv) break;
+        const int64_t m = mb + r;
+        const int64_t i = AX0 ? x : m;  // position along the pass axis
+        float res = acc[r];
+        if (i == 0 || i == n - 1) {  // the taps the forward clamped onto the edge voxels
+          const char* const line = AX0 ? io + m * a.in_pitch[md] - x * ap : io;
+          if (i == 0)
+            for (int d = 0; d < R && d < n; ++d)
+              res = fmaf(T.aux[R - 1 - d], *reinterpret_cast<const float*>(line + d * ap), res);
+          if (i == n - 1)
+            for (int d = 0; d < R && d < n; ++d)
+              res = fmaf(T.aux[R - 1 - d], *reinterpret_cast<const float*>(line + (n - 1 - d) * ap), res);
+        }
+        float* const po = reinterpret_cast<float*>(oo + m * a.out_pitch[md]);
+        *po = a.accumulate ? *po + res : res;
+      }
+    }
+  }
+}
+
+template <int R, int RUN, bool AX0>
+__global__ void __launch_bounds__(kThreads, 2) k_dual_small(const VjpAxisArgs a, const Taps T) {
+  constexpr int K = 2 * R + 1;
+  const int64_t x = (int64_t)blockIdx.x * kThreads + threadIdx.x;
+  if (x >= a.size[0]) return;
+  const int axis = AX0 ? 0 : a.axis;
+  const int md = axis == 2 ? 2 : 1, od = axis == 2 ? 1 : 2;
+  const int64_t n = a.size[axis], mn = a.size[md], on = a.size[od];
+  const int64_t ap = a.in_pitch[axis];
+  const bool has_d = a.din != nullptr;
+  const int64_t dbase = has_d ? reinterpret_cast<const char*>(a.din) - reinterpret_cast<const char*>(a.in) : 0;
+  const char* const ix = reinterpret_cast<const char*>(a.in) + x * a.in_pitch[0];
+  const int64_t oxo = x * a.out_pitch[0];
+  for (int64_t o = blockIdx.z; o < on; o += gridDim.z) {
+    const char* const io = ix + o * a.in_pitch[od];
+    const int64_t oo = oxo + o * a.out_pitch[od];
+    for (int64_t mb = (int64_t)blockIdx.y * RUN; mb < mn; mb += (int64_t)gridDim.y * RUN) {
+      const int nv = (int)(mn - mb < RUN ? mn - mb : RUN);
+      float v[RUN], dv[RUN];
+      if constexpr (AX0) {
+        // clamped taps along x, shared by the RUN rows
+        const char* rows[RUN];
+#pragma unroll
+        for (int r = 0; r < RUN; ++r) {
+          v[r] = 0.0f;
+          dv[r] = 0.0f;
+          rows[r] = io + (mb + (r < nv ? r : 0)) * a.in_pitch[md];
+        }
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+          int64_t sx = x + k - R;
+          sx = sx < 0 ? 0 : (sx >= n ? n - 1 : sx);
+          const int64_t off = (sx - x) * ap;
+#pragma unroll
+          for (int r = 0; r < RUN; ++r) {
+            const float xv = __ldg(reinterpret_cast<const float*>(rows[r] + off));
+            v[r] = fmaf(T.w[k], xv, v[r]);
+            dv[r] = fmaf(T.aux[k], xv, dv[r]);
+            if (has_d) dv[r] = fmaf(T.w[k], __ldg(reinterpret_cast<const float*>(rows[r] + dbase + off)), dv[r]);
+          }
+        }
+      } else {
+        // positions mb - R .. mb + RUN - 1 + R clamped to [0, n - 1] and, beyond the
+        // last valid output's taps, to its last tap
+        const int64_t top = mb + nv - 1 + R < n - 1 ? mb + nv - 1 + R : n - 1;
+        float w[K + RUN - 1], dw[K + RUN - 1];
+#pragma unroll
+        for (int j = 0; j < K + RUN - 1; ++j) {
+          int64_t s = mb - R + j;
+          s = s < 0 ? 0 : (s > top ? top : s);
+          w[j] = __ldg(reinterpret_cast<const float*>(io + s * ap));
+          dw[j] = has_d ? __ldg(reinterpret_cast<const float*>(io + dbase + s * ap)) : 0.0f;
+        }
+#pragma unroll
+        for (int r = 0; r < RUN; ++r) {
+          v[r] = 0.0f;
+          dv[r] = 0.0f;
+#pragma unroll
+          for (int k = 0; k < K; ++k) {
+            v[r] = fmaf(T.w[k], w[r + k], v[r]);
+            dv[r] = fmaf(T.aux[k], w[r + k], dv[r]);
+            if (has_d) dv[r] = fmaf(T.w[k], dw[r + k], dv[r]);
+          }
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < RUN; ++r) {
+        if (r >= nv) break;
+        const int64_t off = oo + (mb + r) * a.out_pitch[md];
+        *reinterpret_cast<float*>(reinterpret_cast<char*>(a.out) + off) = v[r];
+        *reinterpret_cast<float*>(reinterpret_cast<char*>(a.dout) + off) = dv[r];
+      }
+    }
+  }
+}
+
+using VjpFn = void (*)(const VjpAxisArgs, const Taps);
+constexpr int kAdjRun = 4, kDualRun = 2;
+struct VjpPair {
+  VjpFn ax0, ax12;  // passes along x; along y or z
+};
+template <int R>
+constexpr VjpPair adj_fn() { return {k_adjoint_small<R, kAdjRun, true>, k_adjoint_small<R, kAdjRun, false>}; }
+template <int R>
+constexpr VjpPair dual_fn() { return {k_dual_small<R, kDualRun, true>, k_dual_small<R, kDualRun, false>}; }
+#define ITKG_VJP_TABLE(F)                                                                                    \
+  {{nullptr, nullptr}, F<1>(), F<2>(),  F<3>(),  F<4>(),  F<5>(),  F<6>(),  F<7>(),  F<8>(),  F<9>(),  F<10>(), \
+   F<11>(), F<12>(), F<13>(), F<14>(), F<15>(), F<16>(), F<17>(), F<18>(), F<19>(), F<20>(), F<21>(), F<22>(),   \
+   F<23>(), F<24>()}
+const VjpPair kAdjSmall[kMaxSmallVjpR + 1] = ITKG_VJP_TABLE(adj_fn);
+const VjpPair kDualSmall[kMaxSmallVjpR + 1] = ITKG_VJP_TABLE(dual_fn);
+#undef ITKG_VJP_TABLE
+
+dim3 grid_small(const VjpAxisArgs& a, int run) {
+  const int md = a.axis == 2 ? 2 : 1, od = a.axis == 2 ? 1 : 2;
+  const int64_t gx = (a.size[0] + kThreads - 1) / kThreads;
+  const int64_t gy = (a.size[md] + run - 1) / run;
+  return dim3((unsigned)gx, (unsigned)(gy < 65535 ? gy : 65535), (unsigned)(a.size[od] < 65535 ? a.size[od] : 65535));
+}
+
 // Per-block f64 partial sums of sum(p * q) over a pitched image.
 __global__ void __launch_bounds__(kThreads) k_dot_partials(const DotArgs d, double* partials) {
   const int64_t nx = d.size[0], nxy = d.size[0] * d.size[1];
@@ -117,22 +296,40 @@ __global__ void __launch_bounds__(kThreads) k_dot_partials(const DotArgs d, doub
 // Squared-error loss against a target t, per voxel: d = y - t,
 // ybar = 2 d (written densely), and per-block f64 partials of sum d^2 and of
 // sum ybar * dy (the sigma gradient).  partials: [nblocks] loss, [nblocks] sigma.
+// Block b takes a contiguous run of the image's rows (x lines); a thread sums
+// its voxels' products in f32 for up to 8 rows at a time and folds them into
+// f64 (f64 arithmetic on this GPU is scarce; the f32 runs keep each partial's
+// relative error near 1e-7).
 __global__ void __launch_bounds__(kThreads) k_sqerr(const float* __restrict__ y,
                                                      const float* __restrict__ dy, const DotArgs t,
                                                      float* __restrict__ ybar, double* partials) {
-  const int64_t nx = t.size[0], nxy = t.size[0] * t.size[1];
-  const int64_t n = nxy * t.size[2];
+  const int64_t nx = t.size[0], ny = t.size[1];
+  const int64_t rows = ny * t.size[2];
+  const int64_t r0 = rows * blockIdx.x / gridDim.x, r1 = rows * (blockIdx.x + 1) / gridDim.x;
   double sl = 0.0, ss = 0.0;
-  for (int64_t i = (int64_t)blockIdx.x * kThreads + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * kThreads) {
-    const int64_t x = i % nx, yy = (i / nx) % t.size[1], z = i / nxy;
-    const float tv = *reinterpret_cast<const float*>(px(t.q, t.q_pitch, x, yy, z));
-    const float d = y[i] - tv;
-    const float g = 2.0f * d;
-    ybar[i] = g;
-    sl += (double)d * (double)d;
-    if (dy) ss += (double)g * (double)dy[i];
+  float fl = 0.0f, fs = 0.0f;
+  int run = 0;
+  for (int64_t row = r0; row < r1; ++row) {
+    const int64_t yy = row % ny, z = row / ny;
+    const char* const trow = reinterpret_cast<const char*>(t.q) + yy * t.q_pitch[1] + z * t.q_pitch[2];
+    const int64_t base = row * nx;
+    for (int64_t x = threadIdx.x; x < nx; x += kThreads) {
+      const float tv = *reinterpret_cast<const float*>(trow + x * t.q_pitch[0]);
+      const float d = y[base + x] - tv;
+      const float g = 2.0f * d;
+      ybar[base + x] = g;
+      fl = fmaf(d, d, fl);
+      if (dy) fs = fmaf(g, dy[base + x], fs);
+    }
+    if (++run == 8) {
+      sl += (double)fl;
+      ss += (double)fs;
+      fl = fs = 0.0f;
+      run = 0;
+    }
   }
+  sl += (double)fl;
+  ss += (double)fs;
   __shared__ double red[2][kThreads];
   red[0][threadIdx.x] = sl;
   red[1][threadIdx.x] = ss;
@@ -192,16 +389,28 @@ itkg_status launch_adjoint_axis(const VjpAxisArgs& a, const float* w, const floa
                                 void* stream) {
   if (2 * a.radius + 1 > kMaxVjpTaps)
     return set_error(ITKG_ERROR_UNSUPPORTED, "VJP radius %d exceeds %d", a.radius, (kMaxVjpTaps - 1) / 2);
-  k_adjoint_axis<<<grid_for(a), kThreads, 0, static_cast<cudaStream_t>(stream)>>>(
-      a, make_taps(w, prefix, 2 * a.radius + 1));
+  const Taps T = make_taps(w, prefix, 2 * a.radius + 1);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (a.radius >= 1 && a.radius <= kMaxSmallVjpR && a.size[0] <= INT32_MAX) {
+    const VjpFn fn = a.axis == 0 ? kAdjSmall[a.radius].ax0 : kAdjSmall[a.radius].ax12;
+    fn<<<grid_small(a, kAdjRun), kThreads, 0, s>>>(a, T);
+    return launched("adjoint_axis_f32");
+  }
+  k_adjoint_axis<<<grid_for(a), kThreads, 0, s>>>(a, T);
   return launched("adjoint_axis_f32");
 }
 
 itkg_status launch_dual_axis(const VjpAxisArgs& a, const float* w, const float* dw, void* stream) {
   if (2 * a.radius + 1 > kMaxVjpTaps)
     return set_error(ITKG_ERROR_UNSUPPORTED, "VJP radius %d exceeds %d", a.radius, (kMaxVjpTaps - 1) / 2);
-  k_dual_axis<<<grid_for(a), kThreads, 0, static_cast<cudaStream_t>(stream)>>>(
-      a, make_taps(w, dw, 2 * a.radius + 1));
+  const Taps T = make_taps(w, dw, 2 * a.radius + 1);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (a.radius >= 1 && a.radius <= kMaxSmallVjpR && a.size[0] <= INT32_MAX) {
+    const VjpFn fn = a.axis == 0 ? kDualSmall[a.radius].ax0 : kDualSmall[a.radius].ax12;
+    fn<<<grid_small(a, kDualRun), kThreads, 0, s>>>(a, T);
+    return launched("dual_axis_f32");
+  }
+  k_dual_axis<<<grid_for(a), kThreads, 0, s>>>(a, T);
   return launched("dual_axis_f32");
 }
 
