@@ -288,6 +288,71 @@ def recursive_gaussian_f32(img, sigma, spacing=None, axis=-1, requested=None, in
     return _crop(full, requested, index).astype(np.float32)
 
 
+REC_GRADIENT_MAGNITUDE, REC_LAPLACIAN, REC_DERIVATIVE, REC_GRADIENT, REC_HESSIAN = 0, 1, 2, 3, 4
+
+
+def recursive_derivative(img, sigma, kind, spacing=None, axis=0, order=1, requested=None, index=None):
+    """The derivative users of RecursiveGaussianFilter (edges.rs:686-950): the
+    smoothed image is RecursiveGaussianFilter::generate_region(requested) in the
+    input's pixel type (f32 or u8), then a central-difference stencil clamped to
+    the requested region's bounds (the smoothed image is the stencil's whole
+    source), in f64 with every operation rounded in the reference's order:
+      GRADIENT_MAGNITUDE  sqrt(sum_a ((s[+1] - s[-1]) / (2 h_a))^2)      (edges.rs:162-189)
+      LAPLACIAN           sum_a ((s[+1] - 2 s[0]) + s[-1]) / (h_a h_a)    (edges.rs:219-247)
+      DERIVATIVE          order 1 or 2 of the above along `axis`, else 0  (edges.rs:48-78)
+      GRADIENT            per axis (s[+1] - s[-1]) / (2 h_a) as f32      (edges.rs:848-877)
+      HESSIAN (2-D)       [h00, h11, h01] as f32                          (edges.rs:920-950)
+    Returns the output array (pixel type for the first three, f32 components last axis otherwise)."""
+    x = np.asarray(img)
+    D = x.ndim
+    sp = list(spacing) if spacing is not None else [1.0] * D
+    full = recursive_gaussian_f64(x, sigma, sp)
+    sm = _crop(full, requested, index)
+    sm = from_f64_u8(sm).astype(np.float64) if x.dtype == np.uint8 else sm.astype(np.float32).astype(np.float64)
+
+    def shifted(a, ax_ref, off):  # a[clamp(i + off)] along reference axis ax_ref, clamped to the array
+        ax = D - 1 - ax_ref
+        n = a.shape[ax]
+        idx = np.clip(np.arange(n) + off, 0, n - 1)
+        return np.take(a, idx, axis=ax)
+
+    def pixel_out(v):
+        return from_f64_u8(v) if x.dtype == np.uint8 else v.astype(np.float32)
+
+    if kind == REC_GRADIENT_MAGNITUDE:
+        mag2 = np.zeros_like(sm)
+        for a in range(D):
+            d = (shifted(sm, a, 1) - shifted(sm, a, -1)) / (2.0 * sp[a])
+            mag2 = mag2 + d * d
+        return pixel_out(np.sqrt(mag2))
+    if kind == REC_LAPLACIAN:
+        lap = np.zeros_like(sm)
+        for a in range(D):
+            lap = lap + ((shifted(sm, a, 1) - 2.0 * sm) + shifted(sm, a, -1)) / (sp[a] * sp[a])
+        return pixel_out(lap)
+    if kind == REC_DERIVATIVE:
+        if order == 1:
+            v = (shifted(sm, axis, 1) - shifted(sm, axis, -1)) / (2.0 * sp[axis])
+        elif order == 2:
+            v = ((shifted(sm, axis, 1) - 2.0 * sm) + shifted(sm, axis, -1)) / (sp[axis] * sp[axis])
+        else:
+            v = np.zeros_like(sm)
+        return pixel_out(v)
+    if kind == REC_GRADIENT:
+        comps = [((shifted(sm, a, 1) - shifted(sm, a, -1)) / (2.0 * sp[a])).astype(np.float32) for a in range(D)]
+        return np.stack(comps, axis=-1)
+    if kind == REC_HESSIAN:
+        if D != 2:
+            raise ValueError("the Hessian filter is 2-D")
+        hx, hy = sp[0], sp[1]
+        xp, xm = shifted(sm, 0, 1), shifted(sm, 0, -1)
+        h00 = ((xp - 2.0 * sm) + xm) / (hx * hx)
+        h11 = ((shifted(sm, 1, 1) - 2.0 * sm) + shifted(sm, 1, -1)) / (hy * hy)
+        h01 = (((shifted(xp, 1, 1) - shifted(xp, 1, -1)) - shifted(xm, 1, 1)) + shifted(xm, 1, -1)) / (4.0 * hx * hy)
+        return np.stack([h00.astype(np.float32), h11.astype(np.float32), h01.astype(np.float32)], axis=-1)
+    raise ValueError(f"unknown kind {kind}")
+
+
 def _crop(full, requested, index):
     if requested is None:
         return full

@@ -385,6 +385,86 @@ def main():
     cases.update(rec_case("rand3d_axis1_s0p3", rrng.random((5, 7, 6), dtype=np.float32), 0.3, axis=1))
     cases.update(rec_case("u8_2d_s2", rrng.integers(0, 256, (9, 11), dtype=np.uint8), 2.0))
     cases.update(rec_case("thin3d_s2", rrng.random((1, 6, 7), dtype=np.float32), 2.0))
+
+    # derivative users of RecursiveGaussianFilter (edges.rs:686-950): stencils on the
+    # smoothed image (pixel type of the input), clamped to the requested region
+    def rec_deriv_case(name, arr, sigma, kind, spacing=None, axis=0, order=1, requested=None):
+        D = arr.ndim
+        spacing = spacing or [1.0] * D
+        img = to_ref(arr)
+        vals = recursive_region(img, spacing, sigma)
+        ri, rs = requested if requested else (img[0], img[1])
+        full_idx, full_size = img[0], img[1]
+        def u8_from_f64(v):  # pixel.rs:36: round half away from zero, clamp, NaN -> 0
+            if v != v:
+                return 0.0
+            a = abs(v)
+            r = (math.floor(a) + (1.0 if a - math.floor(a) >= 0.5 else 0.0)) * (1.0 if v >= 0 else -1.0)
+            return float(min(max(r, 0.0), 255.0))
+
+        conv = u8_from_f64 if arr.dtype == np.uint8 else (lambda v: float(np.float32(v)))
+        sm = {tuple(p): conv(vals[flat_index(full_idx, full_size, p)]) for p in iter_region(ri, rs)}
+
+        def get(p, a, off):
+            q = list(p)
+            q[a] = min(max(p[a] + off, ri[a]), ri[a] + rs[a] - 1)
+            return sm[tuple(q)]
+
+        out = []
+        for p in iter_region(ri, rs):
+            p = tuple(p)
+            if kind == 0:
+                mag2 = 0.0
+                for a in range(D):
+                    dd = (get(p, a, 1) - get(p, a, -1)) / (2.0 * spacing[a])
+                    mag2 += dd * dd
+                out.append([math.sqrt(mag2)])
+            elif kind == 1:
+                lap = 0.0
+                for a in range(D):
+                    lap += (get(p, a, 1) - 2.0 * get(p, a, 0) + get(p, a, -1)) / (spacing[a] * spacing[a])
+                out.append([lap])
+            elif kind == 2:
+                h = spacing[axis]
+                v = ((get(p, axis, 1) - get(p, axis, -1)) / (2.0 * h) if order == 1 else
+                     (get(p, axis, 1) - 2.0 * get(p, axis, 0) + get(p, axis, -1)) / (h * h) if order == 2 else 0.0)
+                out.append([v])
+            elif kind == 3:
+                out.append([(get(p, a, 1) - get(p, a, -1)) / (2.0 * spacing[a]) for a in range(D)])
+            else:
+                hx, hy = spacing
+                x0, y0 = p
+
+                def g2(xi, yi):
+                    return sm[(min(max(xi, ri[0]), ri[0] + rs[0] - 1), min(max(yi, ri[1]), ri[1] + rs[1] - 1))]
+                h00 = (g2(x0 + 1, y0) - 2.0 * g2(x0, y0) + g2(x0 - 1, y0)) / (hx * hx)
+                h11 = (g2(x0, y0 + 1) - 2.0 * g2(x0, y0) + g2(x0, y0 - 1)) / (hy * hy)
+                h01 = (g2(x0 + 1, y0 + 1) - g2(x0 + 1, y0 - 1) - g2(x0 - 1, y0 + 1) + g2(x0 - 1, y0 - 1)) / (4.0 * hx * hy)
+                out.append([h00, h11, h01])
+        vec = kind >= 3
+        shape = tuple(reversed(rs)) + ((len(out[0]),) if vec else ())
+        if vec:
+            res = np.array(out, dtype=np.float64).astype(np.float32).reshape(shape)
+        elif arr.dtype == np.uint8:
+            res = np.array([conv(o[0]) for o in out], dtype=np.float64).astype(np.uint8).reshape(shape)
+        else:
+            res = np.array([o[0] for o in out], dtype=np.float64).astype(np.float32).reshape(shape)
+        return {f"recd_{name}__in": arr, f"recd_{name}__out": res,
+                f"recd_{name}__meta": np.array([sigma, kind, axis, order] + list(spacing) + list(ri) + list(rs),
+                                               dtype=np.float64)}
+
+    d2 = rrng.random((11, 13), dtype=np.float32)
+    d3 = (rrng.standard_normal((6, 7, 8)) * 3).astype(np.float32)
+    cases.update(rec_deriv_case("gm2d", d2, 1.5, 0))
+    cases.update(rec_deriv_case("gm3d_sub", d3, 1.2, 0, spacing=[0.8, 1.0, 1.5], requested=([1, 2, 1], [5, 4, 3])))
+    cases.update(rec_deriv_case("lap2d", d2, 2.0, 1, spacing=[0.7, 1.3]))
+    cases.update(rec_deriv_case("deriv3d_o1_a2", d3, 1.0, 2, axis=2, order=1))
+    cases.update(rec_deriv_case("deriv2d_o2_a0_sub", d2, 1.7, 2, axis=0, order=2, requested=([3, 2], [6, 7])))
+    cases.update(rec_deriv_case("deriv2d_o3", d2, 1.7, 2, axis=1, order=3))
+    cases.update(rec_deriv_case("grad3d", d3, 1.4, 3, spacing=[1.0, 0.5, 2.0]))
+    cases.update(rec_deriv_case("hess2d", d2, 1.1, 4, spacing=[0.9, 1.2]))
+    cases.update(rec_deriv_case("hess2d_sub", d2, 1.1, 4, requested=([2, 3], [7, 6])))
+    cases.update(rec_deriv_case("gm_u8_2d", rrng.integers(0, 256, (9, 10), dtype=np.uint8), 1.5, 0))
     # kernels
     for s, sp in [(1.5, 1.0), (2.0, 1.0), (1.5, 0.7), (1.5, 2.5), (0.5, 1.0), (8.0, 1.0)]:
         cases[f"kernel_{s}_{sp}"] = np.array(build_kernel(s / sp, kernel_radius(s, sp)),

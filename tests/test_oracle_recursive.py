@@ -77,3 +77,40 @@ def test_u8_output_conversion():
     """u8::from_f64 (pixel.rs:36): round half away from zero, clamp, NaN -> 0."""
     v = np.array([0.49999999999999994, 0.5, 1.5, 2.5, -0.5, 255.5, np.nan, -3.0, 254.4])
     assert list(oracle.from_f64_u8(v)) == [0, 1, 2, 3, 0, 255, 0, 0, 254]
+
+
+RECD = ["gm2d", "gm3d_sub", "lap2d", "deriv3d_o1_a2", "deriv2d_o2_a0_sub", "deriv2d_o3", "grad3d", "hess2d",
+        "hess2d_sub", "gm_u8_2d"]
+
+
+def recd_meta(golden, name):
+    m = golden[f"recd_{name}__meta"]
+    x = golden[f"recd_{name}__in"]
+    D = x.ndim
+    sigma, kind, axis, order = float(m[0]), int(m[1]), int(m[2]), int(m[3])
+    sp = [float(v) for v in m[4:4 + D]]
+    ri = tuple(int(v) for v in m[4 + D:4 + 2 * D])
+    rs = tuple(int(v) for v in m[4 + 2 * D:4 + 3 * D])
+    return x, sigma, kind, axis, order, sp, (ri, rs)
+
+
+@pytest.mark.parametrize("name", RECD)
+def test_recursive_derivative_oracle_matches_golden(golden, name):
+    """The derivative users (edges.rs:686-950) against the pure-Python transcription."""
+    x, sigma, kind, axis, order, sp, req = recd_meta(golden, name)
+    got = oracle.recursive_derivative(x, sigma, kind, sp, axis, order, requested=req)
+    want = golden[f"recd_{name}__out"]
+    assert got.shape == want.shape
+    if want.dtype == np.uint8:
+        assert np.array_equal(got, want)
+    else:
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+def test_recursive_derivative_of_a_ramp():
+    """The first derivative is the central difference of the smoothed image, in f64."""
+    x = np.tile(np.arange(16, dtype=np.float32) * 0.5, (12, 1))
+    g = oracle.recursive_derivative(x, 0.5, oracle.REC_DERIVATIVE, axis=0, order=1)
+    sm = oracle.recursive_gaussian_f32(x, 0.5)
+    want = (sm[:, 2:].astype(np.float64) - sm[:, :-2]) / 2.0
+    assert np.array_equal(g[:, 1:-1], want.astype(np.float32))
