@@ -285,6 +285,37 @@ itkg_status itkg_recursive_gaussian_generate_region(const itkg_image *input, con
                                                     const itkg_recursive_params *params,
                                                     itkg_image *output, void *stream);
 
+/* The derivative users of RecursiveGaussianFilter (edges.rs:686-950): the
+ * smoothed image RecursiveGaussianFilter::generate_region(requested), in the
+ * input's pixel type (f32 or u8), then a central-difference stencil clamped to
+ * the requested region (the smoothed image is the stencil's whole source),
+ * in f64 with every operation rounded in the reference's order.
+ *   kind                                  output
+ *   ITKG_REC_GRADIENT_MAGNITUDE  (686-722) pixel type, 1 component
+ *   ITKG_REC_LAPLACIAN           (730-766) pixel type, 1 component
+ *   ITKG_REC_DERIVATIVE          (772-810) pixel type; `axis`, `order` (1, 2; else 0)
+ *   ITKG_REC_GRADIENT            (819-878) f32, dim components (VecPixel<f32, D>)
+ *   ITKG_REC_HESSIAN             (892-950) 2-D only; f32, 3 components (h00, h11, h01)
+ * sigma, rounding: as for itkg_recursive_gaussian_generate_region. */
+#define ITKG_REC_GRADIENT_MAGNITUDE 0
+#define ITKG_REC_LAPLACIAN 1
+#define ITKG_REC_DERIVATIVE 2
+#define ITKG_REC_GRADIENT 3
+#define ITKG_REC_HESSIAN 4
+typedef struct itkg_recursive_derivative_params {
+    double sigma;
+    int32_t kind;
+    int32_t axis;
+    int32_t order;
+    int32_t rounding;
+    int32_t reserved[2]; /* 0 */
+} itkg_recursive_derivative_params;
+
+itkg_status itkg_recursive_gaussian_derivative_generate_region(const itkg_image *input, const itkg_region *largest,
+                                                               const itkg_region *requested,
+                                                               const itkg_recursive_derivative_params *params,
+                                                               itkg_image *output, void *stream);
+
 /* ---- derivatives (not in the reference: it has no VJP) ---------------------
  * Vector-Jacobian product of GaussianFilter over a whole image: x is the
  * filter input (requested region = largest region = x->region), ybar = dL/dy

@@ -600,6 +600,8 @@ static itkg_status generate_region(const itkg_image* input, const itkg_region* l
                                    const itkg_gaussian_params* prm, const itkg_image* output, cudaStream_t s) {
   ITKG_TRY(validate_image(input, "input"));
   ITKG_TRY(validate_image(output, "output"));
+  ITKG_TRY(filter_components(input, "input"));
+  ITKG_TRY(filter_components(output, "output"));
   ITKG_TRY(check_params(prm));
   KernelSpec gauss;
   gauss.sigma = prm->sigma;
@@ -814,8 +816,8 @@ itkg_status itkg_stream_synchronize(void* stream) {
 itkg_status itkg_image_alloc_device(itkg_image* img, int32_t dim, int32_t dtype, int32_t components,
                                     const itkg_region* region, const double* spacing,
                                     const double* origin) {
-  if (!img || !region || dim < 1 || dim > kMaxDim || dtype_size(dtype) == 0 ||
-      (components != 1 && components != 3))
+  if (!img || !region || dim < 1 || dim > kMaxDim || dtype_size(dtype) == 0 || components < 1 ||
+      components > 3)
     return set_error(ITKG_ERROR_INVALID_ARGUMENT, "bad argument");
   std::memset(img, 0, sizeof *img);
   img->dim = dim;
@@ -934,6 +936,79 @@ itkg_status itkg_recursive_gaussian_generate_region(const itkg_image* input, con
   return st;
 }
 
+itkg_status itkg_recursive_gaussian_derivative_generate_region(const itkg_image* input, const itkg_region* largest,
+                                                               const itkg_region* requested,
+                                                               const itkg_recursive_derivative_params* params,
+                                                               itkg_image* output, void* stream) {
+  ITKG_TRY(validate_image(input, "input"));
+  if (!output) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "output is NULL");
+  if (!params) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "params is NULL");
+  if (!largest || !requested) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "region is NULL");
+  const int D = input->dim;
+  const int kind = params->kind;
+  if (kind < ITKG_REC_GRADIENT_MAGNITUDE || kind > ITKG_REC_HESSIAN)
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "unknown kind %d", kind);
+  if (kind == ITKG_REC_HESSIAN && D != 2)
+    return set_error(ITKG_ERROR_UNSUPPORTED, "the Hessian filter is 2-D (edges.rs:905)");
+  if (kind == ITKG_REC_DERIVATIVE && (params->axis < 0 || params->axis >= D))
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "axis %d outside [0, %d)", params->axis, D);
+  if (params->rounding != ITKG_ROUND_REFERENCE && params->rounding != ITKG_ROUND_FMA)
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "unknown rounding %d", params->rounding);
+  if (params->reserved[0] != 0 || params->reserved[1] != 0)
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "reserved must be 0");
+  if (input->components != 1 || (input->dtype != ITKG_F32 && input->dtype != ITKG_U8))
+    return set_error(ITKG_ERROR_UNSUPPORTED, "the smoothed image is scalar f32 or u8 (its NumericPixel)");
+  // the output: the pixel type for the scalar filters, f32 vectors for the gradient and the Hessian
+  const int want_dtype = kind <= ITKG_REC_DERIVATIVE ? input->dtype : ITKG_F32;
+  const int want_comps = kind <= ITKG_REC_DERIVATIVE ? 1 : (kind == ITKG_REC_GRADIENT ? D : 3);
+  if (output->dim != D || output->dtype != want_dtype || output->components != want_comps)
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "output must be dim %d, dtype %d, %d component(s)", D, want_dtype,
+                     want_comps);
+  if (output->location != ITKG_DEVICE && output->location != ITKG_HOST)
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "output: unknown location");
+  if (output->pitch[0] != (int64_t)want_comps * dtype_size(want_dtype))
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "output: pitch[0] must equal the pixel size");
+  for (int d = 1; d < D; ++d)
+    if (output->pitch[d] <= 0) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "output: pitch[%d] invalid", d);
+  if (region_len(*requested, D) == 0) return ITKG_SUCCESS;
+  if (!output->data) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "output: data is NULL");
+  if (!region_contains(*largest, *requested, D))
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "requested region lies outside the largest region");
+  if (!region_contains(output->region, *requested, D))
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "output buffer does not contain the requested region");
+  if (!region_contains(input->region, *largest, D))
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "input buffer does not cover the largest region");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const bool host_in = input->location == ITKG_HOST, host_out = output->location == ITKG_HOST;
+  itkg_image din = *input, dout = *output;
+  void* pin = nullptr;
+  void* pout = nullptr;
+  itkg_status st = ITKG_SUCCESS;
+  if (host_in) {
+    din.location = ITKG_DEVICE;
+    din.region = *largest;
+    dense_layout(&din, 16);
+    st = scratch_alloc(&pin, image_bytes(din), s);
+    din.data = pin;
+    if (st == ITKG_SUCCESS) st = copy_region(din, *input, *largest, s);
+  }
+  if (st == ITKG_SUCCESS && host_out) {
+    dout.location = ITKG_DEVICE;
+    dout.region = *requested;
+    dense_layout(&dout, 16);
+    st = scratch_alloc(&pout, image_bytes(dout), s);
+    dout.data = pout;
+  }
+  if (st == ITKG_SUCCESS)
+    st = launch_recursive_derivative(din, *largest, *requested, params->sigma, kind, params->axis, params->order,
+                                     params->rounding, dout, s);
+  if (st == ITKG_SUCCESS && host_out) st = copy_region(*output, dout, *requested, s);
+  scratch_free(pin, s);
+  scratch_free(pout, s);
+  if (st == ITKG_SUCCESS && (host_in || host_out)) ITKG_CUDA(cudaStreamSynchronize(s));
+  return st;
+}
+
 itkg_status itkg_separable_input_region_for_output(const itkg_region* output_region,
                                                    const itkg_region* largest, int32_t dim,
                                                    const uint64_t* radius, uint64_t repetitions,
@@ -987,6 +1062,8 @@ itkg_status itkg_stream_full(const itkg_image* input, const itkg_region* largest
                              itkg_image* output, void* stream) {
   ITKG_TRY(validate_image(input, "input"));
   ITKG_TRY(validate_image(output, "output"));
+  ITKG_TRY(filter_components(input, "input"));
+  ITKG_TRY(filter_components(output, "output"));
   if (!largest) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "largest is NULL");
   const int D = input->dim;
   if (!region_contains(output->region, *largest, D))

@@ -149,6 +149,7 @@ itkg_status choose_algorithm(const itkg_batch::Fwd& f, bool tune, cudaStream_t s
 
 itkg_status check_device_item(const itkg_image* im, const char* name) {
   ITKG_TRY(validate_image(im, name));
+  ITKG_TRY(filter_components(im, name));
   if (im->location != ITKG_DEVICE)
     return set_error(ITKG_ERROR_INVALID_ARGUMENT, "%s: batch items take device buffers", name);
   return ITKG_SUCCESS;

@@ -111,8 +111,8 @@ inline itkg_status validate_image(const itkg_image* im, const char* name) {
     return set_error(ITKG_ERROR_INVALID_ARGUMENT, "%s: dim %d not in 1..3", name, im->dim);
   if (dtype_size(im->dtype) == 0)
     return set_error(ITKG_ERROR_INVALID_ARGUMENT, "%s: unknown dtype %d", name, im->dtype);
-  if (im->components != 1 && im->components != 3)
-    return set_error(ITKG_ERROR_UNSUPPORTED, "%s: components must be 1 or 3", name);
+  if (im->components < 1 || im->components > 3)
+    return set_error(ITKG_ERROR_UNSUPPORTED, "%s: components must be 1, 2 or 3", name);
   if (im->location != ITKG_DEVICE && im->location != ITKG_HOST)
     return set_error(ITKG_ERROR_INVALID_ARGUMENT, "%s: unknown location", name);
   const int64_t pb = (int64_t)im->components * dtype_size(im->dtype);
@@ -124,6 +124,14 @@ inline itkg_status validate_image(const itkg_image* im, const char* name) {
       return set_error(ITKG_ERROR_INVALID_ARGUMENT, "%s: pitch[%d] invalid", name, d);
   if (!im->data && region_len(im->region, im->dim) != 0)
     return set_error(ITKG_ERROR_INVALID_ARGUMENT, "%s: data is NULL", name);
+  return ITKG_SUCCESS;
+}
+
+// The smoothing filters take scalar pixels or VecPixel<_, 3> (2-component
+// images exist as the gradient filter's output only).
+inline itkg_status filter_components(const itkg_image* im, const char* name) {
+  if (im->components != 1 && im->components != 3)
+    return set_error(ITKG_ERROR_UNSUPPORTED, "%s: components must be 1 or 3", name);
   return ITKG_SUCCESS;
 }
 

@@ -170,6 +170,12 @@ itkg_status launch_vjp_two_pass(const VjpTwoPass& v, void* stream, bool dry_run)
 void yvv_coeffs(double sigma, double out[4]);
 itkg_status launch_recursive(const itkg_image& in, const itkg_region& largest, const itkg_region& requested,
                              double sigma, int axis, int rounding, const itkg_image& out, void* stream);
+// Its derivative users: smoothing of `requested` in the input's pixel type,
+// then the `kind` stencil (0 gradient magnitude, 1 Laplacian, 2 derivative,
+// 3 gradient, 4 2-D Hessian) into `out`.
+itkg_status launch_recursive_derivative(const itkg_image& in, const itkg_region& largest,
+                                        const itkg_region& requested, double sigma, int kind, int axis, int order,
+                                        int rounding, const itkg_image& out, void* stream);
 
 // Bumps the launch counter by n (graph replays).
 void note_launches(uint64_t n, const char* name);

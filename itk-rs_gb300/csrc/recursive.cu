@@ -104,9 +104,8 @@ __global__ void __launch_bounds__(kT) k_rec_lines(T* d, RecGeom g, int axis, T B
 }
 
 __device__ __forceinline__ float out_f32(double v) { return __double2float_rn(v); }
-template <typename T>
-__device__ __forceinline__ uint8_t out_u8(T v) {  // round half away from zero, clamp, NaN -> 0
-  double r = round((double)v);
+__device__ __forceinline__ uint8_t out_u8_of(double v) {  // round half away from zero, clamp, NaN -> 0
+  double r = round(v);
   r = fmin(fmax(r, 0.0), 255.0);
   return (uint8_t)r;
 }
@@ -122,8 +121,78 @@ __global__ void __launch_bounds__(kT) k_rec_store(const T* d, RecGeom g, int64_t
       const int64_t x = r0 + i, y = r1 + j, z = r2 + k;  // absolute
       const T v = d[((z - g.lo[2]) * g.n[1] + (y - g.lo[1])) * g.n[0] + (x - g.lo[0])];
       char* p = dst + (x - do0) * dp0 + (y - do1) * dp1 + (z - do2) * dp2;
-      if (OUT == ITKG_U8) *reinterpret_cast<uint8_t*>(p) = out_u8(v);
+      if (OUT == ITKG_U8) *reinterpret_cast<uint8_t*>(p) = out_u8_of((double)v);
       else *reinterpret_cast<float*>(p) = out_f32(v);
+    }
+}
+
+// The derivative users (edges.rs:686-950): stencils on the smoothed image `s`
+// (a dense image of the requested region, m0 x m1 x m2, in the input's pixel
+// type), clamped to that region, in f64 with every operation rounded in the
+// reference's order.  kind: 0 gradient magnitude, 1 Laplacian, 2 derivative
+// (axis, order), 3 gradient (one f32 component per axis), 4 2-D Hessian
+// (f32 components h00, h11, h01).
+template <typename Tp>
+__device__ __forceinline__ double sval(const Tp* s, int64_t m0, int64_t m1, int64_t x, int64_t y, int64_t z) {
+  return (double)s[(z * m1 + y) * m0 + x];
+}
+
+template <typename Tp>
+__global__ void __launch_bounds__(kT) k_rec_deriv(const Tp* s, int64_t m0, int64_t m1, int64_t m2, int D, int kind,
+                                                   int axis, int order, double h0, double h1, double h2, char* dst,
+                                                   int64_t dp0, int64_t dp1, int64_t dp2, int out_u8) {
+  const int64_t x = (int64_t)blockIdx.x * kT + threadIdx.x;
+  if (x >= m0) return;
+  const int64_t m[3] = {m0, m1, m2};
+  const double h[3] = {h0, h1, h2};
+  for (int64_t z = blockIdx.z; z < m2; z += gridDim.z)
+    for (int64_t y = blockIdx.y; y < m1; y += gridDim.y) {
+      const int64_t p[3] = {x, y, z};
+      // s at p with coordinate a moved by off, clamped to the region
+      auto get = [&](int a, int off) {
+        int64_t q[3] = {p[0], p[1], p[2]};
+        q[a] = q[a] + off < 0 ? 0 : (q[a] + off >= m[a] ? m[a] - 1 : q[a] + off);
+        return sval(s, m0, m1, q[0], q[1], q[2]);
+      };
+      auto first = [&](int a) {  // (s[+1] - s[-1]) / (2 h)
+        return __ddiv_rn(__dsub_rn(get(a, 1), get(a, -1)), __dmul_rn(2.0, h[a]));
+      };
+      auto second = [&](int a) {  // ((s[+1] - 2 s[0]) + s[-1]) / (h h)
+        return __ddiv_rn(__dadd_rn(__dsub_rn(get(a, 1), __dmul_rn(2.0, get(a, 0))), get(a, -1)),
+                         __dmul_rn(h[a], h[a]));
+      };
+      char* const o = dst + x * dp0 + y * dp1 + z * dp2;
+      if (kind <= 2) {
+        double v = 0.0;
+        if (kind == 0) {
+          for (int a = 0; a < D; ++a) {
+            const double d = first(a);
+            v = __dadd_rn(v, __dmul_rn(d, d));
+          }
+          v = __dsqrt_rn(v);
+        } else if (kind == 1) {
+          for (int a = 0; a < D; ++a) v = __dadd_rn(v, second(a));
+        } else {
+          v = order == 1 ? first(axis) : (order == 2 ? second(axis) : 0.0);
+        }
+        if (out_u8) *reinterpret_cast<uint8_t*>(o) = out_u8_of(v);
+        else *reinterpret_cast<float*>(o) = __double2float_rn(v);
+      } else if (kind == 3) {
+        for (int a = 0; a < D; ++a) reinterpret_cast<float*>(o)[a] = __double2float_rn(first(a));
+      } else {
+        const double h00 = second(0), h11 = second(1);
+        auto g2 = [&](int dx, int dy) {
+          const int64_t xi = x + dx < 0 ? 0 : (x + dx >= m0 ? m0 - 1 : x + dx);
+          const int64_t yi = y + dy < 0 ? 0 : (y + dy >= m1 ? m1 - 1 : y + dy);
+          return sval(s, m0, m1, xi, yi, z);
+        };
+        const double num = __dadd_rn(__dsub_rn(__dsub_rn(g2(1, 1), g2(1, -1)), g2(-1, 1)), g2(-1, -1));
+        const double h01 = __ddiv_rn(num, __dmul_rn(__dmul_rn(4.0, h0), h1));
+        float* const f = reinterpret_cast<float*>(o);
+        f[0] = __double2float_rn(h00);
+        f[1] = __double2float_rn(h11);
+        f[2] = __double2float_rn(h01);
+      }
     }
 }
 
@@ -217,6 +286,56 @@ itkg_status launch_recursive(const itkg_image& in, const itkg_region& largest, c
   }
   scratch_free(buf, stream);
   if (st == ITKG_SUCCESS) set_last_kernel(ref ? "recursive_lines_f64" : "recursive_lines_f64_fma");
+  return st;
+}
+
+itkg_status launch_recursive_derivative(const itkg_image& in, const itkg_region& largest,
+                                        const itkg_region& requested, double sigma, int kind, int axis, int order,
+                                        int rounding, const itkg_image& out, void* stream) {
+  const int D = in.dim;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // the smoothed image: RecursiveGaussianFilter::generate_region(requested) in the input's pixel type
+  itkg_image sm;
+  std::memset(&sm, 0, sizeof sm);
+  sm.dim = D;
+  sm.dtype = in.dtype;
+  sm.components = 1;
+  sm.location = ITKG_DEVICE;
+  sm.region = requested;
+  int64_t m[3] = {1, 1, 1};
+  for (int d = 0; d < D; ++d) m[d] = (int64_t)requested.size[d], sm.spacing[d] = in.spacing[d];
+  const int64_t esz = in.dtype == ITKG_U8 ? 1 : 4;
+  sm.pitch[0] = esz;
+  sm.pitch[1] = esz * m[0];
+  sm.pitch[2] = esz * m[0] * m[1];
+  void* buf = nullptr;
+  {
+    const itkg_status sa = scratch_alloc(&buf, (size_t)(esz * m[0] * m[1] * m[2]), stream);
+    if (sa != ITKG_SUCCESS) return sa;
+  }
+  sm.data = buf;
+  itkg_status st = launch_recursive(in, largest, requested, sigma, -1, rounding, sm, stream);
+  if (st == ITKG_SUCCESS) {
+    double h[3] = {1.0, 1.0, 1.0};
+    for (int d = 0; d < D; ++d) h[d] = in.spacing[d];
+    int64_t dp[3] = {0, 0, 0};
+    for (int d = 0; d < 3; ++d) dp[d] = d < D ? out.pitch[d] : 0;
+    char* dst = static_cast<char*>(out.data);
+    for (int d = 0; d < D; ++d) dst += (requested.index[d] - out.region.index[d]) * out.pitch[d];
+    const dim3 gr = grid3(m[0], m[1], m[2]);
+    const int u8 = out.dtype == ITKG_U8 ? 1 : 0;
+    if (in.dtype == ITKG_U8)
+      k_rec_deriv<uint8_t><<<gr, kT, 0, s>>>(static_cast<const uint8_t*>(buf), m[0], m[1], m[2], D, kind, axis, order,
+                                             h[0], h[1], h[2], dst, dp[0], dp[1], dp[2], u8);
+    else
+      k_rec_deriv<float><<<gr, kT, 0, s>>>(static_cast<const float*>(buf), m[0], m[1], m[2], D, kind, axis, order,
+                                           h[0], h[1], h[2], dst, dp[0], dp[1], dp[2], u8);
+    note_launch("recursive_derivative");
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) st = set_error(ITKG_ERROR_CUDA, "recursive derivative launch: %s", cudaGetErrorString(e));
+  }
+  scratch_free(buf, stream);
+  if (st == ITKG_SUCCESS) set_last_kernel("recursive_derivative");
   return st;
 }
 

@@ -24,8 +24,8 @@ import numpy as np
 
 from ._abi import (ALGO_AUTO, ALGO_FUSED, ALGO_PER_AXIS, ALGO_TWO_PASS, ARITH_F32, ARITH_PIXEL_U8, BF16,
                    DEVICE, F16, F32, HOST, I16, ROUND_FMA, ROUND_REFERENCE, U8, ItkgError, check,
-                   itkg_gaussian_params, itkg_image, itkg_recursive_params, itkg_region,
-                   itkg_separable_params, lib)
+                   itkg_gaussian_params, itkg_image, itkg_recursive_derivative_params, itkg_recursive_params,
+                   itkg_region, itkg_separable_params, lib)
 
 __all__ = [
     "Region", "Image", "DeviceImage", "GaussianFilter", "CastFilter", "stream_full",
@@ -33,7 +33,9 @@ __all__ = [
     "F16", "ROUND_REFERENCE", "ROUND_FMA", "ALGO_AUTO", "ALGO_FUSED", "ALGO_PER_AXIS",
     "ALGO_TWO_PASS", "ARITH_F32", "ARITH_PIXEL_U8", "gaussian", "Stream", "SeparableFilter",
     "MeanFilter", "BoxMeanFilterN", "BinomialBlurFilter", "box_kernel", "BINOMIAL_KERNEL",
-    "RecursiveGaussianFilter", "RecursiveGaussianAxisFilter", "yvv_coeffs",
+    "RecursiveGaussianFilter", "RecursiveGaussianAxisFilter", "yvv_coeffs", "RecursiveGaussianDerivativeFilter",
+    "GradientMagnitudeRecursiveGaussianFilter", "LaplacianRecursiveGaussianFilter",
+    "DiscreteGaussianDerivativeFilter", "GradientRecursiveGaussianFilter", "HessianRecursiveGaussianFilter",
 ]
 
 _NP_OF = {F32: np.float32, I16: np.int16, U8: np.uint8, F16: np.float16}
@@ -509,6 +511,83 @@ class RecursiveGaussianAxisFilter(RecursiveGaussianFilter):
 
     def __init__(self, source, sigma: float, axis: int, rounding: int = ROUND_REFERENCE):
         super().__init__(source, sigma, axis, rounding)
+
+
+REC_GRADIENT_MAGNITUDE, REC_LAPLACIAN, REC_DERIVATIVE, REC_GRADIENT, REC_HESSIAN = 0, 1, 2, 3, 4
+
+
+class RecursiveGaussianDerivativeFilter(RecursiveGaussianFilter):
+    """The derivative users of RecursiveGaussianFilter (edges.rs:686-950): the
+    smoothed requested region, then a central-difference stencil of `kind`."""
+
+    def __init__(self, source, sigma: float, kind: int, axis: int = 0, order: int = 1,
+                 rounding: int = ROUND_REFERENCE):
+        super().__init__(source, sigma, None, rounding)
+        self.kind, self.deriv_axis, self.order = int(kind), int(axis), int(order)
+
+    def _out_layout(self):
+        D = len(self.source.largest_region().size)
+        if self.kind <= REC_DERIVATIVE:
+            return self.source.dtype, 1
+        return F32, (D if self.kind == REC_GRADIENT else 3)
+
+    def generate_region(self, requested: Region, stream: Stream = _DEFAULT_STREAM, out_dtype: int | None = None):
+        src = self.source
+        dtype, comps = self._out_layout()
+        p = itkg_recursive_derivative_params()
+        p.sigma, p.kind, p.axis, p.order, p.rounding = self.sigma, self.kind, self.deriv_axis, self.order, self.rounding
+        largest = src.largest_region().to_c()
+        req = requested.to_c()
+        sc = src.to_c()
+        if isinstance(src, Image):
+            shape = tuple(reversed(requested.size)) + ((comps,) if comps > 1 else ())
+            res = Image(np.empty(shape, dtype=_storage_np(dtype)), index=requested.index, spacing=src.spacing,
+                        origin=src.origin, components=comps)
+            oc = res.to_c()
+            check(lib().itkg_recursive_gaussian_derivative_generate_region(
+                ctypes.byref(sc), ctypes.byref(largest), ctypes.byref(req), ctypes.byref(p), ctypes.byref(oc),
+                stream.ptr))
+            return res
+        dev = DeviceImage(requested, dtype, comps, src.spacing, src.origin)
+        check(lib().itkg_recursive_gaussian_derivative_generate_region(
+            ctypes.byref(sc), ctypes.byref(largest), ctypes.byref(req), ctypes.byref(p), ctypes.byref(dev.c),
+            stream.ptr))
+        return dev
+
+
+class GradientMagnitudeRecursiveGaussianFilter(RecursiveGaussianDerivativeFilter):
+    """GradientMagnitudeRecursiveGaussianFilter { source, sigma } (edges.rs:686-722)."""
+
+    def __init__(self, source, sigma: float, **kw):
+        super().__init__(source, sigma, REC_GRADIENT_MAGNITUDE, **kw)
+
+
+class LaplacianRecursiveGaussianFilter(RecursiveGaussianDerivativeFilter):
+    """LaplacianRecursiveGaussianFilter { source, sigma } (edges.rs:730-766)."""
+
+    def __init__(self, source, sigma: float, **kw):
+        super().__init__(source, sigma, REC_LAPLACIAN, **kw)
+
+
+class DiscreteGaussianDerivativeFilter(RecursiveGaussianDerivativeFilter):
+    """DiscreteGaussianDerivativeFilter { source, sigma, axis, order } (edges.rs:772-810)."""
+
+    def __init__(self, source, sigma: float, axis: int, order: int = 1, **kw):
+        super().__init__(source, sigma, REC_DERIVATIVE, axis=axis, order=order, **kw)
+
+
+class GradientRecursiveGaussianFilter(RecursiveGaussianDerivativeFilter):
+    """GradientRecursiveGaussianFilter { source, sigma } (edges.rs:819-878): VecPixel<f32, D>."""
+
+    def __init__(self, source, sigma: float, **kw):
+        super().__init__(source, sigma, REC_GRADIENT, **kw)
+
+
+class HessianRecursiveGaussianFilter(RecursiveGaussianDerivativeFilter):
+    """HessianRecursiveGaussianFilter { source, sigma } (edges.rs:892-950): 2-D, VecPixel<f32, 3>."""
+
+    def __init__(self, source, sigma: float, **kw):
+        super().__init__(source, sigma, REC_HESSIAN, **kw)
 
 
 def stream_full(source: GaussianFilter, num_pieces: int, stream: Stream = _DEFAULT_STREAM,

@@ -80,6 +80,17 @@ class itkg_recursive_params(ctypes.Structure):
     ]
 
 
+class itkg_recursive_derivative_params(ctypes.Structure):
+    _fields_ = [
+        ("sigma", ctypes.c_double),
+        ("kind", ctypes.c_int32),
+        ("axis", ctypes.c_int32),
+        ("order", ctypes.c_int32),
+        ("rounding", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 2),
+    ]
+
+
 # name -> (restype, argtypes); every symbol include/itkg.h declares.
 P = ctypes.c_void_p
 R = ctypes.POINTER(itkg_region)
@@ -117,6 +128,9 @@ SIGNATURES = {
     "itkg_box_kernel": (st, [ctypes.c_uint64, P]),
     "itkg_yvv_coeffs": (st, [ctypes.c_double, P]),
     "itkg_recursive_gaussian_generate_region": (st, [I, R, R, ctypes.POINTER(itkg_recursive_params), I, P]),
+    "itkg_recursive_gaussian_derivative_generate_region": (st, [I, R, R,
+                                                                ctypes.POINTER(itkg_recursive_derivative_params),
+                                                                I, P]),
     "itkg_separable_input_region_for_output": (st, [R, R, ctypes.c_int32, P, ctypes.c_uint64, R]),
     "itkg_separable_generate_region": (st, [I, R, R, ctypes.POINTER(itkg_separable_params), I, P]),
     "itkg_gaussian_vjp": (st, [I, I, G, I, ctypes.POINTER(ctypes.c_double), ctypes.c_int32, P]),

@@ -105,3 +105,68 @@ def test_coefficients_match_oracle_on_this_host(gpu, sigma):
     """The library's host-side coefficients are the oracle's bit for bit on the
     machine that runs the GPU tests too (no host-compiler FMA contraction)."""
     assert np.array_equal(gpu.yvv_coeffs(sigma), oracle.yvv_coeffs(sigma))
+
+
+# ---- the derivative users (edges.rs:686-950) --------------------------------
+from test_oracle_recursive import RECD, recd_meta  # noqa: E402
+
+
+def run_deriv(itkg, arr, sigma, kind, spacing=None, axis=0, order=1, requested=None, index=None, host=False,
+              rounding=0):
+    img = itkg.Image(arr, index=index, spacing=spacing)
+    src = img if host else itkg.DeviceImage.from_host(img)
+    f = itkg.RecursiveGaussianDerivativeFilter(src, sigma, kind, axis=axis, order=order, rounding=rounding)
+    req = itkg.Region(*requested) if requested else img.region
+    out = f.generate_region(req)
+    return out.data if host else out.download()
+
+
+def _same(got, want):
+    if want.dtype == np.uint8:
+        return np.array_equal(got, want)
+    return got.shape == want.shape and bits_equal(got, want)
+
+
+@pytest.mark.parametrize("name", RECD)
+def test_derivative_golden_bit_exact(gpu, golden, name):
+    x, sigma, kind, axis, order, sp, req = recd_meta(golden, name)
+    got = run_deriv(gpu, x, sigma, kind, sp, axis, order, requested=req)
+    assert _same(got, golden[f"recd_{name}__out"]), gpu.last_kernel()
+
+
+@pytest.mark.parametrize("kind,axis,order", [(0, 0, 1), (1, 0, 1), (2, 1, 1), (2, 2, 2), (3, 0, 1)])
+def test_derivative_random_3d(gpu, kind, axis, order):
+    x = np.random.default_rng(100 + kind).standard_normal((20, 26, 31)).astype(np.float32)
+    sp = (0.8, 1.1, 1.7)
+    req = ((3, 2, 4), (25, 21, 12))
+    want = oracle.recursive_derivative(x, 2.2, kind, sp, axis, order, requested=req)
+    got = run_deriv(gpu, x, 2.2, kind, sp, axis, order, requested=req)
+    assert _same(got, want)
+    assert gpu.last_kernel() == "recursive_derivative"
+
+
+def test_hessian_2d_and_host_buffers(gpu):
+    x = np.random.default_rng(110).random((40, 52), dtype=np.float32)
+    want = oracle.recursive_derivative(x, 1.6, oracle.REC_HESSIAN, (0.9, 1.3))
+    assert _same(run_deriv(gpu, x, 1.6, 4, (0.9, 1.3),
+                           host=True), want)
+    want = oracle.recursive_derivative(x, 1.6, oracle.REC_GRADIENT, (0.9, 1.3))
+    assert _same(run_deriv(gpu, x, 1.6, 3, (0.9, 1.3)), want)  # 2 components
+
+
+def test_derivative_u8(gpu):
+    x = np.random.default_rng(111).integers(0, 256, (18, 22), dtype=np.uint8)
+    for kind in (0, 1):
+        want = oracle.recursive_derivative(x, 1.3, kind)
+        assert _same(run_deriv(gpu, x, 1.3, kind), want)
+
+
+def test_derivative_convenience_classes(gpu):
+    x = np.random.default_rng(112).standard_normal((10, 12, 14)).astype(np.float32)
+    d = gpu.DeviceImage.from_host(gpu.Image(x))
+    g = gpu.GradientMagnitudeRecursiveGaussianFilter(d, 1.5).generate_region(d.region).download()
+    assert _same(g, oracle.recursive_derivative(x, 1.5, 0))
+    g = gpu.DiscreteGaussianDerivativeFilter(d, 1.5, axis=2, order=2).generate_region(d.region).download()
+    assert _same(g, oracle.recursive_derivative(x, 1.5, 2, axis=2, order=2))
+    g = gpu.GradientRecursiveGaussianFilter(d, 1.5).generate_region(d.region).download()
+    assert _same(g, oracle.recursive_derivative(x, 1.5, 3))
