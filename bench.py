@@ -666,6 +666,21 @@ def extra_workload(args):
             lines[name] = {"voxels_per_s": n * nvox / (ms * 1e-3), "ms_per_call": ms / n,
                            "kernel": itkg.last_kernel(), "normwise_rel_vs_ref": _normwise(got, want),
                            "bit_exact": bool(np.array_equal(got.view(np.uint32), want.view(np.uint32)))}
+        # a derivative user: GradientMagnitudeRecursiveGaussianFilter (smoothing + gradient stencil)
+        p = _abi.itkg_recursive_derivative_params()
+        p.sigma, p.kind, p.rounding = SIGMA, 0, itkg.ROUND_REFERENCE
+
+        def step_gm(p=p):
+            for d, o in zip(devs, outs):
+                _abi.check(L.itkg_recursive_gaussian_derivative_generate_region(
+                    ctypes.byref(d.c), ctypes.byref(lg), ctypes.byref(rq), ctypes.byref(p),
+                    ctypes.byref(o.c), sp.ptr))
+        ms = _timed(stream, step_gm, max(2, args.steps // 8), args.warmup)
+        gm = outs[0].download()
+        want_gm = oracle.recursive_derivative(vol, SIGMA, oracle.REC_GRADIENT_MAGNITUDE)
+        lines["gradient_magnitude_f64_reference"] = {
+            "voxels_per_s": n * nvox / (ms * 1e-3), "ms_per_call": ms / n, "kernel": itkg.last_kernel(),
+            "bit_exact": bool(np.array_equal(gm.view(np.uint32), want_gm.view(np.uint32)))}
         cpu = None
         if args.cpu_seconds > 0:
             sub = vol[:, :64, :64]  # the recursion is sequential per line: time a 256 x 64 x 64 block
