@@ -111,7 +111,8 @@ typedef struct itkg_region {
 typedef struct itkg_image {
     int32_t dim;
     int32_t dtype;      /* itkg_dtype */
-    int32_t components; /* 1 = scalar, 3 = VecPixel<_, 3> (interleaved) */
+    int32_t components; /* 1 = scalar, 3 = VecPixel<_, 3> (interleaved); 2 = VecPixel<f32, 2>
+                           (2-D gradient outputs only) */
     int32_t location;   /* itkg_location */
     itkg_region region; /* buffered region (BufferedRegion) */
     int64_t pitch[ITKG_MAX_DIM]; /* bytes between neighbours along each axis */
@@ -296,14 +297,17 @@ itkg_status itkg_recursive_gaussian_generate_region(const itkg_image *input, con
  *   ITKG_REC_DERIVATIVE          (772-810) pixel type; `axis`, `order` (1, 2; else 0)
  *   ITKG_REC_GRADIENT            (819-878) f32, dim components (VecPixel<f32, D>)
  *   ITKG_REC_HESSIAN             (892-950) 2-D only; f32, 3 components (h00, h11, h01)
+ *   ITKG_REC_DIFFERENCE_OF_GAUSSIANS (955-1009) pixel type: s(sigma) - s(sigma2) in f64
  * sigma, rounding: as for itkg_recursive_gaussian_generate_region. */
 #define ITKG_REC_GRADIENT_MAGNITUDE 0
 #define ITKG_REC_LAPLACIAN 1
 #define ITKG_REC_DERIVATIVE 2
 #define ITKG_REC_GRADIENT 3
 #define ITKG_REC_HESSIAN 4
+#define ITKG_REC_DIFFERENCE_OF_GAUSSIANS 5 /* (955-1009) smoothing(sigma) - smoothing(sigma2), pixel type */
 typedef struct itkg_recursive_derivative_params {
     double sigma;
+    double sigma2; /* ITKG_REC_DIFFERENCE_OF_GAUSSIANS: the second smoothing */
     int32_t kind;
     int32_t axis;
     int32_t order;

@@ -145,7 +145,7 @@ itkg_status device_fault_word(unsigned int** out);
 itkg_status encode_input_map(const FusedGeom& g, int box_w, int box_h, void* map_out);
 
 // two_pass.cu: the 3-D forward as an x-y slice kernel plus a z kernel through
-// an L2-sized f32 intermediate (rx == ry <= 8, rz <= 8, TMA-aligned input).
+// an L2-sized f32 intermediate (rx == ry <= 12, rz <= 12, TMA-aligned input).
 // ITKG_ERROR_UNSUPPORTED (no error set) when it does not apply.
 itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], void* stream,
                             bool dry_run);
@@ -172,10 +172,10 @@ itkg_status launch_recursive(const itkg_image& in, const itkg_region& largest, c
                              double sigma, int axis, int rounding, const itkg_image& out, void* stream);
 // Its derivative users: smoothing of `requested` in the input's pixel type,
 // then the `kind` stencil (0 gradient magnitude, 1 Laplacian, 2 derivative,
-// 3 gradient, 4 2-D Hessian) into `out`.
+// 3 gradient, 4 2-D Hessian; 5 the difference of two smoothings) into `out`.
 itkg_status launch_recursive_derivative(const itkg_image& in, const itkg_region& largest,
-                                        const itkg_region& requested, double sigma, int kind, int axis, int order,
-                                        int rounding, const itkg_image& out, void* stream);
+                                        const itkg_region& requested, double sigma, double sigma2, int kind,
+                                        int axis, int order, int rounding, const itkg_image& out, void* stream);
 
 // Bumps the launch counter by n (graph replays).
 void note_launches(uint64_t n, const char* name);

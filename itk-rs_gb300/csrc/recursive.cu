@@ -196,6 +196,22 @@ __global__ void __launch_bounds__(kT) k_rec_deriv(const Tp* s, int64_t m0, int64
     }
 }
 
+// DifferenceOfGaussiansFilter (edges.rs:995-1006): s1 - s2 in f64, converted.
+template <typename Tp>
+__global__ void __launch_bounds__(kT) k_rec_sub(const Tp* s1, const Tp* s2, int64_t m0, int64_t m1, int64_t m2,
+                                                 char* dst, int64_t dp0, int64_t dp1, int64_t dp2, int out_u8) {
+  const int64_t x = (int64_t)blockIdx.x * kT + threadIdx.x;
+  if (x >= m0) return;
+  for (int64_t z = blockIdx.z; z < m2; z += gridDim.z)
+    for (int64_t y = blockIdx.y; y < m1; y += gridDim.y) {
+      const int64_t i = (z * m1 + y) * m0 + x;
+      const double v = __dsub_rn((double)s1[i], (double)s2[i]);
+      char* const o = dst + x * dp0 + y * dp1 + z * dp2;
+      if (out_u8) *reinterpret_cast<uint8_t*>(o) = out_u8_of(v);
+      else *reinterpret_cast<float*>(o) = __double2float_rn(v);
+    }
+}
+
 dim3 grid3(int64_t n0, int64_t n1, int64_t n2) {
   return dim3((unsigned)((n0 + kT - 1) / kT), (unsigned)std::min<int64_t>(std::max<int64_t>(n1, 1), 65535),
               (unsigned)std::min<int64_t>(std::max<int64_t>(n2, 1), 65535));
@@ -290,8 +306,8 @@ itkg_status launch_recursive(const itkg_image& in, const itkg_region& largest, c
 }
 
 itkg_status launch_recursive_derivative(const itkg_image& in, const itkg_region& largest,
-                                        const itkg_region& requested, double sigma, int kind, int axis, int order,
-                                        int rounding, const itkg_image& out, void* stream) {
+                                        const itkg_region& requested, double sigma, double sigma2, int kind,
+                                        int axis, int order, int rounding, const itkg_image& out, void* stream) {
   const int D = in.dim;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   // the smoothed image: RecursiveGaussianFilter::generate_region(requested) in the input's pixel type
@@ -308,13 +324,46 @@ itkg_status launch_recursive_derivative(const itkg_image& in, const itkg_region&
   sm.pitch[0] = esz;
   sm.pitch[1] = esz * m[0];
   sm.pitch[2] = esz * m[0] * m[1];
+  const bool dog = kind == 5;
+  const size_t sm_bytes = (size_t)(esz * m[0] * m[1] * m[2]);
   void* buf = nullptr;
+  void* buf2 = nullptr;
   {
-    const itkg_status sa = scratch_alloc(&buf, (size_t)(esz * m[0] * m[1] * m[2]), stream);
-    if (sa != ITKG_SUCCESS) return sa;
+    itkg_status sa = scratch_alloc(&buf, sm_bytes, stream);
+    if (sa == ITKG_SUCCESS && dog) sa = scratch_alloc(&buf2, sm_bytes, stream);
+    if (sa != ITKG_SUCCESS) {
+      scratch_free(buf, stream);
+      return sa;
+    }
   }
   sm.data = buf;
   itkg_status st = launch_recursive(in, largest, requested, sigma, -1, rounding, sm, stream);
+  if (st == ITKG_SUCCESS && dog) {  // the second smoothing, then s1 - s2
+    itkg_image sm2 = sm;
+    sm2.data = buf2;
+    st = launch_recursive(in, largest, requested, sigma2, -1, rounding, sm2, stream);
+    if (st == ITKG_SUCCESS) {
+      int64_t dp[3] = {0, 0, 0};
+      for (int d = 0; d < 3; ++d) dp[d] = d < D ? out.pitch[d] : 0;
+      char* dst = static_cast<char*>(out.data);
+      for (int d = 0; d < D; ++d) dst += (requested.index[d] - out.region.index[d]) * out.pitch[d];
+      const dim3 gr = grid3(m[0], m[1], m[2]);
+      const int u8 = out.dtype == ITKG_U8 ? 1 : 0;
+      if (in.dtype == ITKG_U8)
+        k_rec_sub<uint8_t><<<gr, kT, 0, s>>>(static_cast<const uint8_t*>(buf), static_cast<const uint8_t*>(buf2), m[0],
+                                             m[1], m[2], dst, dp[0], dp[1], dp[2], u8);
+      else
+        k_rec_sub<float><<<gr, kT, 0, s>>>(static_cast<const float*>(buf), static_cast<const float*>(buf2), m[0], m[1],
+                                           m[2], dst, dp[0], dp[1], dp[2], u8);
+      note_launch("recursive_difference");
+      const cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) st = set_error(ITKG_ERROR_CUDA, "recursive difference launch: %s", cudaGetErrorString(e));
+    }
+    scratch_free(buf, stream);
+    scratch_free(buf2, stream);
+    if (st == ITKG_SUCCESS) set_last_kernel("recursive_difference");
+    return st;
+  }
   if (st == ITKG_SUCCESS) {
     double h[3] = {1.0, 1.0, 1.0};
     for (int d = 0; d < D; ++d) h[d] = in.spacing[d];

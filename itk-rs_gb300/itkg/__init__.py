@@ -36,6 +36,7 @@ __all__ = [
     "RecursiveGaussianFilter", "RecursiveGaussianAxisFilter", "yvv_coeffs", "RecursiveGaussianDerivativeFilter",
     "GradientMagnitudeRecursiveGaussianFilter", "LaplacianRecursiveGaussianFilter",
     "DiscreteGaussianDerivativeFilter", "GradientRecursiveGaussianFilter", "HessianRecursiveGaussianFilter",
+    "DifferenceOfGaussiansFilter",
 ]
 
 _NP_OF = {F32: np.float32, I16: np.int16, U8: np.uint8, F16: np.float16}
@@ -513,7 +514,7 @@ class RecursiveGaussianAxisFilter(RecursiveGaussianFilter):
         super().__init__(source, sigma, axis, rounding)
 
 
-REC_GRADIENT_MAGNITUDE, REC_LAPLACIAN, REC_DERIVATIVE, REC_GRADIENT, REC_HESSIAN = 0, 1, 2, 3, 4
+REC_GRADIENT_MAGNITUDE, REC_LAPLACIAN, REC_DERIVATIVE, REC_GRADIENT, REC_HESSIAN, REC_DOG = 0, 1, 2, 3, 4, 5
 
 
 class RecursiveGaussianDerivativeFilter(RecursiveGaussianFilter):
@@ -521,13 +522,13 @@ class RecursiveGaussianDerivativeFilter(RecursiveGaussianFilter):
     smoothed requested region, then a central-difference stencil of `kind`."""
 
     def __init__(self, source, sigma: float, kind: int, axis: int = 0, order: int = 1,
-                 rounding: int = ROUND_REFERENCE):
+                 rounding: int = ROUND_REFERENCE, sigma2: float = 0.0):
         super().__init__(source, sigma, None, rounding)
-        self.kind, self.deriv_axis, self.order = int(kind), int(axis), int(order)
+        self.kind, self.deriv_axis, self.order, self.sigma2 = int(kind), int(axis), int(order), float(sigma2)
 
     def _out_layout(self):
         D = len(self.source.largest_region().size)
-        if self.kind <= REC_DERIVATIVE:
+        if self.kind <= REC_DERIVATIVE or self.kind == REC_DOG:
             return self.source.dtype, 1
         return F32, (D if self.kind == REC_GRADIENT else 3)
 
@@ -536,6 +537,7 @@ class RecursiveGaussianDerivativeFilter(RecursiveGaussianFilter):
         dtype, comps = self._out_layout()
         p = itkg_recursive_derivative_params()
         p.sigma, p.kind, p.axis, p.order, p.rounding = self.sigma, self.kind, self.deriv_axis, self.order, self.rounding
+        p.sigma2 = self.sigma2
         largest = src.largest_region().to_c()
         req = requested.to_c()
         sc = src.to_c()
@@ -581,6 +583,13 @@ class GradientRecursiveGaussianFilter(RecursiveGaussianDerivativeFilter):
 
     def __init__(self, source, sigma: float, **kw):
         super().__init__(source, sigma, REC_GRADIENT, **kw)
+
+
+class DifferenceOfGaussiansFilter(RecursiveGaussianDerivativeFilter):
+    """DifferenceOfGaussiansFilter { source, sigma1, sigma2 } (edges.rs:955-1009)."""
+
+    def __init__(self, source, sigma1: float, sigma2: float, **kw):
+        super().__init__(source, sigma1, REC_DOG, sigma2=sigma2, **kw)
 
 
 class HessianRecursiveGaussianFilter(RecursiveGaussianDerivativeFilter):

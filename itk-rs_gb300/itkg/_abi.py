@@ -83,6 +83,7 @@ class itkg_recursive_params(ctypes.Structure):
 class itkg_recursive_derivative_params(ctypes.Structure):
     _fields_ = [
         ("sigma", ctypes.c_double),
+        ("sigma2", ctypes.c_double),
         ("kind", ctypes.c_int32),
         ("axis", ctypes.c_int32),
         ("order", ctypes.c_int32),

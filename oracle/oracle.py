@@ -288,7 +288,21 @@ def recursive_gaussian_f32(img, sigma, spacing=None, axis=-1, requested=None, in
     return _crop(full, requested, index).astype(np.float32)
 
 
-REC_GRADIENT_MAGNITUDE, REC_LAPLACIAN, REC_DERIVATIVE, REC_GRADIENT, REC_HESSIAN = 0, 1, 2, 3, 4
+REC_GRADIENT_MAGNITUDE, REC_LAPLACIAN, REC_DERIVATIVE, REC_GRADIENT, REC_HESSIAN, REC_DOG = 0, 1, 2, 3, 4, 5
+
+
+def recursive_difference_of_gaussians(img, sigma1, sigma2, spacing=None, requested=None, index=None):
+    """DifferenceOfGaussiansFilter (edges.rs:955-1009): both smoothings of the requested
+    region in the pixel type, then P::from_f64(s1 - s2)."""
+    x = np.asarray(img)
+    D = x.ndim
+    sp = list(spacing) if spacing is not None else [1.0] * D
+    s = []
+    for sg in (sigma1, sigma2):
+        full = _crop(recursive_gaussian_f64(x, sg, sp), requested, index)
+        s.append(from_f64_u8(full).astype(np.float64) if x.dtype == np.uint8 else full.astype(np.float32).astype(np.float64))
+    v = s[0] - s[1]
+    return from_f64_u8(v) if x.dtype == np.uint8 else v.astype(np.float32)
 
 
 def recursive_derivative(img, sigma, kind, spacing=None, axis=0, order=1, requested=None, index=None):

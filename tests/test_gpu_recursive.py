@@ -170,3 +170,15 @@ def test_derivative_convenience_classes(gpu):
     assert _same(g, oracle.recursive_derivative(x, 1.5, 2, axis=2, order=2))
     g = gpu.GradientRecursiveGaussianFilter(d, 1.5).generate_region(d.region).download()
     assert _same(g, oracle.recursive_derivative(x, 1.5, 3))
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.uint8])
+def test_difference_of_gaussians(gpu, dtype):
+    rng = np.random.default_rng(113)
+    x = (rng.random((16, 20, 24)) * 200).astype(dtype)
+    req = ((2, 3, 1), (19, 15, 12))
+    want = oracle.recursive_difference_of_gaussians(x, 1.2, 3.0, (0.9, 1.0, 1.4), requested=req)
+    d = gpu.DeviceImage.from_host(gpu.Image(x, spacing=(0.9, 1.0, 1.4)))
+    got = gpu.DifferenceOfGaussiansFilter(d, 1.2, 3.0).generate_region(gpu.Region(*req)).download()
+    assert _same(got, want)
+    assert gpu.last_kernel() == "recursive_difference"

@@ -114,3 +114,13 @@ def test_recursive_derivative_of_a_ramp():
     sm = oracle.recursive_gaussian_f32(x, 0.5)
     want = (sm[:, 2:].astype(np.float64) - sm[:, :-2]) / 2.0
     assert np.array_equal(g[:, 1:-1], want.astype(np.float32))
+
+
+def test_difference_of_gaussians_oracle():
+    """DifferenceOfGaussiansFilter (edges.rs:995-1006): the f64 difference of the two
+    smoothings, each first converted to the pixel type."""
+    x = np.random.default_rng(7).random((9, 11), dtype=np.float32)
+    s1 = oracle.recursive_gaussian_f32(x, 1.0).astype(np.float64)
+    s2 = oracle.recursive_gaussian_f32(x, 2.5).astype(np.float64)
+    got = oracle.recursive_difference_of_gaussians(x, 1.0, 2.5)
+    assert np.array_equal(got.view(np.uint32), (s1 - s2).astype(np.float32).view(np.uint32))
