@@ -259,6 +259,34 @@ itkg_status itkg_separable_generate_region(const itkg_image *input, const itkg_r
                                            const itkg_separable_params *params,
                                            itkg_image *output, void *stream);
 
+/* ---- UnsharpMaskFilter (edges.rs:374-452) ----------------------------------
+ * out = |I - blur(I)| > threshold ? I + amount * (I - blur(I)) : I, in f64,
+ * converted to the pixel type (f32 `v as f32`; u8 round half away from zero,
+ * clamped to [0, 255]).  blur is the convolve_axis family's pass over every
+ * axis with one kernel: radius ceil(3 sigma), weights exp(-d^2 / (2 sigma^2))
+ * divided by their f64 sum, sigma in pixels on every axis (the reference
+ * ignores the spacing here), accumulated in the pixel type like
+ * itkg_separable_generate_region.  Vector pixels: the formula reads the first
+ * component and writes its result to every component (pixel.rs:93-98).
+ * Input and output: same dtype (f32 or u8) and components; the input buffer
+ * must contain itkg_separable_input_region_for_output(requested) with that
+ * radius and one repetition. */
+typedef struct itkg_unsharp_params {
+    double sigma;     /* > 0, pixels */
+    double amount;    /* UnsharpMaskFilter::new: 0.5 */
+    double threshold; /* UnsharpMaskFilter::new: 0.0 */
+    int32_t rounding; /* of the blur: itkg_rounding */
+    int32_t reserved; /* 0 */
+} itkg_unsharp_params;
+
+/* The blur kernel of UnsharpMaskFilter (edges.rs:408, 415-424): *radius_out =
+ * ceil(3 sigma); weights_out (may be NULL) receives its 2 * radius + 1 weights. */
+itkg_status itkg_unsharp_kernel(double sigma, uint64_t *radius_out, double *weights_out, uint64_t capacity);
+
+itkg_status itkg_unsharp_mask_generate_region(const itkg_image *input, const itkg_region *largest,
+                                              const itkg_region *requested, const itkg_unsharp_params *params,
+                                              itkg_image *output, void *stream);
+
 /* ---- RecursiveGaussianFilter (recursive_gaussian.rs) -----------------------
  * Young & van Vliet 3rd-order IIR Gaussian: RecursiveGaussianFilter (axis -1,
  * every axis; recursive_gaussian.rs:133-181) and RecursiveGaussianAxisFilter

@@ -1058,6 +1058,136 @@ itkg_status itkg_separable_generate_region(const itkg_image* input, const itkg_r
   return generate_region(input, largest, requested, &ks, &opts, output, static_cast<cudaStream_t>(stream));
 }
 
+itkg_status itkg_unsharp_kernel(double sigma, uint64_t* radius_out, double* weights_out, uint64_t capacity) {
+  if (!radius_out) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "radius_out is NULL");
+  if (!(sigma > 0.0) || !std::isfinite(sigma))
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "sigma must be finite and > 0 (got %g)", sigma);
+  // radius = (3.0 * sigma).ceil() as usize (edges.rs:408)
+  const double rr = std::ceil(3.0 * sigma);
+  if (rr > (double)(1u << 20)) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "sigma %g gives too large a radius", sigma);
+  const uint64_t r = (uint64_t)rr;
+  *radius_out = r;
+  if (!weights_out) return ITKG_SUCCESS;
+  if (capacity < 2 * r + 1)
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "weights_out holds %llu weights, %llu needed",
+                     (unsigned long long)capacity, (unsigned long long)(2 * r + 1));
+  // edges.rs:416-424: exp(-(d * d) / (2 sigma sigma)), then divided by the
+  // left-to-right f64 sum (this file is compiled without FP contraction).
+  const double two_s2 = 2.0 * sigma * sigma;
+  for (uint64_t i = 0; i <= 2 * r; ++i) {
+    const double d = (double)i - (double)r;
+    weights_out[i] = std::exp(-(d * d) / two_s2);
+  }
+  double sum = 0.0;
+  for (uint64_t i = 0; i <= 2 * r; ++i) sum += weights_out[i];
+  for (uint64_t i = 0; i <= 2 * r; ++i) weights_out[i] /= sum;
+  return ITKG_SUCCESS;
+}
+
+itkg_status itkg_unsharp_mask_generate_region(const itkg_image* input, const itkg_region* largest,
+                                              const itkg_region* requested, const itkg_unsharp_params* params,
+                                              itkg_image* output, void* stream) {
+  if (!params) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "params is NULL");
+  ITKG_TRY(validate_image(input, "input"));
+  ITKG_TRY(validate_image(output, "output"));
+  ITKG_TRY(filter_components(input, "input"));
+  ITKG_TRY(filter_components(output, "output"));
+  if (!largest || !requested) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "region is NULL");
+  if (params->reserved != 0) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "reserved must be 0");
+  if (params->rounding != ITKG_ROUND_REFERENCE && params->rounding != ITKG_ROUND_FMA)
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "unknown rounding %d", params->rounding);
+  if (input->dtype != ITKG_F32 && input->dtype != ITKG_U8)
+    return set_error(ITKG_ERROR_UNSUPPORTED, "the pixel type is f32 or u8");
+  if (output->dtype != input->dtype || output->components != input->components || output->dim != input->dim)
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "output must have the input's dim, dtype and components");
+  const int D = input->dim;
+  uint64_t r = 0;
+  ITKG_TRY(itkg_unsharp_kernel(params->sigma, &r, nullptr, 0));
+  std::vector<double> w(2 * r + 1);
+  ITKG_TRY(itkg_unsharp_kernel(params->sigma, &r, w.data(), w.size()));
+  if (region_len(*requested, D) == 0) return ITKG_SUCCESS;
+  if (!region_contains(*largest, *requested, D))
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "requested region lies outside the largest region");
+  if (!region_contains(output->region, *requested, D))
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "output buffer does not contain the requested region");
+  uint64_t pad[kMaxDim] = {r, r, r};
+  const itkg_region in_reg = clipped(padded(*requested, D, pad), D, *largest);
+  if (!region_contains(input->region, in_reg, D))
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "input buffer does not cover input_region_for_output(requested)");
+
+  KernelSpec ks;
+  ks.gaussian = false;
+  ks.reps = 1;
+  for (int d = 0; d < D; ++d) {
+    ks.radius[d] = r;
+    ks.w[d] = w.data();
+  }
+  itkg_gaussian_params opts;
+  std::memset(&opts, 0, sizeof opts);
+  opts.arithmetic = input->dtype == ITKG_U8 ? ITKG_ARITH_PIXEL_U8 : ITKG_ARITH_F32;
+  opts.rounding = params->rounding;
+  opts.algorithm = ITKG_ALGO_AUTO;
+
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const bool host_in = input->location == ITKG_HOST, host_out = output->location == ITKG_HOST;
+  itkg_image din = *input, dout = *output, blur = *input;
+  void* pin = nullptr;
+  void* pout = nullptr;
+  void* pblur = nullptr;
+  itkg_status st = ITKG_SUCCESS;
+  if (host_in) {
+    din.location = ITKG_DEVICE;
+    din.region = in_reg;
+    dense_layout(&din, 16);
+    st = scratch_alloc(&pin, image_bytes(din), s);
+    din.data = pin;
+    if (st == ITKG_SUCCESS) st = copy_region(din, *input, in_reg, s);
+  }
+  if (st == ITKG_SUCCESS && host_out) {
+    dout.location = ITKG_DEVICE;
+    dout.region = *requested;
+    dense_layout(&dout, 16);
+    st = scratch_alloc(&pout, image_bytes(dout), s);
+    dout.data = pout;
+  }
+  if (st == ITKG_SUCCESS) {
+    blur.location = ITKG_DEVICE;
+    blur.region = *requested;
+    dense_layout(&blur, 16);
+    st = scratch_alloc(&pblur, image_bytes(blur), s);
+    blur.data = pblur;
+  }
+  if (st == ITKG_SUCCESS) st = generate_region(&din, largest, requested, &ks, &opts, &blur, s);
+  if (st == ITKG_SUCCESS) {
+    auto at = [&](const itkg_image& im) {
+      int64_t off = 0;
+      for (int d = 0; d < D; ++d) off += (requested->index[d] - im.region.index[d]) * im.pitch[d];
+      return static_cast<char*>(im.data) + off;
+    };
+    int64_t ip[kMaxDim] = {0, 0, 0}, bp[kMaxDim] = {0, 0, 0}, op[kMaxDim] = {0, 0, 0}, m[kMaxDim] = {1, 1, 1};
+    for (int d = 0; d < D; ++d) {
+      ip[d] = din.pitch[d];
+      bp[d] = blur.pitch[d];
+      op[d] = dout.pitch[d];
+      m[d] = (int64_t)requested->size[d];
+    }
+    st = launch_unsharp(input->dtype, input->components, at(din), ip, at(blur), bp, at(dout), op, m, params->amount,
+                        params->threshold, s);
+  }
+  if (st == ITKG_SUCCESS && host_out) st = copy_region(*output, dout, *requested, s);
+  scratch_free(pblur, s);
+  scratch_free(pin, s);
+  scratch_free(pout, s);
+  if (st == ITKG_SUCCESS && (host_in || host_out)) {
+    const unsigned int* fw = nullptr;
+    ITKG_TRY(fault_word_async(s, &fw));
+    const cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_status(e, "cudaStreamSynchronize");
+    return check_fault_word(fw);
+  }
+  return st;
+}
+
 itkg_status itkg_stream_full(const itkg_image* input, const itkg_region* largest,
                              const itkg_gaussian_params* params, uint64_t num_pieces,
                              itkg_image* output, void* stream) {

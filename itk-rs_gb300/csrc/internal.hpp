@@ -177,6 +177,13 @@ itkg_status launch_recursive_derivative(const itkg_image& in, const itkg_region&
                                         const itkg_region& requested, double sigma, double sigma2, int kind,
                                         int axis, int order, int rounding, const itkg_image& out, void* stream);
 
+// UnsharpMaskFilter's point-wise step (unsharp.cu): in / blur / out point at
+// the first requested voxel of each image; pitches in bytes; m the requested
+// size (unused axes 1).
+itkg_status launch_unsharp(int dtype, int comps, const void* in, const int64_t* ip, const void* blur,
+                           const int64_t* bp, void* out, const int64_t* op, const int64_t* m, double amount,
+                           double threshold, void* stream);
+
 // Bumps the launch counter by n (graph replays).
 void note_launches(uint64_t n, const char* name);
 

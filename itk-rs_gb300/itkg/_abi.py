@@ -80,6 +80,16 @@ class itkg_recursive_params(ctypes.Structure):
     ]
 
 
+class itkg_unsharp_params(ctypes.Structure):
+    _fields_ = [
+        ("sigma", ctypes.c_double),
+        ("amount", ctypes.c_double),
+        ("threshold", ctypes.c_double),
+        ("rounding", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+    ]
+
+
 class itkg_recursive_derivative_params(ctypes.Structure):
     _fields_ = [
         ("sigma", ctypes.c_double),
@@ -132,6 +142,8 @@ SIGNATURES = {
     "itkg_recursive_gaussian_derivative_generate_region": (st, [I, R, R,
                                                                 ctypes.POINTER(itkg_recursive_derivative_params),
                                                                 I, P]),
+    "itkg_unsharp_kernel": (st, [ctypes.c_double, ctypes.POINTER(ctypes.c_uint64), P, ctypes.c_uint64]),
+    "itkg_unsharp_mask_generate_region": (st, [I, R, R, ctypes.POINTER(itkg_unsharp_params), I, P]),
     "itkg_separable_input_region_for_output": (st, [R, R, ctypes.c_int32, P, ctypes.c_uint64, R]),
     "itkg_separable_generate_region": (st, [I, R, R, ctypes.POINTER(itkg_separable_params), I, P]),
     "itkg_gaussian_vjp": (st, [I, I, G, I, ctypes.POINTER(ctypes.c_double), ctypes.c_int32, P]),

@@ -14,6 +14,7 @@ reference's axis order: ``index=(ix, iy, iz)``, ``size=(sx, sy, sz)``.
 from __future__ import annotations
 
 import ctypes
+import math
 import os
 import subprocess
 
@@ -251,6 +252,44 @@ def binomial_f32(img, repetitions, **kw):
     """BinomialBlurFilter (binomial_blur.rs:17-89)."""
     D = _dims(np.asarray(img), kw.get("comps", 1))[0]
     return separable_f32(img, [BINOMIAL_KERNEL] * D, repetitions, **kw)
+
+
+def unsharp_kernel(sigma: float) -> np.ndarray:
+    """UnsharpMaskFilter's blur kernel (edges.rs:408, 415-424): radius ceil(3 sigma),
+    exp(-(d d) / (2 sigma sigma)) through the C library's exp, divided by the
+    left-to-right f64 sum."""
+    sigma = float(sigma)
+    r = int(math.ceil(3.0 * sigma))
+    w = [math.exp(-((float(i) - float(r)) * (float(i) - float(r))) / (2.0 * sigma * sigma)) for i in range(2 * r + 1)]
+    s = 0.0
+    for v in w:
+        s += v
+    return np.array([v / s for v in w], dtype=np.float64)
+
+
+def unsharp_mask(img, sigma, amount=0.5, threshold=0.0, index=None, requested=None, comps=1):
+    """UnsharpMaskFilter::generate_region (edges.rs:406-452) over Image<f32> or
+    Image<u8>: the family blur with unsharp_kernel on every axis, then per voxel
+    edge = orig - blur, |edge| > threshold ? orig + amount * edge : orig in f64,
+    P::from_f64.  Vector pixels read component 0 and fill every component."""
+    x = np.ascontiguousarray(img)
+    D, sizes = _dims(x, comps)
+    k = unsharp_kernel(sigma)
+    sep = separable_u8 if x.dtype == np.uint8 else separable_f32
+    blur = sep(x, [k] * D, 1, index=index, requested=requested, comps=comps)
+    idx = tuple(index) if index is not None else (0,) * D
+    ri, rs = requested if requested is not None else (idx, tuple(sizes))
+    sl = tuple(slice(ri[d] - idx[d], ri[d] - idx[d] + rs[d]) for d in reversed(range(D)))
+    orig = x[sl]
+    if comps > 1:
+        orig, blur = orig[..., 0], blur[..., 0]
+    o = orig.astype(np.float64)
+    edge = o - blur.astype(np.float64)
+    v = np.where(np.abs(edge) > float(threshold), o + float(amount) * edge, o)
+    out = from_f64_u8(v) if x.dtype == np.uint8 else v.astype(np.float32)
+    if comps > 1:
+        out = np.repeat(out[..., None], comps, axis=-1)
+    return np.ascontiguousarray(out)
 
 
 def yvv_coeffs(sigma: float) -> np.ndarray:

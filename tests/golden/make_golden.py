@@ -465,6 +465,47 @@ def main():
     cases.update(rec_deriv_case("hess2d", d2, 1.1, 4, spacing=[0.9, 1.2]))
     cases.update(rec_deriv_case("hess2d_sub", d2, 1.1, 4, requested=([2, 3], [7, 6])))
     cases.update(rec_deriv_case("gm_u8_2d", rrng.integers(0, 256, (9, 10), dtype=np.uint8), 1.5, 0))
+
+    # UnsharpMaskFilter (edges.rs:406-452): the family blur with its own kernel on
+    # every axis, then the f64 point-wise step on the requested region
+    urng = np.random.default_rng(20261206)
+
+    def unsharp_case(name, arr, sigma, amount, threshold, requested=None, comps=1):
+        D = len(arr.shape) - (1 if comps > 1 else 0)
+        kind = "u8" if arr.dtype == np.uint8 else "f32"
+        r = int(math.ceil(3.0 * sigma))
+        k = [math.exp(-((float(i) - float(r)) * (float(i) - float(r))) / (2.0 * sigma * sigma))
+             for i in range(2 * r + 1)]
+        s = 0.0
+        for v in k:
+            s += v
+        k = [v / s for v in k]
+        img = to_ref(arr, comps)
+        ri, rs = requested if requested else (img[0], img[1])
+        blur = separable_region(img, [k] * D, 1, list(ri), list(rs), kind)
+        out = []
+        for p, b in zip(iter_region(list(ri), list(rs)), blur[2]):
+            orig = float(img[2][flat_index(img[0], img[1], p)][0])
+            edge = orig - float(b[0])
+            v = orig + amount * edge if abs(edge) > threshold else orig
+            if kind == "u8":
+                a = abs(v)
+                q = (math.floor(a) + (1.0 if a - math.floor(a) >= 0.5 else 0.0)) * (1.0 if v >= 0 else -1.0)
+                v = int(min(max(q, 0.0), 255.0))
+            out.append(tuple([v] * comps))
+        res = from_ref((list(ri), list(rs), out), comps, np.float32 if kind == "f32" else np.uint8)
+        return {f"ush_{name}__in": arr, f"ush_{name}__out": res,
+                f"ush_{name}__meta": np.array([sigma, amount, threshold, comps] + list(ri) + list(rs),
+                                              dtype=np.float64)}
+
+    u2 = urng.random((12, 15), dtype=np.float32)
+    u3 = (urng.standard_normal((6, 7, 9)) * 2).astype(np.float32)
+    cases.update(unsharp_case("f32_2d_s1", u2, 1.0, 0.5, 0.0))
+    cases.update(unsharp_case("f32_2d_sub_s1p3", u2, 1.3, 1.5, 0.05, requested=([3, 2], [8, 7])))
+    cases.update(unsharp_case("f32_3d_s0p8", u3, 0.8, 0.7, 0.5))
+    cases.update(unsharp_case("f32_1d_s2", urng.random((30,), dtype=np.float32), 2.0, 0.5, 0.0))
+    cases.update(unsharp_case("vec2d_s1", urng.random((7, 8, 3), dtype=np.float32), 1.0, 0.5, 0.0, comps=3))
+    cases.update(unsharp_case("u8_2d_s1p5", urng.integers(0, 256, (10, 11), dtype=np.uint8), 1.5, 0.9, 3.0))
     # kernels
     for s, sp in [(1.5, 1.0), (2.0, 1.0), (1.5, 0.7), (1.5, 2.5), (0.5, 1.0), (8.0, 1.0)]:
         cases[f"kernel_{s}_{sp}"] = np.array(build_kernel(s / sp, kernel_radius(s, sp)),

@@ -285,3 +285,45 @@ def test_recursive_invalid_arguments_return_status(itkg_lib):
     assert call(p, out=bad) == itkg._abi.ERROR_UNSUPPORTED
     empty = itkg.Region((0, 0, 0), (8, 0, 6)).to_c()
     assert call(p, req=empty) == 0
+
+
+@pytest.mark.parametrize("sigma", [0.2, 1.0, 1.3, 3.7, 6.0])
+def test_unsharp_kernel_matches_oracle(itkg_lib, sigma):
+    import itkg
+    assert np.array_equal(itkg.unsharp_kernel(sigma), oracle.unsharp_kernel(sigma))
+
+
+def test_unsharp_invalid_arguments_return_status(itkg_lib):
+    import itkg
+    E = itkg._abi.ERROR_INVALID_ARGUMENT
+    a, b, _ = _host_pair()
+    ac, bc = a.to_c(), b.to_c()
+    lg, rq = a.region.to_c(), a.region.to_c()
+
+    def call(p, inp=ac, out=bc, req=rq):
+        return itkg_lib.itkg_unsharp_mask_generate_region(
+            ctypes.byref(inp), ctypes.byref(lg), ctypes.byref(req), ctypes.byref(p) if p is not None else None,
+            ctypes.byref(out), None)
+    assert call(None) == E
+    p = itkg._abi.itkg_unsharp_params()
+    p.sigma, p.amount = 0.0, 0.5
+    assert call(p) == E and "sigma" in itkg_lib.itkg_last_error().decode()
+    p.sigma = float("nan")
+    assert call(p) == E
+    p.sigma, p.rounding = 1.0, 4
+    assert call(p) == E
+    p.rounding, p.reserved = 0, 1
+    assert call(p) == E
+    p.reserved = 0
+    # output dtype must be the input's
+    bad = itkg.Image(np.zeros((6, 7, 8), np.uint8)).to_c()
+    assert call(p, out=bad) == E
+    # the input must cover the padded request
+    small = itkg.Image(np.zeros((6, 7, 4), np.float32)).to_c()
+    assert call(p, inp=small) == E and "input_region_for_output" in itkg_lib.itkg_last_error().decode()
+    empty = itkg.Region((0, 0, 0), (8, 0, 6)).to_c()
+    assert call(p, req=empty) == 0
+    r = ctypes.c_uint64()
+    w = np.zeros(3)
+    assert itkg_lib.itkg_unsharp_kernel(1.0, ctypes.byref(r), w.ctypes.data, 3) == E  # 7 weights needed
+    assert r.value == 3
