@@ -82,3 +82,32 @@ def test_threshold_and_amount_edges(gpu):
     assert bits_equal(run(gpu, x, 1.0, 0.8, np.inf), x)
     assert bits_equal(run(gpu, x, 1.0, 0.0, 0.0), x)
     assert bits_equal(run(gpu, x, 1.0, -0.5, 0.1), oracle.unsharp_mask(x, 1.0, -0.5, 0.1))
+
+
+def test_epilogue_edge_values(gpu):
+    # The f32 point-wise step decides most voxels in f32 and the rest in f64:
+    # thresholds equal to some |orig - blur| exactly, amounts that create
+    # exact f32 ties (0.5, 1.5) or are not f32 (0.1), values over a wide
+    # exponent range, zeros of both signs, infinities and NaN.
+    rng = np.random.default_rng(41)
+    x = (rng.standard_normal((12, 20, 24)) * np.exp(rng.uniform(-30, 30, (12, 20, 24)))).astype(np.float32)
+    x[0, :4, :4] = 0.0
+    x[1, :4, :4] = -0.0
+    x[2, 0, :3] = [np.inf, -np.inf, np.nan]
+    x[3] = np.float32(1.0) + np.arange(20 * 24, dtype=np.float32).reshape(20, 24) * np.float32(2.0 ** -23)
+    blur = oracle.separable_f32(x, [oracle.unsharp_kernel(1.1)] * 3)
+    e = np.abs(x[4:].astype(np.float64) - blur[4:].astype(np.float64))
+    e = e[np.isfinite(e) & (e > 0)]
+    for amount in (0.5, 1.5, 0.1, -2.0):
+        for thr in (0.0, float(e[7]), float(e[123]), -1.0, np.inf):
+            want = oracle.unsharp_mask(x, 1.1, amount, thr)
+            got = run(gpu, x, 1.1, amount, thr)
+            assert bits_equal(got, want), (amount, thr)
+
+
+def test_exact_ties_from_small_integers(gpu):
+    # integer-valued f32 images with amount 0.5: orig + amount * edge often
+    # lands exactly halfway between two f32 values at large magnitudes
+    x = np.random.default_rng(43).integers(-2 ** 24, 2 ** 24, (16, 18, 20)).astype(np.float32)
+    for amount in (0.5, 0.25, 3.0):
+        assert bits_equal(run(gpu, x, 0.9, amount, 0.0), oracle.unsharp_mask(x, 0.9, amount, 0.0))
