@@ -326,6 +326,9 @@ itkg_status itkg_recursive_gaussian_generate_region(const itkg_image *input, con
  *   ITKG_REC_GRADIENT            (819-878) f32, dim components (VecPixel<f32, D>)
  *   ITKG_REC_HESSIAN             (892-950) 2-D only; f32, 3 components (h00, h11, h01)
  *   ITKG_REC_DIFFERENCE_OF_GAUSSIANS (955-1009) pixel type: s(sigma) - s(sigma2) in f64
+ *   ITKG_REC_ZERO_CROSSING_EDGES (1019-1052) pixel type: the Laplacian stencil
+ *                                into the pixel type, then 1 where it changes
+ *                                sign to a neighbour along an axis, else 0
  * sigma, rounding: as for itkg_recursive_gaussian_generate_region. */
 #define ITKG_REC_GRADIENT_MAGNITUDE 0
 #define ITKG_REC_LAPLACIAN 1
@@ -333,6 +336,7 @@ itkg_status itkg_recursive_gaussian_generate_region(const itkg_image *input, con
 #define ITKG_REC_GRADIENT 3
 #define ITKG_REC_HESSIAN 4
 #define ITKG_REC_DIFFERENCE_OF_GAUSSIANS 5 /* (955-1009) smoothing(sigma) - smoothing(sigma2), pixel type */
+#define ITKG_REC_ZERO_CROSSING_EDGES 6     /* (1019-1052) ZeroCrossingBasedEdgeDetectionFilter */
 typedef struct itkg_recursive_derivative_params {
     double sigma;
     double sigma2; /* ITKG_REC_DIFFERENCE_OF_GAUSSIANS: the second smoothing */

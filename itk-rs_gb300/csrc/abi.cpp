@@ -946,7 +946,7 @@ itkg_status itkg_recursive_gaussian_derivative_generate_region(const itkg_image*
   if (!largest || !requested) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "region is NULL");
   const int D = input->dim;
   const int kind = params->kind;
-  if (kind < ITKG_REC_GRADIENT_MAGNITUDE || kind > ITKG_REC_DIFFERENCE_OF_GAUSSIANS)
+  if (kind < ITKG_REC_GRADIENT_MAGNITUDE || kind > ITKG_REC_ZERO_CROSSING_EDGES)
     return set_error(ITKG_ERROR_INVALID_ARGUMENT, "unknown kind %d", kind);
   if (kind == ITKG_REC_HESSIAN && D != 2)
     return set_error(ITKG_ERROR_UNSUPPORTED, "the Hessian filter is 2-D (edges.rs:905)");
@@ -959,7 +959,8 @@ itkg_status itkg_recursive_gaussian_derivative_generate_region(const itkg_image*
   if (input->components != 1 || (input->dtype != ITKG_F32 && input->dtype != ITKG_U8))
     return set_error(ITKG_ERROR_UNSUPPORTED, "the smoothed image is scalar f32 or u8 (its NumericPixel)");
   // the output: the pixel type for the scalar filters, f32 vectors for the gradient and the Hessian
-  const bool scalar_out = kind <= ITKG_REC_DERIVATIVE || kind == ITKG_REC_DIFFERENCE_OF_GAUSSIANS;
+  const bool scalar_out =
+      kind <= ITKG_REC_DERIVATIVE || kind == ITKG_REC_DIFFERENCE_OF_GAUSSIANS || kind == ITKG_REC_ZERO_CROSSING_EDGES;
   const int want_dtype = scalar_out ? input->dtype : ITKG_F32;
   const int want_comps = scalar_out ? 1 : (kind == ITKG_REC_GRADIENT ? D : 3);
   if (output->dim != D || output->dtype != want_dtype || output->components != want_comps)

@@ -172,7 +172,8 @@ itkg_status launch_recursive(const itkg_image& in, const itkg_region& largest, c
                              double sigma, int axis, int rounding, const itkg_image& out, void* stream);
 // Its derivative users: smoothing of `requested` in the input's pixel type,
 // then the `kind` stencil (0 gradient magnitude, 1 Laplacian, 2 derivative,
-// 3 gradient, 4 2-D Hessian; 5 the difference of two smoothings) into `out`.
+// 3 gradient, 4 2-D Hessian; 5 the difference of two smoothings; 6 zero
+// crossings of the Laplacian) into `out`.
 itkg_status launch_recursive_derivative(const itkg_image& in, const itkg_region& largest,
                                         const itkg_region& requested, double sigma, double sigma2, int kind,
                                         int axis, int order, int rounding, const itkg_image& out, void* stream);

@@ -212,6 +212,33 @@ __global__ void __launch_bounds__(kT) k_rec_sub(const Tp* s1, const Tp* s2, int6
     }
 }
 
+// ZeroCrossingFilter (edges.rs:480-514) over the Laplacian image `l` (dense,
+// the requested region): 1 where center * neighbour < 0 (f64; exact for f32
+// and u8 values) for a neighbour along some axis, clamped to the region;
+// else 0, in the pixel type.
+template <typename Tp>
+__global__ void __launch_bounds__(kT) k_rec_zero(const Tp* l, int64_t m0, int64_t m1, int64_t m2, int D, char* dst,
+                                                  int64_t dp0, int64_t dp1, int64_t dp2, int out_u8) {
+  const int64_t x = (int64_t)blockIdx.x * kT + threadIdx.x;
+  if (x >= m0) return;
+  const int64_t m[3] = {m0, m1, m2};
+  for (int64_t z = blockIdx.z; z < m2; z += gridDim.z)
+    for (int64_t y = blockIdx.y; y < m1; y += gridDim.y) {
+      const int64_t p[3] = {x, y, z};
+      const double c = sval(l, m0, m1, x, y, z);
+      bool zc = false;
+      for (int a = 0; a < D && !zc; ++a)
+        for (int off = -1; off <= 1 && !zc; off += 2) {
+          int64_t q[3] = {p[0], p[1], p[2]};
+          q[a] = q[a] + off < 0 ? 0 : (q[a] + off >= m[a] ? m[a] - 1 : q[a] + off);
+          zc = __dmul_rn(c, sval(l, m0, m1, q[0], q[1], q[2])) < 0.0;
+        }
+      char* const o = dst + x * dp0 + y * dp1 + z * dp2;
+      if (out_u8) *reinterpret_cast<uint8_t*>(o) = zc ? 1 : 0;
+      else *reinterpret_cast<float*>(o) = zc ? 1.0f : 0.0f;
+    }
+}
+
 dim3 grid3(int64_t n0, int64_t n1, int64_t n2) {
   return dim3((unsigned)((n0 + kT - 1) / kT), (unsigned)std::min<int64_t>(std::max<int64_t>(n1, 1), 65535),
               (unsigned)std::min<int64_t>(std::max<int64_t>(n2, 1), 65535));
@@ -373,18 +400,38 @@ itkg_status launch_recursive_derivative(const itkg_image& in, const itkg_region&
     for (int d = 0; d < D; ++d) dst += (requested.index[d] - out.region.index[d]) * out.pitch[d];
     const dim3 gr = grid3(m[0], m[1], m[2]);
     const int u8 = out.dtype == ITKG_U8 ? 1 : 0;
-    if (in.dtype == ITKG_U8)
-      k_rec_deriv<uint8_t><<<gr, kT, 0, s>>>(static_cast<const uint8_t*>(buf), m[0], m[1], m[2], D, kind, axis, order,
-                                             h[0], h[1], h[2], dst, dp[0], dp[1], dp[2], u8);
-    else
-      k_rec_deriv<float><<<gr, kT, 0, s>>>(static_cast<const float*>(buf), m[0], m[1], m[2], D, kind, axis, order,
-                                           h[0], h[1], h[2], dst, dp[0], dp[1], dp[2], u8);
-    note_launch("recursive_derivative");
-    const cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) st = set_error(ITKG_ERROR_CUDA, "recursive derivative launch: %s", cudaGetErrorString(e));
+    // ZeroCrossingBasedEdgeDetectionFilter (edges.rs:1045-1052): the Laplacian
+    // (kind 1) into a dense scratch image in the pixel type, then zero crossings
+    const bool zero = kind == 6;
+    void* lap = nullptr;
+    if (zero) st = scratch_alloc(&lap, sm_bytes, stream);
+    if (st == ITKG_SUCCESS) {
+      char* const d1 = zero ? static_cast<char*>(lap) : dst;
+      const int64_t p1[3] = {zero ? esz : dp[0], zero ? esz * m[0] : dp[1], zero ? esz * m[0] * m[1] : dp[2]};
+      const int k1 = zero ? 1 : kind;
+      if (in.dtype == ITKG_U8)
+        k_rec_deriv<uint8_t><<<gr, kT, 0, s>>>(static_cast<const uint8_t*>(buf), m[0], m[1], m[2], D, k1, axis, order,
+                                               h[0], h[1], h[2], d1, p1[0], p1[1], p1[2], u8);
+      else
+        k_rec_deriv<float><<<gr, kT, 0, s>>>(static_cast<const float*>(buf), m[0], m[1], m[2], D, k1, axis, order,
+                                             h[0], h[1], h[2], d1, p1[0], p1[1], p1[2], u8);
+      note_launch("recursive_derivative");
+      if (zero) {
+        if (in.dtype == ITKG_U8)
+          k_rec_zero<uint8_t><<<gr, kT, 0, s>>>(static_cast<const uint8_t*>(lap), m[0], m[1], m[2], D, dst, dp[0],
+                                                dp[1], dp[2], u8);
+        else
+          k_rec_zero<float><<<gr, kT, 0, s>>>(static_cast<const float*>(lap), m[0], m[1], m[2], D, dst, dp[0], dp[1],
+                                              dp[2], u8);
+        note_launch("recursive_zero_crossing");
+      }
+      const cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) st = set_error(ITKG_ERROR_CUDA, "recursive derivative launch: %s", cudaGetErrorString(e));
+    }
+    scratch_free(lap, stream);
   }
   scratch_free(buf, stream);
-  if (st == ITKG_SUCCESS) set_last_kernel("recursive_derivative");
+  if (st == ITKG_SUCCESS) set_last_kernel(kind == 6 ? "recursive_zero_crossing" : "recursive_derivative");
   return st;
 }
 

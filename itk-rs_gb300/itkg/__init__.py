@@ -36,7 +36,7 @@ __all__ = [
     "RecursiveGaussianFilter", "RecursiveGaussianAxisFilter", "yvv_coeffs", "RecursiveGaussianDerivativeFilter",
     "GradientMagnitudeRecursiveGaussianFilter", "LaplacianRecursiveGaussianFilter",
     "DiscreteGaussianDerivativeFilter", "GradientRecursiveGaussianFilter", "HessianRecursiveGaussianFilter",
-    "DifferenceOfGaussiansFilter", "UnsharpMaskFilter", "unsharp_kernel",
+    "DifferenceOfGaussiansFilter", "UnsharpMaskFilter", "unsharp_kernel", "ZeroCrossingBasedEdgeDetectionFilter",
 ]
 
 _NP_OF = {F32: np.float32, I16: np.int16, U8: np.uint8, F16: np.float16}
@@ -555,7 +555,7 @@ class RecursiveGaussianAxisFilter(RecursiveGaussianFilter):
         super().__init__(source, sigma, axis, rounding)
 
 
-REC_GRADIENT_MAGNITUDE, REC_LAPLACIAN, REC_DERIVATIVE, REC_GRADIENT, REC_HESSIAN, REC_DOG = 0, 1, 2, 3, 4, 5
+REC_GRADIENT_MAGNITUDE, REC_LAPLACIAN, REC_DERIVATIVE, REC_GRADIENT, REC_HESSIAN, REC_DOG, REC_ZERO_CROSSING = range(7)
 
 
 class RecursiveGaussianDerivativeFilter(RecursiveGaussianFilter):
@@ -569,7 +569,7 @@ class RecursiveGaussianDerivativeFilter(RecursiveGaussianFilter):
 
     def _out_layout(self):
         D = len(self.source.largest_region().size)
-        if self.kind <= REC_DERIVATIVE or self.kind == REC_DOG:
+        if self.kind <= REC_DERIVATIVE or self.kind in (REC_DOG, REC_ZERO_CROSSING):
             return self.source.dtype, 1
         return F32, (D if self.kind == REC_GRADIENT else 3)
 
@@ -631,6 +631,14 @@ class DifferenceOfGaussiansFilter(RecursiveGaussianDerivativeFilter):
 
     def __init__(self, source, sigma1: float, sigma2: float, **kw):
         super().__init__(source, sigma1, REC_DOG, sigma2=sigma2, **kw)
+
+
+class ZeroCrossingBasedEdgeDetectionFilter(RecursiveGaussianDerivativeFilter):
+    """ZeroCrossingBasedEdgeDetectionFilter { source, sigma } (edges.rs:1019-1052): 1 at the
+    zero crossings of the Laplacian of the smoothed image, else 0, in the pixel type."""
+
+    def __init__(self, source, sigma: float, **kw):
+        super().__init__(source, sigma, REC_ZERO_CROSSING, **kw)
 
 
 class HessianRecursiveGaussianFilter(RecursiveGaussianDerivativeFilter):

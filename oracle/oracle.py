@@ -327,7 +327,7 @@ def recursive_gaussian_f32(img, sigma, spacing=None, axis=-1, requested=None, in
     return _crop(full, requested, index).astype(np.float32)
 
 
-REC_GRADIENT_MAGNITUDE, REC_LAPLACIAN, REC_DERIVATIVE, REC_GRADIENT, REC_HESSIAN, REC_DOG = 0, 1, 2, 3, 4, 5
+REC_GRADIENT_MAGNITUDE, REC_LAPLACIAN, REC_DERIVATIVE, REC_GRADIENT, REC_HESSIAN, REC_DOG, REC_ZERO_CROSSING = range(7)
 
 
 def recursive_difference_of_gaussians(img, sigma1, sigma2, spacing=None, requested=None, index=None):
@@ -342,6 +342,25 @@ def recursive_difference_of_gaussians(img, sigma1, sigma2, spacing=None, request
         s.append(from_f64_u8(full).astype(np.float64) if x.dtype == np.uint8 else full.astype(np.float32).astype(np.float64))
     v = s[0] - s[1]
     return from_f64_u8(v) if x.dtype == np.uint8 else v.astype(np.float32)
+
+
+def recursive_zero_crossing_edges(img, sigma, spacing=None, requested=None, index=None):
+    """ZeroCrossingBasedEdgeDetectionFilter (edges.rs:1019-1052): the Laplacian of the
+    smoothed requested region in the pixel type (LaplacianFilter, edges.rs:217-247, over
+    an image whose region is the requested one), then ZeroCrossingFilter (edges.rs:480-514):
+    1 where center * neighbour < 0 for a clamped neighbour along some axis, else 0."""
+    x = np.asarray(img)
+    D = x.ndim
+    lap = recursive_derivative(x, sigma, REC_LAPLACIAN, spacing, requested=requested, index=index)
+    c = lap.astype(np.float64)
+    zc = np.zeros(c.shape, dtype=bool)
+    for ax in range(D):
+        n = c.shape[ax]
+        for off in (-1, 1):
+            nb = np.take(c, np.clip(np.arange(n) + off, 0, n - 1), axis=ax)
+            with np.errstate(invalid="ignore"):
+                zc |= (c * nb) < 0.0
+    return zc.astype(np.uint8 if x.dtype == np.uint8 else np.float32)
 
 
 def recursive_derivative(img, sigma, kind, spacing=None, axis=0, order=1, requested=None, index=None):

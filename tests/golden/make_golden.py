@@ -466,6 +466,33 @@ def main():
     cases.update(rec_deriv_case("hess2d_sub", d2, 1.1, 4, requested=([2, 3], [7, 6])))
     cases.update(rec_deriv_case("gm_u8_2d", rrng.integers(0, 256, (9, 10), dtype=np.uint8), 1.5, 0))
 
+    # ZeroCrossingBasedEdgeDetectionFilter (edges.rs:1019-1052): zero crossings of the
+    # Laplacian case above (same inputs), clamped to the requested region
+    def zc_case(name, lap_name):
+        lap = cases[f"recd_{lap_name}__out"]
+        D = lap.ndim
+        shape = lap.shape
+        flat = lap.reshape(-1).tolist()
+        size = list(reversed(shape))
+        out = []
+        for p in iter_region([0] * D, size):
+            c = float(flat[flat_index([0] * D, size, p)])
+            hit = False
+            for a in range(D):
+                for off in (-1, 1):
+                    q = list(p)
+                    q[a] = min(max(p[a] + off, 0), size[a] - 1)
+                    if c * float(flat[flat_index([0] * D, size, q)]) < 0.0:
+                        hit = True
+            out.append(1.0 if hit else 0.0)
+        res = np.array(out, dtype=lap.dtype).reshape(shape)
+        return {f"recz_{name}__out": res}
+
+    zd3 = (rrng.standard_normal((7, 8, 9)) * 3).astype(np.float32)
+    cases.update(rec_deriv_case("lap3d_zc_sub", zd3, 1.3, 1, spacing=[1.0, 0.8, 1.2], requested=([1, 1, 2], [7, 6, 4])))
+    cases.update(zc_case("lap2d", "lap2d"))
+    cases.update(zc_case("lap3d_sub", "lap3d_zc_sub"))
+
     # UnsharpMaskFilter (edges.rs:406-452): the family blur with its own kernel on
     # every axis, then the f64 point-wise step on the requested region
     urng = np.random.default_rng(20261206)

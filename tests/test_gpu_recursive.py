@@ -108,7 +108,7 @@ def test_coefficients_match_oracle_on_this_host(gpu, sigma):
 
 
 # ---- the derivative users (edges.rs:686-950) --------------------------------
-from test_oracle_recursive import RECD, recd_meta  # noqa: E402
+from test_oracle_recursive import RECD, RECZ, recd_meta  # noqa: E402
 
 
 def run_deriv(itkg, arr, sigma, kind, spacing=None, axis=0, order=1, requested=None, index=None, host=False,
@@ -182,3 +182,25 @@ def test_difference_of_gaussians(gpu, dtype):
     got = gpu.DifferenceOfGaussiansFilter(d, 1.2, 3.0).generate_region(gpu.Region(*req)).download()
     assert _same(got, want)
     assert gpu.last_kernel() == "recursive_difference"
+
+
+@pytest.mark.parametrize("name", sorted(RECZ))
+def test_zero_crossing_golden(gpu, golden, name):
+    x, sigma, kind, axis, order, sp, req = recd_meta(golden, RECZ[name])
+    got = run_deriv(gpu, x, sigma, gpu.REC_ZERO_CROSSING, sp, requested=req)
+    assert _same(got, golden[f"recz_{name}__out"])
+    assert gpu.last_kernel() == "recursive_zero_crossing"
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.uint8])
+def test_zero_crossing_edges(gpu, dtype):
+    rng = np.random.default_rng(114)
+    x = (rng.standard_normal((18, 21, 25)) * 40 + 100).astype(dtype)
+    req = ((2, 1, 3), (20, 18, 13))
+    sp = (1.0, 0.7, 1.6)
+    want = oracle.recursive_zero_crossing_edges(x, 1.4, sp, requested=req)
+    d = gpu.DeviceImage.from_host(gpu.Image(x, spacing=sp))
+    got = gpu.ZeroCrossingBasedEdgeDetectionFilter(d, 1.4).generate_region(gpu.Region(*req)).download()
+    assert _same(got, want)
+    if dtype == np.float32:
+        assert 0 < int(want.sum()) < want.size

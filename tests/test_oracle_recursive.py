@@ -80,7 +80,9 @@ def test_u8_output_conversion():
 
 
 RECD = ["gm2d", "gm3d_sub", "lap2d", "deriv3d_o1_a2", "deriv2d_o2_a0_sub", "deriv2d_o3", "grad3d", "hess2d",
-        "hess2d_sub", "gm_u8_2d"]
+        "hess2d_sub", "gm_u8_2d", "lap3d_zc_sub"]
+# zero crossings of these Laplacian cases (ZeroCrossingBasedEdgeDetectionFilter)
+RECZ = {"lap2d": "lap2d", "lap3d_sub": "lap3d_zc_sub"}
 
 
 def recd_meta(golden, name):
@@ -124,3 +126,22 @@ def test_difference_of_gaussians_oracle():
     s2 = oracle.recursive_gaussian_f32(x, 2.5).astype(np.float64)
     got = oracle.recursive_difference_of_gaussians(x, 1.0, 2.5)
     assert np.array_equal(got.view(np.uint32), (s1 - s2).astype(np.float32).view(np.uint32))
+
+
+@pytest.mark.parametrize("name", sorted(RECZ))
+def test_zero_crossing_edges_oracle_matches_golden(golden, name):
+    """ZeroCrossingBasedEdgeDetectionFilter (edges.rs:1019-1052) against the pure-Python
+    transcription of ZeroCrossingFilter over the Laplacian golden case."""
+    x, sigma, kind, axis, order, sp, req = recd_meta(golden, RECZ[name])
+    got = oracle.recursive_zero_crossing_edges(x, sigma, sp, requested=req)
+    want = golden[f"recz_{name}__out"]
+    assert got.dtype == want.dtype and np.array_equal(got, want)
+
+
+def test_zero_crossings_of_a_sign_change():
+    """A Laplacian that changes sign between two columns marks both columns."""
+    x = np.zeros((6, 12), np.float32)
+    x[:, 6:] = 10.0
+    z = oracle.recursive_zero_crossing_edges(x, 0.8)
+    assert z.dtype == np.float32 and set(np.unique(z)) <= {0.0, 1.0}
+    assert z[:, 5].all() and z[:, 6].all() and not z[:, 0].any() and not z[:, -1].any()
