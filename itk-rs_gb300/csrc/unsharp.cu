@@ -124,12 +124,120 @@ __global__ void __launch_bounds__(kT) k_unsharp(const char* in, int64_t ip0, int
         const uint8_t q = u8_of(unsharp_f64((double)o, (double)b, k.amount, k.threshold));
         for (int c = 0; c < comps; ++c) reinterpret_cast<uint8_t*>(dst)[c] = q;
       } else {
-        float q;
-        if (!k.fast || !unsharp_fast_f32(o, b, k, q))
-          q = __double2float_rn(unsharp_f64((double)o, (double)b, k.amount, k.threshold));
+        const float q = unsharp_f32(o, b, k);
         for (int c = 0; c < comps; ++c) reinterpret_cast<float*>(dst)[c] = q;
       }
     }
+}
+
+__device__ __forceinline__ float unsharp_f32(float o, float b, const UnsharpConsts& k) {
+  float q;
+  if (!k.fast || !unsharp_fast_f32(o, b, k, q))
+    q = __double2float_rn(unsharp_f64((double)o, (double)b, k.amount, k.threshold));
+  return q;
+}
+
+// Scalar f32 rows of 16-byte aligned quads (x pitch 4, width a multiple of 4,
+// 16-byte aligned rows): thread i of the grid takes quads i, i + grid, ... of
+// the rows x quads space, streaming loads and stores.  I: the index type
+// (32-bit when the voxel count allows, for cheaper divisions).
+//
+// Voxels the f32 test cannot decide (a few in a thousand on smooth data) are
+// not computed in place: in f64 a warp would stall on every one of them.  The
+// block appends (quad index * 4 + lane) to its own segment of `defer`
+// (kDeferCap entries; its count in defer_n[block]) and k_unsharp_deferred
+// finishes them afterwards, a handful of f64 sequences per block.  Entries
+// past the segment's capacity are computed in place.
+constexpr int kQT = 256;
+constexpr int kDeferCap = 2048;
+
+template <typename I>
+__device__ __forceinline__ void quad_addr(I i, I nq, I m1, int64_t p1, int64_t p2, int64_t& off, I& qx) {
+  const I row = i / nq;
+  qx = i - row * nq;
+  const I z = row / m1;
+  const I y = row - z * m1;
+  off = (int64_t)y * p1 + (int64_t)z * p2;
+}
+
+template <typename I>
+__global__ void __launch_bounds__(kQT) k_unsharp_quads(const char* in, int64_t ip1, int64_t ip2, const char* blur,
+                                                        int64_t bp1, int64_t bp2, char* out, int64_t op1, int64_t op2,
+                                                        I nq, I m1, I total, const UnsharpConsts k, I* defer,
+                                                        uint32_t* defer_n) {
+  __shared__ uint32_t n_def;
+  if (threadIdx.x == 0) n_def = 0;
+  __syncthreads();
+  I* const seg = defer + (size_t)blockIdx.x * kDeferCap;
+  for (I i = (I)blockIdx.x * kQT + threadIdx.x; i < total; i += (I)gridDim.x * kQT) {
+    const I row = i / nq;
+    const I qx = i - row * nq;
+    const I z = row / m1;
+    const I y = row - z * m1;
+    const float4 o = __ldcs(reinterpret_cast<const float4*>(in + (int64_t)y * ip1 + (int64_t)z * ip2) + qx);
+    const float4 b = __ldcs(reinterpret_cast<const float4*>(blur + (int64_t)y * bp1 + (int64_t)z * bp2) + qx);
+    const float ov[4] = {o.x, o.y, o.z, o.w}, bv[4] = {b.x, b.y, b.z, b.w};
+    float r[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      if (!k.fast || !unsharp_fast_f32(ov[c], bv[c], k, r[c])) {
+        const uint32_t slot = atomicAdd(&n_def, 1u);
+        if (slot < kDeferCap) {
+          seg[slot] = i * 4 + (I)c;
+          r[c] = ov[c];  // overwritten by k_unsharp_deferred
+        } else {
+          r[c] = __double2float_rn(unsharp_f64((double)ov[c], (double)bv[c], k.amount, k.threshold));
+        }
+      }
+    }
+    __stcs(reinterpret_cast<float4*>(out + (int64_t)y * op1 + (int64_t)z * op2) + qx, make_float4(r[0], r[1], r[2], r[3]));
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) defer_n[blockIdx.x] = min(n_def, (uint32_t)kDeferCap);
+}
+
+// The voxels k_unsharp_quads deferred: block b takes segment b.
+template <typename I>
+__global__ void __launch_bounds__(kQT) k_unsharp_deferred(const char* in, int64_t ip1, int64_t ip2, const char* blur,
+                                                           int64_t bp1, int64_t bp2, char* out, int64_t op1,
+                                                           int64_t op2, I nq, I m1, const UnsharpConsts k,
+                                                           const I* defer, const uint32_t* defer_n) {
+  const uint32_t n = defer_n[blockIdx.x];
+  const I* const seg = defer + (size_t)blockIdx.x * kDeferCap;
+  for (uint32_t j = threadIdx.x; j < n; j += kQT) {
+    const I e = seg[j];
+    const I i = e >> 2;
+    const int c = (int)(e & 3);
+    int64_t off;
+    I qx;
+    quad_addr(i, nq, m1, ip1, ip2, off, qx);
+    const float o = reinterpret_cast<const float*>(in + off)[4 * (int64_t)qx + c];
+    quad_addr(i, nq, m1, bp1, bp2, off, qx);
+    const float b = reinterpret_cast<const float*>(blur + off)[4 * (int64_t)qx + c];
+    quad_addr(i, nq, m1, op1, op2, off, qx);
+    reinterpret_cast<float*>(out + off)[4 * (int64_t)qx + c] =
+        __double2float_rn(unsharp_f64((double)o, (double)b, k.amount, k.threshold));
+  }
+}
+
+template <typename I>
+itkg_status launch_quads(const char* ic, const int64_t* ip, const char* bc, const int64_t* bp, char* oc,
+                         const int64_t* op, const int64_t* m, uint64_t total, unsigned blocks, const UnsharpConsts& k,
+                         cudaStream_t s) {
+  void* scratch = nullptr;
+  const size_t list_bytes = (size_t)blocks * kDeferCap * sizeof(I);
+  itkg_status st = scratch_alloc(&scratch, list_bytes + (size_t)blocks * sizeof(uint32_t), s);
+  if (st != ITKG_SUCCESS) return st;
+  I* const defer = static_cast<I*>(scratch);
+  uint32_t* const defer_n = reinterpret_cast<uint32_t*>(static_cast<char*>(scratch) + list_bytes);
+  k_unsharp_quads<I><<<blocks, kQT, 0, s>>>(ic, ip[1], ip[2], bc, bp[1], bp[2], oc, op[1], op[2], (I)(m[0] / 4),
+                                            (I)m[1], (I)total, k, defer, defer_n);
+  note_launch("unsharp");
+  k_unsharp_deferred<I><<<blocks, kQT, 0, s>>>(ic, ip[1], ip[2], bc, bp[1], bp[2], oc, op[1], op[2], (I)(m[0] / 4),
+                                               (I)m[1], k, defer, defer_n);
+  note_launch("unsharp_deferred");
+  scratch_free(scratch, s);
+  return ITKG_SUCCESS;
 }
 
 // The f32 constants of the fast path for `amount` and `threshold`.
@@ -179,13 +287,32 @@ itkg_status launch_unsharp(int dtype, int comps, const void* in, const int64_t* 
   const char* bc = static_cast<const char*>(blur);
   char* oc = static_cast<char*>(out);
   const UnsharpConsts k = make_consts(amount, threshold);
-  if (dtype == ITKG_U8)
+  auto a16 = [](const void* p, int64_t p1, int64_t p2) {
+    return ((uintptr_t)p % 16) == 0 && p1 % 16 == 0 && p2 % 16 == 0;
+  };
+  const bool quads = dtype == ITKG_F32 && k.fast && comps == 1 && ip[0] == 4 && bp[0] == 4 && op[0] == 4 && m[0] % 4 == 0 &&
+                     m[0] / 4 <= UINT32_MAX && m[1] <= UINT32_MAX && a16(in, ip[1], ip[2]) &&
+                     a16(blur, bp[1], bp[2]) && a16(out, op[1], op[2]);
+  if (quads) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const uint64_t total = (uint64_t)(m[0] / 4) * (uint64_t)m[1] * (uint64_t)m[2];
+    const uint64_t blocks = std::min<uint64_t>((total + kQT - 1) / kQT, (uint64_t)std::max(sms, 1) * 8);
+    // quad indices * 4 + 3 must fit the index type
+    const itkg_status st = 4 * (total + (uint64_t)blocks * kQT) < UINT32_MAX
+                               ? launch_quads<uint32_t>(ic, ip, bc, bp, oc, op, m, total, (unsigned)blocks, k, s)
+                               : launch_quads<uint64_t>(ic, ip, bc, bp, oc, op, m, total, (unsigned)blocks, k, s);
+    if (st != ITKG_SUCCESS) return st;
+  } else if (dtype == ITKG_U8) {
     k_unsharp<uint8_t><<<gr, kT, 0, s>>>(ic, ip[0], ip[1], ip[2], bc, bp[0], bp[1], bp[2], oc, op[0], op[1], op[2],
                                          m[0], m[1], m[2], comps, k);
-  else
+    note_launch("unsharp");
+  } else {
     k_unsharp<float><<<gr, kT, 0, s>>>(ic, ip[0], ip[1], ip[2], bc, bp[0], bp[1], bp[2], oc, op[0], op[1], op[2],
                                        m[0], m[1], m[2], comps, k);
-  note_launch("unsharp");
+    note_launch("unsharp");
+  }
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return set_error(ITKG_ERROR_CUDA, "unsharp launch: %s", cudaGetErrorString(e));
   return ITKG_SUCCESS;
