@@ -59,17 +59,22 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& t) {
 //   The threshold test on e = RN64(e*) is decided from |eh| unless |eh| lies
 //   within 2^-20 of the threshold (|e* - eh| <= 2^-24 |eh|).
 //   p = amount * e* as ph + pl (ph + t = ah eh exactly by FMA; the dropped
-//   terms al el and r e* are below 2^-47 |p|), s = o + p as rh + rl (TwoSum).
-//   |rh + rl - (o + amount e*)| <= 2^-43.5 (|o| + |ph|), and the reference's
-//   three f64 roundings move v at most 2^-50 (|o| + |ph|) from o + amount e*;
-//   delta = 2^-40 (|o| + |ph|) bounds both.  RN32(v) = rh whenever
-//   |rl| + delta is below half the gap from rh to its nearer neighbour.
-//   Near a tie (e.g. amount 0.5 adds one bit) that test fails, but when
-//   amount is an f32 and el == 0, o + amount e* = sh + s1 + t; if s1 + t
-//   also sums exactly, rh + rl is the exact value, every f64 step of the
-//   reference was exact too (e*, ah eh and the result need at most 48 bits),
-//   and both round it to f32 the same way, ties to even included.
-//   Magnitude guards keep every step clear of overflow and underflow.
+//   terms al el and r e* are below 2^-47 |p|), and o + p as sh + s2 with
+//   sh + s1 = o + ph exactly (TwoSum), s2 = s1 + pl rounded.  sh + s2 is
+//   within 2^-43 (|o| + |ph|) of o + amount e*, and the reference's three f64
+//   roundings move v at most 2^-50 (|o| + |ph|) from it, so v lies within
+//   delta = 2^-40 (|o| + |ph|) of sh + s2.  Round-to-nearest is monotonic:
+//   when sh + (s2 + delta) and sh + (s2 - delta), bounds rounded outward,
+//   round to the same f32, RN32(v) is that f32.
+//   Otherwise v is within delta of a tie (amount 0.5 adds one bit, so this is
+//   common on real data).  When amount is an f32 and every step is exact --
+//   ah el, t + ah el and s1 + that sum without error, and e* and amount e*
+//   span at most 53 bits (their low parts within 2^-29 of the high ones) --
+//   the reference's e, p and v were exact as well (v, near an f32 tie, spans
+//   at most 50 bits), and RN32(sh + s2) rounds the same exact value.
+//   Magnitude guards keep every step clear of overflow and of underflow below
+//   delta; zero results always fall back (delta separates the bounds), which
+//   also leaves the signs of zero to the f64 sequence.
 __device__ __forceinline__ bool unsharp_fast_f32(float o, float b, const UnsharpConsts& k, float& out) {
   if (!(fmaxf(fabsf(o), fabsf(b)) < 0x1p90f)) return false;  // NaN, inf, huge
   float eh, el;
@@ -88,24 +93,33 @@ __device__ __forceinline__ bool unsharp_fast_f32(float o, float b, const Unsharp
     out = o;
     return true;
   }
-  if (ae < 0x1p-60f) return false;
   const float ph = __fmul_rn(k.ah, eh);
   const float t = __fmaf_rn(k.ah, eh, -ph);
-  const float cross = __fadd_rn(__fmul_rn(k.ah, el), __fmul_rn(k.al, eh));
-  const float pl = __fadd_rn(t, cross);
-  float sh, s1, s2, s2e, rh, rl;
+  const float pl = __fadd_rn(t, __fadd_rn(__fmul_rn(k.ah, el), __fmul_rn(k.al, eh)));
+  float sh, s1;
   two_sum(o, ph, sh, s1);
-  two_sum(s1, pl, s2, s2e);
-  two_sum(sh, s2, rh, rl);
-  const float arh = fabsf(rh);
-  if (!(arh >= 0x1p-60f) || !(fabsf(ph) < 0x1p100f)) return false;
-  const float delta = __fmul_rn(__fadd_ru(fabsf(o), fabsf(ph)), 0x1p-40f);
-  const float pow2 = __uint_as_float(__float_as_uint(arh) & 0x7f800000u);  // 2^exponent(rh)
-  // half the gap to the nearer neighbour: ulp / 2, or ulp / 4 at a power of two
-  const float half = arh == pow2 ? __fmul_rn(pow2, 0x1p-25f) : __fmul_rn(pow2, 0x1p-24f);
-  if (!(__fadd_ru(fabsf(rl), delta) < half) && !(k.a_exact && el == 0.0f && s2e == 0.0f)) return false;
-  out = rh;
-  return true;
+  const float s2 = __fadd_rn(s1, pl);
+  const float scale = __fadd_ru(fabsf(o), fabsf(ph));
+  if (!(scale >= 0x1p-80f) || !(fabsf(ph) < 0x1p100f) || ae < 0x1p-60f) return false;
+  const float delta = __fmul_rn(scale, 0x1p-40f);
+  const float hi = __fadd_rn(sh, __fadd_ru(s2, delta));
+  const float lo = __fadd_rn(sh, __fadd_rd(s2, -delta));
+  if (hi == lo) {
+    out = hi;
+    return true;
+  }
+  if (k.a_exact && (el == 0.0f || fabsf(el) >= __fmul_rn(ae, 0x1p-29f))) {
+    const float c = __fmul_rn(k.ah, el);
+    const float ce = __fmaf_rn(k.ah, el, -c);
+    float p2, p2e, s2x, s2e;
+    two_sum(t, c, p2, p2e);
+    two_sum(s1, p2, s2x, s2e);
+    if (ce == 0.0f && p2e == 0.0f && s2e == 0.0f && (p2 == 0.0f || fabsf(p2) >= __fmul_rn(fabsf(ph), 0x1p-29f))) {
+      out = __fadd_rn(sh, s2x);
+      return true;
+    }
+  }
+  return false;
 }
 
 template <typename Tp>
@@ -169,28 +183,47 @@ __global__ void __launch_bounds__(kQT) k_unsharp_quads(const char* in, int64_t i
   if (threadIdx.x == 0) n_def = 0;
   __syncthreads();
   I* const seg = defer + (size_t)blockIdx.x * kDeferCap;
-  for (I i = (I)blockIdx.x * kQT + threadIdx.x; i < total; i += (I)gridDim.x * kQT) {
-    const I row = i / nq;
-    const I qx = i - row * nq;
-    const I z = row / m1;
-    const I y = row - z * m1;
-    const float4 o = __ldcs(reinterpret_cast<const float4*>(in + (int64_t)y * ip1 + (int64_t)z * ip2) + qx);
-    const float4 b = __ldcs(reinterpret_cast<const float4*>(blur + (int64_t)y * bp1 + (int64_t)z * bp2) + qx);
-    const float ov[4] = {o.x, o.y, o.z, o.w}, bv[4] = {b.x, b.y, b.z, b.w};
-    float r[4];
+  // two quads per step (i and i + stride), their loads issued together
+  const I stride = (I)gridDim.x * kQT;
+  for (I i0 = (I)blockIdx.x * kQT + threadIdx.x; i0 < total; i0 += 2 * stride) {
+    float4 o[2], b[2];
+    int64_t ooff[2];
+    I qxs[2];
+    bool live[2];
 #pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      if (!k.fast || !unsharp_fast_f32(ov[c], bv[c], k, r[c])) {
-        const uint32_t slot = atomicAdd(&n_def, 1u);
-        if (slot < kDeferCap) {
-          seg[slot] = i * 4 + (I)c;
-          r[c] = ov[c];  // overwritten by k_unsharp_deferred
-        } else {
-          r[c] = __double2float_rn(unsharp_f64((double)ov[c], (double)bv[c], k.amount, k.threshold));
+    for (int h = 0; h < 2; ++h) {
+      const I i = i0 + (I)h * stride;
+      live[h] = i < total;
+      if (!live[h]) continue;
+      const I row = i / nq;
+      const I qx = i - row * nq;
+      const I z = row / m1;
+      const I y = row - z * m1;
+      qxs[h] = qx;
+      ooff[h] = (int64_t)y * op1 + (int64_t)z * op2;
+      o[h] = __ldcs(reinterpret_cast<const float4*>(in + (int64_t)y * ip1 + (int64_t)z * ip2) + qx);
+      b[h] = __ldcs(reinterpret_cast<const float4*>(blur + (int64_t)y * bp1 + (int64_t)z * bp2) + qx);
+    }
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      if (!live[h]) continue;
+      const I i = i0 + (I)h * stride;
+      const float ov[4] = {o[h].x, o[h].y, o[h].z, o[h].w}, bv[4] = {b[h].x, b[h].y, b[h].z, b[h].w};
+      float r[4];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        if (!unsharp_fast_f32(ov[c], bv[c], k, r[c])) {
+          const uint32_t slot = atomicAdd(&n_def, 1u);
+          if (slot < kDeferCap) {
+            seg[slot] = i * 4 + (I)c;
+            r[c] = ov[c];  // overwritten by k_unsharp_deferred
+          } else {
+            r[c] = __double2float_rn(unsharp_f64((double)ov[c], (double)bv[c], k.amount, k.threshold));
+          }
         }
       }
+      __stcs(reinterpret_cast<float4*>(out + ooff[h]) + qxs[h], make_float4(r[0], r[1], r[2], r[3]));
     }
-    __stcs(reinterpret_cast<float4*>(out + (int64_t)y * op1 + (int64_t)z * op2) + qx, make_float4(r[0], r[1], r[2], r[3]));
   }
   __syncthreads();
   if (threadIdx.x == 0) defer_n[blockIdx.x] = min(n_def, (uint32_t)kDeferCap);
@@ -298,7 +331,11 @@ itkg_status launch_unsharp(int dtype, int comps, const void* in, const int64_t* 
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const uint64_t total = (uint64_t)(m[0] / 4) * (uint64_t)m[1] * (uint64_t)m[2];
-    const uint64_t blocks = std::min<uint64_t>((total + kQT - 1) / kQT, (uint64_t)std::max(sms, 1) * 8);
+    // one full wave of resident blocks (each thread takes two quads per step)
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_unsharp_quads<uint32_t>, kQT, 0);
+    const uint64_t blocks =
+        std::min<uint64_t>((total + 2 * kQT - 1) / (2 * kQT), (uint64_t)std::max(sms, 1) * std::max(per_sm, 1));
     // quad indices * 4 + 3 must fit the index type
     const itkg_status st = 4 * (total + (uint64_t)blocks * kQT) < UINT32_MAX
                                ? launch_quads<uint32_t>(ic, ip, bc, bp, oc, op, m, total, (unsigned)blocks, k, s)

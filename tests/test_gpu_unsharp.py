@@ -111,3 +111,12 @@ def test_exact_ties_from_small_integers(gpu):
     x = np.random.default_rng(43).integers(-2 ** 24, 2 ** 24, (16, 18, 20)).astype(np.float32)
     for amount in (0.5, 0.25, 3.0):
         assert bits_equal(run(gpu, x, 0.9, amount, 0.0), oracle.unsharp_mask(x, 0.9, amount, 0.0))
+
+
+def test_every_voxel_undecided(gpu):
+    # values past the f32 test's magnitude guard: every voxel takes the f64
+    # sequence, more per block than the deferred list holds (the rest in place)
+    x = (np.float32(2.0 ** 95) * (1 + np.random.default_rng(47).random((160, 256, 256), dtype=np.float32)))
+    x = x.astype(np.float32)
+    want = oracle.unsharp_mask(x, 1.0, 0.5, 0.0)
+    assert bits_equal(run(gpu, x, 1.0, 0.5, 0.0), want)
