@@ -1151,15 +1151,32 @@ itkg_status itkg_unsharp_mask_generate_region(const itkg_image* input, const itk
     st = scratch_alloc(&pout, image_bytes(dout), s);
     dout.data = pout;
   }
-  if (st == ITKG_SUCCESS) {
+  // 3-D f32: the two-pass blur whose z kernel stores the point-wise step
+  // directly (no blur image in memory)
+  bool fused = false;
+  if (st == ITKG_SUCCESS && D == 3 && input->dtype == ITKG_F32 && input->components == 1) {
+    const UnsharpConsts k = unsharp_consts(params->amount, params->threshold);
+    Plan plan;
+    if (k.fast && make_plan(din, *requested, *largest, ks, &plan) == ITKG_SUCCESS && plan.symmetric &&
+        plan.reps == 1) {
+      FusedGeom g;
+      make_fused_geom(din, *largest, *requested, opts, plan, dout, &g);
+      const float* wz[kMaxDim] = {plan.w32[0].data(), plan.w32[1].data(), plan.w32[2].data()};
+      if (launch_two_pass(g, wz, s, /*dry_run=*/true, &k) == ITKG_SUCCESS) {
+        st = launch_two_pass(g, wz, s, false, &k);
+        fused = true;
+      }
+    }
+  }
+  if (st == ITKG_SUCCESS && !fused) {
     blur.location = ITKG_DEVICE;
     blur.region = *requested;
     dense_layout(&blur, 16);
     st = scratch_alloc(&pblur, image_bytes(blur), s);
     blur.data = pblur;
   }
-  if (st == ITKG_SUCCESS) st = generate_region(&din, largest, requested, &ks, &opts, &blur, s);
-  if (st == ITKG_SUCCESS) {
+  if (st == ITKG_SUCCESS && !fused) st = generate_region(&din, largest, requested, &ks, &opts, &blur, s);
+  if (st == ITKG_SUCCESS && !fused) {
     auto at = [&](const itkg_image& im) {
       int64_t off = 0;
       for (int d = 0; d < D; ++d) off += (requested->index[d] - im.region.index[d]) * im.pitch[d];

@@ -147,8 +147,12 @@ itkg_status encode_input_map(const FusedGeom& g, int box_w, int box_h, void* map
 // two_pass.cu: the 3-D forward as an x-y slice kernel plus a z kernel through
 // an L2-sized f32 intermediate (rx == ry <= 12, rz <= 12, TMA-aligned input).
 // ITKG_ERROR_UNSUPPORTED (no error set) when it does not apply.
+// ush: if non-NULL, the z kernel stores UnsharpMaskFilter's point-wise step
+// applied to the blur and to the input voxel instead of the blur itself (f32
+// input and output with 16-byte aligned rows of whole quads; else unsupported).
+struct UnsharpConsts;
 itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], void* stream,
-                            bool dry_run);
+                            bool dry_run, const UnsharpConsts* ush = nullptr);
 
 // vjp2.cu: the 3-D VJP as z-adjoint and x-y kernels (rx == ry <= 12, rz <= 12,
 // f32, whole image, 16-byte aligned rows of x and ybar).  sigma_out is a
@@ -177,6 +181,19 @@ itkg_status launch_recursive(const itkg_image& in, const itkg_region& largest, c
 itkg_status launch_recursive_derivative(const itkg_image& in, const itkg_region& largest,
                                         const itkg_region& requested, double sigma, double sigma2, int kind,
                                         int axis, int order, int rounding, const itkg_image& out, void* stream);
+
+// UnsharpMaskFilter's point-wise step: its amount and threshold as the f32
+// test (unsharp.cuh) uses them.
+struct UnsharpConsts {
+  double amount, threshold;  // the reference's values (the f64 sequence)
+  float ah, al;              // amount = ah + al + r, |r| <= 2^-48 |amount|
+  float thr_up, thr_dn;      // |e| > thr_up: the test passes; |e| < thr_dn: it fails
+  int thr_neg;               // threshold < 0 (the test for e = 0)
+  int a_exact;               // amount == ah exactly
+  int fast;                  // 0: every voxel takes the f64 sequence
+};
+
+UnsharpConsts unsharp_consts(double amount, double threshold);
 
 // UnsharpMaskFilter's point-wise step (unsharp.cu): in / blur / out point at
 // the first requested voxel of each image; pitches in bytes; m the requested

@@ -25,7 +25,8 @@ const ZEntry kZ[] = {make_z<1>(), make_z<2>(), make_z<3>(),  make_z<4>(),  make_
                      make_z<7>(), make_z<8>(), make_z<9>(),  make_z<10>(), make_z<11>(), make_z<12>()};
 }  // namespace
 
-ZFn z_fn(int r, bool ref, bool vec) {
+ZFn z_fn(int r, bool ref, bool vec, bool ush) {
+  if (ush) return z_ush_fn(r, ref);
   for (const ZEntry& z : kZ)
     if (z.r == r) return z.fn[ref ? 1 : 0][vec ? 1 : 0];
   return nullptr;
@@ -115,7 +116,8 @@ int z_split(int64_t qblocks, int64_t nz, int rz, int64_t grid, int32_t* split) {
 
 }  // namespace
 
-itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], void* stream, bool dry_run) {
+itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], void* stream, bool dry_run,
+                            const UnsharpConsts* ush) {
   if (g.dim != 3 || g.comps != 1 || g.out_dtype == ITKG_I16) return ITKG_ERROR_UNSUPPORTED;
   if (g.radius[0] != g.radius[1] || g.radius[2] < 1 || g.radius[2] > twopass::kMaxR)
     return ITKG_ERROR_UNSUPPORTED;
@@ -142,6 +144,16 @@ itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], v
   if (!fits_i32(nx) || !fits_i32(ny)) return ITKG_ERROR_UNSUPPORTED;
   const int64_t ntx = (nx + twopass::kTileX - 1) / twopass::kTileX;
   const int64_t nty = (ny + e->ty - 1) / e->ty;
+  // 16-byte f32 stores when every quad of the output is full and aligned
+  char* const dst0 = static_cast<char*>(g.dst) + (g.req_index[0] - g.dst_origin[0]) * g.dst_pitch[0] +
+                     (g.req_index[1] - g.dst_origin[1]) * g.dst_pitch[1];
+  const bool vec = g.out_dtype == ITKG_F32 && g.dst_pitch[0] == 4 && ((uintptr_t)dst0 & 15) == 0 &&
+                   (g.dst_pitch[1] & 15) == 0 && (g.dst_pitch[2] & 15) == 0 && nx % 4 == 0;
+  // the unsharp store reads the input's quads at the output's positions (the
+  // TMA checks above make them 16-byte aligned for f32 input)
+  const char* const src0 = static_cast<const char*>(g.src) + (g.req_index[0] - g.src_origin[0]) * g.src_pitch[0] +
+                           (g.req_index[1] - g.src_origin[1]) * g.src_pitch[1];
+  if (ush && (!vec || g.in_dtype != ITKG_F32 || ((uintptr_t)src0 & 15))) return ITKG_ERROR_UNSUPPORTED;
   if (dry_run) return ITKG_SUCCESS;
 
   cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -173,12 +185,7 @@ itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], v
   std::memset(&za, 0, sizeof za);
   if (st == ITKG_SUCCESS) st = device_fault_word(&xa.fault);
   int res_xy = 0, res_z = 0;
-  // 16-byte f32 stores when every quad of the output is full and aligned
-  char* const dst0 = static_cast<char*>(g.dst) + (g.req_index[0] - g.dst_origin[0]) * g.dst_pitch[0] +
-                     (g.req_index[1] - g.dst_origin[1]) * g.dst_pitch[1];
-  const bool vec = g.out_dtype == ITKG_F32 && g.dst_pitch[0] == 4 && ((uintptr_t)dst0 & 15) == 0 &&
-                   (g.dst_pitch[1] & 15) == 0 && (g.dst_pitch[2] & 15) == 0 && nx % 4 == 0;
-  const twopass::ZFn zfn = twopass::z_fn(rz, ref, vec);
+  const twopass::ZFn zfn = twopass::z_fn(rz, ref, vec, ush != nullptr);
   const twopass::XYFn xyfn = e->fn[ref ? 1 : 0];
   if (st == ITKG_SUCCESS) st = max_resident_ctas(reinterpret_cast<const void*>(xyfn), e->smem, e->nt, &res_xy);
   if (st == ITKG_SUCCESS)
@@ -249,6 +256,12 @@ itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], v
   za.dst_pitch[1] = g.dst_pitch[1];
   za.dst_pitch[2] = g.dst_pitch[2];
   za.vec_store = vec ? 1 : 0;
+  if (ush) {
+    za.ush = *ush;
+    za.ush_pitch[0] = g.src_pitch[0];
+    za.ush_pitch[1] = g.src_pitch[1];
+    za.ush_pitch[2] = g.src_pitch[2];
+  }
   for (int k = 0; k < 2 * rz + 1; ++k) za.wz[k] = w[2][k], za.wz2[k] = splat2_host(w[2][k]);
   const int64_t qblocks = ntx * nty * (tile_floats / 4 / twopass::CfgZ<1>::QB);
   za.tile_rows = e->ty;
@@ -289,6 +302,7 @@ itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], v
     za.nz = (int32_t)(c1 - c0);
     za.units = qblocks * za.nz;
     za.dst = dst0 + (oz0 - g.dst_origin[2]) * g.dst_pitch[2];
+    if (ush) za.ush_src = src0 + (oz0 - g.src_origin[2]) * g.src_pitch[2];
     int64_t gz = std::min<int64_t>(za.units, res_z);
     za.nsplit = z_split(qblocks, za.nz, rz, gz, za.split);
     if (za.nsplit > 0) gz = za.nsplit;
@@ -296,7 +310,7 @@ itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], v
     cfg.blockDim = dim3(256);
     cfg.dynamicSmemBytes = z_smem(rz);
     err = cudaLaunchKernelEx(&cfg, zfn, za);
-    note_launch(ref ? "z_pass_f32_ref" : "z_pass_f32_fma");
+    note_launch(ush ? (ref ? "z_pass_unsharp_ref" : "z_pass_unsharp_fma") : (ref ? "z_pass_f32_ref" : "z_pass_f32_fma"));
     if (err == cudaSuccess) err = cudaGetLastError();
     if (err != cudaSuccess) st = set_error(ITKG_ERROR_CUDA, "z pass launch: %s", cudaGetErrorString(err));
   }

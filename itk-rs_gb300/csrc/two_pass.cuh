@@ -33,6 +33,7 @@
 #pragma once
 
 #include "fused_kernel.cuh"
+#include "unsharp.cuh"
 
 namespace itkg {
 namespace twopass {
@@ -97,6 +98,9 @@ struct ZArgs {
   int64_t dst_pitch[3];    // bytes
   int32_t out_dtype;
   int32_t vec_store;       // 1: the 16-byte store variant (see k_z_pass)
+  const char* ush_src;     // UnsharpMaskFilter variant: input voxel (x0, y0, z0)
+  int64_t ush_pitch[3];    // bytes
+  UnsharpConsts ush;
   float wz[kMaxK];
   f2_t wz2[kMaxK];
   int32_t nsplit;          // > 0: CTA b processes units [split[b], split[b + 1]); 0: an even split
@@ -452,9 +456,12 @@ timeout:
 // ---------------------------------------------------------------------------
 // z pass
 // VEC: f32 output whose rows allow 16-byte stores and whose width is a
-// multiple of 4 (every quad full).
-template <int RZ, bool REF, bool VEC>
+// multiple of 4 (every quad full).  USH (with VEC): store UnsharpMaskFilter's
+// point-wise step of the input voxel and the blur (unsharp.cuh) instead of the
+// blur; the input quad is loaded when its step starts.
+template <int RZ, bool REF, bool VEC, bool USH = false>
 __global__ void __launch_bounds__(256, RZ <= 8 ? 2 : 1) k_z_pass(const __grid_constant__ ZArgs a) {
+  static_assert(!USH || VEC, "the unsharp variant stores whole quads");
   using C = CfgZ<RZ>;
   constexpr int KZ = C::KZ, S = C::S, NT = C::NT;
   static_assert(C::QPT == 1, "one quad per thread");
@@ -508,10 +515,17 @@ __global__ void __launch_bounds__(256, RZ <= 8 ? 2 : 1) k_z_pass(const __grid_co
     const int ncols = min(4, a.nx - cx);
     char* dz = a.dst + (int64_t)cx * a.dst_pitch[0] + (int64_t)cy * a.dst_pitch[1] +
                (int64_t)(z0 - a.z0) * a.dst_pitch[2];
+    const char* sz = nullptr;
+    if constexpr (USH)
+      sz = a.ush_src + (int64_t)cx * 4 + (int64_t)cy * a.ush_pitch[1] + (int64_t)(z0 - a.z0) * a.ush_pitch[2];
     // One slice at phase p (a constant once the callers' loops are unrolled):
     // slice j = (period start) + p sits in stage p; push it, refill the stage
     // with slice j + S, pop output j - RZ and store it if `store`.
     auto step = [&](int p, bool store) {
+      float4 og;
+      if constexpr (USH) {
+        if (store) og = __ldcs(reinterpret_cast<const float4*>(sz));
+      }
       fusedk::cp_async_wait<S - 1>();
       const float4 f = zring[p * NT + tid];
       f2_t v[2] = {pack2(f.x, f.y), pack2(f.z, f.w)};
@@ -543,7 +557,10 @@ __global__ void __launch_bounds__(256, RZ <= 8 ? 2 : 1) k_z_pass(const __grid_co
       float o[4];
       unpack2(d0, o[0], o[1]);
       unpack2(d1, o[2], o[3]);
-      if constexpr (VEC) {
+      if constexpr (USH) {
+        __stcs(reinterpret_cast<float4*>(dz), unsharp_quad(og, o[0], o[1], o[2], o[3], a.ush));
+        sz += a.ush_pitch[2];
+      } else if constexpr (VEC) {
         __stcs(reinterpret_cast<float4*>(dz), make_float4(o[0], o[1], o[2], o[3]));
       } else {
 #pragma unroll
@@ -606,7 +623,8 @@ const XYEntry* xy_entries_i16(int* n);
 const XYEntry* xy_entries_u8(int* n);
 const XYEntry* xy_entries_bf16(int* n);
 const XYEntry* xy_entries_f16(int* n);
-ZFn z_fn(int r, bool ref, bool vec);
+ZFn z_fn(int r, bool ref, bool vec, bool ush = false);
+ZFn z_ush_fn(int r, bool ref);  // two_pass_ush.cu
 
 #define ITKG_XY_TABLE(T, DT)                                                                      \
   {                                                                                              \

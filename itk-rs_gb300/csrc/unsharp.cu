@@ -17,109 +17,17 @@
 #include <cmath>
 
 #include "internal.hpp"
+#include "unsharp.cuh"
 
 namespace itkg {
 namespace {
 
 constexpr int kT = 256;
 
-// amount and threshold as the f32 path uses them (built on the host)
-struct UnsharpConsts {
-  double amount, threshold;  // the reference's values (the f64 sequence)
-  float ah, al;              // amount = ah + al + r, |r| <= 2^-48 |amount|
-  float thr_up, thr_dn;      // |e| > thr_up: the test passes; |e| < thr_dn: it fails
-  int thr_neg;               // threshold < 0 (the test for e = 0)
-  int a_exact;               // amount == ah exactly
-  int fast;                  // 0: every voxel takes the f64 sequence
-};
-
 __device__ __forceinline__ uint8_t u8_of(double v) {
   double r = round(v);
   r = fmin(fmax(r, 0.0), 255.0);
   return (uint8_t)r;
-}
-
-// The reference's sequence in f64 (edges.rs:440-448).
-__device__ __noinline__ double unsharp_f64(double o, double b, double amount, double threshold) {
-  const double e = __dsub_rn(o, b);
-  return fabs(e) > threshold ? __dadd_rn(o, __dmul_rn(amount, e)) : o;
-}
-
-// Error-free sum: s + t == a + b exactly, s = RN(a + b) (Knuth's TwoSum).
-__device__ __forceinline__ void two_sum(float a, float b, float& s, float& t) {
-  s = __fadd_rn(a, b);
-  const float a1 = __fsub_rn(s, b);
-  const float b1 = __fsub_rn(s, a1);
-  t = __fadd_rn(__fsub_rn(a, a1), __fsub_rn(b, b1));
-}
-
-// RN32 of the reference's f64 result for f32 o, b, from f32 arithmetic.
-// Returns false when it cannot decide (the caller takes the f64 sequence).
-//   e* = o - b exactly as eh + el (TwoSum).  eh == 0 means e = 0 exactly.
-//   The threshold test on e = RN64(e*) is decided from |eh| unless |eh| lies
-//   within 2^-20 of the threshold (|e* - eh| <= 2^-24 |eh|).
-//   p = amount * e* as ph + pl (ph + t = ah eh exactly by FMA; the dropped
-//   terms al el and r e* are below 2^-47 |p|), and o + p as sh + s2 with
-//   sh + s1 = o + ph exactly (TwoSum), s2 = s1 + pl rounded.  sh + s2 is
-//   within 2^-43 (|o| + |ph|) of o + amount e*, and the reference's three f64
-//   roundings move v at most 2^-50 (|o| + |ph|) from it, so v lies within
-//   delta = 2^-40 (|o| + |ph|) of sh + s2.  Round-to-nearest is monotonic:
-//   when sh + (s2 + delta) and sh + (s2 - delta), bounds rounded outward,
-//   round to the same f32, RN32(v) is that f32.
-//   Otherwise v is within delta of a tie (amount 0.5 adds one bit, so this is
-//   common on real data).  When amount is an f32 and every step is exact --
-//   ah el, t + ah el and s1 + that sum without error, and e* and amount e*
-//   span at most 53 bits (their low parts within 2^-29 of the high ones) --
-//   the reference's e, p and v were exact as well (v, near an f32 tie, spans
-//   at most 50 bits), and RN32(sh + s2) rounds the same exact value.
-//   Magnitude guards keep every step clear of overflow and of underflow below
-//   delta; zero results always fall back (delta separates the bounds), which
-//   also leaves the signs of zero to the f64 sequence.
-__device__ __forceinline__ bool unsharp_fast_f32(float o, float b, const UnsharpConsts& k, float& out) {
-  if (!(fmaxf(fabsf(o), fabsf(b)) < 0x1p90f)) return false;  // NaN, inf, huge
-  float eh, el;
-  two_sum(o, -b, eh, el);
-  if (eh == 0.0f) {  // e = 0: |e| > threshold only for a negative threshold
-    // o + amount * 0 with IEEE signed-zero rules (the same in f32 and f64)
-    out = k.thr_neg ? __fadd_rn(o, __fmul_rn(k.ah, eh)) : o;
-    return true;
-  }
-  const float ae = fabsf(eh);
-  bool pass;
-  if (ae > k.thr_up) pass = true;
-  else if (ae < k.thr_dn) pass = false;
-  else return false;
-  if (!pass) {
-    out = o;
-    return true;
-  }
-  const float ph = __fmul_rn(k.ah, eh);
-  const float t = __fmaf_rn(k.ah, eh, -ph);
-  const float pl = __fadd_rn(t, __fadd_rn(__fmul_rn(k.ah, el), __fmul_rn(k.al, eh)));
-  float sh, s1;
-  two_sum(o, ph, sh, s1);
-  const float s2 = __fadd_rn(s1, pl);
-  const float scale = __fadd_ru(fabsf(o), fabsf(ph));
-  if (!(scale >= 0x1p-80f) || !(fabsf(ph) < 0x1p100f) || ae < 0x1p-60f) return false;
-  const float delta = __fmul_rn(scale, 0x1p-40f);
-  const float hi = __fadd_rn(sh, __fadd_ru(s2, delta));
-  const float lo = __fadd_rn(sh, __fadd_rd(s2, -delta));
-  if (hi == lo) {
-    out = hi;
-    return true;
-  }
-  if (k.a_exact && (el == 0.0f || fabsf(el) >= __fmul_rn(ae, 0x1p-29f))) {
-    const float c = __fmul_rn(k.ah, el);
-    const float ce = __fmaf_rn(k.ah, el, -c);
-    float p2, p2e, s2x, s2e;
-    two_sum(t, c, p2, p2e);
-    two_sum(s1, p2, s2x, s2e);
-    if (ce == 0.0f && p2e == 0.0f && s2e == 0.0f && (p2 == 0.0f || fabsf(p2) >= __fmul_rn(fabsf(ph), 0x1p-29f))) {
-      out = __fadd_rn(sh, s2x);
-      return true;
-    }
-  }
-  return false;
 }
 
 template <typename Tp>
@@ -144,12 +52,6 @@ __global__ void __launch_bounds__(kT) k_unsharp(const char* in, int64_t ip0, int
     }
 }
 
-__device__ __forceinline__ float unsharp_f32(float o, float b, const UnsharpConsts& k) {
-  float q;
-  if (!k.fast || !unsharp_fast_f32(o, b, k, q))
-    q = __double2float_rn(unsharp_f64((double)o, (double)b, k.amount, k.threshold));
-  return q;
-}
 
 // Scalar f32 rows of 16-byte aligned quads (x pitch 4, width a multiple of 4,
 // 16-byte aligned rows): thread i of the grid takes quads i, i + grid, ... of
@@ -273,8 +175,10 @@ itkg_status launch_quads(const char* ic, const int64_t* ip, const char* bc, cons
   return ITKG_SUCCESS;
 }
 
+}  // namespace
+
 // The f32 constants of the fast path for `amount` and `threshold`.
-UnsharpConsts make_consts(double amount, double threshold) {
+UnsharpConsts unsharp_consts(double amount, double threshold) {
   UnsharpConsts k{};
   k.amount = amount;
   k.threshold = threshold;
@@ -305,8 +209,6 @@ UnsharpConsts make_consts(double amount, double threshold) {
   return k;
 }
 
-}  // namespace
-
 // in / blur / out: the first requested voxel of each image and their pitches
 // (bytes); m: the requested size; comps: components per pixel.
 itkg_status launch_unsharp(int dtype, int comps, const void* in, const int64_t* ip, const void* blur,
@@ -319,7 +221,7 @@ itkg_status launch_unsharp(int dtype, int comps, const void* in, const int64_t* 
   const char* ic = static_cast<const char*>(in);
   const char* bc = static_cast<const char*>(blur);
   char* oc = static_cast<char*>(out);
-  const UnsharpConsts k = make_consts(amount, threshold);
+  const UnsharpConsts k = unsharp_consts(amount, threshold);
   auto a16 = [](const void* p, int64_t p1, int64_t p2) {
     return ((uintptr_t)p % 16) == 0 && p1 % 16 == 0 && p2 % 16 == 0;
   };

@@ -120,3 +120,19 @@ def test_every_voxel_undecided(gpu):
     x = x.astype(np.float32)
     want = oracle.unsharp_mask(x, 1.0, 0.5, 0.0)
     assert bits_equal(run(gpu, x, 1.0, 0.5, 0.0), want)
+
+
+@pytest.mark.parametrize("rounding", [0, 1])
+def test_fused_z_store_and_fallback_paths(gpu, rounding):
+    # 3-D f32 with whole aligned quads: the two-pass z kernel stores the
+    # point-wise step; an odd width takes the blur image + point-wise kernels
+    rng = np.random.default_rng(53)
+    for shape, fused in (((24, 28, 64), True), ((24, 28, 30), False)):
+        x = rng.standard_normal(shape).astype(np.float32)
+        want = oracle.unsharp_mask(x, 1.3, 0.7, 0.01)
+        got = run(gpu, x, 1.3, 0.7, 0.01, rounding=rounding)
+        if rounding == 0:
+            assert bits_equal(got, want)
+        else:
+            assert normwise(got, want) <= TOL_FMA
+        assert gpu.last_kernel().startswith("z_pass_unsharp") == fused, gpu.last_kernel()
