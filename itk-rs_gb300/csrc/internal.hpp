@@ -148,8 +148,9 @@ itkg_status encode_input_map(const FusedGeom& g, int box_w, int box_h, void* map
 // an L2-sized f32 intermediate (rx == ry <= 12, rz <= 12, TMA-aligned input).
 // ITKG_ERROR_UNSUPPORTED (no error set) when it does not apply.
 // ush: if non-NULL, the z kernel stores UnsharpMaskFilter's point-wise step
-// applied to the blur and to the input voxel instead of the blur itself (f32
-// input and output with 16-byte aligned rows of whole quads; else unsupported).
+// applied to the blur and to the input voxel instead of the blur itself (FMA
+// rounding and ush->cheap, f32 input and output with 16-byte aligned rows of
+// whole quads; else unsupported).
 struct UnsharpConsts;
 itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], void* stream,
                             bool dry_run, const UnsharpConsts* ush = nullptr);
@@ -191,16 +192,17 @@ struct UnsharpConsts {
   int thr_neg;               // threshold < 0 (the test for e = 0)
   int a_exact;               // amount == ah exactly
   int fast;                  // 0: every voxel takes the f64 sequence
+  int cheap;                 // FMA rounding: o + amount e by one f32 FMA
 };
 
-UnsharpConsts unsharp_consts(double amount, double threshold);
+UnsharpConsts unsharp_consts(double amount, double threshold, bool cheap);
 
 // UnsharpMaskFilter's point-wise step (unsharp.cu): in / blur / out point at
 // the first requested voxel of each image; pitches in bytes; m the requested
 // size (unused axes 1).
 itkg_status launch_unsharp(int dtype, int comps, const void* in, const int64_t* ip, const void* blur,
                            const int64_t* bp, void* out, const int64_t* op, const int64_t* m, double amount,
-                           double threshold, void* stream);
+                           double threshold, int rounding, void* stream);
 
 // Bumps the launch counter by n (graph replays).
 void note_launches(uint64_t n, const char* name);

@@ -456,12 +456,13 @@ timeout:
 // ---------------------------------------------------------------------------
 // z pass
 // VEC: f32 output whose rows allow 16-byte stores and whose width is a
-// multiple of 4 (every quad full).  USH (with VEC): store UnsharpMaskFilter's
-// point-wise step of the input voxel and the blur (unsharp.cuh) instead of the
-// blur; the input quad is loaded when its step starts.
+// multiple of 4 (every quad full).  USH (with VEC, FMA rounding): store
+// UnsharpMaskFilter's point-wise step of the input voxel and the blur
+// (unsharp_cheap_f32) instead of the blur; the input quad is loaded when its
+// step starts.
 template <int RZ, bool REF, bool VEC, bool USH = false>
 __global__ void __launch_bounds__(256, RZ <= 8 ? 2 : 1) k_z_pass(const __grid_constant__ ZArgs a) {
-  static_assert(!USH || VEC, "the unsharp variant stores whole quads");
+  static_assert(!USH || (VEC && !REF), "the unsharp variant stores whole quads, FMA rounding");
   using C = CfgZ<RZ>;
   constexpr int KZ = C::KZ, S = C::S, NT = C::NT;
   static_assert(C::QPT == 1, "one quad per thread");
@@ -558,7 +559,9 @@ __global__ void __launch_bounds__(256, RZ <= 8 ? 2 : 1) k_z_pass(const __grid_co
       unpack2(d0, o[0], o[1]);
       unpack2(d1, o[2], o[3]);
       if constexpr (USH) {
-        __stcs(reinterpret_cast<float4*>(dz), unsharp_quad(og, o[0], o[1], o[2], o[3], a.ush));
+        __stcs(reinterpret_cast<float4*>(dz),
+               make_float4(unsharp_cheap_f32(og.x, o[0], a.ush), unsharp_cheap_f32(og.y, o[1], a.ush),
+                           unsharp_cheap_f32(og.z, o[2], a.ush), unsharp_cheap_f32(og.w, o[3], a.ush)));
         sz += a.ush_pitch[2];
       } else if constexpr (VEC) {
         __stcs(reinterpret_cast<float4*>(dz), make_float4(o[0], o[1], o[2], o[3]));

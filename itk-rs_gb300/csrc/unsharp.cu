@@ -8,9 +8,12 @@
 // component.  The blur itself is the convolve_axis family's
 // (itkg_separable_generate_region) with the filter's own kernel.
 //
-// f64 arithmetic runs at a small fraction of the f32 rate on this GPU, so the
-// f32 kernel gets the reference's result from f32 arithmetic and falls back to
-// the f64 sequence only for voxels it cannot decide (see unsharp_fast_f32).
+// f64 arithmetic runs at a small fraction of the f32 rate on this GPU, so in
+// reference rounding the f32 kernel gets the reference's result from f32
+// arithmetic and falls back to the f64 sequence only for voxels it cannot
+// decide (unsharp_fast_f32); FMA rounding takes one f32 FMA per voxel
+// (unsharp_cheap_f32), and in 3-D the two-pass z kernel applies it as it
+// stores the blur.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -114,7 +117,9 @@ __global__ void __launch_bounds__(kQT) k_unsharp_quads(const char* in, int64_t i
       float r[4];
 #pragma unroll
       for (int c = 0; c < 4; ++c) {
-        if (!unsharp_fast_f32(ov[c], bv[c], k, r[c])) {
+        if (k.cheap) {
+          r[c] = unsharp_cheap_f32(ov[c], bv[c], k);
+        } else if (!unsharp_fast_f32(ov[c], bv[c], k, r[c])) {
           const uint32_t slot = atomicAdd(&n_def, 1u);
           if (slot < kDeferCap) {
             seg[slot] = i * 4 + (I)c;
@@ -178,8 +183,9 @@ itkg_status launch_quads(const char* ic, const int64_t* ip, const char* bc, cons
 }  // namespace
 
 // The f32 constants of the fast path for `amount` and `threshold`.
-UnsharpConsts unsharp_consts(double amount, double threshold) {
+UnsharpConsts unsharp_consts(double amount, double threshold, bool cheap) {
   UnsharpConsts k{};
+  k.cheap = cheap ? 1 : 0;
   k.amount = amount;
   k.threshold = threshold;
   const double aa = std::fabs(amount);
@@ -213,7 +219,7 @@ UnsharpConsts unsharp_consts(double amount, double threshold) {
 // (bytes); m: the requested size; comps: components per pixel.
 itkg_status launch_unsharp(int dtype, int comps, const void* in, const int64_t* ip, const void* blur,
                            const int64_t* bp, void* out, const int64_t* op, const int64_t* m, double amount,
-                           double threshold, void* stream) {
+                           double threshold, int rounding, void* stream) {
   if (m[0] * m[1] * m[2] == 0) return ITKG_SUCCESS;
   const dim3 gr((unsigned)((m[0] + kT - 1) / kT), (unsigned)std::min<int64_t>(m[1], 65535),
                 (unsigned)std::min<int64_t>(m[2], 65535));
@@ -221,7 +227,7 @@ itkg_status launch_unsharp(int dtype, int comps, const void* in, const int64_t* 
   const char* ic = static_cast<const char*>(in);
   const char* bc = static_cast<const char*>(blur);
   char* oc = static_cast<char*>(out);
-  const UnsharpConsts k = unsharp_consts(amount, threshold);
+  const UnsharpConsts k = unsharp_consts(amount, threshold, rounding == ITKG_ROUND_FMA);
   auto a16 = [](const void* p, int64_t p1, int64_t p2) {
     return ((uintptr_t)p % 16) == 0 && p1 % 16 == 0 && p2 % 16 == 0;
   };

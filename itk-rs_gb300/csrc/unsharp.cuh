@@ -92,19 +92,24 @@ __device__ __forceinline__ bool unsharp_fast_f32(float o, float b, const Unsharp
   return false;
 }
 
+// FMA rounding (k.cheap, k.fast): o + amount e by one f32 FMA with e = o - b
+// rounded to f32 -- within a few f32 ulps of the reference -- and the
+// threshold test still decided as the reference decides it (in f64 when
+// |o - b| lies within 2^-20 of the threshold, or is NaN).
+__device__ __forceinline__ float unsharp_cheap_f32(float o, float b, const UnsharpConsts& k) {
+  const float eh = __fsub_rn(o, b);
+  const float ae = fabsf(eh);
+  if (ae > k.thr_up) return __fmaf_rn(k.ah, eh, o);
+  if (ae < k.thr_dn || eh == 0.0f) return o;  // e = 0 passes only a negative threshold: o + amount 0 = o
+  return __double2float_rn(unsharp_f64((double)o, (double)b, k.amount, k.threshold));
+}
+
 __device__ __forceinline__ float unsharp_f32(float o, float b, const UnsharpConsts& k) {
+  if (k.cheap && k.fast) return unsharp_cheap_f32(o, b, k);
   float q;
   if (!k.fast || !unsharp_fast_f32(o, b, k, q))
     q = __double2float_rn(unsharp_f64((double)o, (double)b, k.amount, k.threshold));
   return q;
-}
-
-// One quad of input voxels o and blurred values b; not inlined, so that a
-// caller unrolled over many steps carries one copy.
-__device__ __noinline__ inline float4 unsharp_quad(float4 o, float b0, float b1, float b2, float b3,
-                                                   const UnsharpConsts& k) {
-  return make_float4(unsharp_f32(o.x, b0, k), unsharp_f32(o.y, b1, k), unsharp_f32(o.z, b2, k),
-                     unsharp_f32(o.w, b3, k));
 }
 
 }  // namespace itkg
