@@ -287,6 +287,28 @@ itkg_status itkg_unsharp_mask_generate_region(const itkg_image *input, const itk
                                               const itkg_region *requested, const itkg_unsharp_params *params,
                                               itkg_image *output, void *stream);
 
+/* ---- in-crate callers of GaussianFilter ------------------------------------
+ * SliceBySliceFilter { source, sigma } (filters/spatial.rs:1284-1340), 3-D:
+ * every z slice of `requested` is smoothed by a 2-D GaussianFilter with the x
+ * and y spacing, clamped to the request's x-y window (the reference builds
+ * each slice as an Image over that window).  `input` must contain `requested`
+ * (the reference asks its source for exactly that region); params as for
+ * itkg_gaussian_generate_region. */
+itkg_status itkg_slice_by_slice_generate_region(const itkg_image *input, const itkg_region *requested,
+                                               const itkg_gaussian_params *params, itkg_image *output,
+                                               void *stream);
+
+/* BSplineDownsampleFilter { source } (filters/spatial.rs:1128-1166): GaussianFilter
+ * with sigma 1.0 (params->sigma is not read) over the whole largest region,
+ * then every other voxel from the region's index: output voxel i is smoothed
+ * voxel index + 2 (i - index).  The reference returns the whole downsampled
+ * region (size (n + 1) / 2 per axis, same index) whatever is requested, so
+ * `output` must contain it and `input` the largest region.  The output's dtype
+ * is the smoothed image's (params->arithmetic as for the Gaussian). */
+itkg_status itkg_bspline_downsample_generate_region(const itkg_image *input, const itkg_region *largest,
+                                                    const itkg_gaussian_params *params, itkg_image *output,
+                                                    void *stream);
+
 /* ---- RecursiveGaussianFilter (recursive_gaussian.rs) -----------------------
  * Young & van Vliet 3rd-order IIR Gaussian: RecursiveGaussianFilter (axis -1,
  * every axis; recursive_gaussian.rs:133-181) and RecursiveGaussianAxisFilter

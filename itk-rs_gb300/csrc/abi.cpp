@@ -207,7 +207,15 @@ static itkg_status run_per_axis(const itkg_image& in, const itkg_region& largest
     set_last_kernel("copy");
     return ITKG_SUCCESS;
   }
-  const int npass = reps == 0 ? 1 : (int)std::min<uint64_t>(reps * (uint64_t)D, (uint64_t)INT32_MAX);
+  int npass = reps == 0 ? 1 : (int)std::min<uint64_t>(reps * (uint64_t)D, (uint64_t)INT32_MAX);
+  // One round whose last axes have the 1-tap kernel [1] (SliceBySliceFilter's z):
+  // those passes would copy their input, and after a real pass no value is -0
+  // (every sum starts at +0), so they are left out; the last real pass writes
+  // `requested` to the output.
+  if (reps == 1)
+    while (npass > 1 && plan.radii[npass - 1] == 0 && plan.w64[npass - 1].size() == 1 &&
+           plan.w64[npass - 1][0] == 1.0)
+      --npass;
   auto region_of = [&](int p) {
     if (p + 1 == npass) return requested;
     const uint64_t rep = (uint64_t)(p / D), remaining = reps - rep - 1;
@@ -1204,6 +1212,102 @@ itkg_status itkg_unsharp_mask_generate_region(const itkg_image* input, const itk
     if (e != cudaSuccess) return cuda_status(e, "cudaStreamSynchronize");
     return check_fault_word(fw);
   }
+  return st;
+}
+
+itkg_status itkg_slice_by_slice_generate_region(const itkg_image* input, const itkg_region* requested,
+                                               const itkg_gaussian_params* params, itkg_image* output,
+                                               void* stream) {
+  ITKG_TRY(validate_image(input, "input"));
+  ITKG_TRY(check_params(params));
+  if (!requested) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "requested is NULL");
+  if (input->dim != 3) return set_error(ITKG_ERROR_UNSUPPORTED, "SliceBySliceFilter is 3-D (spatial.rs:1295)");
+  // Each z slice of `requested` is a 2-D Image whose region is the request's
+  // x-y window (spatial.rs:1317-1323), smoothed by GaussianFilter with the x
+  // and y spacing: one round of the 2-D Gaussian's kernels on x and y, the
+  // 1-tap kernel [1] on z, clamped to the request itself.
+  uint64_t r[kMaxDim] = {0, 0, 0};
+  std::vector<double> w[kMaxDim];
+  for (int d = 0; d < 2; ++d) {
+    r[d] = kernel_radius(params->sigma, input->spacing[d]);
+    if (r[d] > (1u << 20))
+      return set_error(ITKG_ERROR_INVALID_ARGUMENT, "kernel radius %llu on axis %d is not allocatable",
+                       (unsigned long long)r[d], d);
+    w[d].resize(2 * r[d] + 1);
+    build_kernel(params->sigma / input->spacing[d], r[d], w[d].data());
+  }
+  w[2].assign(1, 1.0);
+  KernelSpec ks;
+  ks.gaussian = false;
+  ks.reps = 1;
+  for (int d = 0; d < 3; ++d) {
+    ks.radius[d] = r[d];
+    ks.w[d] = w[d].data();
+  }
+  itkg_gaussian_params opts = *params;
+  opts.sigma = 0.0;
+  return generate_region(input, requested, requested, &ks, &opts, output, static_cast<cudaStream_t>(stream));
+}
+
+itkg_status itkg_bspline_downsample_generate_region(const itkg_image* input, const itkg_region* largest,
+                                                    const itkg_gaussian_params* params, itkg_image* output,
+                                                    void* stream) {
+  ITKG_TRY(validate_image(input, "input"));
+  ITKG_TRY(validate_image(output, "output"));
+  ITKG_TRY(filter_components(input, "input"));
+  ITKG_TRY(filter_components(output, "output"));
+  ITKG_TRY(check_params(params));
+  if (!largest) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "largest is NULL");
+  const int D = input->dim;
+  if (output->dim != D || output->components != input->components)
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "output must have the input's dim and components");
+  // the downsampled largest region (spatial.rs:1142-1147)
+  itkg_region half = *largest;
+  for (int d = 0; d < D; ++d) half.size[d] = (largest->size[d] + 1) / 2;
+  if (region_len(half, D) == 0) return ITKG_SUCCESS;
+  if (!region_contains(output->region, half, D))
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "output buffer does not contain the downsampled largest region");
+  if (!region_contains(input->region, *largest, D))
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "input buffer does not cover the largest region");
+  // GaussianFilter { sigma: 1.0 } over the whole largest region (spatial.rs:1157-1158), in the output's
+  // pixel type, into device scratch; then every other voxel
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  itkg_gaussian_params g = *params;
+  g.sigma = 1.0;
+  itkg_image sm = *output;
+  sm.location = ITKG_DEVICE;
+  sm.region = *largest;
+  dense_layout(&sm, 16);
+  void* psm = nullptr;
+  ITKG_TRY(scratch_alloc(&psm, image_bytes(sm), s));
+  sm.data = psm;
+  itkg_status st = generate_region(input, largest, largest, nullptr, &g, &sm, s);
+  itkg_image dout = *output;
+  void* pout = nullptr;
+  const bool host_out = output->location == ITKG_HOST;
+  if (st == ITKG_SUCCESS && host_out) {
+    dout.location = ITKG_DEVICE;
+    dout.region = half;
+    dense_layout(&dout, 16);
+    st = scratch_alloc(&pout, image_bytes(dout), s);
+    dout.data = pout;
+  }
+  if (st == ITKG_SUCCESS) {
+    int64_t sp[kMaxDim] = {0, 0, 0}, dp[kMaxDim] = {0, 0, 0}, m[kMaxDim] = {1, 1, 1};
+    char* dst = static_cast<char*>(dout.data);
+    for (int d = 0; d < D; ++d) {
+      sp[d] = sm.pitch[d];
+      dp[d] = dout.pitch[d];
+      m[d] = (int64_t)half.size[d];
+      dst += (half.index[d] - dout.region.index[d]) * dout.pitch[d];
+    }
+    st = launch_subsample2(sm.data, sp, dst, dp, m, output->components * dtype_size(output->dtype), s);
+  }
+  if (st == ITKG_SUCCESS && host_out) st = copy_region(*output, dout, half, s);
+  scratch_free(psm, s);
+  scratch_free(pout, s);
+  if (st == ITKG_SUCCESS && (host_out || input->location == ITKG_HOST)) ITKG_CUDA(cudaStreamSynchronize(s));
+  if (st == ITKG_SUCCESS) set_last_kernel("subsample2");
   return st;
 }
 

@@ -204,6 +204,12 @@ itkg_status launch_unsharp(int dtype, int comps, const void* in, const int64_t* 
                            const int64_t* bp, void* out, const int64_t* op, const int64_t* m, double amount,
                            double threshold, int rounding, void* stream);
 
+// BSplineDownsampleFilter's subsampling (callers.cu): dst[i] = src[2 i] on
+// every axis; pointers at the region's first voxel, pitches in bytes, m the
+// downsampled size (unused axes 1), elem the pixel's bytes.
+itkg_status launch_subsample2(const void* src, const int64_t* sp, void* dst, const int64_t* dp, const int64_t* m,
+                              int elem, void* stream);
+
 // Bumps the launch counter by n (graph replays).
 void note_launches(uint64_t n, const char* name);
 

@@ -37,6 +37,7 @@ __all__ = [
     "GradientMagnitudeRecursiveGaussianFilter", "LaplacianRecursiveGaussianFilter",
     "DiscreteGaussianDerivativeFilter", "GradientRecursiveGaussianFilter", "HessianRecursiveGaussianFilter",
     "DifferenceOfGaussiansFilter", "UnsharpMaskFilter", "unsharp_kernel", "ZeroCrossingBasedEdgeDetectionFilter",
+    "SliceBySliceFilter", "BSplineDownsampleFilter",
 ]
 
 _NP_OF = {F32: np.float32, I16: np.int16, U8: np.uint8, F16: np.float16}
@@ -450,6 +451,60 @@ class BinomialBlurFilter(SeparableFilter):
     def effective_sigma_pixels(repetitions: int) -> float:
         """binomial_blur.rs:28-30"""
         return (repetitions / 4.0) ** 0.5
+
+
+class SliceBySliceFilter(GaussianFilter):
+    """SliceBySliceFilter { source, sigma } (spatial.rs:1284-1340): a 2-D GaussianFilter on every
+    z slice of the request, clamped to the request's x-y window; 3-D only."""
+
+    def input_region_for_output(self, out: Region) -> Region:
+        return out  # the reference asks its source for the request itself (spatial.rs:1305)
+
+    def _call(self, src, largest, req, out_c, stream):
+        prm = self.params()
+        check(lib().itkg_slice_by_slice_generate_region(ctypes.byref(src), ctypes.byref(req), ctypes.byref(prm),
+                                                        ctypes.byref(out_c), stream.ptr))
+
+
+class BSplineDownsampleFilter(GaussianFilter):
+    """BSplineDownsampleFilter { source } (spatial.rs:1128-1166): GaussianFilter sigma 1.0 over the
+    whole largest region, then every other voxel.  largest_region() is the downsampled region;
+    generate_region returns all of it whatever is requested, as the reference does."""
+
+    def __init__(self, source, rounding: int = ROUND_REFERENCE, algorithm: int = ALGO_AUTO,
+                 arithmetic: int | None = None):
+        super().__init__(source, 1.0, rounding, algorithm, arithmetic)
+
+    def largest_region(self) -> Region:
+        r = self.source.largest_region()
+        return Region(tuple(r.index), tuple((n + 1) // 2 for n in r.size))
+
+    @property
+    def spacing(self):
+        return tuple(2.0 * v for v in self._leaf().spacing)
+
+    def input_region_for_output(self, out: Region) -> Region:
+        return self.source.largest_region()
+
+    def generate_region(self, requested: Region = None, stream: Stream = _DEFAULT_STREAM, out_dtype: int | None = None):
+        leaf = self._leaf()
+        prm = self.params()
+        if out_dtype is None:
+            out_dtype = U8 if prm.arithmetic == ARITH_PIXEL_U8 else F32
+        half = self.largest_region()
+        largest = leaf.largest_region().to_c()
+        src = leaf.to_c()
+        if isinstance(leaf, Image):
+            shape = tuple(reversed(half.size)) + ((leaf.components,) if leaf.components > 1 else ())
+            res = Image(np.empty(shape, dtype=_storage_np(out_dtype)), index=half.index, spacing=self.spacing,
+                        origin=leaf.origin, components=leaf.components)
+            oc = res.to_c()
+        else:
+            res = DeviceImage(half, out_dtype, leaf.components, self.spacing, leaf.origin)
+            oc = res.c
+        check(lib().itkg_bspline_downsample_generate_region(ctypes.byref(src), ctypes.byref(largest),
+                                                            ctypes.byref(prm), ctypes.byref(oc), stream.ptr))
+        return res
 
 
 def unsharp_kernel(sigma: float) -> np.ndarray:

@@ -144,6 +144,8 @@ SIGNATURES = {
                                                                 I, P]),
     "itkg_unsharp_kernel": (st, [ctypes.c_double, ctypes.POINTER(ctypes.c_uint64), P, ctypes.c_uint64]),
     "itkg_unsharp_mask_generate_region": (st, [I, R, R, ctypes.POINTER(itkg_unsharp_params), I, P]),
+    "itkg_slice_by_slice_generate_region": (st, [I, R, G, I, P]),
+    "itkg_bspline_downsample_generate_region": (st, [I, R, G, I, P]),
     "itkg_separable_input_region_for_output": (st, [R, R, ctypes.c_int32, P, ctypes.c_uint64, R]),
     "itkg_separable_generate_region": (st, [I, R, R, ctypes.POINTER(itkg_separable_params), I, P]),
     "itkg_gaussian_vjp": (st, [I, I, G, I, ctypes.POINTER(ctypes.c_double), ctypes.c_int32, P]),

@@ -254,6 +254,33 @@ def binomial_f32(img, repetitions, **kw):
     return separable_f32(img, [BINOMIAL_KERNEL] * D, repetitions, **kw)
 
 
+def slice_by_slice(img, sigma, spacing=None, index=None, requested=None, comps=1):
+    """SliceBySliceFilter (spatial.rs:1304-1339) over a 3-D Image<f32> or Image<u8>: every
+    z slice of the requested region, as a 2-D Image over the request's x-y window with the
+    x and y spacing, through GaussianFilter (clamped to that window)."""
+    x = np.asarray(img)
+    D, sizes = _dims(x, comps)
+    if D != 3:
+        raise ValueError("SliceBySliceFilter is 3-D")
+    idx = tuple(index) if index is not None else (0, 0, 0)
+    ri, rs = requested if requested is not None else (idx, tuple(sizes))
+    sl = tuple(slice(ri[d] - idx[d], ri[d] - idx[d] + rs[d]) for d in reversed(range(3)))
+    crop = x[sl]
+    sp2 = list(spacing[:2]) if spacing is not None else [1.0, 1.0]
+    fn = gaussian_u8 if x.dtype == np.uint8 else gaussian_f32
+    return np.ascontiguousarray(np.stack([fn(crop[k], sigma, sp2, comps=comps) for k in range(crop.shape[0])]))
+
+
+def bspline_downsample(img, spacing=None, comps=1):
+    """BSplineDownsampleFilter (spatial.rs:1155-1166): GaussianFilter sigma 1.0 over the whole
+    image, then every other voxel from the first on every axis."""
+    x = np.asarray(img)
+    fn = gaussian_u8 if x.dtype == np.uint8 else gaussian_f32
+    full = fn(x, 1.0, spacing, comps=comps)
+    D = _dims(x, comps)[0]
+    return np.ascontiguousarray(full[tuple([slice(None, None, 2)] * D)])
+
+
 def unsharp_kernel(sigma: float) -> np.ndarray:
     """UnsharpMaskFilter's blur kernel (edges.rs:408, 415-424): radius ceil(3 sigma),
     exp(-(d d) / (2 sigma sigma)) through the C library's exp, divided by the

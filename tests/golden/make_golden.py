@@ -533,6 +533,35 @@ def main():
     cases.update(unsharp_case("f32_1d_s2", urng.random((30,), dtype=np.float32), 2.0, 0.5, 0.0))
     cases.update(unsharp_case("vec2d_s1", urng.random((7, 8, 3), dtype=np.float32), 1.0, 0.5, 0.0, comps=3))
     cases.update(unsharp_case("u8_2d_s1p5", urng.integers(0, 256, (10, 11), dtype=np.uint8), 1.5, 0.9, 3.0))
+    # in-crate callers of GaussianFilter (spatial.rs): SliceBySliceFilter, BSplineDownsampleFilter
+    crng = np.random.default_rng(20261207)
+
+    def slice_case(name, arr, sigma, spacing, requested, kind="f32"):
+        ri, rs = requested
+        out = []
+        for z in range(rs[2]):
+            pix = [(arr[ri[2] + z, ri[1] + y, ri[0] + x],) for y in range(rs[1]) for x in range(rs[0])]
+            img2 = ([ri[0], ri[1]], [rs[0], rs[1]], pix)
+            res = generate_region(img2, spacing[:2], sigma, [ri[0], ri[1]], [rs[0], rs[1]], kind)
+            out.append(from_ref(res, 1, np.float32 if kind == "f32" else np.uint8))
+        return {f"cal_{name}__in": arr, f"cal_{name}__out": np.stack(out),
+                f"cal_{name}__meta": np.array([0, sigma] + list(spacing) + list(ri) + list(rs), dtype=np.float64)}
+
+    def bspline_case(name, arr, spacing, kind="f32"):
+        img = to_ref(arr)
+        res = generate_region(img, spacing, 1.0, img[0], img[1], kind)
+        full = from_ref(res, 1, np.float32 if kind == "f32" else np.uint8)
+        D = arr.ndim
+        sub = np.ascontiguousarray(full[tuple([slice(None, None, 2)] * D)])
+        return {f"cal_{name}__in": arr, f"cal_{name}__out": sub,
+                f"cal_{name}__meta": np.array([1, 1.0] + list(spacing), dtype=np.float64)}
+
+    c3 = (crng.standard_normal((5, 9, 11)) * 2).astype(np.float32)
+    cases.update(slice_case("slices_s1p2", c3, 1.2, [1.0, 0.8, 2.0], ([1, 2, 1], [9, 6, 3])))
+    cases.update(slice_case("slices_u8_s1", crng.integers(0, 256, (3, 7, 8), dtype=np.uint8), 1.0, [1.0, 1.0, 1.0],
+                            ([0, 0, 0], [8, 7, 3]), kind="u8"))
+    cases.update(bspline_case("bspline3d_odd", c3, [1.0, 1.0, 1.0]))
+    cases.update(bspline_case("bspline2d_aniso", (crng.random((9, 12), dtype=np.float32)), [0.7, 1.5]))
     # kernels
     for s, sp in [(1.5, 1.0), (2.0, 1.0), (1.5, 0.7), (1.5, 2.5), (0.5, 1.0), (8.0, 1.0)]:
         cases[f"kernel_{s}_{sp}"] = np.array(build_kernel(s / sp, kernel_radius(s, sp)),
