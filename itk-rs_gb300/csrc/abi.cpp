@@ -415,6 +415,10 @@ static itkg_status generate_device(const itkg_image& in, const itkg_region& larg
       if (prm.algorithm == ITKG_ALGO_TWO_PASS)
         return set_error(ITKG_ERROR_UNSUPPORTED, "the two-pass kernels do not cover this geometry");
     }
+    // 3-D with the 1-tap kernel [1] on z (SliceBySliceFilter): the 2-D kernel over every slice
+    if (D == 3 && plan.radii[2] == 0 && plan.w64[2].size() == 1 && plan.w64[2][0] == 1.0 &&
+        launch_fused2d(g, w, s, /*dry_run=*/true) == ITKG_SUCCESS)
+      return launch_fused2d(g, w, s, false);
     itkg_status st = launch_fused(g, w, s, /*dry_run=*/true);
     if (st == ITKG_SUCCESS) return launch_fused(g, w, s, false);
     if (prm.algorithm == ITKG_ALGO_FUSED)

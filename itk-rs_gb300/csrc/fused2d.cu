@@ -49,7 +49,9 @@ struct Fused2DArgs {
   int32_t out_dtype;
   int32_t out_esz;               // bytes of one output component
   int32_t pad_;
-  int64_t units;                 // ntx * requested rows
+  int64_t units;                 // slices * ntx * requested rows
+  int64_t slice_units;           // ntx * requested rows
+  int64_t src_slice, dst_slice;  // bytes between slices (a 3-D image with a 1-tap z kernel)
   float wx[kMax2DK], wy[kMax2DK];
   f2_t wx2[kMax2DK], wy2[kMax2DK];
 };
@@ -132,8 +134,12 @@ __global__ void __launch_bounds__(Cfg2<RX, RY, C>::NT) k_fused2d(const Fused2DAr
   const uint32_t sbase = smem_addr(rows);
 
   for (int64_t u = u_begin; u < u_end;) {
-    const int64_t tile = u / nyr;
-    const int ys = (int)(u % nyr);
+    const int64_t zq = u / a.slice_units;
+    const int64_t uu = u - zq * a.slice_units;
+    const char* const srcz = a.src + zq * a.src_slice;
+    char* const dstz = a.dst + zq * a.dst_slice;
+    const int64_t tile = uu / nyr;
+    const int ys = (int)(uu % nyr);
     const int64_t yrem = ys + (u_end - u);
     const int ye = yrem < nyr ? (int)yrem : nyr;
     u += ye - ys;
@@ -153,7 +159,7 @@ __global__ void __launch_bounds__(Cfg2<RX, RY, C>::NT) k_fused2d(const Fused2DAr
       soff[i] = (uint32_t)(e * 4);
     }
     auto issue = [&](int row, int st) {
-      const char* base = a.src + (int64_t)(row - a.src_origin[1]) * a.src_pitch[1];
+      const char* base = srcz + (int64_t)(row - a.src_origin[1]) * a.src_pitch[1];
       const uint32_t sb = sbase + (uint32_t)(st * ROW * 4);
 #pragma unroll
       for (int i = 0; i < NLD; ++i)
@@ -177,7 +183,7 @@ __global__ void __launch_bounds__(Cfg2<RX, RY, C>::NT) k_fused2d(const Fused2DAr
     const int px0 = tx0 + lt * MXP;  // first output pixel of this thread
     int npx = a.req_hi[0] - px0 + 1;
     npx = npx < 0 ? 0 : (npx > MXP ? MXP : npx);
-    char* const obase = a.dst + (int64_t)(px0 - a.dst_origin[0]) * a.dst_pitch[0] + comp * a.out_esz;
+    char* const obase = dstz + (int64_t)(px0 - a.dst_origin[0]) * a.dst_pitch[0] + comp * a.out_esz;
     int prev = INT_MIN, cons = 0, p = 0;
     for (int j = jb; j <= je; ++j) {
       const int rr = clampi2(j, a.lo[1], a.hi[1]);
@@ -319,7 +325,9 @@ bool fits32(int64_t v) { return v >= INT_MIN && v <= INT_MAX; }
 }  // namespace
 
 itkg_status launch_fused2d(const FusedGeom& g, const float* const w[kMaxDim], void* stream, bool dry_run) {
-  if (g.dim != 2 || g.in_dtype != ITKG_F32 || g.out_dtype == ITKG_I16) return ITKG_ERROR_UNSUPPORTED;
+  // 2-D, or 3-D with the 1-tap kernel [1] on z (each slice filtered alone)
+  const bool slices = g.dim == 3 && g.radius[2] == 0 && w[2] && w[2][0] == 1.0f;
+  if ((g.dim != 2 && !slices) || g.in_dtype != ITKG_F32 || g.out_dtype == ITKG_I16) return ITKG_ERROR_UNSUPPORTED;
   if (g.radius[0] != g.radius[1] || g.radius[0] < 1) return ITKG_ERROR_UNSUPPORTED;
   const Entry2* e = nullptr;
   for (const Entry2& t : kTable2)
@@ -330,7 +338,8 @@ itkg_status launch_fused2d(const FusedGeom& g, const float* const w[kMaxDim], vo
         !fits32(g.req_index[d] + g.req_size[d]) || !fits32(g.req_index[d] - 64))
       return ITKG_ERROR_UNSUPPORTED;
   if (!fits32((g.hi[0] - g.src_origin[0] + 1) * g.src_pitch[0])) return ITKG_ERROR_UNSUPPORTED;
-  if (g.src_pitch[0] != 4 * g.comps || ((uintptr_t)g.src & 3) || (g.src_pitch[1] & 3))
+  if (g.src_pitch[0] != 4 * g.comps || ((uintptr_t)g.src & 3) || (g.src_pitch[1] & 3) ||
+      (slices && (g.src_pitch[2] & 3)))
     return ITKG_ERROR_UNSUPPORTED;
   if (dry_run) return ITKG_SUCCESS;
 
@@ -338,6 +347,14 @@ itkg_status launch_fused2d(const FusedGeom& g, const float* const w[kMaxDim], vo
   std::memset(&a, 0, sizeof a);
   a.src = static_cast<const char*>(g.src);
   a.dst = static_cast<char*>(g.dst);
+  int64_t nz = 1;
+  if (slices) {  // start at the first requested slice
+    nz = g.req_size[2];
+    a.src += (g.req_index[2] - g.src_origin[2]) * g.src_pitch[2];
+    a.dst += (g.req_index[2] - g.dst_origin[2]) * g.dst_pitch[2];
+    a.src_slice = g.src_pitch[2];
+    a.dst_slice = g.dst_pitch[2];
+  }
   for (int d = 0; d < 2; ++d) {
     a.src_pitch[d] = g.src_pitch[d];
     a.dst_pitch[d] = g.dst_pitch[d];
@@ -350,7 +367,8 @@ itkg_status launch_fused2d(const FusedGeom& g, const float* const w[kMaxDim], vo
     a.hi[d] = (int32_t)std::min<int64_t>(g.hi[d], g.src_origin[d] + g.src_size[d] - 1);
   }
   a.ntx = (int32_t)((g.req_size[0] + e->txw - 1) / e->txw);
-  a.units = (int64_t)a.ntx * g.req_size[1];
+  a.slice_units = (int64_t)a.ntx * g.req_size[1];
+  a.units = a.slice_units * nz;
   a.out_dtype = g.out_dtype;
   a.out_esz = dtype_size(g.out_dtype);
   for (int k = 0; k < 2 * e->r + 1; ++k) {

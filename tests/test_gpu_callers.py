@@ -72,3 +72,13 @@ def test_bspline_random(gpu, shape):
 def test_bspline_u8(gpu):
     x = np.random.default_rng(64).integers(0, 256, (15, 17, 19), dtype=np.uint8)
     assert np.array_equal(run_bspline(gpu, x), oracle.bspline_downsample(x))
+
+
+def test_slices_take_the_fused_2d_kernel(gpu):
+    x = np.random.default_rng(65).standard_normal((9, 33, 70)).astype(np.float32)
+    for rounding, name in ((0, "fused2d_f32_ref"), (1, "fused2d_f32_fma")):
+        got = run_slices(gpu, x, 1.7, rounding=rounding)
+        assert gpu.last_kernel() == name
+        want = oracle.slice_by_slice(x, 1.7)
+        assert bits_equal(got, want) if rounding == 0 else normwise(got, want) <= 1e-5
+
