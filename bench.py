@@ -802,7 +802,7 @@ def extra_workload(args):
                                "l2": "8 distinct 64 MiB input/output pairs per step (1 GiB > L2)"},
                     "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                                  "frac": achieved / peak,
-                                 "note": "SliceBySlice, algorithmic 8 B per voxel per call (two per-axis passes)"}})
+                                 "note": "SliceBySlice, algorithmic 8 B per voxel per call (the fused 2-D kernel over every slice)"}})
     print(json.dumps(out))
     return 0
 
