@@ -65,7 +65,10 @@ const XYEntry* find_xy(int r, int dtype) {
 
 bool fits_i32(int64_t v) { return v >= INT_MIN && v <= INT_MAX; }
 
-size_t z_smem(int rz) { return (size_t)(2 * rz + 1) * 256 * 16 * twopass::CfgZ<1>::QPT; }
+// the z kernel's rings: T quads, and for the unsharp store the input quads too
+size_t z_smem(int rz, bool ush = false) {
+  return (size_t)(2 * rz + 1) * 256 * 16 * twopass::CfgZ<1>::QPT * (ush ? 2 : 1);
+}
 
 const char* xy_name(int dtype, bool ref) {
   static const char* names[5][2] = {{"xy_pass_f32_fma", "xy_pass_f32_ref"},
@@ -191,7 +194,7 @@ itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], v
   const twopass::XYFn xyfn = e->fn[ref ? 1 : 0];
   if (st == ITKG_SUCCESS) st = max_resident_ctas(reinterpret_cast<const void*>(xyfn), e->smem, e->nt, &res_xy);
   if (st == ITKG_SUCCESS)
-    st = max_resident_ctas(reinterpret_cast<const void*>(zfn), z_smem(rz), 256, &res_z);
+    st = max_resident_ctas(reinterpret_cast<const void*>(zfn), z_smem(rz, ush != nullptr), 256, &res_z);
   if (st != ITKG_SUCCESS) {
     scratch_free(t, stream);
     return st;
@@ -310,7 +313,7 @@ itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], v
     if (za.nsplit > 0) gz = za.nsplit;
     cfg.gridDim = dim3((unsigned)gz);
     cfg.blockDim = dim3(256);
-    cfg.dynamicSmemBytes = z_smem(rz);
+    cfg.dynamicSmemBytes = z_smem(rz, ush != nullptr);
     err = cudaLaunchKernelEx(&cfg, zfn, za);
     note_launch(ush ? "z_pass_unsharp_fma" : (ref ? "z_pass_f32_ref" : "z_pass_f32_fma"));
     if (err == cudaSuccess) err = cudaGetLastError();

@@ -458,19 +458,21 @@ timeout:
 // VEC: f32 output whose rows allow 16-byte stores and whose width is a
 // multiple of 4 (every quad full).  USH (with VEC, FMA rounding): store
 // UnsharpMaskFilter's point-wise step of the input voxel and the blur
-// (unsharp_cheap_f32) instead of the blur; the input quad is loaded when its
-// step starts.
+// (unsharp_cheap_f32) instead of the blur; the input quads travel in a second
+// cp.async ring beside the T quads (the input quad of output z rides with T
+// slice z + RZ).
 template <int RZ, bool REF, bool VEC, bool USH = false>
 __global__ void __launch_bounds__(256, RZ <= 8 ? 2 : 1) k_z_pass(const __grid_constant__ ZArgs a) {
   static_assert(!USH || (VEC && !REF), "the unsharp variant stores whole quads, FMA rounding");
   using C = CfgZ<RZ>;
   constexpr int KZ = C::KZ, S = C::S, NT = C::NT;
   static_assert(C::QPT == 1, "one quad per thread");
-  extern __shared__ __align__(16) float4 zring[];  // [S][NT]
+  extern __shared__ __align__(16) float4 zring[];  // [S][NT], then (USH) the input ring [S][NT]
   const int tid = threadIdx.x;
   const int64_t u_begin = a.nsplit > 0 ? (int64_t)a.split[blockIdx.x] : a.units * blockIdx.x / gridDim.x;
   const int64_t u_end = a.nsplit > 0 ? (int64_t)a.split[blockIdx.x + 1] : a.units * (blockIdx.x + 1) / gridDim.x;
   const uint32_t my_slot0 = smem_u32(zring + tid);
+  const uint32_t my_oslot0 = smem_u32(zring + S * NT + tid);
   const uint64_t pol_t = policy_evict_first();
   // the next call's x-y grid may be scheduled now; it waits for this grid
   // before its first global memory access
@@ -500,8 +502,13 @@ __global__ void __launch_bounds__(256, RZ <= 8 ? 2 : 1) k_z_pass(const __grid_co
     const float* const tq = a.t + tl * (4 * tile_q) + 4 * w;
     int jn = jb;
     const float* pn = tq + (int64_t)(clampi(jn, a.t_s0, a.t_s1) - a.t_s0) * a.t_slice;
+    const char* const oq = USH ? a.ush_src + (int64_t)cx * 4 + (int64_t)cy * a.ush_pitch[1] : nullptr;
     auto prefetch = [&](int stage) {
       cp_async16_hint(my_slot0 + (uint32_t)(stage * NT * 16), pn, pol_t);
+      if constexpr (USH) {  // the input quad of output jn - RZ (clamped to this run's outputs)
+        const int zo = clampi(jn - RZ, z0, z1 - 1);
+        cp_async16_hint(my_oslot0 + (uint32_t)(stage * NT * 16), oq + (int64_t)(zo - a.z0) * a.ush_pitch[2], pol_t);
+      }
       fusedk::cp_async_commit();
       ++jn;
       pn += (jn > a.t_s0 && jn <= a.t_s1) ? a.t_slice : 0;
@@ -516,19 +523,14 @@ __global__ void __launch_bounds__(256, RZ <= 8 ? 2 : 1) k_z_pass(const __grid_co
     const int ncols = min(4, a.nx - cx);
     char* dz = a.dst + (int64_t)cx * a.dst_pitch[0] + (int64_t)cy * a.dst_pitch[1] +
                (int64_t)(z0 - a.z0) * a.dst_pitch[2];
-    const char* sz = nullptr;
-    if constexpr (USH)
-      sz = a.ush_src + (int64_t)cx * 4 + (int64_t)cy * a.ush_pitch[1] + (int64_t)(z0 - a.z0) * a.ush_pitch[2];
     // One slice at phase p (a constant once the callers' loops are unrolled):
     // slice j = (period start) + p sits in stage p; push it, refill the stage
     // with slice j + S, pop output j - RZ and store it if `store`.
     auto step = [&](int p, bool store) {
-      float4 og;
-      if constexpr (USH) {
-        if (store) og = __ldcs(reinterpret_cast<const float4*>(sz));
-      }
       fusedk::cp_async_wait<S - 1>();
       const float4 f = zring[p * NT + tid];
+      float4 og;
+      if constexpr (USH) og = zring[S * NT + p * NT + tid];
       f2_t v[2] = {pack2(f.x, f.y), pack2(f.z, f.w)};
       prefetch(p);
 #pragma unroll
@@ -562,7 +564,6 @@ __global__ void __launch_bounds__(256, RZ <= 8 ? 2 : 1) k_z_pass(const __grid_co
         __stcs(reinterpret_cast<float4*>(dz),
                make_float4(unsharp_cheap_f32(og.x, o[0], a.ush), unsharp_cheap_f32(og.y, o[1], a.ush),
                            unsharp_cheap_f32(og.z, o[2], a.ush), unsharp_cheap_f32(og.w, o[3], a.ush)));
-        sz += a.ush_pitch[2];
       } else if constexpr (VEC) {
         __stcs(reinterpret_cast<float4*>(dz), make_float4(o[0], o[1], o[2], o[3]));
       } else {
