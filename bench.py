@@ -741,6 +741,22 @@ def extra_workload(args):
             cpu = {"value": nx * ny * sl / run(sl), "unit": "voxels/s", "cores": threads, "kind": "port",
                    "sample": f"the blur of {sl} output slices of 256x256 (C restatement, {threads} threads; "
                              "the point-wise step is not timed)"}
+        # Image<u8, 3>: the blobs volume scaled to 0..255 (u8 pixel arithmetic, bit-exact)
+        vol8 = np.clip(np.rint(vol * 100.0), 0, 255).astype(np.uint8)
+        d8 = [itkg.DeviceImage.from_host(itkg.Image(vol8)) for _ in range(NVOL)]
+        o8 = [itkg.DeviceImage(d8[0].region, itkg.U8) for _ in range(NVOL)]
+        p8 = _abi.itkg_unsharp_params()
+        p8.sigma, p8.amount, p8.threshold, p8.rounding = usig, amount, 0.0, itkg.ROUND_REFERENCE
+
+        def step8():
+            for d, o in zip(d8, o8):
+                _abi.check(L.itkg_unsharp_mask_generate_region(ctypes.byref(d.c), ctypes.byref(lg), ctypes.byref(rq),
+                                                               ctypes.byref(p8), ctypes.byref(o.c), sp.ptr))
+        ms8 = _timed(stream, step8, args.steps, args.warmup)
+        got8 = o8[0].download()
+        lines["u8_reference"] = {"voxels_per_s": NVOL * nvox / (ms8 * 1e-3), "ms_per_call": ms8 / NVOL,
+                                 "kernel": itkg.last_kernel(),
+                                 "bit_exact": bool(np.array_equal(got8, oracle.unsharp_mask(vol8, usig, amount, 0.0)))}
         best = lines["fma"]
         out.update({"value": best["voxels_per_s"], "ms_per_step": best["ms_per_call"] * NVOL, "dtype": "f32",
                     "config": {"workload": "UnsharpMaskFilter sigma 1.5 amount 0.5, Image<f32,3> 256^3 blobs+noise, "

@@ -193,6 +193,7 @@ struct UnsharpConsts {
   int a_exact;               // amount == ah exactly
   int fast;                  // 0: every voxel takes the f64 sequence
   int cheap;                 // FMA rounding: o + amount e by one f32 FMA
+  float u8_min_pass;         // u8 pixels: |e| (an integer) passes the threshold test iff |e| >= this
 };
 
 UnsharpConsts unsharp_consts(double amount, double threshold, bool cheap);

@@ -46,7 +46,8 @@ __global__ void __launch_bounds__(kT) k_unsharp(const char* in, int64_t ip0, int
       const Tp b = *reinterpret_cast<const Tp*>(blur + x * bp0 + y * bp1 + z * bp2);
       char* const dst = out + x * op0 + y * op1 + z * op2;
       if constexpr (sizeof(Tp) == 1) {
-        const uint8_t q = u8_of(unsharp_f64((double)o, (double)b, k.amount, k.threshold));
+        uint8_t q;
+        if (!k.fast || !unsharp_fast_u8(o, b, k, q)) q = u8_of(unsharp_f64((double)o, (double)b, k.amount, k.threshold));
         for (int c = 0; c < comps; ++c) reinterpret_cast<uint8_t*>(dst)[c] = q;
       } else {
         const float q = unsharp_f32(o, b, k);
@@ -194,6 +195,10 @@ UnsharpConsts unsharp_consts(double amount, double threshold, bool cheap) {
   k.al = (float)(amount - (double)k.ah);
   k.a_exact = (double)k.ah == amount ? 1 : 0;
   k.thr_neg = threshold < 0.0 ? 1 : 0;
+  // |e| > threshold for an integer |e| <= 255: |e| >= floor(threshold) + 1
+  if (std::isnan(threshold)) k.u8_min_pass = INFINITY;
+  else if (threshold < 0.0) k.u8_min_pass = 0.0f;
+  else k.u8_min_pass = threshold >= 256.0 ? 256.0f : (float)(std::floor(threshold) + 1.0);
   if (std::isnan(threshold)) {  // |e| > NaN never holds
     k.thr_up = INFINITY;
     k.thr_dn = INFINITY;

@@ -92,6 +92,45 @@ __device__ __forceinline__ bool unsharp_fast_f32(float o, float b, const Unsharp
   return false;
 }
 
+// u8 pixels (o, b in 0..255): u8::from_f64 (round half away from zero, clamp
+// to [0, 255]) of the reference's f64 result, from f32 arithmetic; false when
+// undecided.  e = o - b is exact, the threshold test on the integer |e| is
+// exact (k.u8_min_pass), and v lies within delta of sh + s2 as for f32 pixels;
+// from_f64 is monotonic, so equal conversions of the outward-rounded bounds
+// decide it.  At an exact tie (amount 0.5 and an odd e) the bounds straddle a
+// half-integer; when amount is an f32 and ah e and o + ah e are exact in f32
+// (t == 0, s1 == 0), the reference's f64 steps were exact too and the tie is
+// converted as the reference converts it.
+__device__ __forceinline__ uint8_t u8_from_f32(float v) {
+  return (uint8_t)fminf(fmaxf(roundf(v), 0.0f), 255.0f);
+}
+
+__device__ __forceinline__ bool unsharp_fast_u8(uint8_t ob, uint8_t bb, const UnsharpConsts& k, uint8_t& out) {
+  const float o = (float)ob, e = __fsub_rn(o, (float)bb);
+  if (!(fabsf(e) >= k.u8_min_pass) || e == 0.0f) {  // v = o (o + amount 0 = o for e = 0)
+    out = ob;
+    return true;
+  }
+  const float ph = __fmul_rn(k.ah, e);
+  const float t = __fmaf_rn(k.ah, e, -ph);
+  const float pl = __fadd_rn(t, __fmul_rn(k.al, e));
+  float sh, s1;
+  two_sum(o, ph, sh, s1);
+  const float s2 = __fadd_rn(s1, pl);
+  const float delta = __fmul_rn(__fadd_ru(o, fabsf(ph)), 0x1p-40f);
+  const uint8_t qh = u8_from_f32(__fadd_ru(sh, __fadd_ru(s2, delta)));
+  const uint8_t ql = u8_from_f32(__fadd_rd(sh, __fadd_rd(s2, -delta)));
+  if (qh == ql) {
+    out = qh;
+    return true;
+  }
+  if (k.a_exact && t == 0.0f && s1 == 0.0f) {
+    out = u8_from_f32(sh);
+    return true;
+  }
+  return false;
+}
+
 // FMA rounding (k.cheap, k.fast): o + amount e by one f32 FMA with e = o - b
 // rounded to f32 -- within a few f32 ulps of the reference -- and the
 // threshold test still decided as the reference decides it (in f64 when

@@ -137,3 +137,11 @@ def test_fused_z_store_and_fallback_paths(gpu, rounding):
         else:
             assert normwise(got, want) <= TOL_FMA
         assert gpu.last_kernel().startswith("z_pass_unsharp") == (fused and rounding == 1), gpu.last_kernel()
+
+
+@pytest.mark.parametrize("amount,threshold", [(0.5, 0.0), (1.5, 3.0), (0.1, 2.5), (3.0, -1.0), (0.7, float("nan"))])
+def test_u8_amounts_and_thresholds(gpu, amount, threshold):
+    # u8 pixels: integer edges, exact ties at amount 0.5 / 1.5, integer thresholds met exactly
+    x = np.random.default_rng(71).integers(0, 256, (20, 26, 36), dtype=np.uint8)
+    want = oracle.unsharp_mask(x, 1.2, amount, threshold)
+    assert np.array_equal(run(gpu, x, 1.2, amount, threshold), want)
