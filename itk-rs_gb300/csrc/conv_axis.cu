@@ -67,20 +67,25 @@ __global__ void __launch_bounds__(kThreads)
 
 // GaussianFilter<Image<u8>>: NumericPixel for u8 (src/pixel.rs:430-435).  Each
 // tap is round(x as f64 * w).clamp(0, 255) as u8 and the accumulator is a u8
-// with wrapping adds.  The per-tap products are tabulated once per block:
-// lut[k][v] for all 256 values of v, computed in f64 exactly as the reference
-// does (an f64 product and round-half-away-from-zero are exact operations), so
-// the pass itself is table lookups and byte adds.
+// with wrapping adds.  The per-tap products are tabulated once per pass by
+// k_u8_lut: lut[k][v] for all 256 values of v, computed in f64 exactly as the
+// reference does (an f64 product and round-half-away-from-zero are exact
+// operations); each block copies the table into shared memory, so the pass
+// itself is table lookups and byte adds.
+__global__ void __launch_bounds__(kThreads) k_u8_lut(const AxisWeightsF64 W, int K, uint8_t* lut) {
+  const int i = blockIdx.x * kThreads + threadIdx.x;
+  if (i >= K * 256) return;
+  const int k = i >> 8, v = i & 255;
+  double p = round((double)v * W.w[k]);
+  p = p < 0.0 ? 0.0 : (p > 255.0 ? 255.0 : p);
+  lut[i] = (uint8_t)p;
+}
+
 __global__ void __launch_bounds__(kThreads)
-    k_conv_axis_u8(const AxisArgs a, const AxisWeightsF64 W) {
+    k_conv_axis_u8(const AxisArgs a, const uint32_t* glut) {
   extern __shared__ uint8_t lut[];
   const int K = 2 * a.radius + 1;
-  for (int i = threadIdx.x; i < K * 256; i += kThreads) {
-    const int k = i >> 8, v = i & 255;
-    double p = round((double)v * W.w[k]);
-    p = p < 0.0 ? 0.0 : (p > 255.0 ? 255.0 : p);
-    lut[i] = (uint8_t)p;
-  }
+  for (int i = threadIdx.x; i < K * 64; i += kThreads) reinterpret_cast<uint32_t*>(lut)[i] = glut[i];
   __syncthreads();
   const int64_t rowlen = a.out_size[0] * a.comps;
   const int64_t t = (int64_t)blockIdx.x * kThreads + threadIdx.x;
@@ -307,8 +312,19 @@ itkg_status launch_conv_axis_u8(const AxisArgs& a, const double* w, void* stream
   cudaFuncSetAttribute(k_conv_axis_u8, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        256 * (2 * kMaxU8Radius + 1));
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  k_conv_axis_u8<<<grid_for(a), kThreads, smem, s>>>(a, W);
+  void* glut = nullptr;
+  {
+    const itkg_status st = scratch_alloc(&glut, smem, s);  // K * 256 bytes: a whole number of uint32 words
+    if (st != ITKG_SUCCESS) return st;
+  }
+  k_u8_lut<<<(unsigned)((K * 256 + kThreads - 1) / kThreads), kThreads, 0, s>>>(W, K, static_cast<uint8_t*>(glut));
+  note_launch("u8_lut");
+  // a few dozen rows per block, so that copying the table is a small part of a block's work
+  dim3 grid = grid_for(a);
+  grid.y = (unsigned)std::min<int64_t>((int64_t)grid.y, std::max<int64_t>(1, 4096 / (int64_t)grid.x));
+  k_conv_axis_u8<<<grid, kThreads, smem, s>>>(a, static_cast<const uint32_t*>(glut));
   note_launch("conv_axis_u8_pixel");
+  scratch_free(glut, s);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return set_error(ITKG_ERROR_CUDA, "conv_axis_u8 launch: %s", cudaGetErrorString(e));
   return ITKG_SUCCESS;
