@@ -1163,11 +1163,10 @@ itkg_status itkg_unsharp_mask_generate_region(const itkg_image* input, const itk
     st = scratch_alloc(&pout, image_bytes(dout), s);
     dout.data = pout;
   }
-  // 3-D f32 in FMA rounding: the two-pass blur whose z kernel stores the
-  // point-wise step directly (no blur image in memory)
+  // 3-D f32: the two-pass blur whose z kernel stores the point-wise step
+  // directly (no blur image in memory)
   bool fused = false;
-  if (st == ITKG_SUCCESS && D == 3 && input->dtype == ITKG_F32 && input->components == 1 &&
-      params->rounding == ITKG_ROUND_FMA) {
+  if (st == ITKG_SUCCESS && D == 3 && input->dtype == ITKG_F32 && input->components == 1) {
     const UnsharpConsts k = unsharp_consts(params->amount, params->threshold, params->rounding == ITKG_ROUND_FMA);
     Plan plan;
     if (k.fast && make_plan(din, *requested, *largest, ks, &plan) == ITKG_SUCCESS && plan.symmetric &&

@@ -148,9 +148,9 @@ itkg_status encode_input_map(const FusedGeom& g, int box_w, int box_h, void* map
 // an L2-sized f32 intermediate (rx == ry <= 12, rz <= 12, TMA-aligned input).
 // ITKG_ERROR_UNSUPPORTED (no error set) when it does not apply.
 // ush: if non-NULL, the z kernel stores UnsharpMaskFilter's point-wise step
-// applied to the blur and to the input voxel instead of the blur itself (FMA
-// rounding and ush->cheap, f32 input and output with 16-byte aligned rows of
-// whole quads; else unsupported).
+// applied to the blur and to the input voxel instead of the blur itself
+// (ush->cheap in FMA rounding, not in reference rounding; f32 input and output
+// with 16-byte aligned rows of whole quads; else unsupported).
 struct UnsharpConsts;
 itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], void* stream,
                             bool dry_run, const UnsharpConsts* ush = nullptr);

@@ -156,7 +156,8 @@ itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], v
   // TMA checks above make them 16-byte aligned for f32 input)
   const char* const src0 = static_cast<const char*>(g.src) + (g.req_index[0] - g.src_origin[0]) * g.src_pitch[0] +
                            (g.req_index[1] - g.src_origin[1]) * g.src_pitch[1];
-  if (ush && (!vec || g.in_dtype != ITKG_F32 || g.rounding == ITKG_ROUND_REFERENCE || !ush->cheap ||
+  // the point-wise step's arithmetic follows the blur's rounding
+  if (ush && (!vec || g.in_dtype != ITKG_F32 || (g.rounding == ITKG_ROUND_REFERENCE) == (ush->cheap != 0) ||
               ((uintptr_t)src0 & 15)))
     return ITKG_ERROR_UNSUPPORTED;
   if (dry_run) return ITKG_SUCCESS;
@@ -315,7 +316,7 @@ itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], v
     cfg.blockDim = dim3(256);
     cfg.dynamicSmemBytes = z_smem(rz, ush != nullptr);
     err = cudaLaunchKernelEx(&cfg, zfn, za);
-    note_launch(ush ? "z_pass_unsharp_fma" : (ref ? "z_pass_f32_ref" : "z_pass_f32_fma"));
+    note_launch(ush ? (ref ? "z_pass_unsharp_ref" : "z_pass_unsharp_fma") : (ref ? "z_pass_f32_ref" : "z_pass_f32_fma"));
     if (err == cudaSuccess) err = cudaGetLastError();
     if (err != cudaSuccess) st = set_error(ITKG_ERROR_CUDA, "z pass launch: %s", cudaGetErrorString(err));
   }

@@ -456,14 +456,15 @@ timeout:
 // ---------------------------------------------------------------------------
 // z pass
 // VEC: f32 output whose rows allow 16-byte stores and whose width is a
-// multiple of 4 (every quad full).  USH (with VEC, FMA rounding): store
-// UnsharpMaskFilter's point-wise step of the input voxel and the blur
-// (unsharp_cheap_f32) instead of the blur; the input quads travel in a second
-// cp.async ring beside the T quads (the input quad of output z rides with T
-// slice z + RZ).
+// multiple of 4 (every quad full).  USH (with VEC): store UnsharpMaskFilter's
+// point-wise step of the input voxel and the blur instead of the blur --
+// unsharp_cheap_f32 in FMA rounding, the exact f32 test (unsharp_quad_exact,
+// one out-of-line copy) in reference rounding; the input quads travel in a
+// second cp.async ring beside the T quads (the input quad of output z rides
+// with T slice z + RZ).
 template <int RZ, bool REF, bool VEC, bool USH = false>
 __global__ void __launch_bounds__(256, RZ <= 8 ? 2 : 1) k_z_pass(const __grid_constant__ ZArgs a) {
-  static_assert(!USH || (VEC && !REF), "the unsharp variant stores whole quads, FMA rounding");
+  static_assert(!USH || VEC, "the unsharp variant stores whole quads");
   using C = CfgZ<RZ>;
   constexpr int KZ = C::KZ, S = C::S, NT = C::NT;
   static_assert(C::QPT == 1, "one quad per thread");
@@ -561,9 +562,12 @@ __global__ void __launch_bounds__(256, RZ <= 8 ? 2 : 1) k_z_pass(const __grid_co
       unpack2(d0, o[0], o[1]);
       unpack2(d1, o[2], o[3]);
       if constexpr (USH) {
-        __stcs(reinterpret_cast<float4*>(dz),
-               make_float4(unsharp_cheap_f32(og.x, o[0], a.ush), unsharp_cheap_f32(og.y, o[1], a.ush),
-                           unsharp_cheap_f32(og.z, o[2], a.ush), unsharp_cheap_f32(og.w, o[3], a.ush)));
+        if constexpr (REF)
+          __stcs(reinterpret_cast<float4*>(dz), unsharp_quad_exact(og, o[0], o[1], o[2], o[3], a.ush));
+        else
+          __stcs(reinterpret_cast<float4*>(dz),
+                 make_float4(unsharp_cheap_f32(og.x, o[0], a.ush), unsharp_cheap_f32(og.y, o[1], a.ush),
+                             unsharp_cheap_f32(og.z, o[2], a.ush), unsharp_cheap_f32(og.w, o[3], a.ush)));
       } else if constexpr (VEC) {
         __stcs(reinterpret_cast<float4*>(dz), make_float4(o[0], o[1], o[2], o[3]));
       } else {

@@ -1,5 +1,5 @@
 // The z kernels of the two-pass 3-D forward that store UnsharpMaskFilter's
-// point-wise step in FMA rounding (k_z_pass<R, false, true, true>), in their own translation
+// point-wise step (k_z_pass<R, REF, true, true>), in their own translation
 // unit so they compile beside the plain ones.
 #include "two_pass.cuh"
 
@@ -8,11 +8,11 @@ namespace twopass {
 namespace {
 struct ZUshEntry {
   int r;
-  ZFn fn;  // FMA rounding only
+  ZFn fn[2];  // [ref]
 };
 template <int R>
 ZUshEntry make_z_ush() {
-  return ZUshEntry{R, k_z_pass<R, false, true, true>};
+  return ZUshEntry{R, {k_z_pass<R, false, true, true>, k_z_pass<R, true, true, true>}};
 }
 const ZUshEntry kZUsh[] = {make_z_ush<1>(), make_z_ush<2>(),  make_z_ush<3>(),  make_z_ush<4>(),
                            make_z_ush<5>(), make_z_ush<6>(),  make_z_ush<7>(),  make_z_ush<8>(),
@@ -20,9 +20,8 @@ const ZUshEntry kZUsh[] = {make_z_ush<1>(), make_z_ush<2>(),  make_z_ush<3>(),  
 }  // namespace
 
 ZFn z_ush_fn(int r, bool ref) {
-  if (ref) return nullptr;
   for (const ZUshEntry& z : kZUsh)
-    if (z.r == r) return z.fn;
+    if (z.r == r) return z.fn[ref ? 1 : 0];
   return nullptr;
 }
 }  // namespace twopass

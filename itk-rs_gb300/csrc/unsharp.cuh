@@ -151,4 +151,18 @@ __device__ __forceinline__ float unsharp_f32(float o, float b, const UnsharpCons
   return q;
 }
 
+// Reference rounding, one quad: the exact f32 test per voxel, f64 where it
+// cannot decide.  Out of line, so that a caller unrolled over many steps
+// carries one copy.
+__device__ __noinline__ inline float4 unsharp_quad_exact(float4 o, float b0, float b1, float b2, float b3,
+                                                         const UnsharpConsts& k) {
+  const float ov[4] = {o.x, o.y, o.z, o.w}, bv[4] = {b0, b1, b2, b3};
+  float r[4];
+#pragma unroll
+  for (int c = 0; c < 4; ++c)
+    if (!k.fast || !unsharp_fast_f32(ov[c], bv[c], k, r[c]))
+      r[c] = __double2float_rn(unsharp_f64((double)ov[c], (double)bv[c], k.amount, k.threshold));
+  return make_float4(r[0], r[1], r[2], r[3]);
+}
+
 }  // namespace itkg
