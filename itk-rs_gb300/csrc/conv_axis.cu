@@ -299,6 +299,62 @@ itkg_status launch_conv_axis_f32(const AxisArgs& a, const float* w, int in_dtype
   }
 }
 
+// Scalar u8 images (x pitch 1): four consecutive x outputs per thread, so the
+// tap positions (and, on x, the loaded window of 4 + 2r pixels) are shared.
+// The u8 adds wrap, so their order does not change the result.
+__global__ void __launch_bounds__(kThreads)
+    k_conv_axis_u8_x4(const AxisArgs a, const uint32_t* glut) {
+  extern __shared__ uint8_t lut[];
+  const int K = 2 * a.radius + 1;
+  for (int i = threadIdx.x; i < K * 64; i += kThreads) reinterpret_cast<uint32_t*>(lut)[i] = glut[i];
+  __syncthreads();
+  const int64_t t = (int64_t)blockIdx.x * kThreads + threadIdx.x;
+  const int64_t x = a.out_index[0] + 4 * t;
+  const int64_t xe = a.out_index[0] + a.out_size[0];
+  if (x >= xe) return;
+  const int n = xe - x < 4 ? (int)(xe - x) : 4;
+  const int64_t nrows = a.out_size[1] * a.out_size[2];
+  const int axis = a.axis;
+  for (int64_t row = blockIdx.y; row < nrows; row += gridDim.y) {
+    const int64_t y = row % a.out_size[1] + a.out_index[1];
+    const int64_t z = row / a.out_size[1] + a.out_index[2];
+    uint32_t acc[4] = {0, 0, 0, 0};
+    const uint8_t* const src = static_cast<const uint8_t*>(a.src);
+    if (axis == 0) {
+      const uint8_t* sb = src + (y - a.src_origin[1]) * a.src_pitch[1] + (z - a.src_origin[2]) * a.src_pitch[2];
+      for (int i = 0; i < K + n - 1; ++i) {  // window position x - r + i: the taps of outputs x .. x + n - 1
+        int64_t s = x - a.radius + i;
+        s = s < a.lo ? a.lo : (s > a.hi ? a.hi : s);
+        const uint32_t v = sb[s - a.src_origin[0]];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const int k = i - j;
+          if (k >= 0 && k < K) acc[j] += lut[(k << 8) | v];
+        }
+      }
+    } else {
+      const int64_t oa = axis == 1 ? y : z;
+      const uint8_t* sb = src + (x - a.src_origin[0]) +
+                          (axis == 1 ? (z - a.src_origin[2]) * a.src_pitch[2] : (y - a.src_origin[1]) * a.src_pitch[1]);
+      const int64_t ap = a.src_pitch[axis];
+      const int64_t ao = a.src_origin[axis];
+      for (int k = 0; k < K; ++k) {
+        int64_t s = oa + k - a.radius;
+        s = s < a.lo ? a.lo : (s > a.hi ? a.hi : s);
+        const uint8_t* p = sb + (s - ao) * ap;
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+          if (j < n) acc[j] += lut[(k << 8) | p[j]];
+      }
+    }
+    uint8_t* db = static_cast<uint8_t*>(a.dst) + (x - a.dst_origin[0]) + (y - a.dst_origin[1]) * a.dst_pitch[1] +
+                  (z - a.dst_origin[2]) * a.dst_pitch[2];
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      if (j < n) db[j] = (uint8_t)acc[j];
+  }
+}
+
 itkg_status launch_conv_axis_u8(const AxisArgs& a, const double* w, void* stream) {
   const int K = 2 * a.radius + 1;
   if (a.radius > kMaxU8Radius)
@@ -320,9 +376,16 @@ itkg_status launch_conv_axis_u8(const AxisArgs& a, const double* w, void* stream
   k_u8_lut<<<(unsigned)((K * 256 + kThreads - 1) / kThreads), kThreads, 0, s>>>(W, K, static_cast<uint8_t*>(glut));
   note_launch("u8_lut");
   // a few dozen rows per block, so that copying the table is a small part of a block's work
+  const bool x4 = a.comps == 1 && a.src_pitch[0] == 1 && a.dst_pitch[0] == 1;
   dim3 grid = grid_for(a);
+  if (x4) grid.x = (unsigned)(((a.out_size[0] + 3) / 4 + kThreads - 1) / kThreads);
   grid.y = (unsigned)std::min<int64_t>((int64_t)grid.y, std::max<int64_t>(1, 4096 / (int64_t)grid.x));
-  k_conv_axis_u8<<<grid, kThreads, smem, s>>>(a, static_cast<const uint32_t*>(glut));
+  if (x4) {
+    cudaFuncSetAttribute(k_conv_axis_u8_x4, cudaFuncAttributeMaxDynamicSharedMemorySize, 256 * (2 * kMaxU8Radius + 1));
+    k_conv_axis_u8_x4<<<grid, kThreads, smem, s>>>(a, static_cast<const uint32_t*>(glut));
+  } else {
+    k_conv_axis_u8<<<grid, kThreads, smem, s>>>(a, static_cast<const uint32_t*>(glut));
+  }
   note_launch("conv_axis_u8_pixel");
   scratch_free(glut, s);
   cudaError_t e = cudaGetLastError();
