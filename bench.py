@@ -433,7 +433,7 @@ def extra_workload(args):
             ctypes.byref(outimg.c), sp.ptr))
 
     if args.workload == "fwd2d":
-        # configs[0]: Image<f32,2> 512x512, U[0,1), sigma 1.5 (r = 5)
+        # 2-D workload: Image<f32,2> 512x512, U[0,1), sigma 1.5 (r = 5)
         n = 64
         imgs = [rng.random((512, 512), dtype=np.float32) for _ in range(4)]
         devs = [itkg.DeviceImage.from_host(itkg.Image(imgs[i % 4])) for i in range(n)]
@@ -451,7 +451,7 @@ def extra_workload(args):
                                  "unit": "GB/s", "frac": vox * 8 / (ms * 1e-3) / 1e9 / peak},
                     "accuracy": {"normwise_rel_vs_ref_f32": err}})
     elif args.workload == "ct16":
-        # configs[2]: Image<i16,3> 512x512x384 CT-like, spacing (0.7,0.7,2.5), sigma 1.5 mm
+        # CT workload: Image<i16,3> 512x512x384 CT-like, spacing (0.7,0.7,2.5), sigma 1.5 mm
         shape = (384, 512, 512)
         z = np.arange(shape[0])[:, None, None]
         y = np.arange(shape[1])[None, :, None]
@@ -491,7 +491,7 @@ def extra_workload(args):
                     "dtype": "i16->f32", "config": {"workload": "CT i16 512x512x384, spacing (0.7,0.7,2.5), sigma 1.5 mm, r=(7,7,2)",
                                                    "outputs": lines}})
     elif args.workload in ("batch", "batch_vjp"):
-        # configs[3]: 64 Image<f32,3> dims U{32..320}, sigma U[0.5,4]; 256 RGB 2-D sides U{64..1024}
+        # batch workload: 64 Image<f32,3> dims U{32..320}, sigma U[0.5,4]; 256 RGB 2-D sides U{64..1024}
         vols = []
         for i in range(64):
             shape = tuple(int(v) for v in rng.integers(32, 321, 3))
@@ -550,7 +550,7 @@ def extra_workload(args):
         if sb.value:
             L.itkg_device_free(sb)
     elif args.workload == "vjp_stack":
-        # configs[4]: 8 x 192^3 blobs+noise, sigma {1,2,4,8}; loss sum_l |G_l x - t|^2
+        # multi-scale VJP workload: 8 x 192^3 blobs+noise, sigma {1,2,4,8}; loss sum_l |G_l x - t|^2
         n = 8
         shape = (192, 192, 192)
         xs = [blobs_volume(shape, 100 + i) for i in range(n)]
