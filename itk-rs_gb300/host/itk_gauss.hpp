@@ -526,6 +526,94 @@ SeparableFilter<S> make_binomial(S s, uint64_t repetitions) {
 template <typename S>
 auto spacing_of(const SeparableFilter<S>& f) { return f.spacing(); }
 
+// UnsharpMaskFilter { source, sigma, amount, threshold } (edges.rs:374-452):
+// I + amount (I - blur(I)) where |I - blur(I)| > threshold; the blur kernel
+// has radius ceil(3 sigma) on every axis (itkg_unsharp_kernel).
+template <typename S>
+struct UnsharpMaskFilter {
+  S source;
+  double sigma;
+  double amount = 0.5;     // UnsharpMaskFilter::new (edges.rs:387-389)
+  double threshold = 0.0;
+  int rounding = ITKG_ROUND_REFERENCE;
+
+  static constexpr int Dim = std::decay_t<S>::Dim;
+  using Pixel = typename std::decay_t<S>::Pixel;
+
+  UnsharpMaskFilter(S s, double sg) : source(std::forward<S>(s)), sigma(sg) {}
+  UnsharpMaskFilter& with_amount(double a) {  // edges.rs:390
+    amount = a;
+    return *this;
+  }
+
+  Region<Dim> largest_region() const { return source.largest_region(); }
+  std::array<double, Dim> spacing() const { return spacing_of(source); }
+
+  Region<Dim> input_region_for_output(const Region<Dim>& out) const {
+    uint64_t r = 0;
+    check(itkg_unsharp_kernel(sigma, &r, nullptr, 0));
+    itkg_region o = out.to_c(), l = largest_region().to_c(), in;
+    const uint64_t rr[3] = {r, r, r};
+    check(itkg_separable_input_region_for_output(&o, &l, Dim, rr, 1, &in));
+    return Region<Dim>::from_c(in);
+  }
+
+  auto generate_region(const Region<Dim>& requested) const {
+    auto in = source.generate_region(input_region_for_output(requested));
+    auto out = Image<Pixel, Dim>::allocate(requested, in.spacing, in.origin, Pixel{});
+    itkg_unsharp_params p;
+    std::memset(&p, 0, sizeof p);
+    p.sigma = sigma;
+    p.amount = amount;
+    p.threshold = threshold;
+    p.rounding = rounding;
+    itkg_region l = largest_region().to_c(), r = requested.to_c();
+    itkg_image ic = in.desc(), oc = out.desc();
+    check(itkg_unsharp_mask_generate_region(&ic, &l, &r, &p, &oc, nullptr));
+    return out;
+  }
+};
+
+template <typename S>
+auto spacing_of(const UnsharpMaskFilter<S>& f) { return f.spacing(); }
+
+// SliceBySliceFilter { source, sigma } (spatial.rs:1284-1340), 3-D: every z
+// slice of the request through a 2-D GaussianFilter over the request's x-y
+// window.
+template <typename S>
+struct SliceBySliceFilter {
+  S source;
+  double sigma;
+  int rounding = ITKG_ROUND_REFERENCE;
+
+  static constexpr int Dim = std::decay_t<S>::Dim;
+  using Pixel = typename std::decay_t<S>::Pixel;
+  static_assert(Dim == 3, "SliceBySliceFilter is 3-D");
+
+  SliceBySliceFilter(S s, double sg) : source(std::forward<S>(s)), sigma(sg) {}
+
+  Region<Dim> largest_region() const { return source.largest_region(); }
+  std::array<double, Dim> spacing() const { return spacing_of(source); }
+  Region<Dim> input_region_for_output(const Region<Dim>& out) const { return out; }
+
+  auto generate_region(const Region<Dim>& requested) const {
+    auto in = source.generate_region(requested);  // spatial.rs:1305
+    auto out = Image<Pixel, Dim>::allocate(requested, in.spacing, in.origin, Pixel{});
+    itkg_gaussian_params p;
+    std::memset(&p, 0, sizeof p);
+    p.sigma = sigma;
+    p.arithmetic = PixelTraits<Pixel>::arith;
+    p.rounding = rounding;
+    itkg_region r = requested.to_c();
+    itkg_image ic = in.desc(), oc = out.desc();
+    check(itkg_slice_by_slice_generate_region(&ic, &r, &p, &oc, nullptr));
+    return out;
+  }
+};
+
+template <typename S>
+auto spacing_of(const SliceBySliceFilter<S>& f) { return f.spacing(); }
+
 // stream_full (source.rs:81-98): allocate the full output once, fill it piece
 // by piece along the slowest axis.
 template <typename S>

@@ -193,6 +193,38 @@ static void test_binomial_blur() {
   CHECK(std::fabs(sum - 1.0f) < 0.05f, "sum=%g", sum);
 }
 
+// UnsharpMaskFilter (edges.rs:374-452): a constant stays constant (to the
+// f32 blur's rounding); a step gets an undershoot and an overshoot.
+static void test_unsharp_mask() {
+  auto c = solid_image<2>({9, 7}, 4.0f);
+  UnsharpMaskFilter<Image<float, 2>> u(c, 1.0);
+  auto out = u.generate_region(u.largest_region());
+  for (float v : out.data) CHECK(std::fabs(v - 4.0f) < 1e-5f, "constant: %g", v);
+  auto step = solid_image<1>({20}, 0.0f);
+  for (int64_t i = 10; i < 20; ++i) step.set_pixel({{i}}, 1.0f);
+  UnsharpMaskFilter<Image<float, 1>> us(step, 1.0);
+  us.with_amount(1.0);
+  auto o = us.generate_region(us.largest_region());
+  CHECK(o.get_pixel({{9}}) < 0.0f && o.get_pixel({{10}}) > 1.0f, "step: %g %g", o.get_pixel({{9}}),
+        o.get_pixel({{10}}));
+  auto sub = us.generate_region(Region<1>{{{5}}, {{10}}});
+  for (int64_t i = 5; i < 15; ++i)
+    CHECK(sub.get_pixel({{i}}) == o.get_pixel({{i}}), "sub-region at %lld", (long long)i);
+}
+
+// SliceBySliceFilter (spatial.rs:1284-1340): slices are smoothed on their own,
+// so a volume constant on every slice comes back unchanged.
+static void test_slice_by_slice() {
+  auto v = solid_image<3>({6, 5, 4}, 0.0f);
+  for (int64_t z = 0; z < 4; ++z)
+    for (int64_t y = 0; y < 5; ++y)
+      for (int64_t x = 0; x < 6; ++x) v.set_pixel({{x, y, z}}, (float)z);
+  SliceBySliceFilter<Image<float, 3>> f(v, 1.5);
+  auto out = f.generate_region(f.largest_region());
+  for (int64_t z = 0; z < 4; ++z)
+    CHECK(std::fabs(out.get_pixel({{2, 2, z}}) - (float)z) < 1e-5f, "slice %lld", (long long)z);
+}
+
 int main() {
   int ndev = 0;
   itkg_device_count(&ndev);
@@ -211,6 +243,8 @@ int main() {
       {"device_source_matches_host", test_device_source_matches_host},
       {"mean_filters", test_mean_filters},
       {"binomial_blur", test_binomial_blur},
+      {"unsharp_mask", test_unsharp_mask},
+      {"slice_by_slice", test_slice_by_slice},
   };
   for (auto& t : tests) {
     const int before = g_fail;
