@@ -5,7 +5,6 @@
 
 #include <cuda_runtime.h>
 
-#include "f32x2.cuh"
 #include "internal.hpp"
 
 namespace itkg {
@@ -152,110 +151,18 @@ __device__ __forceinline__ float unsharp_f32(float o, float b, const UnsharpCons
   return q;
 }
 
-// Packed f32x2 forms of the operations unsharp_fast_f32 uses (the same IEEE
-// operations on two lanes at once; sign flips and |.| by bit masks).
-__device__ __forceinline__ f2_t sub2(f2_t a, f2_t b) {
-  f2_t d;
-  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-  return d;
-}
-__device__ __forceinline__ f2_t add2_ru(f2_t a, f2_t b) {
-  f2_t d;
-  asm("add.rp.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-  return d;
-}
-__device__ __forceinline__ f2_t add2_rd(f2_t a, f2_t b) {
-  f2_t d;
-  asm("add.rm.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-  return d;
-}
-__device__ __forceinline__ f2_t neg2(f2_t a) { return a ^ 0x8000000080000000ull; }
-__device__ __forceinline__ f2_t abs2(f2_t a) { return a & 0x7fffffff7fffffffull; }
-__device__ __forceinline__ void two_sum2(f2_t a, f2_t b, f2_t& s, f2_t& t) {
-  s = add2(a, b);
-  const f2_t a1 = sub2(s, b);
-  const f2_t b1 = sub2(s, a1);
-  t = add2(sub2(a, a1), sub2(b, b1));
-}
-
-// unsharp_fast_f32 on two voxels: the arithmetic of the decided path in
-// packed f32x2 operations (the same roundings lane by lane), the decisions
-// lane by lane in the same order; f64 where it cannot decide.
-__device__ __forceinline__ void unsharp_pair_exact(float o0, float o1, float b0, float b1, const UnsharpConsts& k,
-                                                   float& r0, float& r1) {
-  const f2_t O = pack2(o0, o1), B = pack2(b0, b1);
-  f2_t EH, EL;
-  two_sum2(O, neg2(B), EH, EL);
-  const f2_t AH = pack2(k.ah, k.ah), AL = pack2(k.al, k.al);
-  const f2_t PH = mul2(AH, EH);
-  const f2_t T = fma2(AH, EH, neg2(PH));
-  const f2_t PL = add2(T, add2(mul2(AH, EL), mul2(AL, EH)));
-  f2_t SH, S1;
-  two_sum2(O, PH, SH, S1);
-  const f2_t S2 = add2(S1, PL);
-  const f2_t SCALE = add2_ru(abs2(O), abs2(PH));
-  const f2_t DELTA = mul2(SCALE, pack2(0x1p-40f, 0x1p-40f));
-  const f2_t HI = add2(SH, add2_ru(S2, DELTA));
-  const f2_t LO = add2(SH, add2_rd(S2, neg2(DELTA)));
-  float ov[2], bv[2], eh[2], el[2], ph[2], t[2], s1[2], pl[2], sh[2], scale[2], hi[2], lo[2];
-  unpack2(O, ov[0], ov[1]);
-  unpack2(B, bv[0], bv[1]);
-  unpack2(EH, eh[0], eh[1]);
-  unpack2(EL, el[0], el[1]);
-  unpack2(PH, ph[0], ph[1]);
-  unpack2(T, t[0], t[1]);
-  unpack2(S1, s1[0], s1[1]);
-  unpack2(PL, pl[0], pl[1]);
-  unpack2(SH, sh[0], sh[1]);
-  unpack2(SCALE, scale[0], scale[1]);
-  unpack2(HI, hi[0], hi[1]);
-  unpack2(LO, lo[0], lo[1]);
-  float r[2];
-#pragma unroll
-  for (int j = 0; j < 2; ++j) {
-    bool done = false;
-    if (!k.fast || !(fmaxf(fabsf(ov[j]), fabsf(bv[j])) < 0x1p90f)) {
-    } else if (eh[j] == 0.0f) {
-      r[j] = k.thr_neg ? __fadd_rn(ov[j], __fmul_rn(k.ah, eh[j])) : ov[j];
-      done = true;
-    } else {
-      const float ae = fabsf(eh[j]);
-      if (ae > k.thr_up) {
-        if (!(scale[j] >= 0x1p-80f) || !(fabsf(ph[j]) < 0x1p100f) || ae < 0x1p-60f) {
-        } else if (hi[j] == lo[j]) {
-          r[j] = hi[j];
-          done = true;
-        } else if (k.a_exact && (el[j] == 0.0f || fabsf(el[j]) >= __fmul_rn(ae, 0x1p-29f))) {
-          const float c = __fmul_rn(k.ah, el[j]);
-          const float ce = __fmaf_rn(k.ah, el[j], -c);
-          float p2, p2e, s2x, s2e;
-          two_sum(t[j], c, p2, p2e);
-          two_sum(s1[j], p2, s2x, s2e);
-          if (ce == 0.0f && p2e == 0.0f && s2e == 0.0f && (p2 == 0.0f || fabsf(p2) >= __fmul_rn(fabsf(ph[j]), 0x1p-29f))) {
-            r[j] = __fadd_rn(sh[j], s2x);
-            done = true;
-          }
-        }
-      } else if (ae < k.thr_dn) {
-        r[j] = ov[j];
-        done = true;
-      }
-    }
-    if (!done) r[j] = __double2float_rn(unsharp_f64((double)ov[j], (double)bv[j], k.amount, k.threshold));
-  }
-  r0 = r[0];
-  r1 = r[1];
-  (void)pl;
-}
-
-// Reference rounding, one quad: unsharp_pair_exact on its two pairs.  Out of
-// line, so that a caller unrolled over many steps carries one copy.
+// Reference rounding, one quad: the exact f32 test per voxel, f64 where it
+// cannot decide.  Out of line, so that a caller unrolled over many steps
+// carries one copy.
 __device__ __noinline__ inline float4 unsharp_quad_exact(float4 o, float b0, float b1, float b2, float b3,
                                                          const UnsharpConsts& k) {
-  float4 r;
-  unsharp_pair_exact(o.x, o.y, b0, b1, k, r.x, r.y);
-  unsharp_pair_exact(o.z, o.w, b2, b3, k, r.z, r.w);
-  return r;
+  const float ov[4] = {o.x, o.y, o.z, o.w}, bv[4] = {b0, b1, b2, b3};
+  float r[4];
+#pragma unroll
+  for (int c = 0; c < 4; ++c)
+    if (!k.fast || !unsharp_fast_f32(ov[c], bv[c], k, r[c]))
+      r[c] = __double2float_rn(unsharp_f64((double)ov[c], (double)bv[c], k.amount, k.threshold));
+  return make_float4(r[0], r[1], r[2], r[3]);
 }
 
 }  // namespace itkg
