@@ -327,3 +327,30 @@ def test_unsharp_invalid_arguments_return_status(itkg_lib):
     w = np.zeros(3)
     assert itkg_lib.itkg_unsharp_kernel(1.0, ctypes.byref(r), w.ctypes.data, 3) == E  # 7 weights needed
     assert r.value == 3
+
+
+def test_callers_invalid_arguments_return_status(itkg_lib):
+    import itkg
+    E = itkg._abi.ERROR_INVALID_ARGUMENT
+    a, b, p = _host_pair()
+    ac, bc = a.to_c(), b.to_c()
+    rq = a.region.to_c()
+    # SliceBySliceFilter: 3-D only, the input must contain the request
+    assert itkg_lib.itkg_slice_by_slice_generate_region(ctypes.byref(ac), ctypes.byref(rq), None,
+                                                        ctypes.byref(bc), None) == E
+    img2 = itkg.Image(np.zeros((5, 6), np.float32)).to_c()
+    rq2 = itkg.Region((0, 0), (6, 5)).to_c()
+    assert itkg_lib.itkg_slice_by_slice_generate_region(ctypes.byref(img2), ctypes.byref(rq2), ctypes.byref(p),
+                                                        ctypes.byref(img2), None) == itkg._abi.ERROR_UNSUPPORTED
+    big = itkg.Region((0, 0, 0), (8, 7, 9)).to_c()
+    assert itkg_lib.itkg_slice_by_slice_generate_region(ctypes.byref(ac), ctypes.byref(big), ctypes.byref(p),
+                                                        ctypes.byref(bc), None) == E
+    # BSplineDownsampleFilter: the output must hold the downsampled largest region
+    lg = a.region.to_c()
+    small = itkg.Image(np.zeros((2, 2, 2), np.float32)).to_c()
+    assert itkg_lib.itkg_bspline_downsample_generate_region(ctypes.byref(ac), ctypes.byref(lg), ctypes.byref(p),
+                                                            ctypes.byref(small), None) == E
+    assert "downsampled" in itkg_lib.itkg_last_error().decode()
+    half = itkg.Image(np.zeros((3, 4, 4), np.float32)).to_c()
+    assert itkg_lib.itkg_bspline_downsample_generate_region(ctypes.byref(small), ctypes.byref(lg), ctypes.byref(p),
+                                                            ctypes.byref(half), None) == E
