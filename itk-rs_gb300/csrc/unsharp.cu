@@ -161,6 +161,30 @@ __global__ void __launch_bounds__(kQT) k_unsharp_deferred(const char* in, int64_
   }
 }
 
+// Scalar u8 rows of 4-byte aligned quads (x pitch 1, width a multiple of 4):
+// four voxels per thread from 4-byte loads; undecided voxels in f64 in place
+// (none on smooth data).
+__global__ void __launch_bounds__(kQT) k_unsharp_u8_quads(const char* in, int64_t ip1, int64_t ip2, const char* blur,
+                                                           int64_t bp1, int64_t bp2, char* out, int64_t op1,
+                                                           int64_t op2, uint32_t nq, uint32_t m1, uint32_t total,
+                                                           const UnsharpConsts k) {
+  for (uint32_t i = blockIdx.x * kQT + threadIdx.x; i < total; i += gridDim.x * kQT) {
+    const uint32_t row = i / nq;
+    const uint32_t qx = i - row * nq;
+    const uint32_t z = row / m1;
+    const uint32_t y = row - z * m1;
+    const uchar4 o = reinterpret_cast<const uchar4*>(in + (int64_t)y * ip1 + (int64_t)z * ip2)[qx];
+    const uchar4 b = reinterpret_cast<const uchar4*>(blur + (int64_t)y * bp1 + (int64_t)z * bp2)[qx];
+    const uint8_t ov[4] = {o.x, o.y, o.z, o.w}, bv[4] = {b.x, b.y, b.z, b.w};
+    uint8_t r[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+      if (!k.fast || !unsharp_fast_u8(ov[c], bv[c], k, r[c]))
+        r[c] = u8_of(unsharp_f64((double)ov[c], (double)bv[c], k.amount, k.threshold));
+    reinterpret_cast<uchar4*>(out + (int64_t)y * op1 + (int64_t)z * op2)[qx] = make_uchar4(r[0], r[1], r[2], r[3]);
+  }
+}
+
 template <typename I>
 itkg_status launch_quads(const char* ic, const int64_t* ip, const char* bc, const int64_t* bp, char* oc,
                          const int64_t* op, const int64_t* m, uint64_t total, unsigned blocks, const UnsharpConsts& k,
@@ -254,6 +278,19 @@ itkg_status launch_unsharp(int dtype, int comps, const void* in, const int64_t* 
                                ? launch_quads<uint32_t>(ic, ip, bc, bp, oc, op, m, total, (unsigned)blocks, k, s)
                                : launch_quads<uint64_t>(ic, ip, bc, bp, oc, op, m, total, (unsigned)blocks, k, s);
     if (st != ITKG_SUCCESS) return st;
+  } else if (dtype == ITKG_U8 && comps == 1 && ip[0] == 1 && bp[0] == 1 && op[0] == 1 && m[0] % 4 == 0 &&
+             (uint64_t)(m[0] / 4) * (uint64_t)m[1] * (uint64_t)m[2] + (uint64_t)kQT * 65536 < UINT32_MAX &&
+             ((uintptr_t)in % 4) == 0 && ((uintptr_t)blur % 4) == 0 && ((uintptr_t)out % 4) == 0 &&
+             ip[1] % 4 == 0 && ip[2] % 4 == 0 && bp[1] % 4 == 0 && bp[2] % 4 == 0 && op[1] % 4 == 0 &&
+             op[2] % 4 == 0) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const uint32_t total = (uint32_t)((m[0] / 4) * m[1] * m[2]);
+    const uint32_t blocks = std::min<uint32_t>((total + kQT - 1) / kQT, (uint32_t)std::max(sms, 1) * 8);
+    k_unsharp_u8_quads<<<blocks, kQT, 0, s>>>(ic, ip[1], ip[2], bc, bp[1], bp[2], oc, op[1], op[2],
+                                             (uint32_t)(m[0] / 4), (uint32_t)m[1], total, k);
+    note_launch("unsharp_u8");
   } else if (dtype == ITKG_U8) {
     k_unsharp<uint8_t><<<gr, kT, 0, s>>>(ic, ip[0], ip[1], ip[2], bc, bp[0], bp[1], bp[2], oc, op[0], op[1], op[2],
                                          m[0], m[1], m[2], comps, k);
