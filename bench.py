@@ -15,6 +15,16 @@ resident in HBM; `e2e` = the same metric through the C ABI with host
 C restatement of itk-rs's rayon path (serial index build + parallel loop over
 output voxels), on a bounded slab of the same workload per step.
 
+--workload selects another line (the default above is fwd3d):
+  fwd2d        2-D Image<f32> 512x512, sigma 1.5, 64 images per step
+  ct16         CT Image<i16> 512x512x384 -> f32 / bf16 / f16
+  batch        64 volumes + 256 RGB images in one graph (batch_vjp: with the VJP)
+  vjp_stack    multi-scale loss VJP, 8 x 192^3, sigma {1, 2, 4, 8}
+  mean3d       MeanFilter radius 2        binomial3d  BinomialBlurFilter 4 rounds
+  recursive3d  RecursiveGaussianFilter (and gradient magnitude), f64 lines
+  unsharp3d    UnsharpMaskFilter, both roundings and Image<u8>
+  callers3d    SliceBySliceFilter and BSplineDownsampleFilter
+
 Prints ONE JSON line (rank 0).
 """
 from __future__ import annotations
@@ -407,7 +417,7 @@ def _normwise(a, ref):
 
 
 def extra_workload(args):
-    """One JSON line for configs 1, 3, 4 or 5 (see --workload)."""
+    """One JSON line for a workload other than the default (see --workload)."""
     import torch
     import itkg
     from itkg import _abi

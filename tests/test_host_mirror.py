@@ -29,3 +29,20 @@ def test_host_mirror_pipeline_tests(gpu):
     print(r.stdout)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "FAIL" not in r.stdout
+
+
+def test_python_filters_region_logic():
+    """Host-side geometry of the Python mirror's filters (no device needed)."""
+    import numpy as np
+    import itkg
+    img = itkg.Image(np.zeros((9, 10, 11), np.float32), index=(2, -1, 0))
+    u = itkg.UnsharpMaskFilter(img, 1.2)  # radius ceil(3.6) = 4
+    out = itkg.Region((4, 0, 1), (3, 2, 2))
+    assert u.input_region_for_output(out) == itkg.Region((2, -1, 0), (9, 7, 7))
+    assert u.with_amount(0.9).amount == 0.9
+    assert itkg.SliceBySliceFilter(img, 2.0).input_region_for_output(out) == out
+    b = itkg.BSplineDownsampleFilter(img)
+    assert b.largest_region() == itkg.Region((2, -1, 0), (6, 5, 5))
+    assert b.spacing == (2.0, 2.0, 2.0)
+    assert b.input_region_for_output(out) == img.region
+    assert len(itkg.unsharp_kernel(1.2)) == 9
