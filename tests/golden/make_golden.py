@@ -14,9 +14,17 @@ and sum rounds to f32 separately, exactly as Rust evaluates `acc + x * (w as f32
   padded/clipped    src/image.rs:28-64
   split_region      src/region_splitter.rs:17-48
   stream_full       src/source.rs:81-98
+and, for the rows beyond the Gaussian (case prefixes):
+  sep_   MeanFilter / BoxMeanFilterN / BinomialBlurFilter   mean.rs, binomial_blur.rs
+  rec_   RecursiveGaussianFilter (f64 before conversion)     recursive_gaussian.rs:33-239
+  recd_  its derivative users (stencils on the smoothing)    filters/edges.rs:686-950
+  recz_  ZeroCrossingBasedEdgeDetectionFilter               filters/edges.rs:1019-1052, 480-514
+  ush_   UnsharpMaskFilter                                  filters/edges.rs:374-452
+  cal_   SliceBySliceFilter, BSplineDownsampleFilter        filters/spatial.rs:1128-1166, 1284-1340
 
-The C oracle (oracle/gauss_oracle.c) is checked bit-exactly against these
-vectors by tests/test_oracle.py, and the GPU path by tests/test_gpu_parity.py.
+The oracle (oracle/gauss_oracle.c, oracle/oracle.py) is checked bit-exactly
+against these vectors by tests/test_oracle*.py, and the GPU path by the
+tests/test_gpu_*.py golden tests.
 Run: python tests/golden/make_golden.py   (about a minute; pure Python loops)
 """
 from __future__ import annotations
