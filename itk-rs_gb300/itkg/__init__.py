@@ -18,7 +18,7 @@ libitkg.so; there is no CPU fallback.
 from __future__ import annotations
 
 import ctypes
-from dataclasses import dataclass, field
+from dataclasses import dataclass
 
 import numpy as np
 

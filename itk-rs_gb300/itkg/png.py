@@ -107,12 +107,10 @@ def _samples(rows: np.ndarray, width: int, channels: int, depth: int) -> np.ndar
 
 def _decode(path, want_color: int, sixteen: bool):
     data = open(path, "rb").read()
-    ihdr, plte, idat, trns = None, None, [], None
+    ihdr, idat, trns = None, [], None
     for kind, body in _chunks(data):
         if kind == b"IHDR":
             ihdr = struct.unpack(">IIBBBBB", body)
-        elif kind == b"PLTE":
-            plte = body
         elif kind == b"tRNS":
             trns = body
         elif kind == b"IDAT":

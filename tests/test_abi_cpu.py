@@ -2,7 +2,6 @@
 include/itkg.h declares, its host-side geometry matches the reference
 restatement, and invalid calls fail with a status (never a crash)."""
 import ctypes
-import math
 import os
 import re
 
