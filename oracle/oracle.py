@@ -3,7 +3,15 @@
 Only tests/, the smoke check in __graft_entry__.py and bench.py's CPU-baseline
 leg import this module; the product never does.  It wraps the C restatement
 in gauss_oracle.c (reference semantics, see that file's header for the
-file:line map) and adds numpy FP64 helpers for the adjoint checks.
+file:line map) and adds numpy FP64 helpers for the adjoint checks.  The rows
+beyond the Gaussian are restated here on top of the C core, each function
+citing the reference lines it follows:
+  separable_* / mean_f32 / binomial_f32   mean.rs, binomial_blur.rs (C core)
+  recursive_gaussian_f64 / _f32           recursive_gaussian.rs:33-239 (C core)
+  recursive_derivative / _difference_of_gaussians / _zero_crossing_edges
+                                          filters/edges.rs:686-1052 (numpy f64)
+  unsharp_kernel / unsharp_mask           filters/edges.rs:374-452 (math.exp, numpy f64)
+  slice_by_slice / bspline_downsample     filters/spatial.rs:1128-1166, 1284-1340
 
 Array convention used throughout the tests: a reference ``Image<P, D>`` with
 axis 0 fastest is a C-ordered numpy array whose LAST spatial axis is the
