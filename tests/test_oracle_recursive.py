@@ -145,3 +145,30 @@ def test_zero_crossings_of_a_sign_change():
     z = oracle.recursive_zero_crossing_edges(x, 0.8)
     assert z.dtype == np.float32 and set(np.unique(z)) <= {0.0, 1.0}
     assert z[:, 5].all() and z[:, 6].all() and not z[:, 0].any() and not z[:, -1].any()
+
+
+def _ramp(n):
+    return np.arange(n, dtype=np.float32)
+
+
+def test_reference_stencil_tests_through_the_smoothing():
+    """The reference's stencil tests (edges.rs:1614-1662: derivative of a ramp is 1,
+    second derivative of x^2 is 2, gradient magnitude of a ramp is 1, Laplacian of a
+    ramp is 0), re-run on the derivative users: the recursive smoothing keeps ramps and
+    quadratics up to a constant away from the edges, so the same values hold inside."""
+    r = _ramp(80)
+    inner = slice(20, 60)
+    d = oracle.recursive_derivative(r, 1.0, oracle.REC_DERIVATIVE, axis=0, order=1)
+    assert np.all(np.abs(d[inner] - 1.0) < 1e-3)
+    q = (np.arange(80, dtype=np.float64) ** 2).astype(np.float32)
+    d2 = oracle.recursive_derivative(q, 1.0, oracle.REC_DERIVATIVE, axis=0, order=2)
+    assert np.all(np.abs(d2[inner] - 2.0) < 1e-2)
+    g = oracle.recursive_derivative(r, 1.0, oracle.REC_GRADIENT_MAGNITUDE)
+    assert np.all(np.abs(g[inner] - 1.0) < 1e-3)
+    lap = oracle.recursive_derivative(r, 1.0, oracle.REC_LAPLACIAN)
+    assert np.all(np.abs(lap[inner]) < 1e-3)
+    # a flat image has no edges (edges.rs:1665-1671 for Sobel; here every derivative user)
+    flat = np.ones((6, 7), np.float32)
+    for kind in (oracle.REC_GRADIENT_MAGNITUDE, oracle.REC_LAPLACIAN):
+        assert np.all(np.abs(oracle.recursive_derivative(flat, 1.5, kind)) < 1e-5)
+    assert not oracle.recursive_zero_crossing_edges(flat, 1.5).any()
