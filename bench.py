@@ -51,26 +51,7 @@ BYTES_PER_VOXEL = 8  # f32 in + f32 out (compulsory traffic)
 FALLBACK_HBM_GBS = 6800.0
 
 
-def blobs_volume(shape, seed, nblobs=32, noise=0.05):
-    """Sum of `nblobs` seeded Gaussian blobs (centres uniform in the volume,
-    amplitude U[0.5, 2], std U[4, 24] voxels) plus N(0, noise)."""
-    rng = np.random.default_rng(seed)
-    nz, ny, nx = shape
-    z = np.arange(nz, dtype=np.float32)[:, None, None]
-    y = np.arange(ny, dtype=np.float32)[None, :, None]
-    x = np.arange(nx, dtype=np.float32)[None, None, :]
-    vol = np.zeros(shape, np.float32)
-    for _ in range(nblobs):
-        cz, cy, cx = rng.uniform(0, nz), rng.uniform(0, ny), rng.uniform(0, nx)
-        amp = rng.uniform(0.5, 2.0)
-        sd = rng.uniform(4.0, 24.0)
-        k = np.float32(-0.5 / (sd * sd))
-        gz = np.exp(k * (z - cz) ** 2)
-        gy = np.exp(k * (y - cy) ** 2)
-        gx = np.exp(k * (x - cx) ** 2)
-        vol += np.float32(amp) * (gz * gy * gx)
-    vol += rng.normal(0.0, noise, shape).astype(np.float32)
-    return vol
+from itkg.workloads import blobs_volume, ct_volume  # noqa: E402  (seeded synthetic inputs)
 
 
 def measured_peak():
@@ -364,6 +345,18 @@ def gpu_arm(args):
                "sample": f"{SHAPE[2]}x{SHAPE[1]}x{s} slab of the 256^3 volume, {t:.1f} s; "
                          "C restatement of the reference rayon path"}
 
+    # the metric's second half: batched forward + VJP against the plain per-volume calls
+    batch = None
+    if rank == 0 and world == 1 and args.batch_steps > 0:
+        sp = itkg.Stream(stream.cuda_stream)
+        bm = batch_measure(itkg, L, stream, sp, True, args.batch_steps, 3)
+        batch = {"value": bm["value"], "unit": "voxels/s (forward + VJP voxel-passes)",
+                 "ms_per_step": bm["ms_per_step"], "workload": bm["config"]["workload"],
+                 "batch_launches_per_step": bm["config"]["batch_launches_per_step"],
+                 "plain_per_volume": bm["plain_per_volume"],
+                 "batched_over_plain": bm["batched_over_plain"],
+                 "accuracy": bm["accuracy"]}
+
     if reports(rank):
         line = {
             "metric": METRIC, "value": value, "unit": "voxels/s", "n_gpus": world,
@@ -384,7 +377,7 @@ def gpu_arm(args):
                          "avg_launch_us": avg_launch_s * 1e6,
                          "frac_of_8TBs": achieved / 8000.0},
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
-            "accuracy": acc, "clocks": clk,
+            "accuracy": acc, "clocks": clk, "batch_fwd_vjp": batch,
         }
         print(json.dumps(line))
     if dist is not None:
@@ -414,6 +407,98 @@ def _timed(stream, fn, steps, warmup):
 def _normwise(a, ref):
     ref = np.asarray(ref, np.float64)
     return float(np.abs(np.asarray(a, np.float64) - ref).max() / max(np.abs(ref).max(), 1e-300))
+
+
+def _gen_call(L, f, req, outimg, sp):
+    """One generate_region call of filter f into outimg on stream sp, as a closure."""
+    from itkg import _abi
+    p = f.params()
+    lg = f._leaf().largest_region().to_c()
+    rq = req.to_c()
+    src = f._leaf().to_c()
+    return lambda: _abi.check(L.itkg_gaussian_generate_region(
+        ctypes.byref(src), ctypes.byref(lg), ctypes.byref(rq), ctypes.byref(p),
+        ctypes.byref(outimg.c), sp.ptr))
+
+
+def batch_measure(itkg, L, stream, sp, vjp, steps, warmup):
+    """The batch workload: 64 Image<f32,3> with dims U{32..320} and sigma
+    U[0.5, 4] (plus, forward only, 256 RGB Image<VecPixel<f32,3>,2> with sides
+    U{64..1024}), as one planned batch replayed as a CUDA graph, against the
+    plain per-volume calls a user makes without the batch API: the library's
+    default generate_region (and, with vjp, the default gaussian_vjp) per
+    volume, in a loop on the same stream.  Returns the JSON fields."""
+    from itkg import _abi
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    rng = np.random.default_rng(0)
+    vols = []
+    for i in range(64):
+        shape = tuple(int(v) for v in rng.integers(32, 321, 3))
+        vols.append((rng.random(shape, dtype=np.float32), float(rng.uniform(0.5, 4.0)), 1))
+    for i in range(0 if vjp else 256):
+        shape = tuple(int(v) for v in rng.integers(64, 1025, 2))
+        vols.append((rng.random(shape + (3,), dtype=np.float32), float(rng.uniform(0.5, 4.0)), 3))
+    outs, calls = [], []
+    b = itkg.Batch()
+    vjp_items = []
+    sb = ctypes.c_void_p()
+    if vjp:
+        _abi.check(L.itkg_device_alloc(8 * len(vols), ctypes.byref(sb)))
+    nvox = 0
+    for i, (arr, sigma, comps) in enumerate(vols):
+        d = itkg.DeviceImage.from_host(itkg.Image(arr, components=comps))
+        o = itkg.DeviceImage(d.region, itkg.F32, comps)
+        outs.append(o)
+        nvox += arr.size // comps
+        b.add(d, sigma, out=o, rounding=itkg.ROUND_FMA)
+        plain = itkg.GaussianFilter(d, sigma, rounding=itkg.ROUND_FMA, algorithm=itkg.ALGO_AUTO)
+        calls.append(_gen_call(L, plain, d.region, o, sp))
+        if vjp:
+            yb = itkg.DeviceImage.from_host(itkg.Image(rng.standard_normal(arr.shape).astype(np.float32)))
+            xb = b.add_vjp(d, yb, sigma, sigma_bar_dev=sb.value + 8 * i)
+            vjp_items.append((d, yb, sigma, xb, i))
+    b.plan(stream=sp)
+    ms_batch = _timed(stream, lambda: b.run(sp), steps, warmup)
+    launches0 = L.itkg_launch_counter()
+    b.run(sp)
+    stream.synchronize()
+    batch_launches = L.itkg_launch_counter() - launches0
+
+    def plain_all():
+        for c in calls:
+            c()
+        for d, yb, sigma, xb, i in vjp_items:
+            p = _abi.itkg_gaussian_params()
+            p.sigma = sigma
+            p.rounding = itkg.ROUND_FMA
+            p.algorithm = itkg.ALGO_AUTO  # the library's default VJP kernels per volume
+            _abi.check(L.itkg_gaussian_vjp(ctypes.byref(d.c), ctypes.byref(yb.c), ctypes.byref(p),
+                                           ctypes.byref(xb.c),
+                                           ctypes.cast(ctypes.c_void_p(sb.value + 8 * i), ctypes.POINTER(ctypes.c_double)),
+                                           4, sp.ptr))
+    ms_plain = _timed(stream, plain_all, max(1, steps // 2), max(1, warmup // 2))
+    launches0 = L.itkg_launch_counter()
+    plain_all()
+    stream.synchronize()
+    plain_launches = L.itkg_launch_counter() - launches0
+    units = nvox * (2 if vjp else 1)
+    got = outs[0].download()
+    err = _normwise(got, oracle.gaussian_f32(vols[0][0], vols[0][1], comps=vols[0][2]))
+    if sb.value:
+        L.itkg_device_free(sb)
+    return {"value": units / (ms_batch * 1e-3), "ms_per_step": ms_batch, "dtype": "f32",
+            "config": {"workload": ("64 Image<f32,3> U{32..320}^3 + 256 RGB 2-D U{64..1024}^2, sigma U[0.5,4], one graph"
+                                    if not vjp else
+                                    "64 Image<f32,3> U{32..320}^3, sigma U[0.5,4]: forward + VJP (x and sigma), one graph"),
+                       "voxels": nvox, "plan": b.describe().strip().splitlines()[:12],
+                       "batch_launches_per_step": int(batch_launches)},
+            "plain_per_volume": {"value": units / (ms_plain * 1e-3), "ms_per_step": ms_plain,
+                                 "launches_per_step": int(plain_launches),
+                                 "kernel": "default generate_region per volume" +
+                                           (" + default gaussian_vjp per volume" if vjp else "")},
+            "batched_over_plain": ms_plain / ms_batch,
+            "accuracy": {"normwise_rel_vs_ref_f32_item0": err}}
 
 
 def extra_workload(args):
@@ -462,20 +547,7 @@ def extra_workload(args):
                     "accuracy": {"normwise_rel_vs_ref_f32": err}})
     elif args.workload == "ct16":
         # CT workload: Image<i16,3> 512x512x384 CT-like, spacing (0.7,0.7,2.5), sigma 1.5 mm
-        shape = (384, 512, 512)
-        z = np.arange(shape[0])[:, None, None]
-        y = np.arange(shape[1])[None, :, None]
-        x = np.arange(shape[2])[None, None, :]
-        vol = np.full(shape, -1000.0, np.float32)
-        for _ in range(12):
-            c = rng.uniform(0.2, 0.8, 3) * np.array(shape)
-            ax = rng.uniform(0.05, 0.35, 3) * np.array(shape)
-            val = rng.uniform(-1000, 1500)
-            m = ((z - c[0]) / ax[0]) ** 2 + ((y - c[1]) / ax[1]) ** 2 + ((x - c[2]) / ax[2]) ** 2 <= 1
-            vol[m] = val
-        vol += rng.normal(0, 20, shape).astype(np.float32)
-        ct = np.clip(np.rint(vol), -32768, 32767).astype(np.int16)
-        del vol
+        ct = ct_volume((384, 512, 512), seed=0)
         spacing = (0.7, 0.7, 2.5)
         dev = itkg.DeviceImage.from_host(itkg.Image(ct, spacing=spacing))
         lines = {}
@@ -501,64 +573,7 @@ def extra_workload(args):
                     "dtype": "i16->f32", "config": {"workload": "CT i16 512x512x384, spacing (0.7,0.7,2.5), sigma 1.5 mm, r=(7,7,2)",
                                                    "outputs": lines}})
     elif args.workload in ("batch", "batch_vjp"):
-        # batch workload: 64 Image<f32,3> dims U{32..320}, sigma U[0.5,4]; 256 RGB 2-D sides U{64..1024}
-        vols = []
-        for i in range(64):
-            shape = tuple(int(v) for v in rng.integers(32, 321, 3))
-            vols.append((rng.random(shape, dtype=np.float32), float(rng.uniform(0.5, 4.0)), 1))
-        for i in range(256 if args.workload == "batch" else 0):
-            shape = tuple(int(v) for v in rng.integers(64, 1025, 2))
-            vols.append((rng.random(shape + (3,), dtype=np.float32), float(rng.uniform(0.5, 4.0)), 3))
-        devs, outs, calls = [], [], []
-        b = itkg.Batch()
-        vjp_items = []
-        sb = ctypes.c_void_p()
-        if args.workload == "batch_vjp":
-            _abi.check(L.itkg_device_alloc(8 * len(vols), ctypes.byref(sb)))
-        nvox = 0
-        for i, (arr, sigma, comps) in enumerate(vols):
-            d = itkg.DeviceImage.from_host(itkg.Image(arr, components=comps))
-            o = itkg.DeviceImage(d.region, itkg.F32, comps)
-            devs.append(d)
-            outs.append(o)
-            nvox += arr.size // comps
-            b.add(d, sigma, out=o, rounding=itkg.ROUND_FMA)
-            plain = itkg.GaussianFilter(d, sigma, rounding=itkg.ROUND_FMA, algorithm=itkg.ALGO_PER_AXIS)
-            calls.append(gen(plain, d.region, o))
-            if args.workload == "batch_vjp":
-                yb = itkg.DeviceImage.from_host(itkg.Image(rng.standard_normal(arr.shape).astype(np.float32)))
-                xb = b.add_vjp(d, yb, sigma, sigma_bar_dev=sb.value + 8 * i)
-                vjp_items.append((d, yb, sigma, xb))
-        b.plan(stream=sp)
-        ms_batch = _timed(stream, lambda: b.run(sp), args.steps, args.warmup)
-
-        def plain_all():
-            for c in calls:
-                c()
-            for d, yb, sigma, xb in vjp_items:
-                p = _abi.itkg_gaussian_params()
-                p.sigma = sigma
-                p.rounding = itkg.ROUND_FMA
-                p.algorithm = itkg.ALGO_PER_AXIS  # plain: per-axis adjoint and dual passes
-                _abi.check(L.itkg_gaussian_vjp(ctypes.byref(d.c), ctypes.byref(yb.c), ctypes.byref(p),
-                                               ctypes.byref(xb.c), ctypes.cast(ctypes.c_void_p(sb.value), ctypes.POINTER(ctypes.c_double)),
-                                               4, sp.ptr))
-        ms_plain = _timed(stream, plain_all, max(1, args.steps // 4), 1)
-        units = nvox * (2 if args.workload == "batch_vjp" else 1)
-        got = outs[0].download()
-        err = _normwise(got, oracle.gaussian_f32(vols[0][0], vols[0][1], comps=vols[0][2]))
-        out.update({"value": units / (ms_batch * 1e-3), "ms_per_step": ms_batch, "dtype": "f32",
-                    "config": {"workload": ("64 Image<f32,3> U{32..320}^3 + 256 RGB 2-D U{64..1024}^2, sigma U[0.5,4], one graph"
-                                            if args.workload == "batch" else
-                                            "64 Image<f32,3> U{32..320}^3, sigma U[0.5,4]: forward + VJP (x and sigma), one graph"),
-                               "voxels": nvox, "plan": b.describe().strip().splitlines()[:12]},
-                    "plain_per_volume": {"value": units / (ms_plain * 1e-3), "ms_per_step": ms_plain,
-                                         "kernel": "per-axis generate_region per volume" +
-                                                   (" + per-axis VJP per volume" if vjp_items else "")},
-                    "batched_over_plain": ms_plain / ms_batch,
-                    "accuracy": {"normwise_rel_vs_ref_f32_item0": err}})
-        if sb.value:
-            L.itkg_device_free(sb)
+        out.update(batch_measure(itkg, L, stream, sp, args.workload == "batch_vjp", args.steps, args.warmup))
     elif args.workload == "vjp_stack":
         # multi-scale VJP workload: 8 x 192^3 blobs+noise, sigma {1,2,4,8}; loss sum_l |G_l x - t|^2
         n = 8
@@ -845,6 +860,8 @@ def main():
     ap.add_argument("--rounding", choices=["fma", "reference"], default="fma")
     ap.add_argument("--algo", choices=["auto", "fused", "per_axis", "two_pass"], default="auto")
     ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--batch-steps", type=int, default=10,
+                    help="steps of the batched forward + VJP measurement added to the default line (0: skip)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-check", dest="check", action="store_false")
     args = ap.parse_args()

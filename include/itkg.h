@@ -142,6 +142,21 @@ const char *itkg_last_kernel(void);
 /* Number of CUDA kernels this library has launched in this process. */
 uint64_t itkg_launch_counter(void);
 
+/* ---- diagnostics and fault injection (no counterpart in the reference) ---- */
+
+/* Number of device scratch allocations (stream-ordered allocations from the
+ * library's memory pool, made inside filter calls) in this process.
+ * itkg_device_alloc and itkg_image_alloc_device are not counted. */
+uint64_t itkg_scratch_alloc_counter(void);
+/* Test hook: the scratch allocation after the next `after` ones fails with
+ * ITKG_ERROR_OUT_OF_MEMORY (once); a negative value cancels. */
+void itkg_debug_fail_scratch_alloc(int64_t after);
+/* Test hook: a kernel's bounded wait on a tile load gives up after `cycles`
+ * clock cycles instead of about 2^31 (values <= 0 restore that default).
+ * A wait that gives up sets the calling thread's device fault word (see
+ * itkg_device_fault); the kernel still lets its loads land before it exits. */
+void itkg_debug_set_wait_limit(int64_t cycles);
+
 /* ---- host-side geometry (no device needed) ------------------------------ */
 
 /* GaussianFilter::kernel_radius (gaussian.rs:24-27): ceil(3*sigma/spacing)
@@ -181,9 +196,16 @@ itkg_status itkg_host_free_pinned(void *ptr);
 itkg_status itkg_memcpy(void *dst, const void *src, size_t bytes, int32_t kind, void *stream);
 itkg_status itkg_memset_device(void *dst, int32_t value, size_t bytes, void *stream);
 itkg_status itkg_stream_synchronize(void *stream);
-/* Device-side fault word of the current device: non-zero after a fused
- * kernel's bounded wait on a tile load gave up (the kernel then returned
- * early and its output is incomplete).  clear != 0 resets it. */
+/* A non-blocking stream on the current device (for callers with no CUDA
+ * runtime of their own, e.g. one stream per host thread), and its release. */
+itkg_status itkg_stream_create(void **stream);
+itkg_status itkg_stream_destroy(void *stream);
+/* Device-side fault word of the calling host thread on the current device:
+ * non-zero after a kernel launched by this thread gave up a bounded wait on a
+ * tile load (the kernel then returned early and its output is incomplete).
+ * Each host thread has its own word (64 words; threads beyond the 64th share
+ * them), so one thread's timeout does not fail another's calls.  clear != 0
+ * resets it. */
 itkg_status itkg_device_fault(int32_t clear, uint32_t *flag);
 
 /* Fill *img for a freshly allocated device image of `region`, with rows and
@@ -449,14 +471,19 @@ const char *itkg_batch_describe(itkg_batch *batch);
  * the per-axis intermediates live in one fixed 32 MiB device array inside the
  * library (held on every GPU that loads the library until the process exits).
  *   - input and output must be device buffers (ITKG_DEVICE);
- *   - a request whose intermediates exceed 32 MiB (two of them for D = 3, one
- *     for D = 2; each is the requested region padded by the radius on the axes
- *     not yet filtered, 4 bytes per component) fails with
- *     ITKG_ERROR_INVALID_ARGUMENT;
+ *   - a request that does not fit the 32 MiB fails with
+ *     ITKG_ERROR_INVALID_ARGUMENT.  It holds the intermediates: two for D = 3,
+ *     one for D = 2, none for D = 1, each the requested region padded by the
+ *     radius on the axes not yet filtered, at 4 bytes per component with f32
+ *     arithmetic and 1 byte with u8 pixel arithmetic; u8 pixel arithmetic also
+ *     keeps its per-tap table there, (2r + 1) * 256 bytes for the largest
+ *     radius r;
  *   - all calls share the array; calls whose GPU work overlaps (e.g. on two
  *     streams) race on it and must be serialised by the caller;
- *   - the first call on each device looks up the array's device address, so
- *     make that first call before any stream capture. */
+ *   - the first call on each device that uses the array (D >= 2, or u8 pixel
+ *     arithmetic) looks up the array's device address, so make that first
+ *     call before any stream capture.
+ * itkg_scratch_alloc_counter() does not move across these calls. */
 itkg_status itkg_gaussian_generate_region_noalloc(const itkg_image *input,
                                                   const itkg_region *largest,
                                                   const itkg_region *requested,

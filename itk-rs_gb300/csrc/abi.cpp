@@ -84,7 +84,20 @@ static itkg_status device_pool(cudaMemPool_t* out) {
   return ITKG_SUCCESS;
 }
 
+namespace {
+std::atomic<uint64_t> g_scratch_allocs{0};
+std::atomic<int64_t> g_fail_after{-1};  // allocations to grant before an injected failure; -1: none
+std::atomic<long long> g_wait_limit{1ll << 31};
+}  // namespace
+
+long long wait_limit_cycles() { return g_wait_limit.load(std::memory_order_relaxed); }
+
 itkg_status scratch_alloc(void** p, size_t bytes, void* stream) {
+  int64_t f = g_fail_after.load(std::memory_order_relaxed);
+  while (f >= 0 && !g_fail_after.compare_exchange_weak(f, f - 1, std::memory_order_relaxed)) {
+  }
+  if (f == 0) return set_error(ITKG_ERROR_OUT_OF_MEMORY, "device scratch allocation failed (injected)");
+  g_scratch_allocs.fetch_add(1, std::memory_order_relaxed);
   cudaMemPool_t pool;
   ITKG_TRY(device_pool(&pool));
   if (bytes == 0) bytes = 256;
@@ -452,14 +465,13 @@ itkg_status fused_geom_for(const itkg_image& in, const itkg_region& largest,
 }
 
 // ---- host buffers: pipelined staging ---------------------------------------
-// Helper streams of the current device for the staged host-buffer path (created
-// once, never destroyed).
+// Helper streams of the current device for the staged host-buffer path, per
+// host thread (created on a thread's first staged call, never destroyed), so
+// that staged calls from several threads run side by side.
 static itkg_status staging_streams(cudaStream_t out[3]) {
-  static std::mutex mu;
-  static std::vector<std::array<cudaStream_t, 3>> per_dev;
+  thread_local std::vector<std::array<cudaStream_t, 3>> per_dev;
   int dev = 0;
   ITKG_CUDA(cudaGetDevice(&dev));
-  std::lock_guard<std::mutex> lk(mu);
   if ((int)per_dev.size() <= dev) per_dev.resize(dev + 1, {nullptr, nullptr, nullptr});
   for (int i = 0; i < 3; ++i) {
     if (!per_dev[dev][i]) ITKG_CUDA(cudaStreamCreateWithFlags(&per_dev[dev][i], cudaStreamNonBlocking));
@@ -681,6 +693,9 @@ static itkg_status generate_region(const itkg_image* input, const itkg_region* l
     if (e != cudaSuccess) return cuda_status(e, "cudaStreamSynchronize");
     return check_fault_word(fw);
   }
+  // a failed call still returns only once no copy from or to the caller's
+  // host buffers is in flight
+  cudaStreamSynchronize(s);
   return st;
 }
 
@@ -693,6 +708,9 @@ extern "C" {
 int32_t itkg_abi_version(void) { return ITKG_ABI_VERSION; }
 const char* itkg_last_error(void) { return t_error.c_str(); }
 const char* itkg_last_kernel(void) { return t_kernel.c_str(); }
+uint64_t itkg_scratch_alloc_counter(void) { return g_scratch_allocs.load(std::memory_order_relaxed); }
+void itkg_debug_fail_scratch_alloc(int64_t after) { g_fail_after.store(after < 0 ? -1 : after); }
+void itkg_debug_set_wait_limit(int64_t cycles) { g_wait_limit.store(cycles > 0 ? cycles : (1ll << 31)); }
 uint64_t itkg_launch_counter(void) { return g_launches.load(std::memory_order_relaxed); }
 
 uint64_t itkg_kernel_radius(double sigma, double spacing) { return kernel_radius(sigma, spacing); }
@@ -817,6 +835,19 @@ itkg_status itkg_device_fault(int32_t clear, uint32_t* flag) {
   unsigned int f = 0;
   ITKG_TRY(fused_fault_flag(&f, clear != 0));
   *flag = f;
+  return ITKG_SUCCESS;
+}
+
+itkg_status itkg_stream_create(void** stream) {
+  if (!stream) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "stream is NULL");
+  cudaStream_t s = nullptr;
+  ITKG_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  *stream = s;
+  return ITKG_SUCCESS;
+}
+
+itkg_status itkg_stream_destroy(void* stream) {
+  if (stream) ITKG_CUDA(cudaStreamDestroy(static_cast<cudaStream_t>(stream)));
   return ITKG_SUCCESS;
 }
 

@@ -355,7 +355,7 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
-itkg_status launch_conv_axis_u8(const AxisArgs& a, const double* w, void* stream) {
+itkg_status launch_conv_axis_u8(const AxisArgs& a, const double* w, void* stream, void* lut_buf) {
   const int K = 2 * a.radius + 1;
   if (a.radius > kMaxU8Radius)
     return set_error(ITKG_ERROR_UNSUPPORTED, "u8 pixel arithmetic supports radius <= %d",
@@ -368,9 +368,11 @@ itkg_status launch_conv_axis_u8(const AxisArgs& a, const double* w, void* stream
   cudaFuncSetAttribute(k_conv_axis_u8, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        256 * (2 * kMaxU8Radius + 1));
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  void* glut = nullptr;
-  {
-    const itkg_status st = scratch_alloc(&glut, smem, s);  // K * 256 bytes: a whole number of uint32 words
+  // The table (K * 256 bytes: a whole number of uint32 words) lives in the
+  // caller's buffer when one is given, else in stream-ordered scratch.
+  void* glut = lut_buf;
+  if (!glut) {
+    const itkg_status st = scratch_alloc(&glut, smem, s);
     if (st != ITKG_SUCCESS) return st;
   }
   k_u8_lut<<<(unsigned)((K * 256 + kThreads - 1) / kThreads), kThreads, 0, s>>>(W, K, static_cast<uint8_t*>(glut));
@@ -387,7 +389,7 @@ itkg_status launch_conv_axis_u8(const AxisArgs& a, const double* w, void* stream
     k_conv_axis_u8<<<grid, kThreads, smem, s>>>(a, static_cast<const uint32_t*>(glut));
   }
   note_launch("conv_axis_u8_pixel");
-  scratch_free(glut, s);
+  if (!lut_buf) scratch_free(glut, s);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return set_error(ITKG_ERROR_CUDA, "conv_axis_u8 launch: %s", cudaGetErrorString(e));
   return ITKG_SUCCESS;

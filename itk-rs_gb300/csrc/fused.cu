@@ -33,6 +33,8 @@
 //
 // Work balance.  The (tile, z) units of the request are split evenly over a
 // grid of (SMs x resident CTAs) CTAs; a CTA's share is one or two z-segments.
+#include <atomic>
+
 #include "fused_kernel.cuh"
 
 namespace itkg {
@@ -55,7 +57,17 @@ using fusedk::Fused3DArgs;
 using KernelFn = void (*)(const CUtensorMap, const Fused3DArgs);
 using MultiFn = void (*)(const FusedItem*, const CUtensorMap*, int, int64_t);
 
-__device__ unsigned int g_fused_fault_word = 0;  // set when a bounded wait gives up
+// Fault words, set when a bounded wait gives up: one per host thread (slot =
+// the thread's ordinal modulo kFaultSlots), so that a wait given up under one
+// thread's call does not fail another thread's call.
+constexpr int kFaultSlots = 64;
+__device__ unsigned int g_fused_fault_word[kFaultSlots];
+
+std::atomic<int> g_next_fault_slot{0};
+int fault_slot() {
+  thread_local const int slot = g_next_fault_slot.fetch_add(1, std::memory_order_relaxed) % kFaultSlots;
+  return slot;
+}
 
 #define ITKG_CUDA_ST(call)                                                            \
   do {                                                                                \
@@ -128,7 +140,7 @@ itkg_status fault_address(unsigned int** out) {
     ITKG_CUDA_ST(cudaGetSymbolAddress(&p, g_fused_fault_word));
     g_fault_addr[dev] = static_cast<unsigned int*>(p);
   }
-  *out = g_fault_addr[dev];
+  *out = g_fault_addr[dev] + fault_slot();
   return ITKG_SUCCESS;
 }
 
@@ -194,6 +206,7 @@ itkg_status build_args(const FusedGeom& g, const float* const w[kMaxDim], const 
   a.units = (int64_t)a.ntx * a.nty * g.req_size[2];
   a.out_dtype = g.out_dtype;
   ITKG_TRY_ST(fault_address(&a.fault));
+  a.wait_limit = wait_limit_cycles();
   for (int k = 0; k < 2 * e->rx + 1; ++k) a.wx[k] = w[0][k], a.wx2[k] = splat2_host(w[0][k]);
   for (int k = 0; k < 2 * e->ry + 1; ++k) a.wy[k] = w[1][k], a.wy2[k] = splat2_host(w[1][k]);
   for (int k = 0; k < 2 * e->rz + 1; ++k) a.wz[k] = w[2][k], a.wz2[k] = splat2_host(w[2][k]);
@@ -425,11 +438,12 @@ void fused_multi_free(FusedMultiPlan* plan) {
 }
 
 itkg_status fused_fault_flag(unsigned int* flag, bool clear) {
-  cudaError_t e = cudaMemcpyFromSymbol(flag, g_fused_fault_word, sizeof(unsigned int));
+  const size_t off = sizeof(unsigned int) * (size_t)fault_slot();
+  cudaError_t e = cudaMemcpyFromSymbol(flag, g_fused_fault_word, sizeof(unsigned int), off);
   if (e != cudaSuccess) return set_error(ITKG_ERROR_CUDA, "fault flag: %s", cudaGetErrorString(e));
   if (clear && *flag) {
     const unsigned int zero = 0;
-    e = cudaMemcpyToSymbol(g_fused_fault_word, &zero, sizeof zero);
+    e = cudaMemcpyToSymbol(g_fused_fault_word, &zero, sizeof zero, off);
     if (e != cudaSuccess) return set_error(ITKG_ERROR_CUDA, "fault flag: %s", cudaGetErrorString(e));
   }
   return ITKG_SUCCESS;

@@ -50,6 +50,7 @@ struct Fused3DArgs {
   int32_t out_dtype;
   int32_t pad_;
   unsigned int* fault;  // device fault word, set when a bounded wait gives up
+  long long wait_limit; // clock cycles a wait on a tile load may take
   // kDot: ybar (f32) at the output positions, and one f64 partial per CTA
   const char* ybar;
   int64_t ybar_pitch[3];
@@ -99,12 +100,32 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-// Bounded wait: gives up after ~2^31 cycles (about a second) and reports false.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-  if (mbar_try_wait(bar, parity)) return true;
+__device__ __forceinline__ bool mbar_test_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait: gives up after `limit` clock cycles (by default 2^31, about a
+// second) and reports false.  With a limit below kWaitSpinBelow the wait polls
+// without suspending (a try_wait may suspend the thread for a while by
+// itself), so that a short limit set for a test is kept to.
+constexpr long long kWaitDefault = 1ll << 31;
+constexpr long long kWaitSpinBelow = 1ll << 16;
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, long long limit = kWaitDefault) {
+  if (mbar_test_wait(bar, parity)) return true;
   const long long t0 = clock64();
+  if (limit < kWaitSpinBelow) {
+    while (!mbar_test_wait(bar, parity))
+      if (clock64() - t0 > limit) return false;
+    return true;
+  }
   while (!mbar_try_wait(bar, parity))
-    if (clock64() - t0 > (1ll << 31)) return false;
+    if (clock64() - t0 > limit) return false;
   return true;
 }
 __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, int x, int y, int z,
@@ -311,7 +332,7 @@ __device__ __forceinline__ bool fused_range(const Fused3DArgs& a, const CUtensor
     auto stage_and_xpass = [&](int st, float* xbuf) -> bool {
       Tin* const tile = reinterpret_cast<Tin*>(stage0 + st * C::STAGE);
       if constexpr (TMA) {
-        const bool ok = mbar_wait(bbase + 8 * st, (phase_bits >> st) & 1u);
+        const bool ok = mbar_wait(bbase + 8 * st, (phase_bits >> st) & 1u, a.wait_limit);
         phase_bits ^= 1u << st;
         if (!ok) return false;
         if (MODE != kAdj && edge) {
@@ -395,17 +416,18 @@ __device__ __forceinline__ bool fused_range(const Fused3DArgs& a, const CUtensor
       }
       return true;
     };
-    // A tile load never completed: record it, let every other issued load
-    // land (bounded), and leave.
+    // A tile load did not complete in time: record it, let every issued load
+    // land (the one given up on included, whose phase bit was already
+    // flipped; default bound), and leave.
 #define ITKG_ON_TIMEOUT(CONS_NOW)                                                  \
   do {                                                                             \
     if (tid == 0) {                                                                \
-      atomicExch(a.fault, 1u);                                              \
+      atomicExch(a.fault, 1u);                                                     \
       if (TMA)                                                                     \
-        for (int q_ = 1; q_ < S; ++q_) {                                           \
+        for (int q_ = 0; q_ < S; ++q_) {                                           \
           const int sq_ = ((CONS_NOW) + q_) % S;                                   \
           if (s_first + (CONS_NOW) + q_ <= s_last)                                 \
-            mbar_wait(bbase + 8 * sq_, (phase_bits >> sq_) & 1u);                  \
+            mbar_wait(bbase + 8 * sq_, ((phase_bits >> sq_) & 1u) ^ (q_ == 0 ? 1u : 0u)); \
         }                                                                          \
     }                                                                              \
   } while (0)

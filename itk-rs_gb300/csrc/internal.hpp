@@ -70,7 +70,11 @@ struct AxisWeightsF64 {  // u8 pixel path: exact f64 weights
 // conv_axis.cu
 itkg_status launch_conv_axis_f32(const AxisArgs& a, const float* w, int in_dtype,
                                  int out_dtype, int rounding, void* stream);
-itkg_status launch_conv_axis_u8(const AxisArgs& a, const double* w, void* stream);
+// lut_buf: 256-byte aligned device buffer of at least (2 radius + 1) * 256
+// bytes for the per-tap table, or NULL to take it from scratch_alloc.  The
+// table kernel and the filter kernel run in order on `stream`, so one buffer
+// may serve consecutive calls on that stream.
+itkg_status launch_conv_axis_u8(const AxisArgs& a, const double* w, void* stream, void* lut_buf = nullptr);
 
 // ---- fused whole-filter kernels ---------------------------------------------
 // Geometry shared by every fused launch.  All indices absolute; the clamp
@@ -260,6 +264,10 @@ itkg_status launch_sum_partials(const double* partials, int n, double* out, bool
 itkg_status launch_sqerr(const float* y, const float* dy, const DotArgs& t, float* ybar,
                          double* partials, int nblocks, double* loss_out, double* sigma_out,
                          bool accumulate_loss, void* stream);
+
+// Clock cycles a kernel's bounded wait on a tile load may take before it
+// gives up (abi.cpp; 2^31 unless a test lowered it).
+long long wait_limit_cycles();
 
 // ---- device scratch ---------------------------------------------------------
 // Stream-ordered scratch from a library-owned memory pool of the current

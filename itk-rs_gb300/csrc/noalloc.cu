@@ -15,16 +15,20 @@
 //     library is loaded keeps this array for the life of the process.
 //   - A 3-D request needs two intermediates, a 2-D request one, a 1-D request
 //     none; each intermediate covers the requested region padded by the kernel
-//     radius on the axes not yet filtered.  A request whose intermediates do
-//     not fit is rejected with ITKG_ERROR_INVALID_ARGUMENT.
+//     radius on the axes not yet filtered, at 4 bytes per component (f32
+//     arithmetic) or 1 byte (u8 pixel arithmetic).  u8 pixel arithmetic also
+//     keeps its per-tap table, (2r + 1) * 256 bytes for the largest radius r,
+//     in the array.  A request that does not fit is rejected with
+//     ITKG_ERROR_INVALID_ARGUMENT.
 //   - All calls share the one array, which keeps whatever the last call left
 //     in it.  Each pass writes every element of its intermediate before the
 //     next pass reads it, so no clearing is needed.  Calls whose GPU work
 //     overlaps (for example on two streams at once) race on the array and
 //     must be serialised by the caller.
-//   - The first call on a device looks up the array's device address (one
-//     cudaGetSymbolAddress per device, made with that device current).  Make
-//     that first call before any stream capture.
+//   - The first call on a device that needs the array (any request of two or
+//     more dimensions, and every u8 pixel-arithmetic request) looks up the
+//     array's device address (one cudaGetSymbolAddress per device, made with
+//     that device current).  Make that first call before any stream capture.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -141,18 +145,17 @@ extern "C" itkg_status itkg_gaussian_generate_region_noalloc(
 
   // Radii and weights (gaussian.rs:24-40), input region (gaussian.rs:52-57).
   uint64_t radii[kMaxDim] = {0, 0, 0};
-  std::vector<double> w64[kMaxDim];
-  std::vector<float> w32[kMaxDim];
+  // Host weights on the stack: the call makes no heap allocation either.
+  double w64[kMaxDim][kMaxParamTaps];
+  float w32[kMaxDim][kMaxParamTaps];
   for (int d = 0; d < D; ++d) {
     radii[d] = itkg_kernel_radius(params->sigma, input->spacing[d]);
     if (radii[d] > (uint64_t)(kMaxParamTaps - 1) / 2)
       return set_error(ITKG_ERROR_INVALID_ARGUMENT, "kernel radius %llu exceeds %d",
                        (unsigned long long)radii[d], (kMaxParamTaps - 1) / 2);
-    w64[d].resize(2 * radii[d] + 1);
-    if ((st = itkg_build_kernel(params->sigma / input->spacing[d], radii[d], w64[d].data())) != ITKG_SUCCESS)
+    if ((st = itkg_build_kernel(params->sigma / input->spacing[d], radii[d], w64[d])) != ITKG_SUCCESS)
       return st;
-    w32[d].resize(w64[d].size());
-    for (size_t k = 0; k < w64[d].size(); ++k) w32[d][k] = (float)w64[d][k];
+    for (uint64_t k = 0; k < 2 * radii[d] + 1; ++k) w32[d][k] = (float)w64[d][k];
   }
   itkg_region in_reg;
   if ((st = itkg_gaussian_input_region_for_output(requested, largest, D, input->spacing,
@@ -180,16 +183,27 @@ extern "C" itkg_status itkg_gaussian_generate_region_noalloc(
     }
   }
   // Pass a writes slot a % 2; slot 1 starts at a 256-byte boundary after slot 0.
+  // u8 pixel arithmetic also keeps its per-tap table of (2r + 1) * 256 bytes
+  // (r the largest radius) in the array, after the slots; every pass rebuilds
+  // the table in place before it filters, in order on the caller's stream.
   const size_t slot0 = D > 1 ? bytes[0] : 0;
   const size_t slot1 = D > 2 ? bytes[1] : 0;
   const size_t off1 = (slot0 + 255) / 256 * 256;
-  if (off1 + slot1 > kNoAllocScratchBytes || slot0 > kNoAllocScratchBytes)
+  const size_t off_lut = (off1 + slot1 + 255) / 256 * 256;
+  uint64_t rmax = 0;
+  for (int d = 0; d < D; ++d) rmax = radii[d] > rmax ? radii[d] : rmax;
+  const size_t lut_bytes = u8pix ? (size_t)(2 * rmax + 1) * 256 : 0;
+  if (u8pix && rmax > (uint64_t)kMaxU8Radius)
+    return set_error(ITKG_ERROR_UNSUPPORTED, "u8 pixel arithmetic supports radius <= %d", kMaxU8Radius);
+  const size_t need = u8pix ? off_lut + lut_bytes : off1 + slot1;
+  if (need > kNoAllocScratchBytes || slot0 > kNoAllocScratchBytes)
     return set_error(ITKG_ERROR_INVALID_ARGUMENT,
                      "intermediates need %zu bytes; the no-allocation scratch holds %zu bytes",
-                     off1 + slot1, kNoAllocScratchBytes);
+                     need, kNoAllocScratchBytes);
   void* scratch = nullptr;
-  if (D > 1 && (st = scratch_address(&scratch)) != ITKG_SUCCESS) return st;
+  if ((D > 1 || u8pix) && (st = scratch_address(&scratch)) != ITKG_SUCCESS) return st;
   char* slots[2] = {static_cast<char*>(scratch), static_cast<char*>(scratch) + off1};
+  void* lut = u8pix ? static_cast<void*>(static_cast<char*>(scratch) + off_lut) : nullptr;
 
   // D passes, each a convolve_axis (conv.rs:11-41).
   const itkg_image* cur = input;
@@ -227,11 +241,11 @@ extern "C" itkg_status itkg_gaussian_generate_region_noalloc(
     args.radius = (int32_t)radii[a];
     args.comps = input->components;
     if (u8pix) {
-      st = launch_conv_axis_u8(args, w64[a].data(), stream);
+      st = launch_conv_axis_u8(args, w64[a], stream, lut);
     } else {
       const int in_dt = a == 0 ? input->dtype : ITKG_F32;
       const int out_dt = a + 1 < D ? ITKG_F32 : output->dtype;
-      st = launch_conv_axis_f32(args, w32[a].data(), in_dt, out_dt, params->rounding, stream);
+      st = launch_conv_axis_f32(args, w32[a], in_dt, out_dt, params->rounding, stream);
     }
     if (st != ITKG_SUCCESS) return st;
     cur = nxt;

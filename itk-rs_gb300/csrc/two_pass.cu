@@ -190,6 +190,7 @@ itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], v
   std::memset(&xa, 0, sizeof xa);
   std::memset(&za, 0, sizeof za);
   if (st == ITKG_SUCCESS) st = device_fault_word(&xa.fault);
+  xa.wait_limit = wait_limit_cycles();
   int res_xy = 0, res_z = 0;
   const twopass::ZFn zfn = twopass::z_fn(rz, ref, vec, ush != nullptr);
   const twopass::XYFn xyfn = e->fn[ref ? 1 : 0];

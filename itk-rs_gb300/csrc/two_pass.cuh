@@ -65,6 +65,7 @@ struct XYArgs {
   int32_t ntx, nty;      // tiles along x and y
   int64_t units;         // ntx * nty * ns
   unsigned int* fault;
+  long long wait_limit;  // clock cycles a wait on a tile load may take
   float wx[kMaxK], wy[kMaxK];
   f2_t wx2[kMaxK], wy2[kMaxK];
   // FMA rounding, x pass: weight pairs for an output whose first tap is at an
@@ -313,6 +314,7 @@ __global__ void __launch_bounds__(288, CfgXY<R, Tin>::MINB)
   };
   int st_issue = 0, st_use = 0;       // stage ring positions (uniform)
   int64_t n_issued = 0, n_consumed = 0;  // tile loads issued / waited for (uniform)
+  uint32_t issue_bits = 0;
 
   // The CTA's units are a run of slices of one tile, or the tail of one tile's
   // slices and the head of the next: one or two segments, each marching z.
@@ -352,12 +354,13 @@ __global__ void __launch_bounds__(288, CfgXY<R, Tin>::MINB)
         tma_load_3d_hint(sbase + (uint32_t)(st_issue * C::STAGE), &tmap, gx0 - a.src_origin[0],
                          gy0 - a.src_origin[1], sl - a.src_origin[2], bar, pol_in);
       }
+      issue_bits ^= 1u << st_issue;  // parity of the loads issued into this stage
       st_issue = st_issue + 1 == S ? 0 : st_issue + 1;
       ++n_issued;
     };
     auto xpass = [&](float* xb) {  // waits for the oldest load, x pass into xb
       const Tin* const tile_s = reinterpret_cast<const Tin*>(stage0 + st_use * C::STAGE);
-      if (!mbar_wait(bbase + 8 * st_use, (phase_bits >> st_use) & 1u)) s_fail = 1;  // checked after the next barrier
+      if (!mbar_wait(bbase + 8 * st_use, (phase_bits >> st_use) & 1u, a.wait_limit)) s_fail = 1;  // checked after the next barrier
       phase_bits ^= 1u << st_use;
       st_use = st_use + 1 == S ? 0 : st_use + 1;
       ++n_consumed;
@@ -444,12 +447,10 @@ __global__ void __launch_bounds__(288, CfgXY<R, Tin>::MINB)
 timeout:
   if (tid == 0) {
     atomicExch(a.fault, 1u);
-    // let this CTA's other tile loads in flight land (bounded) before it exits
-    for (int64_t k = n_consumed; k < n_issued; ++k) {
-      mbar_wait(bbase + 8 * st_use, (phase_bits >> st_use) & 1u);
-      phase_bits ^= 1u << st_use;
-      st_use = st_use + 1 == S ? 0 : st_use + 1;
-    }
+    // let every tile load this CTA issued land before it exits (default
+    // bound): the latest load into each stage, the one given up on included
+    (void)n_consumed;
+    for (int q = 0; q < S && q < n_issued; ++q) mbar_wait(bbase + 8 * q, ((issue_bits >> q) & 1u) ^ 1u);
   }
 }
 

@@ -141,6 +141,7 @@ itkg_status launch_vjp_two_pass(const VjpTwoPass& v, void* stream, bool dry_run)
   vjp2::prefix(v.dw[0], R, xa.pdx);
   vjp2::prefix(v.dw[1], R, xa.pdy);
   if (st == ITKG_SUCCESS) st = device_fault_word(&xa.fault);
+  xa.wait_limit = wait_limit_cycles();
   for (int mode = 0; mode < 2 && st == ITKG_SUCCESS; ++mode) {
     if (mode == vjp2::kAdjoint && !v.xbar) continue;
     if (mode == vjp2::kDualDot && !want_s) continue;

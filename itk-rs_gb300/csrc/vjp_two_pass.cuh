@@ -41,6 +41,7 @@ struct XYVArgs {
   int32_t ns;            // slices
   int64_t units;         // tiles * slices
   unsigned int* fault;
+  long long wait_limit;  // clock cycles a wait on a tile load may take
   // adjoint mode: xbar (f32), byte pitches; accumulate: xbar += result
   char* out;
   int64_t out_pitch[3];
@@ -207,6 +208,7 @@ __global__ void __launch_bounds__(256, 2)
 
   int st_issue = 0, st_use = 0;
   int64_t n_issued = 0, n_consumed = 0;
+  uint32_t issue_bits = 0;
   for (int64_t u = u_begin; u < u_end;) {
     const int64_t tile = u / a.ns;
     const int s_a = a.lo[2] + (int)(u - tile * a.ns);
@@ -230,12 +232,13 @@ __global__ void __launch_bounds__(256, 2)
         tma_load_3d_hint(sbase + (uint32_t)(st_issue * C::STAGE), &tmap, gx0 - a.src_origin[0],
                          gy0 - a.src_origin[1], sl - a.src_origin[2], bar, pol_in);
       }
+      issue_bits ^= 1u << st_issue;  // parity of the loads issued into this stage
       st_issue = st_issue + 1 == S ? 0 : st_issue + 1;
       ++n_issued;
     };
     auto xpass = [&](float* xb) {
       const float* const tile_s = reinterpret_cast<const float*>(stage0 + st_use * C::STAGE);
-      if (!mbar_wait(bbase + 8 * st_use, (phase_bits >> st_use) & 1u)) s_fail = 1;
+      if (!mbar_wait(bbase + 8 * st_use, (phase_bits >> st_use) & 1u, a.wait_limit)) s_fail = 1;
       phase_bits ^= 1u << st_use;
       st_use = st_use + 1 == S ? 0 : st_use + 1;
       ++n_consumed;
@@ -377,11 +380,10 @@ __global__ void __launch_bounds__(256, 2)
 timeout:
   if (tid == 0) {
     atomicExch(a.fault, 1u);
-    for (int64_t k = n_consumed; k < n_issued; ++k) {
-      mbar_wait(bbase + 8 * st_use, (phase_bits >> st_use) & 1u);
-      phase_bits ^= 1u << st_use;
-      st_use = st_use + 1 == S ? 0 : st_use + 1;
-    }
+    // let every tile load this CTA issued land before it exits (default
+    // bound): the latest load into each stage, the one given up on included
+    (void)n_consumed;
+    for (int q = 0; q < S && q < n_issued; ++q) mbar_wait(bbase + 8 * q, ((issue_bits >> q) & 1u) ^ 1u);
     if constexpr (MODE == kDualDot) a.partials[blockIdx.x] = 0.0;
   }
 }

@@ -113,6 +113,9 @@ SIGNATURES = {
     "itkg_last_error": (ctypes.c_char_p, []),
     "itkg_last_kernel": (ctypes.c_char_p, []),
     "itkg_launch_counter": (ctypes.c_uint64, []),
+    "itkg_scratch_alloc_counter": (ctypes.c_uint64, []),
+    "itkg_debug_fail_scratch_alloc": (None, [ctypes.c_int64]),
+    "itkg_debug_set_wait_limit": (None, [ctypes.c_int64]),
     "itkg_kernel_radius": (ctypes.c_uint64, [ctypes.c_double, ctypes.c_double]),
     "itkg_build_kernel": (st, [ctypes.c_double, ctypes.c_uint64, P]),
     "itkg_region_padded_per_axis": (st, [R, ctypes.c_int32, P, R]),
@@ -129,6 +132,8 @@ SIGNATURES = {
     "itkg_memcpy": (st, [P, P, ctypes.c_size_t, ctypes.c_int32, P]),
     "itkg_memset_device": (st, [P, ctypes.c_int32, ctypes.c_size_t, P]),
     "itkg_stream_synchronize": (st, [P]),
+    "itkg_stream_create": (st, [ctypes.POINTER(ctypes.c_void_p)]),
+    "itkg_stream_destroy": (st, [P]),
     "itkg_device_fault": (st, [ctypes.c_int32, ctypes.POINTER(ctypes.c_uint32)]),
     "itkg_image_alloc_device": (st, [I, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, R, P, P]),
     "itkg_image_free": (st, [I]),

@@ -7,8 +7,10 @@ of the per-axis Gaussian whose intermediates live in a fixed device array
 inside the library.  These tests call it through the C ABI and check it
 against the regular entry point (per-axis algorithm, reference rounding, so
 the results must be bit-identical), twice in a row so the second call runs on
-whatever the first left in the shared array, and check that a request too
-large for the array is refused.
+whatever the first left in the shared array, check through the library's
+scratch-allocation counter that the calls allocate nothing (f32 and u8 pixel
+arithmetic, one to three dimensions), and check that a request too large for
+the array is refused.
 
 The file is named to be collected last: it runs after every other test, and
 passes alone in a fresh process as well.
@@ -87,6 +89,57 @@ def test_noalloc_u8_pixel_arithmetic_twice(gpu):
         _abi.check(_call(gpu, L.itkg_gaussian_generate_region_noalloc, src, host.region,
                          host.region, prm, got_img))
         assert np.array_equal(got_img.download(), want), attempt
+
+
+@pytest.mark.parametrize("shape", [(300,), (30, 41), (19, 23, 31)])
+def test_noalloc_u8_pixel_arithmetic_each_dimension(gpu, shape):
+    from itkg import _abi
+    L = _abi.lib()
+    rng = np.random.default_rng(len(shape))
+    arr = rng.integers(0, 256, shape).astype(np.uint8)
+    host, src = _images(gpu, arr)
+    prm = _params(gpu, 1.2, arithmetic=gpu.ARITH_PIXEL_U8)
+    want_img = gpu.DeviceImage(host.region, gpu.U8)
+    _abi.check(_call(gpu, L.itkg_gaussian_generate_region, src, host.region, host.region, prm,
+                     want_img))
+    want = want_img.download()
+    got_img = gpu.DeviceImage(host.region, gpu.U8)
+    _abi.check(_call(gpu, L.itkg_gaussian_generate_region_noalloc, src, host.region,
+                     host.region, prm, got_img))
+    assert np.array_equal(got_img.download(), want)
+
+
+@pytest.mark.parametrize("u8", [False, True])
+@pytest.mark.parametrize("shape", [(300,), (30, 41), (19, 23, 31)])
+def test_noalloc_makes_no_scratch_allocation(gpu, shape, u8):
+    """The library counts every device scratch allocation its calls make; the
+    regular entry point makes some (its intermediates, the u8 per-tap table),
+    the no-allocation entry point none, on the f32 and the u8 path alike."""
+    from itkg import _abi
+    L = _abi.lib()
+    rng = np.random.default_rng(7)
+    if u8:
+        arr = rng.integers(0, 256, shape).astype(np.uint8)
+        prm = _params(gpu, 1.4, arithmetic=gpu.ARITH_PIXEL_U8)
+        dt = gpu.U8
+    else:
+        arr = rng.standard_normal(shape).astype(np.float32)
+        prm = _params(gpu, 1.4)
+        dt = gpu.F32
+    host, src = _images(gpu, arr)
+    out_a = gpu.DeviceImage(host.region, dt)
+    out_b = gpu.DeviceImage(host.region, dt)
+    n0 = L.itkg_scratch_alloc_counter()
+    _abi.check(_call(gpu, L.itkg_gaussian_generate_region, src, host.region, host.region, prm, out_a))
+    n1 = L.itkg_scratch_alloc_counter()
+    if u8 or len(shape) > 1:
+        assert n1 > n0  # the counter sees the regular path's allocations
+    for _ in range(2):
+        _abi.check(_call(gpu, L.itkg_gaussian_generate_region_noalloc, src, host.region,
+                         host.region, prm, out_b))
+    assert L.itkg_scratch_alloc_counter() == n1
+    got, want = out_b.download(), out_a.download()
+    assert np.array_equal(got.view(np.uint8), want.view(np.uint8))
 
 
 def test_noalloc_rejects_requests_beyond_its_scratch(gpu):
