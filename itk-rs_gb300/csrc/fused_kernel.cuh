@@ -334,13 +334,14 @@ __device__ __forceinline__ bool fused_range(const Fused3DArgs& a, const CUtensor
       if constexpr (TMA) {
         const bool ok = mbar_wait(bbase + 8 * st, (phase_bits >> st) & 1u, a.wait_limit);
         phase_bits ^= 1u << st;
-        if (!ok) return false;
         if (MODE != kAdj && edge) {
           // Replicate the image's edge values into the halo: first the
           // columns left of lo / right of hi (nl, nr of them), then whole
           // rows above / below (nt, nb of them).  Sources are in-image
-          // columns and rows, which these loops never write.
-          __syncthreads();
+          // columns and rows, which these loops never write.  Each thread
+          // timed its own wait: the CTA agrees on the outcome at this
+          // barrier, so that every thread leaves here or none does.
+          if (!__syncthreads_and(ok)) return false;
           const int nl = max(0, a.lo[0] - gx0), nr = max(0, gx0 + BW - 1 - a.hi[0]);
           const int ncol = nl + nr;
           for (int e = tid; e < ncol * IH; e += NT) {
@@ -357,6 +358,7 @@ __device__ __forceinline__ bool fused_range(const Fused3DArgs& a, const CUtensor
           }
           __syncthreads();
         }
+        if (!ok) return false;  // no barrier here: the caller's __syncthreads_or sees it
       } else {
         cp_async_wait<S - 1>();
         __syncthreads();

@@ -46,7 +46,7 @@ def _algo(itkg, name):
 
 
 # kernel names a call of each algorithm must report (the last launch of the call)
-FAMILY = {"two_pass": "z_pass_f32", "fused": "fused3d", "per_axis": "conv_axis"}
+FAMILY = {"two_pass": "z_pass_f32", "fused": "fused3d", "per_axis": "per_axis_f32"}
 
 
 # ---- 2-D: 512^2 f32, sigma 1.5 ----------------------------------------------
