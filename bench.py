@@ -237,7 +237,8 @@ def gpu_arm(args):
     prm.sigma = SIGMA
     prm.rounding = rounding
     prm.algorithm = {"auto": itkg.ALGO_AUTO, "fused": itkg.ALGO_FUSED,
-                     "per_axis": itkg.ALGO_PER_AXIS, "two_pass": itkg.ALGO_TWO_PASS}[args.algo]
+                     "per_axis": itkg.ALGO_PER_AXIS, "two_pass": itkg.ALGO_TWO_PASS,
+                     "one_trip": itkg.ALGO_ONE_TRIP}[args.algo]
     lg = region.to_c()
     req = region.to_c()
     in_c = [ctypes.byref(d.c) for d in ins]
@@ -858,7 +859,7 @@ def main():
                                            "mean3d", "binomial3d", "recursive3d", "unsharp3d", "callers3d"],
                     default="fwd3d")
     ap.add_argument("--rounding", choices=["fma", "reference"], default="fma")
-    ap.add_argument("--algo", choices=["auto", "fused", "per_axis", "two_pass"], default="auto")
+    ap.add_argument("--algo", choices=["auto", "fused", "per_axis", "two_pass", "one_trip"], default="auto")
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--batch-steps", type=int, default=10,
                     help="steps of the batched forward + VJP measurement added to the default line (0: skip)")

@@ -91,10 +91,14 @@ typedef enum itkg_algorithm {
     ITKG_ALGO_AUTO = 0,     /* two-pass, else fused, else per-axis: the first that fits */
     ITKG_ALGO_FUSED = 1,    /* one kernel for all passes; ITKG_ERROR_UNSUPPORTED if none fits */
     ITKG_ALGO_PER_AXIS = 2, /* D separate passes through an f32 scratch buffer */
-    ITKG_ALGO_TWO_PASS = 3  /* 3-D: an x-y slice kernel and a z kernel through an f32
+    ITKG_ALGO_TWO_PASS = 3, /* 3-D: an x-y slice kernel and a z kernel through an f32
                                intermediate sized for L2; ITKG_ERROR_UNSUPPORTED if it
                                does not fit (needs rx == ry <= 12, rz <= 12, one component,
                                16-byte aligned input rows) */
+    ITKG_ALGO_ONE_TRIP = 4  /* 3-D: one kernel, x, y and z passes on chip, each voxel
+                               read from and written to HBM once; ITKG_ERROR_UNSUPPORTED
+                               if it does not fit (needs f32 input, rx == ry <= 8,
+                               rz <= 8, one component, 16-byte aligned input rows) */
 } itkg_algorithm;
 
 /* Region<D> (src/image.rs:12-15): index[d], size[d] for d < dim. */

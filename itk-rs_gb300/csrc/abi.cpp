@@ -306,7 +306,7 @@ static itkg_status check_params(const itkg_gaussian_params* prm) {
     return set_error(ITKG_ERROR_INVALID_ARGUMENT, "unknown arithmetic %d", prm->arithmetic);
   if (prm->rounding != ITKG_ROUND_REFERENCE && prm->rounding != ITKG_ROUND_FMA)
     return set_error(ITKG_ERROR_INVALID_ARGUMENT, "unknown rounding %d", prm->rounding);
-  if (prm->algorithm < ITKG_ALGO_AUTO || prm->algorithm > ITKG_ALGO_TWO_PASS)
+  if (prm->algorithm < ITKG_ALGO_AUTO || prm->algorithm > ITKG_ALGO_ONE_TRIP)
     return set_error(ITKG_ERROR_INVALID_ARGUMENT, "unknown algorithm %d", prm->algorithm);
   if (prm->reserved != 0) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "reserved must be 0");
   return ITKG_SUCCESS;
@@ -412,7 +412,7 @@ static itkg_status generate_device(const itkg_image& in, const itkg_region& larg
   // backwards (their y and z passes index the weights by distance from the centre).
   if (!plan.symmetric || plan.reps == 0 ||
       (plan.reps > 1 && (prm.algorithm == ITKG_ALGO_PER_AXIS || prm.arithmetic == ITKG_ARITH_PIXEL_U8))) {
-    if (prm.algorithm == ITKG_ALGO_FUSED || prm.algorithm == ITKG_ALGO_TWO_PASS)
+    if (prm.algorithm == ITKG_ALGO_FUSED || prm.algorithm == ITKG_ALGO_TWO_PASS || prm.algorithm == ITKG_ALGO_ONE_TRIP)
       return set_error(ITKG_ERROR_UNSUPPORTED,
                        "asymmetric kernels, zero rounds and u8 pixel arithmetic over several rounds run per axis only");
     return run_per_axis(in, largest, requested, prm, plan, out, s);
@@ -423,6 +423,10 @@ static itkg_status generate_device(const itkg_image& in, const itkg_region& larg
     make_fused_geom(in, largest, requested, prm, plan, out, &g);
     const float* w[kMaxDim] = {nullptr, nullptr, nullptr};
     for (int d = 0; d < D; ++d) w[d] = plan.w32[d].data();
+    if (prm.algorithm == ITKG_ALGO_ONE_TRIP) {
+      if (launch_one_trip(g, w, s, /*dry_run=*/true) == ITKG_SUCCESS) return launch_one_trip(g, w, s, false);
+      return set_error(ITKG_ERROR_UNSUPPORTED, "the one-trip kernel does not cover this geometry");
+    }
     if (prm.algorithm == ITKG_ALGO_AUTO || prm.algorithm == ITKG_ALGO_TWO_PASS) {
       if (launch_two_pass(g, w, s, /*dry_run=*/true) == ITKG_SUCCESS) return launch_two_pass(g, w, s, false);
       if (prm.algorithm == ITKG_ALGO_TWO_PASS)

@@ -1,6 +1,8 @@
-// Packed two-lane f32 arithmetic (PTX add/mul/fma .f32x2, sm_100+).  Each lane
-// rounds exactly like the scalar instruction, so the reference-rounding form
-// (mul.rn then add.rn) stays bit-identical to scalar __fmul_rn / __fadd_rn.
+// Packed two-lane f32 arithmetic (PTX add/mul/fma .f32x2, sm_100+).
+// Reference rounding does not use these: a packed mul.rn / add.rn pair was
+// measured on the GPU to give results that differ from the scalar
+// __fmul_rn / __fadd_rn sequence (in about 70% of the voxels of a 3-D filter),
+// so every reference-rounding tap is scalar.
 #pragma once
 
 #include <cstdint>
@@ -35,16 +37,6 @@ __device__ __forceinline__ f2_t add2(f2_t a, f2_t b) {
   f2_t d;
   asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
   return d;
-}
-
-// acc + x * w per lane: reference rounding (two roundings) or one FMA.
-template <bool REF>
-__device__ __forceinline__ f2_t tap2(f2_t acc, f2_t x, f2_t w) {
-  if constexpr (REF) {
-    return add2(acc, mul2(x, w));
-  } else {
-    return fma2(x, w, acc);
-  }
 }
 
 // Host-side: the 64-bit pattern of the pair {w, w}.

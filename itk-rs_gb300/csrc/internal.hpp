@@ -159,6 +159,18 @@ struct UnsharpConsts;
 itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], void* stream,
                             bool dry_run, const UnsharpConsts* ush = nullptr);
 
+// two_pass.cu: per-CTA ranges of (block, slice) units, block-major, where a
+// CTA's cost is its units plus 2 rz halo slices per block it touches; the
+// smallest cost budget that lets at most `grid` CTAs (<= 1024) cover all
+// units.  Returns the CTA count and fills split[0 .. count]; 0 if the units do
+// not fit the table.
+int z_split(int64_t qblocks, int64_t nz, int rz, int64_t grid, int32_t* split);
+
+// one_trip.cu: the 3-D forward in one kernel (x, y and z passes on chip; f32
+// input, rx == ry <= 8, rz <= 8, one component, TMA-aligned input).
+// ITKG_ERROR_UNSUPPORTED (no error set) when it does not apply.
+itkg_status launch_one_trip(const FusedGeom& g, const float* const w[kMaxDim], void* stream, bool dry_run);
+
 // vjp2.cu: the 3-D VJP as z-adjoint and x-y kernels (rx == ry <= 12, rz <= 12,
 // f32, whole image, 16-byte aligned rows of x and ybar).  sigma_out is a
 // device double (added to with acc_sigma); xbar may be NULL, sigma_out too.

@@ -79,6 +79,8 @@ const char* xy_name(int dtype, bool ref) {
   return names[dtype][ref ? 1 : 0];
 }
 
+}  // namespace
+
 // Per-CTA unit ranges of the z pass.  Units are (quad block, output slice),
 // block-major; a CTA marches each column segment of its range from 2 rz slices
 // before the segment's first output, so its cost is its units plus 2 rz per
@@ -116,8 +118,6 @@ int z_split(int64_t qblocks, int64_t nz, int rz, int64_t grid, int32_t* split) {
   }
   return (int)cover(lo, split);
 }
-
-}  // namespace
 
 itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], void* stream, bool dry_run,
                             const UnsharpConsts* ush) {

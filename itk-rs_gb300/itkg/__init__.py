@@ -22,7 +22,7 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from ._abi import (ALGO_AUTO, ALGO_FUSED, ALGO_PER_AXIS, ALGO_TWO_PASS, ARITH_F32, ARITH_PIXEL_U8, BF16,
+from ._abi import (ALGO_AUTO, ALGO_FUSED, ALGO_ONE_TRIP, ALGO_PER_AXIS, ALGO_TWO_PASS, ARITH_F32, ARITH_PIXEL_U8, BF16,
                    DEVICE, F16, F32, HOST, I16, ROUND_FMA, ROUND_REFERENCE, U8, ItkgError, check,
                    itkg_gaussian_params, itkg_image, itkg_recursive_derivative_params, itkg_recursive_params,
                    itkg_region, itkg_separable_params, itkg_unsharp_params, lib)
@@ -31,7 +31,7 @@ __all__ = [
     "Region", "Image", "DeviceImage", "GaussianFilter", "CastFilter", "stream_full",
     "split_region", "kernel_radius", "build_kernel", "ItkgError", "F32", "I16", "U8", "BF16",
     "F16", "ROUND_REFERENCE", "ROUND_FMA", "ALGO_AUTO", "ALGO_FUSED", "ALGO_PER_AXIS",
-    "ALGO_TWO_PASS", "ARITH_F32", "ARITH_PIXEL_U8", "gaussian", "Stream", "SeparableFilter",
+    "ALGO_TWO_PASS", "ALGO_ONE_TRIP", "ARITH_F32", "ARITH_PIXEL_U8", "gaussian", "Stream", "SeparableFilter",
     "MeanFilter", "BoxMeanFilterN", "BinomialBlurFilter", "box_kernel", "BINOMIAL_KERNEL",
     "RecursiveGaussianFilter", "RecursiveGaussianAxisFilter", "yvv_coeffs", "RecursiveGaussianDerivativeFilter",
     "GradientMagnitudeRecursiveGaussianFilter", "LaplacianRecursiveGaussianFilter",

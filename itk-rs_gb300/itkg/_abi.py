@@ -24,7 +24,7 @@ F32, I16, U8, BF16, F16 = 0, 1, 2, 3, 4
 DEVICE, HOST = 0, 1
 ARITH_F32, ARITH_PIXEL_U8 = 0, 1
 ROUND_REFERENCE, ROUND_FMA = 0, 1
-ALGO_AUTO, ALGO_FUSED, ALGO_PER_AXIS, ALGO_TWO_PASS = 0, 1, 2, 3
+ALGO_AUTO, ALGO_FUSED, ALGO_PER_AXIS, ALGO_TWO_PASS, ALGO_ONE_TRIP = 0, 1, 2, 3, 4
 
 c_i64_3 = ctypes.c_int64 * 3
 c_u64_3 = ctypes.c_uint64 * 3

@@ -51,10 +51,10 @@ def wait_limit_one_cycle(gpu):
         _fault(L, True)
 
 
-@pytest.mark.parametrize("algo", ["two_pass", "fused"])
+@pytest.mark.parametrize("algo", ["two_pass", "fused", "one_trip"])
 def test_wait_that_runs_out_sets_fault_word_then_recovers(gpu, wait_limit_one_cycle, algo):
     L = wait_limit_one_cycle
-    algorithm = gpu.ALGO_TWO_PASS if algo == "two_pass" else gpu.ALGO_FUSED
+    algorithm = {"two_pass": gpu.ALGO_TWO_PASS, "fused": gpu.ALGO_FUSED, "one_trip": gpu.ALGO_ONE_TRIP}[algo]
     rng = np.random.default_rng(1)
     x = rng.random((48, 64, 96), dtype=np.float32)
     dev = gpu.DeviceImage.from_host(gpu.Image(x))
