@@ -494,6 +494,36 @@ itkg_status itkg_gaussian_generate_region_noalloc(const itkg_image *input,
                                                   const itkg_gaussian_params *params,
                                                   itkg_image *output, void *stream);
 
+/* DemonsRegistrationFilter::compute (src/filters/registration_methods.rs:39-100)
+ * and, with diffeomorphic != 0, DiffeomorphicDemonsRegistrationFilter::compute
+ * (registration_methods.rs:126-148; SyNRegistrationMethod::compute, :211-218,
+ * is the latter with the sum of its iteration counts): `iterations` demons
+ * force updates of a displacement field (in pixels, f64, as the reference
+ * keeps it) from 2-D f32 fixed and moving images, each image's buffered region
+ * being its largest region; with diffeomorphic != 0 each displacement
+ * component is then smoothed by GaussianFilter { sigma: sigma_diff } in
+ * reference rounding.  displacement: 2-D f32, 2 components (VecPixel<f32, 2>),
+ * containing the fixed region.  A warped index outside the moving buffer,
+ * where the reference panics, returns ITKG_ERROR_INVALID_ARGUMENT.  Any buffer
+ * may be host or device memory; the call returns after the result is written. */
+itkg_status itkg_demons_registration(const itkg_image *fixed, const itkg_image *moving, int32_t iterations,
+                                     double max_step_length, int32_t diffeomorphic, double sigma_diff,
+                                     itkg_image *displacement, void *stream);
+
+/* N4BiasFieldCorrectionFilter::generate_region (src/filters/bias_correction.rs:45-83;
+ * MRIBiasFieldCorrectionFilter, :113-121, is this call with sigma 20): the
+ * largest region of a 2-D f32 image, up to `iterations` times: the f64 log of
+ * the corrected image, GaussianFilter { sigma } of its f32 image (reference
+ * rounding), corrected = max(exp(log - smoothed), 1e-6), stopping when the
+ * mean absolute change falls below convergence_threshold; output = corrected
+ * as f32 over the largest region.  *iterations_run (may be NULL) receives the
+ * number of iterations run.  ln and exp are the device's f64 functions, whose
+ * last bit may differ from the host libm's.  Any buffer may be host or device
+ * memory; the call returns after the result is written. */
+itkg_status itkg_n4_bias_field_correction(const itkg_image *input, const itkg_region *largest, int32_t iterations,
+                                          double sigma, double convergence_threshold, itkg_image *output,
+                                          int32_t *iterations_run, void *stream);
+
 /* stream_full(&GaussianFilter{input, sigma}, num_pieces) (source.rs:81-98):
  * output (region == largest) is filled piece by piece along axis D-1.  With a
  * host-resident input and output, only one halo-padded input slab and one

@@ -1369,4 +1369,237 @@ itkg_status itkg_stream_full(const itkg_image* input, const itkg_region* largest
   return ITKG_SUCCESS;
 }
 
+
+// ---- in-crate callers that iterate around the Gaussian -----------------------
+
+namespace {
+// A 2-D f32 scalar image on the device for a point-wise kernel: the image
+// itself, or a dense copy of `reg` in scratch (*owned) when it is host memory.
+itkg_status device_view(const itkg_image& im, const itkg_region& reg, cudaStream_t s, itkg_image* out, void** owned) {
+  *out = im;
+  *owned = nullptr;
+  if (im.location == ITKG_DEVICE) return ITKG_SUCCESS;
+  out->location = ITKG_DEVICE;
+  out->region = reg;
+  dense_layout(out, 16);
+  ITKG_TRY(scratch_alloc(owned, image_bytes(*out), s));
+  out->data = *owned;
+  return copy_region(*out, im, reg, s);
+}
+
+const float* first_pixel(const itkg_image& im, const itkg_region& reg) {
+  return reinterpret_cast<const float*>(static_cast<const char*>(im.data) +
+                                        (reg.index[0] - im.region.index[0]) * im.pitch[0] +
+                                        (reg.index[1] - im.region.index[1]) * im.pitch[1]);
+}
+
+itkg_status check_f32_2d(const itkg_image* im, const char* name, int comps) {
+  ITKG_TRY(validate_image(im, name));
+  if (im->dim != 2 || im->dtype != ITKG_F32 || im->components != comps)
+    return set_error(ITKG_ERROR_UNSUPPORTED, "%s must be a 2-D f32 image with %d component(s)", name, comps);
+  if (im->pitch[1] % 4 != 0) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "%s: row pitch not a multiple of 4", name);
+  return ITKG_SUCCESS;
+}
+}  // namespace
+
+itkg_status itkg_demons_registration(const itkg_image* fixed, const itkg_image* moving, int32_t iterations,
+                                     double max_step_length, int32_t diffeomorphic, double sigma_diff,
+                                     itkg_image* displacement, void* stream) {
+  ITKG_TRY(check_f32_2d(fixed, "fixed", 1));
+  ITKG_TRY(check_f32_2d(moving, "moving", 1));
+  ITKG_TRY(check_f32_2d(displacement, "displacement", 2));
+  if (iterations < 0) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "iterations < 0");
+  const itkg_region freg = fixed->region, mreg = moving->region;
+  if (!region_contains(displacement->region, freg, 2))
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "displacement buffer does not contain the fixed image's region");
+  const int64_t w = (int64_t)freg.size[0], h = (int64_t)freg.size[1], n = w * h;
+  if (n == 0) return ITKG_SUCCESS;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  itkg_image fd, md;
+  void *pf = nullptr, *pm = nullptr, *pd = nullptr, *pw = nullptr, *pout = nullptr;
+  itkg_status st = device_view(*fixed, freg, s, &fd, &pf);
+  if (st == ITKG_SUCCESS) st = device_view(*moving, mreg, s, &md, &pm);
+  // displacement (x, y) in f64, two generations, and the error word
+  const size_t dbytes = (size_t)n * sizeof(double);
+  if (st == ITKG_SUCCESS) st = scratch_alloc(&pd, 4 * dbytes + 256, s);
+  double* d[4] = {nullptr, nullptr, nullptr, nullptr};
+  unsigned int* err = nullptr;
+  if (st == ITKG_SUCCESS) {
+    for (int k = 0; k < 4; ++k) d[k] = reinterpret_cast<double*>(static_cast<char*>(pd) + k * dbytes);
+    err = reinterpret_cast<unsigned int*>(static_cast<char*>(pd) + 4 * dbytes);
+    st = cuda_status(cudaMemsetAsync(pd, 0, 4 * dbytes + 256, s), "cudaMemsetAsync");
+  }
+  DemonsGeom g;
+  g.fixed = first_pixel(fd, freg);
+  g.fp = fd.pitch[1] / 4;
+  g.w = w;
+  g.h = h;
+  g.ox = freg.index[0];
+  g.oy = freg.index[1];
+  g.moving = first_pixel(md, mreg);
+  g.mp = md.pitch[1] / 4;
+  g.mw = (int64_t)mreg.size[0];
+  g.mh = (int64_t)mreg.size[1];
+  g.mox = mreg.index[0];
+  g.moy = mreg.index[1];
+  int cur = 0;  // d[cur], d[cur + 1] hold the current field
+  for (int it = 0; it < iterations && st == ITKG_SUCCESS; ++it) {
+    st = launch_demons_step(g, d[cur], d[cur + 1], d[2 - cur], d[3 - cur], max_step_length, err, s);
+    cur = 2 - cur;
+  }
+  // the output buffer (device, or a dense scratch copy of the fixed region)
+  itkg_image dout = *displacement;
+  if (st == ITKG_SUCCESS && displacement->location == ITKG_HOST) {
+    dout.location = ITKG_DEVICE;
+    dout.region = freg;
+    dense_layout(&dout, 16);
+    st = scratch_alloc(&pout, image_bytes(dout), s);
+    dout.data = pout;
+  }
+  float* const o = const_cast<float*>(first_pixel(dout, freg));
+  const int64_t op = dout.pitch[1] / 8;
+  if (st == ITKG_SUCCESS && !diffeomorphic) {
+    st = launch_demons_to_f32(d[cur], d[cur + 1], w, h, o, op, nullptr, nullptr, 0, s);
+  } else if (st == ITKG_SUCCESS) {
+    // DiffeomorphicDemonsRegistrationFilter (registration_methods.rs:126-148):
+    // GaussianFilter { sigma: sigma_diff } over each component's whole image
+    itkg_image comp;
+    std::memset(&comp, 0, sizeof comp);
+    comp.dim = 2;
+    comp.dtype = ITKG_F32;
+    comp.components = 1;
+    comp.location = ITKG_DEVICE;
+    comp.region = freg;
+    comp.spacing[0] = fixed->spacing[0];
+    comp.spacing[1] = fixed->spacing[1];
+    comp.origin[0] = fixed->origin[0];
+    comp.origin[1] = fixed->origin[1];
+    dense_layout(&comp, 16);
+    const size_t cb = image_bytes(comp);
+    st = scratch_alloc(&pw, 4 * cb, s);
+    if (st == ITKG_SUCCESS) {
+      itkg_image raw[2] = {comp, comp}, sm[2] = {comp, comp};
+      for (int c = 0; c < 2; ++c) {
+        raw[c].data = static_cast<char*>(pw) + c * cb;
+        sm[c].data = static_cast<char*>(pw) + (2 + c) * cb;
+      }
+      // planar components, rows at the dense pitch (w floats rounded up to 16 bytes)
+      const int64_t cp = comp.pitch[1] / 4;
+      st = launch_demons_to_f32(d[cur], d[cur + 1], w, h, nullptr, 0, static_cast<float*>(raw[0].data),
+                                static_cast<float*>(raw[1].data), cp, s);
+      itkg_gaussian_params gp;
+      std::memset(&gp, 0, sizeof gp);
+      gp.sigma = sigma_diff;
+      gp.rounding = ITKG_ROUND_REFERENCE;
+      for (int c = 0; c < 2 && st == ITKG_SUCCESS; ++c)
+        st = generate_region(&raw[c], &freg, &freg, nullptr, &gp, &sm[c], s);
+      if (st == ITKG_SUCCESS)
+        st = launch_interleave2(static_cast<const float*>(sm[0].data), static_cast<const float*>(sm[1].data), cp, w, h,
+                                o, op, s);
+    }
+  }
+  if (st == ITKG_SUCCESS && displacement->location == ITKG_HOST) st = copy_region(*displacement, dout, freg, s);
+  unsigned int herr = 0;
+  if (st == ITKG_SUCCESS) st = cuda_status(cudaMemcpyAsync(&herr, err, sizeof herr, cudaMemcpyDeviceToHost, s), "copy");
+  const cudaError_t es = cudaStreamSynchronize(s);
+  scratch_free(pf, s);
+  scratch_free(pm, s);
+  scratch_free(pd, s);
+  scratch_free(pw, s);
+  scratch_free(pout, s);
+  if (st != ITKG_SUCCESS) return st;
+  if (es != cudaSuccess) return cuda_status(es, "cudaStreamSynchronize");
+  if (herr)
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT,
+                     "a warped index left the moving image's buffer (the reference's Image::get_pixel panics here)");
+  set_last_kernel(diffeomorphic ? "demons_diffeomorphic_f64" : "demons_step_f64");
+  return ITKG_SUCCESS;
+}
+
+itkg_status itkg_n4_bias_field_correction(const itkg_image* input, const itkg_region* largest, int32_t iterations,
+                                          double sigma, double convergence_threshold, itkg_image* output,
+                                          int32_t* iterations_run, void* stream) {
+  ITKG_TRY(check_f32_2d(input, "input", 1));
+  ITKG_TRY(check_f32_2d(output, "output", 1));
+  if (!largest) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "largest is NULL");
+  if (iterations < 0) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "iterations < 0");
+  if (!region_contains(input->region, *largest, 2))
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "input buffer does not cover the largest region");
+  if (!region_contains(output->region, *largest, 2))
+    return set_error(ITKG_ERROR_INVALID_ARGUMENT, "output buffer does not contain the largest region");
+  if (iterations_run) *iterations_run = 0;
+  const int64_t w = (int64_t)largest->size[0], h = (int64_t)largest->size[1], n = w * h;
+  if (n == 0) return ITKG_SUCCESS;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  itkg_image in_d;
+  void *pin = nullptr, *pbuf = nullptr, *pout = nullptr;
+  itkg_status st = device_view(*input, *largest, s, &in_d, &pin);
+  // log image and its smoothing as dense f32 images of the largest region
+  itkg_image lf;
+  std::memset(&lf, 0, sizeof lf);
+  lf.dim = 2;
+  lf.dtype = ITKG_F32;
+  lf.components = 1;
+  lf.location = ITKG_DEVICE;
+  lf.region = *largest;
+  for (int d = 0; d < 2; ++d) {
+    lf.spacing[d] = input->spacing[d];
+    lf.origin[d] = input->origin[d];
+  }
+  lf.pitch[0] = 4;
+  lf.pitch[1] = 4 * w;
+  lf.pitch[2] = 4 * n;
+  itkg_image sm = lf;
+  const int nb = n4_blocks(n);
+  const size_t dbytes = (size_t)n * 8, fbytes = ((size_t)n * 4 + 255) / 256 * 256;
+  if (st == ITKG_SUCCESS) st = scratch_alloc(&pbuf, 2 * dbytes + 2 * fbytes + (size_t)(nb + 1) * 8, s);
+  double *corr = nullptr, *ld = nullptr, *part = nullptr;
+  if (st == ITKG_SUCCESS) {
+    char* b = static_cast<char*>(pbuf);
+    corr = reinterpret_cast<double*>(b);
+    ld = reinterpret_cast<double*>(b + dbytes);
+    lf.data = b + 2 * dbytes;
+    sm.data = b + 2 * dbytes + fbytes;
+    part = reinterpret_cast<double*>(b + 2 * dbytes + 2 * fbytes);
+    st = launch_n4_init(first_pixel(in_d, *largest), in_d.pitch[1] / 4, w, h, corr, s);
+  }
+  itkg_gaussian_params gp;
+  std::memset(&gp, 0, sizeof gp);
+  gp.sigma = sigma;
+  gp.rounding = ITKG_ROUND_REFERENCE;
+  int run = 0;
+  for (int it = 0; it < iterations && st == ITKG_SUCCESS; ++it) {
+    st = launch_n4_log(corr, n, ld, static_cast<float*>(lf.data), s);
+    if (st == ITKG_SUCCESS) st = generate_region(&lf, largest, largest, nullptr, &gp, &sm, s);
+    if (st == ITKG_SUCCESS) st = launch_n4_update(ld, static_cast<const float*>(sm.data), n, corr, part, nb, s);
+    if (st == ITKG_SUCCESS) st = launch_sum_partials(part, nb, part + nb, false, s);
+    double total = 0.0;
+    if (st == ITKG_SUCCESS) st = cuda_status(cudaMemcpyAsync(&total, part + nb, 8, cudaMemcpyDeviceToHost, s), "copy");
+    if (st == ITKG_SUCCESS) st = cuda_status(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+    ++run;
+    // convergence (bias_correction.rs:76-78): mean absolute change
+    if (st == ITKG_SUCCESS && total / (double)n < convergence_threshold) break;
+  }
+  itkg_image dout = *output;
+  if (st == ITKG_SUCCESS && output->location == ITKG_HOST) {
+    dout.location = ITKG_DEVICE;
+    dout.region = *largest;
+    dense_layout(&dout, 16);
+    st = scratch_alloc(&pout, image_bytes(dout), s);
+    dout.data = pout;
+  }
+  if (st == ITKG_SUCCESS)
+    st = launch_n4_store(corr, w, h, const_cast<float*>(first_pixel(dout, *largest)), dout.pitch[1] / 4, s);
+  if (st == ITKG_SUCCESS && output->location == ITKG_HOST) st = copy_region(*output, dout, *largest, s);
+  const cudaError_t es = cudaStreamSynchronize(s);
+  scratch_free(pin, s);
+  scratch_free(pbuf, s);
+  scratch_free(pout, s);
+  if (st != ITKG_SUCCESS) return st;
+  if (es != cudaSuccess) return cuda_status(es, "cudaStreamSynchronize");
+  if (iterations_run) *iterations_run = run;
+  set_last_kernel("n4_update_f64");
+  return ITKG_SUCCESS;
+}
+
 }  // extern "C"

@@ -227,6 +227,31 @@ itkg_status launch_unsharp(int dtype, int comps, const void* in, const int64_t* 
 itkg_status launch_subsample2(const void* src, const int64_t* sp, void* dst, const int64_t* dp, const int64_t* m,
                               int elem, void* stream);
 
+// Demons and N4 point-wise kernels (registration.cu).  DemonsGeom: the fixed
+// image (f32 rows at pitch fp elements, w x h at index (ox, oy)) and the
+// moving image (rows at pitch mp, mw x mh at (mox, moy)), device pointers at
+// each region's first pixel.
+struct DemonsGeom {
+  const float* fixed;
+  int64_t fp, w, h, ox, oy;
+  const float* moving;
+  int64_t mp, mw, mh, mox, moy;
+};
+itkg_status launch_demons_step(const DemonsGeom& g, const double* dxi, const double* dyi, double* dxo, double* dyo,
+                               double max_step, unsigned int* err, void* stream);
+// out: interleaved VecPixel<f32, 2> rows at pitch op (pixels), or, with px and
+// py non-NULL, two planar f32 images with rows at pitch pp (floats)
+itkg_status launch_demons_to_f32(const double* dx, const double* dy, int64_t w, int64_t h, float* out, int64_t op,
+                                 float* px, float* py, int64_t pp, void* stream);
+itkg_status launch_interleave2(const float* a, const float* b, int64_t sp, int64_t w, int64_t h, float* out, int64_t op,
+                               void* stream);
+itkg_status launch_n4_init(const float* in, int64_t ip, int64_t w, int64_t h, double* corr, void* stream);
+itkg_status launch_n4_log(const double* corr, int64_t n, double* ld, float* lf, void* stream);
+int n4_blocks(int64_t n);
+itkg_status launch_n4_update(const double* ld, const float* sm, int64_t n, double* corr, double* partials, int blocks,
+                             void* stream);
+itkg_status launch_n4_store(const double* corr, int64_t w, int64_t h, float* out, int64_t op, void* stream);
+
 // Bumps the launch counter by n (graph replays).
 void note_launches(uint64_t n, const char* name);
 

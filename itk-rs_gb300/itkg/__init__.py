@@ -37,7 +37,9 @@ __all__ = [
     "GradientMagnitudeRecursiveGaussianFilter", "LaplacianRecursiveGaussianFilter",
     "DiscreteGaussianDerivativeFilter", "GradientRecursiveGaussianFilter", "HessianRecursiveGaussianFilter",
     "DifferenceOfGaussiansFilter", "UnsharpMaskFilter", "unsharp_kernel", "ZeroCrossingBasedEdgeDetectionFilter",
-    "SliceBySliceFilter", "BSplineDownsampleFilter",
+    "SliceBySliceFilter", "BSplineDownsampleFilter", "DemonsRegistrationFilter",
+    "DiffeomorphicDemonsRegistrationFilter", "SyNRegistrationMethod", "N4BiasFieldCorrectionFilter",
+    "MRIBiasFieldCorrectionFilter",
 ]
 
 _NP_OF = {F32: np.float32, I16: np.int16, U8: np.uint8, F16: np.float16}
@@ -505,6 +507,117 @@ class BSplineDownsampleFilter(GaussianFilter):
         check(lib().itkg_bspline_downsample_generate_region(ctypes.byref(src), ctypes.byref(largest),
                                                             ctypes.byref(prm), ctypes.byref(oc), stream.ptr))
         return res
+
+
+def _image_leaf(src):
+    if isinstance(src, (Image, DeviceImage)):
+        return src
+    raise TypeError("the source must be an Image or a DeviceImage")
+
+
+class DemonsRegistrationFilter:
+    """DemonsRegistrationFilter { fixed, moving, iterations, max_step_length }
+    (registration_methods.rs:20-100): compute() returns the displacement field
+    (in pixels) of the fixed image's region as a 2-component f32 image
+    (VecPixel<f32, 2>): an Image for host sources, a DeviceImage for device ones."""
+
+    _diffeomorphic = 0
+
+    def __init__(self, fixed, moving, iterations: int, max_step_length: float = 2.0):
+        self.fixed, self.moving = fixed, moving
+        self.iterations = int(iterations)
+        self.max_step_length = float(max_step_length)
+        self.sigma_diff = 1.0
+
+    def compute(self, stream: Stream = _DEFAULT_STREAM):
+        f, m = _image_leaf(self.fixed), _image_leaf(self.moving)
+        reg = f.region
+        if isinstance(f, Image):
+            res = Image(np.empty(tuple(reversed(reg.size)) + (2,), np.float32), index=reg.index, spacing=f.spacing,
+                        origin=f.origin, components=2)
+            oc = res.to_c()
+        else:
+            res = DeviceImage(reg, F32, 2, f.spacing, f.origin)
+            oc = res.c
+        fc, mc = f.to_c(), m.to_c()
+        check(lib().itkg_demons_registration(ctypes.byref(fc), ctypes.byref(mc), self.iterations,
+                                             self.max_step_length, self._diffeomorphic, float(self.sigma_diff),
+                                             ctypes.byref(oc), stream.ptr))
+        return res
+
+
+class DiffeomorphicDemonsRegistrationFilter(DemonsRegistrationFilter):
+    """DiffeomorphicDemonsRegistrationFilter { fixed, moving, iterations, sigma_diff }
+    (registration_methods.rs:108-148): the demons field (max step 2.0), each
+    component smoothed by GaussianFilter { sigma: sigma_diff }."""
+
+    _diffeomorphic = 1
+
+    def __init__(self, fixed, moving, iterations: int, sigma_diff: float = 1.0):
+        super().__init__(fixed, moving, iterations)
+        self.sigma_diff = float(sigma_diff)
+
+
+class SyNRegistrationMethod(DiffeomorphicDemonsRegistrationFilter):
+    """SyNRegistrationMethod { fixed, moving, iterations, sigma } (registration_methods.rs:193-218):
+    the diffeomorphic demons with the sum of its iteration counts (its `sigma`
+    is not read by the reference either; the smoothing uses sigma_diff 1.0)."""
+
+    def __init__(self, fixed, moving, iterations=(20, 10, 5), sigma: float = 1.0):
+        super().__init__(fixed, moving, sum(int(i) for i in iterations))
+        self.sigma = float(sigma)
+
+
+class N4BiasFieldCorrectionFilter:
+    """N4BiasFieldCorrectionFilter { source, iterations, sigma, convergence_threshold }
+    (bias_correction.rs:23-83): generate_region ignores the request and returns the
+    corrected image of the whole largest region (f32).  iterations_run is set by
+    each call."""
+
+    def __init__(self, source, iterations: int = 4, sigma: float = 30.0, convergence_threshold: float = 1e-3):
+        self.source = source
+        self.iterations = int(iterations)
+        self.sigma = float(sigma)
+        self.convergence_threshold = float(convergence_threshold)
+        self.iterations_run = None
+
+    def largest_region(self) -> Region:
+        return self.source.largest_region()
+
+    @property
+    def spacing(self):
+        return _image_leaf(self.source).spacing
+
+    @property
+    def origin(self):
+        return _image_leaf(self.source).origin
+
+    def generate_region(self, requested: Region = None, stream: Stream = _DEFAULT_STREAM):
+        leaf = _image_leaf(self.source)
+        reg = leaf.largest_region()
+        if isinstance(leaf, Image):
+            res = Image(np.empty(tuple(reversed(reg.size)), np.float32), index=reg.index, spacing=leaf.spacing,
+                        origin=leaf.origin)
+            oc = res.to_c()
+        else:
+            res = DeviceImage(reg, F32, 1, leaf.spacing, leaf.origin)
+            oc = res.c
+        src, lg = leaf.to_c(), reg.to_c()
+        run = ctypes.c_int32(0)
+        check(lib().itkg_n4_bias_field_correction(ctypes.byref(src), ctypes.byref(lg), self.iterations, self.sigma,
+                                                  self.convergence_threshold, ctypes.byref(oc), ctypes.byref(run),
+                                                  stream.ptr))
+        self.iterations_run = run.value
+        return res
+
+
+class MRIBiasFieldCorrectionFilter(N4BiasFieldCorrectionFilter):
+    """MRIBiasFieldCorrectionFilter { source, polynomial_degree, iterations }
+    (bias_correction.rs:92-121): N4 with sigma 20 and threshold 1e-3."""
+
+    def __init__(self, source, polynomial_degree: int = 2, iterations: int = 3):
+        super().__init__(source, iterations, 20.0, 1e-3)
+        self.polynomial_degree = int(polynomial_degree)
 
 
 def unsharp_kernel(sigma: float) -> np.ndarray:

@@ -132,6 +132,9 @@ SIGNATURES = {
     "itkg_memcpy": (st, [P, P, ctypes.c_size_t, ctypes.c_int32, P]),
     "itkg_memset_device": (st, [P, ctypes.c_int32, ctypes.c_size_t, P]),
     "itkg_stream_synchronize": (st, [P]),
+    "itkg_demons_registration": (st, [I, I, ctypes.c_int32, ctypes.c_double, ctypes.c_int32, ctypes.c_double, I, P]),
+    "itkg_n4_bias_field_correction": (st, [I, R, ctypes.c_int32, ctypes.c_double, ctypes.c_double, I,
+                                           ctypes.POINTER(ctypes.c_int32), P]),
     "itkg_stream_create": (st, [ctypes.POINTER(ctypes.c_void_p)]),
     "itkg_stream_destroy": (st, [P]),
     "itkg_device_fault": (st, [ctypes.c_int32, ctypes.POINTER(ctypes.c_uint32)]),

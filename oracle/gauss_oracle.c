@@ -554,3 +554,102 @@ void orc_cast_f32_to_u8(const float *in, uint8_t *out, int64_t n) {
         out[i] = (uint8_t)v;
     }
 }
+
+/* ---- DemonsRegistrationFilter::compute (registration_methods.rs:39-100) ---- *
+ * fixed: dense w x h at index freg (index[0..1], size[0..1]); moving: dense mw x mh
+ * at mreg.  disp_x / disp_y: w * h f64 each, zeroed by the caller.  Each f64
+ * operation is one C operation (no contraction).  Returns 0, or 1 where the
+ * reference panics: a warped index whose flat offset (Image::flat_index,
+ * image.rs:111-120, wrapping usize arithmetic) is outside the moving data. */
+static int64_t sat_i64(double v) {  /* Rust's `f64 as i64` */
+    if (v != v) return 0;
+    if (v >= 9.2233720368547758e18) return INT64_MAX;
+    if (v <= -9.2233720368547758e18) return INT64_MIN;
+    return (int64_t)v;
+}
+
+int orc_demons_f64(const float *fixed, const orc_region *freg, const float *moving, const orc_region *mreg,
+                   int iterations, double max_step, double *disp_x, double *disp_y) {
+    const int64_t w = freg->size[0], h = freg->size[1], ox = freg->index[0], oy = freg->index[1];
+    const uint64_t mw = (uint64_t)mreg->size[0], mlen = (uint64_t)(mreg->size[0] * mreg->size[1]);
+    double *nx = (double *)malloc((size_t)(w * h) * sizeof(double) + 8);
+    double *ny = (double *)malloc((size_t)(w * h) * sizeof(double) + 8);
+    if (!nx || !ny) { free(nx); free(ny); return -1; }
+    int err = 0;
+#define FCLAMP(xx, yy) (((yy) < 0 ? 0 : ((yy) > h - 1 ? h - 1 : (yy))) * w + ((xx) < 0 ? 0 : ((xx) > w - 1 ? w - 1 : (xx))))
+    for (int it = 0; it < iterations && !err; it++) {
+        memcpy(nx, disp_x, (size_t)(w * h) * sizeof(double));  /* new = old.clone() (:55-56) */
+        memcpy(ny, disp_y, (size_t)(w * h) * sizeof(double));
+        for (int64_t y = 0; y < h; y++) {
+            for (int64_t x = 0; x < w; x++) {
+                const int64_t i = y * w + x;
+                const double wx = (double)x + disp_x[i];
+                const double wy = (double)y + disp_y[i];
+                const uint64_t xi = (uint64_t)ox + (uint64_t)sat_i64(round(wx));
+                const uint64_t yi = (uint64_t)oy + (uint64_t)sat_i64(round(wy));
+                const uint64_t flat = (xi - (uint64_t)mreg->index[0]) + (yi - (uint64_t)mreg->index[1]) * mw;
+                if (flat >= mlen) { err = 1; break; }
+                const double m_val = (double)moving[flat];
+                const double f_val = (double)fixed[i];
+                const double gx = ((double)fixed[FCLAMP(x + 1, y)] - (double)fixed[FCLAMP(x - 1, y)]) * 0.5;
+                const double gy = ((double)fixed[FCLAMP(x, y + 1)] - (double)fixed[FCLAMP(x, y - 1)]) * 0.5;
+                const double diff = f_val - m_val;
+                const double denom = gx * gx + gy * gy + diff * diff + 1e-6;
+                const double step = diff / denom;
+                const double dx = step * gx;
+                const double dy = step * gy;
+                const double norm = sqrt(dx * dx + dy * dy);
+                const double scale = norm > max_step ? max_step / norm : 1.0;
+                nx[i] = disp_x[i] + dx * scale;
+                ny[i] = disp_y[i] + dy * scale;
+            }
+            if (err) break;
+        }
+        if (!err) {
+            memcpy(disp_x, nx, (size_t)(w * h) * sizeof(double));
+            memcpy(disp_y, ny, (size_t)(w * h) * sizeof(double));
+        }
+    }
+#undef FCLAMP
+    free(nx);
+    free(ny);
+    return err;
+}
+
+/* ---- N4BiasFieldCorrectionFilter::generate_region (bias_correction.rs:45-83) -- *
+ * 2-D f32 image of region `reg` (its largest region); out: dense f32 of reg.
+ * ln and exp are the C library's (the functions Rust's f64::ln / f64::exp
+ * call on this host).  Returns the number of iterations run, or -1. */
+int orc_n4_f32(const float *in, const orc_region *reg, const double *spacing, int iterations, double sigma,
+               double threshold, float *out) {
+    const int64_t n = reg->size[0] * reg->size[1];
+    double *corr = (double *)malloc((size_t)n * sizeof(double) + 8);
+    double *ld = (double *)malloc((size_t)n * sizeof(double) + 8);
+    float *lf = (float *)malloc((size_t)n * sizeof(float) + 8);
+    float *sm = (float *)malloc((size_t)n * sizeof(float) + 8);
+    if (!corr || !ld || !lf || !sm) { free(corr); free(ld); free(lf); free(sm); return -1; }
+    for (int64_t i = 0; i < n; i++) corr[i] = fmax((double)in[i], 1e-6);
+    int run = 0;
+    for (int it = 0; it < iterations; it++) {
+        for (int64_t i = 0; i < n; i++) {
+            ld[i] = log(corr[i]);
+            lf[i] = (float)ld[i];
+        }
+        if (gaussian_region(lf, reg, spacing, 2, 1, sigma, reg, sm, PIX_F32, 1) != 0) { run = -1; break; }
+        double sum = 0.0;
+        for (int64_t i = 0; i < n; i++) {
+            const double prev = corr[i];
+            corr[i] = fmax(exp(ld[i] - (double)sm[i]), 1e-6);
+            sum += fabs(corr[i] - prev);
+        }
+        run++;
+        if (sum / (double)n < threshold) break;
+    }
+    if (run >= 0)
+        for (int64_t i = 0; i < n; i++) out[i] = (float)corr[i];
+    free(corr);
+    free(ld);
+    free(lf);
+    free(sm);
+    return run;
+}

@@ -86,6 +86,10 @@ def lib():
         L.orc_box_kernel.argtypes = [ctypes.c_uint64, P]
         L.orc_cast_f32_to_u8.restype = None
         L.orc_cast_f32_to_u8.argtypes = [P, P, ctypes.c_int64]
+        L.orc_demons_f64.restype = ctypes.c_int
+        L.orc_demons_f64.argtypes = [P, R, P, R, ctypes.c_int, ctypes.c_double, P, P]
+        L.orc_n4_f32.restype = ctypes.c_int
+        L.orc_n4_f32.argtypes = [P, R, P, ctypes.c_int, ctypes.c_double, ctypes.c_double, P]
         _lib = L
     return _lib
 
@@ -578,3 +582,52 @@ def gaussian_dsigma_f64(x: np.ndarray, sigma: float, spacing=None, radii=None):
             y = conv_axis_f64(y, dw if b == a else w, b, D)
         total += y
     return total
+
+
+# ---- Gaussian callers that iterate around it (C core) ------------------------
+
+def demons(fixed, moving, iterations, max_step_length=2.0, fixed_index=(0, 0), moving_index=(0, 0)):
+    """DemonsRegistrationFilter::compute (registration_methods.rs:39-100): the
+    f64 displacement (dx, dy) arrays, shape of `fixed`.  Raises where the
+    reference panics (a warped index outside the moving image)."""
+    f = np.ascontiguousarray(fixed, dtype=np.float32)
+    m = np.ascontiguousarray(moving, dtype=np.float32)
+    freg = make_region(fixed_index, (f.shape[1], f.shape[0]))
+    mreg = make_region(moving_index, (m.shape[1], m.shape[0]))
+    dx = np.zeros(f.shape, np.float64)
+    dy = np.zeros(f.shape, np.float64)
+    rc = lib().orc_demons_f64(_ptr(f), ctypes.byref(freg), _ptr(m), ctypes.byref(mreg), int(iterations),
+                              float(max_step_length), _ptr(dx), _ptr(dy))
+    if rc != 0:
+        raise IndexError("demons: a warped index left the moving image (the reference panics)")
+    return dx, dy
+
+
+def demons_f32(fixed, moving, iterations, max_step_length=2.0, **kw):
+    """The VecPixel<f32, 2> field the reference returns: shape (h, w, 2)."""
+    dx, dy = demons(fixed, moving, iterations, max_step_length, **kw)
+    return np.stack([dx.astype(np.float32), dy.astype(np.float32)], axis=-1)
+
+
+def diffeomorphic_demons(fixed, moving, iterations, sigma_diff=1.0, spacing=None, **kw):
+    """DiffeomorphicDemonsRegistrationFilter::compute (registration_methods.rs:126-148):
+    the f32 demons field, each component smoothed by GaussianFilter { sigma_diff }."""
+    field = demons_f32(fixed, moving, iterations, **kw)
+    index = kw.get("fixed_index", (0, 0))
+    sx = gaussian_f32(field[..., 0], sigma_diff, spacing=spacing, index=index)
+    sy = gaussian_f32(field[..., 1], sigma_diff, spacing=spacing, index=index)
+    return np.stack([sx, sy], axis=-1)
+
+
+def n4(img, iterations=4, sigma=30.0, threshold=1e-3, spacing=None, index=(0, 0)):
+    """N4BiasFieldCorrectionFilter::generate_region (bias_correction.rs:45-83):
+    (the corrected f32 image, the number of iterations run)."""
+    a = np.ascontiguousarray(img, dtype=np.float32)
+    reg = make_region(index, (a.shape[1], a.shape[0]))
+    sp = np.ascontiguousarray(spacing if spacing is not None else [1.0, 1.0], dtype=np.float64)
+    out = np.empty_like(a)
+    run = lib().orc_n4_f32(_ptr(a), ctypes.byref(reg), _ptr(sp), int(iterations), float(sigma), float(threshold),
+                           _ptr(out))
+    if run < 0:
+        raise RuntimeError("oracle: n4 failed")
+    return out, run

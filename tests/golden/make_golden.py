@@ -21,6 +21,8 @@ and, for the rows beyond the Gaussian (case prefixes):
   recz_  ZeroCrossingBasedEdgeDetectionFilter               filters/edges.rs:1019-1052, 480-514
   ush_   UnsharpMaskFilter                                  filters/edges.rs:374-452
   cal_   SliceBySliceFilter, BSplineDownsampleFilter        filters/spatial.rs:1128-1166, 1284-1340
+  dem_   DemonsRegistrationFilter, DiffeomorphicDemons...   filters/registration_methods.rs:39-100, 126-148
+  n4_    N4BiasFieldCorrectionFilter                        filters/bias_correction.rs:45-83
 
 The oracle (oracle/gauss_oracle.c, oracle/oracle.py) is checked bit-exactly
 against these vectors by tests/test_oracle*.py, and the GPU path by the
@@ -281,6 +283,92 @@ def case(name, arr, sigma, spacing=None, requested=None, comps=1, kind="f32"):
     return {f"{name}__in": arr, f"{name}__out": out,
             f"{name}__meta": np.array([sigma] + list(spacing) + [comps] + list(ri) + list(rs),
                                       dtype=np.float64)}
+
+
+# ---- Demons and N4 (the Gaussian callers that iterate) ------------------------
+def rust_round(x):
+    """f64::round: half away from zero (exact: |x| - floor(|x|) is exact)."""
+    a = abs(x)
+    r = math.floor(a)
+    if a - r >= 0.5:
+        r += 1.0
+    return math.copysign(r, x)
+
+
+def rust_as_i64(v):
+    """`f64 as i64`: saturating, NaN -> 0."""
+    if v != v:
+        return 0
+    return int(max(min(v, 9.2233720368547758e18), -9.2233720368547758e18))
+
+
+def demons_compute(fixed, moving, iterations, max_step):
+    """DemonsRegistrationFilter::compute (registration_methods.rs:39-100);
+    images as (index, size, pixels) with 1-tuples of np.float32."""
+    (fidx, fsize, fdata), (midx, msize, mdata) = fixed, moving
+    w, h = fsize
+    ox, oy = fidx
+    M = 1 << 64
+
+    def flat_clamp(x, y):
+        xi = min(max(x - ox, 0), w - 1)
+        yi = min(max(y - oy, 0), h - 1)
+        return yi * w + xi
+
+    def get_moving(xi, yi):  # Image::get_pixel with wrapping usize offsets (image.rs:111-125)
+        off = (((xi - midx[0]) % M) + ((yi - midx[1]) % M) * msize[0]) % M
+        if off >= len(mdata):
+            raise IndexError("the reference panics: index out of bounds")
+        return mdata[off][0]
+
+    disp_x = [0.0] * (w * h)
+    disp_y = [0.0] * (w * h)
+    for _ in range(iterations):
+        new_x = list(disp_x)
+        new_y = list(disp_y)
+        for y in range(h):
+            for x in range(w):
+                i = y * w + x
+                wx = float(x) + disp_x[i]
+                wy = float(y) + disp_y[i]
+                xi = ox + rust_as_i64(rust_round(wx))
+                yi = oy + rust_as_i64(rust_round(wy))
+                m_val = float(get_moving(xi, yi))
+                f_val = float(fdata[i][0])
+                gx = (float(fdata[flat_clamp(ox + x + 1, oy + y)][0]) - float(fdata[flat_clamp(ox + x - 1, oy + y)][0])) * 0.5
+                gy = (float(fdata[flat_clamp(ox + x, oy + y + 1)][0]) - float(fdata[flat_clamp(ox + x, oy + y - 1)][0])) * 0.5
+                intensity_diff = f_val - m_val
+                denom = gx * gx + gy * gy + intensity_diff * intensity_diff + 1e-6
+                step = intensity_diff / denom
+                dx = step * gx
+                dy = step * gy
+                norm = math.sqrt(dx * dx + dy * dy)
+                scale = max_step / norm if norm > max_step else 1.0
+                new_x[i] = disp_x[i] + dx * scale
+                new_y[i] = disp_y[i] + dy * scale
+        disp_x, disp_y = new_x, new_y
+    return disp_x, disp_y
+
+
+def n4_region(img, spacing, iterations, sigma, threshold):
+    """N4BiasFieldCorrectionFilter::generate_region (bias_correction.rs:45-83)."""
+    idx, size, data = img
+    corrected = [max(float(p[0]), 1e-6) for p in data]
+    run = 0
+    for _ in range(iterations):
+        log_data = [math.log(v) for v in corrected]
+        log_img = (idx, size, [(np.float32(v),) for v in log_data])
+        smoothed = generate_region(log_img, spacing, sigma, list(idx), list(size))[2]
+        prev = corrected
+        corrected = [max(math.exp(l - float(s[0])), 1e-6) for l, s in zip(log_data, smoothed)]
+        run += 1
+        diff = 0.0
+        for a, b in zip(corrected, prev):
+            diff += abs(a - b)
+        diff /= float(len(corrected))
+        if diff < threshold:
+            break
+    return [np.float32(v) for v in corrected], run
 
 
 def main():
@@ -574,6 +662,38 @@ def main():
     for s, sp in [(1.5, 1.0), (2.0, 1.0), (1.5, 0.7), (1.5, 2.5), (0.5, 1.0), (8.0, 1.0)]:
         cases[f"kernel_{s}_{sp}"] = np.array(build_kernel(s / sp, kernel_radius(s, sp)),
                                              dtype=np.float64)
+    # Demons (forward field, f32 output) and its diffeomorphic smoothing
+    drng = np.random.default_rng(20261205)
+    # compact blobs well inside the frame: the field stays zero near the edges,
+    # so no warped index leaves the moving image (where the reference panics)
+    yy, xx = np.mgrid[0:14, 0:16].astype(np.float64)
+    fixed = np.maximum(0.0, 1.0 - np.hypot(xx - 7.5, yy - 6.5) / 3.0).astype(np.float32)
+    moving = np.maximum(0.0, 1.0 - np.hypot(xx - 8.0, yy - 7.0) / 3.0).astype(np.float32)
+    moving += np.where(moving > 0, drng.standard_normal(moving.shape) * 0.01, 0.0).astype(np.float32)
+    for name, iters, step, diffeo in [("blob_3", 3, 2.0, False), ("blob_6_step05", 6, 0.5, False),
+                                      ("blob_3_diffeo", 3, 2.0, True)]:
+        dxl, dyl = demons_compute(to_ref(fixed), to_ref(moving), iters, step)
+        field = np.stack([np.array(dxl, np.float64).astype(np.float32).reshape(fixed.shape),
+                          np.array(dyl, np.float64).astype(np.float32).reshape(fixed.shape)], axis=-1)
+        if diffeo:
+            sm = [from_ref(generate_region(to_ref(field[..., c]), [1.0, 1.0], 1.0, [0, 0], [16, 14]), 1, np.float32)
+                  for c in range(2)]
+            field = np.stack(sm, axis=-1)
+        cases[f"dem_{name}__fixed"] = fixed
+        cases[f"dem_{name}__moving"] = moving
+        cases[f"dem_{name}__out"] = field
+        cases[f"dem_{name}__meta"] = np.array([iters, step, 1.0 if diffeo else 0.0, 1.0], dtype=np.float64)
+    # N4: a smooth multiplicative bias over a two-level image
+    yy, xx = np.mgrid[0:6, 0:8].astype(np.float64)
+    bias = 1.0 + 0.3 * (xx / 7.0) + 0.2 * (yy / 5.0)
+    base = np.where((xx - 3.5) ** 2 + (yy - 2.5) ** 2 < 5.0, 100.0, 40.0)
+    n4img = (base * bias + drng.standard_normal(base.shape)).astype(np.float32)
+    for name, iters, sigma, spacing in [("default", 4, 30.0, [1.0, 1.0]), ("s2_aniso", 6, 2.0, [0.8, 1.2]),
+                                        ("s1_one", 1, 1.0, [1.0, 1.0])]:
+        out, run = n4_region(to_ref(n4img), spacing, iters, sigma, 1e-3)
+        cases[f"n4_{name}__in"] = n4img
+        cases[f"n4_{name}__out"] = np.array(out, np.float32).reshape(n4img.shape)
+        cases[f"n4_{name}__meta"] = np.array([iters, sigma, 1e-3, run] + spacing, dtype=np.float64)
     np.savez_compressed(os.path.join(HERE, "golden.npz"), **cases)
     print(f"wrote {len(cases)} arrays to golden.npz")
 
