@@ -72,8 +72,11 @@ def test_demons_offset_regions(gpu):
     """Fixed and moving regions at different indices: the warped index is read
     through the moving image's own region (registration_methods.rs:64-66)."""
     fixed, moving = smooth_pair(40, 50, 8, 4)
-    want = oracle.demons_f32(fixed, moving, 5, 1.0, fixed_index=(3, -2), moving_index=(2, -4))
-    got = run_demons(gpu, fixed, moving, 5, 1.0, fixed_index=(3, -2), moving_index=(2, -4))
+    big = np.zeros((44, 54), np.float32)  # the moving image's region (1, -4) + 54 x 44 covers the fixed one
+    big[2:42, 2:52] = moving
+    want = oracle.demons_f32(fixed, big, 5, 1.0, fixed_index=(3, -2), moving_index=(1, -4))
+    got = run_demons(gpu, fixed, big, 5, 1.0, fixed_index=(3, -2), moving_index=(1, -4))
+    assert np.abs(want).max() > 0.1
     assert bits_equal(got, want)
 
 
