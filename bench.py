@@ -845,6 +845,47 @@ def extra_workload(args):
                     "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                                  "frac": achieved / peak,
                                  "note": "SliceBySlice, algorithmic 8 B per voxel per call (the fused 2-D kernel over every slice)"}})
+    elif args.workload == "registration2d":
+        # the Gaussian callers that iterate: diffeomorphic demons (30 iterations,
+        # max step 0.5, sigma_diff 1) and N4 bias correction (4 iterations, sigma 30)
+        from itkg.workloads import biased_image, registration_pair
+        fixed, moving = registration_pair((512, 512), 0)
+        img = biased_image((512, 512), 0)
+        fd = itkg.DeviceImage.from_host(itkg.Image(fixed))
+        md = itkg.DeviceImage.from_host(itkg.Image(moving))
+        idv = itkg.DeviceImage.from_host(itkg.Image(img))
+        lines = {}
+        dem = itkg.DiffeomorphicDemonsRegistrationFilter(fd, md, 30, sigma_diff=1.0)
+        dem.max_step_length = 0.5
+        n4f = itkg.N4BiasFieldCorrectionFilter(idv, 4, 30.0, 1e-3)
+        for name, fn, ref in (
+                ("diffeomorphic_demons_512sq_30it", lambda: dem.compute(sp),
+                 lambda: oracle.diffeomorphic_demons(fixed, moving, 30, sigma_diff=1.0, max_step_length=0.5)),
+                ("n4_512sq_4it_sigma30", lambda: n4f.generate_region(None, sp),
+                 lambda: oracle.n4(img, 4, 30.0, 1e-3)[0])):
+            for _ in range(max(1, args.warmup)):
+                res = fn()
+            stream.synchronize()
+            n = max(1, args.steps // 20)
+            t0 = time.perf_counter()
+            for _ in range(n):
+                res = fn()
+            stream.synchronize()
+            dt = (time.perf_counter() - t0) / n
+            got = res.download()
+            tc = time.perf_counter()
+            want = ref()
+            cpu = time.perf_counter() - tc
+            lines[name] = {"ms_per_call": dt * 1e3, "pixels_per_s": 512 * 512 / dt, "kernel": itkg.last_kernel(),
+                           "normwise_rel_vs_oracle": _normwise(got, want),
+                           "bit_exact": bool(np.array_equal(got.view(np.uint32), want.view(np.uint32))),
+                           "cpu_port_ms_1_core": cpu * 1e3}
+        d = lines["diffeomorphic_demons_512sq_30it"]
+        out.update({"value": d["pixels_per_s"], "unit": "pixels/s", "ms_per_step": d["ms_per_call"], "dtype": "f64+f32",
+                    "config": {"workload": "DiffeomorphicDemonsRegistrationFilter 512^2 (30 iterations) and "
+                                           "N4BiasFieldCorrectionFilter 512^2 (4 iterations, sigma 30), synthetic",
+                               "variants": lines,
+                               "timing": "host clock around synchronous calls (each call reads a result back)"}})
     print(json.dumps(out))
     return 0
 
@@ -856,7 +897,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=["itkg", "reference"], default="itkg")
     ap.add_argument("--workload", choices=["fwd3d", "fwd2d", "ct16", "batch", "batch_vjp", "vjp_stack",
-                                           "mean3d", "binomial3d", "recursive3d", "unsharp3d", "callers3d"],
+                                           "mean3d", "binomial3d", "recursive3d", "unsharp3d", "callers3d",
+                                           "registration2d"],
                     default="fwd3d")
     ap.add_argument("--rounding", choices=["fma", "reference"], default="fma")
     ap.add_argument("--algo", choices=["auto", "fused", "per_axis", "two_pass", "one_trip"], default="auto")

@@ -12,9 +12,12 @@
 //      radius), the fused kernel against the per-axis passes on the class's
 //      first item and keeps the faster (the "fusion depth": 3 axes in one
 //      kernel, or one axis per kernel); its choices are cached process-wide;
-//   3. the chosen launches (plus the VJP items' passes) are captured on a
-//      private stream into a CUDA graph, instantiated once; itkg_batch_run
-//      replays it on the caller's stream.
+//   3. the chosen launches (plus the VJP items' passes) are captured into a
+//      CUDA graph, instantiated once; itkg_batch_run replays it on the
+//      caller's stream.  The items are independent, so they are spread over
+//      kLanes concurrent lanes (branches of the graph) by longest-processing-
+//      time-first on an estimate of their work (voxels x taps): small volumes
+//      and the tails of large ones then overlap instead of queueing.
 // Scratch the captured work needs comes from graph memory nodes
 // (stream-ordered allocation inside the capture).
 #include <cuda_runtime.h>
@@ -147,6 +150,18 @@ itkg_status choose_algorithm(const itkg_batch::Fwd& f, bool tune, cudaStream_t s
   return ITKG_SUCCESS;
 }
 
+constexpr int kLanes = 4;  // concurrent branches of the batch graph (8 measured slower)
+
+// Work estimate of one filter over an image: voxels x taps summed over the axes.
+double work_of(const itkg_image& im, const itkg_region& reg, double sigma) {
+  double vox = 1.0, taps = 0.0;
+  for (int d = 0; d < im.dim; ++d) {
+    vox *= (double)reg.size[d];
+    taps += 2.0 * (double)kernel_radius(sigma, im.spacing[d]) + 1.0;
+  }
+  return vox * (taps + 4.0) * (double)im.components;
+}
+
 itkg_status check_device_item(const itkg_image* im, const char* name) {
   ITKG_TRY(validate_image(im, name));
   ITKG_TRY(filter_components(im, name));
@@ -250,34 +265,91 @@ itkg_status itkg_batch_plan(itkg_batch* b, int32_t flags, void* stream) {
 
   if (!fused_geoms.empty()) ITKG_TRY(fused_multi_prepare(fused_geoms, fused_w, &b->fused, &b->plan_lines));
 
-  // 3. capture
-  cudaStream_t cap;
-  ITKG_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+  // 3. spread the work over kLanes lanes, longest first onto the least loaded
+  // lane; the multi-request fused launch counts as one job
+  struct Job {
+    double work;
+    int kind;  // 0 fused multi-request launch, 1 forward item, 2 VJP item
+    size_t i;
+  };
+  std::vector<Job> jobs;
+  if (b->fused) {
+    double wsum = 0.0;
+    for (size_t i = 0; i < b->fwd.size(); ++i)
+      if (std::find(per_item.begin(), per_item.end(), i) == per_item.end())
+        wsum += work_of(b->fwd[i].in, b->fwd[i].requested, b->fwd[i].prm.sigma);
+    jobs.push_back({wsum, 0, 0});
+  }
+  for (size_t i : per_item) jobs.push_back({work_of(b->fwd[i].in, b->fwd[i].requested, b->fwd[i].prm.sigma), 1, i});
+  for (size_t i = 0; i < b->vjp.size(); ++i)
+    jobs.push_back({3.0 * work_of(b->vjp[i].x, b->vjp[i].x.region, b->vjp[i].prm.sigma), 2, i});
+  std::stable_sort(jobs.begin(), jobs.end(), [](const Job& a, const Job& c) { return a.work > c.work; });
+  std::vector<int> lane_of(jobs.size());
+  {
+    double load[kLanes] = {0.0};
+    for (size_t j = 0; j < jobs.size(); ++j) {
+      const int l = (int)(std::min_element(load, load + kLanes) - load);
+      lane_of[j] = l;
+      load[l] += jobs[j].work;
+    }
+  }
+
+  // 4. capture: lane 0 is the capture stream, the others fork from it and join back
+  cudaStream_t lanes[kLanes] = {nullptr};
+  cudaEvent_t fork = nullptr, joins[kLanes] = {nullptr};
+  itkg_status st = ITKG_SUCCESS;
+  for (int l = 0; l < kLanes && st == ITKG_SUCCESS; ++l) {
+    st = cuda_status(cudaStreamCreateWithFlags(&lanes[l], cudaStreamNonBlocking), "cudaStreamCreate");
+    if (st == ITKG_SUCCESS) st = cuda_status(cudaEventCreateWithFlags(&joins[l], cudaEventDisableTiming), "event");
+  }
+  if (st == ITKG_SUCCESS) st = cuda_status(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming), "event");
+  auto release = [&]() {
+    for (int l = 0; l < kLanes; ++l) {
+      if (lanes[l]) cudaStreamDestroy(lanes[l]);
+      if (joins[l]) cudaEventDestroy(joins[l]);
+    }
+    if (fork) cudaEventDestroy(fork);
+  };
+  if (st != ITKG_SUCCESS) {
+    release();
+    return st;
+  }
+  cudaStream_t cap = lanes[0];
   const uint64_t launches0 = itkg_launch_counter();
   cudaError_t ce = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
   if (ce != cudaSuccess) {
-    cudaStreamDestroy(cap);
+    release();
     return cuda_status(ce, "cudaStreamBeginCapture");
   }
-  itkg_status st = ITKG_SUCCESS;
-  if (b->fused) st = fused_multi_launch(b->fused, cap);
-  for (size_t i : per_item) {
-    if (st != ITKG_SUCCESS) break;
-    itkg_batch::Fwd f = b->fwd[i];
-    // items without a multi-request kernel (2-D) still take their single fused kernel
-    f.prm.algorithm = (algo[i] == ITKG_ALGO_PER_AXIS || algo[i] == ITKG_ALGO_TWO_PASS) ? algo[i] : ITKG_ALGO_AUTO;
-    st = itkg_gaussian_generate_region(&f.in, &f.largest, &f.requested, &f.prm, &f.out, cap);
-    b->plan_lines.push_back(std::string("item ") + std::to_string(i) + ": " + itkg_last_kernel());
+  st = cuda_status(cudaEventRecord(fork, cap), "cudaEventRecord");
+  for (int l = 1; l < kLanes && st == ITKG_SUCCESS; ++l)
+    st = cuda_status(cudaStreamWaitEvent(lanes[l], fork, 0), "cudaStreamWaitEvent");
+  for (size_t j = 0; j < jobs.size() && st == ITKG_SUCCESS; ++j) {
+    cudaStream_t ls = lanes[lane_of[j]];
+    const std::string lane = " (lane " + std::to_string(lane_of[j]) + ")";
+    if (jobs[j].kind == 0) {
+      st = fused_multi_launch(b->fused, ls);
+      if (st == ITKG_SUCCESS) b->plan_lines.push_back("fused multi-request launches" + lane);
+    } else if (jobs[j].kind == 1) {
+      const size_t i = jobs[j].i;
+      itkg_batch::Fwd f = b->fwd[i];
+      // items without a multi-request kernel (2-D) still take their single fused kernel
+      f.prm.algorithm = (algo[i] == ITKG_ALGO_PER_AXIS || algo[i] == ITKG_ALGO_TWO_PASS) ? algo[i] : ITKG_ALGO_AUTO;
+      st = itkg_gaussian_generate_region(&f.in, &f.largest, &f.requested, &f.prm, &f.out, ls);
+      b->plan_lines.push_back(std::string("item ") + std::to_string(i) + ": " + itkg_last_kernel() + lane);
+    } else {
+      itkg_batch::Vjp& v = b->vjp[jobs[j].i];
+      st = itkg_gaussian_vjp(&v.x, &v.ybar, &v.prm, v.has_xbar ? &v.xbar : nullptr, v.sigma_bar, v.flags, ls);
+      b->plan_lines.push_back(std::string("vjp ") + std::to_string(jobs[j].i) + ": " + itkg_last_kernel() + lane);
+    }
   }
-  for (size_t i = 0; i < b->vjp.size() && st == ITKG_SUCCESS; ++i) {
-    itkg_batch::Vjp& v = b->vjp[i];
-    st = itkg_gaussian_vjp(&v.x, &v.ybar, &v.prm, v.has_xbar ? &v.xbar : nullptr, v.sigma_bar,
-                           v.flags, cap);
-    b->plan_lines.push_back(std::string("vjp ") + std::to_string(i) + ": " + itkg_last_kernel());
+  for (int l = 1; l < kLanes; ++l) {
+    // join every lane back (also after a failure, so that the capture ends cleanly)
+    if (cudaEventRecord(joins[l], lanes[l]) == cudaSuccess) cudaStreamWaitEvent(cap, joins[l], 0);
   }
   cudaGraph_t graph = nullptr;
   ce = cudaStreamEndCapture(cap, &graph);
-  cudaStreamDestroy(cap);
+  release();
   if (st != ITKG_SUCCESS) {
     if (graph) cudaGraphDestroy(graph);
     return st;

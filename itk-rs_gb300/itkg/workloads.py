@@ -59,3 +59,36 @@ def ct_volume(shape=(384, 512, 512), seed=0, n_ellipsoids=12):
 def uniform_image(shape, seed=0):
     """i.i.d. U[0, 1) f32 pixels from `seed`."""
     return np.random.default_rng(seed).random(shape, dtype=np.float32)
+
+
+def registration_pair(shape=(512, 512), seed=0, margin=24, nblobs=40, shift=(1.5, -1.0)):
+    """Fixed / moving Image<f32,2> for the demons registrations: `nblobs`
+    seeded cones (radius U[6, 14]) and the same cones shifted by `shift`
+    pixels, zero within `margin` of the edges (there the field stays zero, so
+    no warped index leaves the image, where the reference panics)."""
+    rng = np.random.default_rng(seed)
+    h, w = shape
+    yy, xx = np.mgrid[0:h, 0:w].astype(np.float64)
+    f = np.zeros(shape)
+    m = np.zeros(shape)
+    for _ in range(nblobs):
+        r = rng.uniform(6, 14)
+        cy, cx = rng.uniform(margin + r, h - margin - r), rng.uniform(margin + r, w - margin - r)
+        f += np.maximum(0.0, 1.0 - np.hypot(xx - cx, yy - cy) / r)
+        m += np.maximum(0.0, 1.0 - np.hypot(xx - cx - shift[0], yy - cy - shift[1]) / r)
+    return f.astype(np.float32), m.astype(np.float32)
+
+
+def biased_image(shape=(512, 512), seed=0):
+    """Image<f32,2> for the bias-field correction: a two-level seeded phantom
+    (ellipses of 120 on 60) times a smooth multiplicative bias, plus N(0, 2)."""
+    rng = np.random.default_rng(seed)
+    h, w = shape
+    yy, xx = np.mgrid[0:h, 0:w].astype(np.float64)
+    bias = 1.0 + 0.4 * (xx / w) - 0.2 * (yy / h) + 0.1 * np.sin(xx / 40.0)
+    base = np.full(shape, 60.0)
+    for _ in range(5):
+        cy, cx = rng.uniform(0.2, 0.8) * h, rng.uniform(0.2, 0.8) * w
+        ay, ax = rng.uniform(0.05, 0.25) * h, rng.uniform(0.05, 0.25) * w
+        base[((yy - cy) / ay) ** 2 + ((xx - cx) / ax) ** 2 < 1.0] = 120.0
+    return (base * bias + rng.normal(0, 2, shape)).astype(np.float32)
