@@ -256,6 +256,28 @@ __global__ void __launch_bounds__(256, 2)
       const int sl = s_a + i;
       const float* const xcur = xbuf0 + (i & 1) * NXB * XBUF;
       const float* const yw = ywin0 + (i & 1) * NXB * XBUF;
+      // dual-dot: this slice's U and U' at the thread's outputs, loaded before
+      // the y pass so that their latency overlaps its arithmetic
+      const bool c0ok = col <= a.hi[0], c1ok = col + 1 <= a.hi[0];
+      float pu[MY][2], pu2[MY][2];
+      if constexpr (MODE == kDualDot) {
+#pragma unroll
+        for (int m = 0; m < MY; ++m) {
+          const int y = ty0 + grp * MY + m;
+          pu[m][0] = pu[m][1] = pu2[m][0] = pu2[m][1] = 0.0f;
+          if (y > a.hi[1] || !c0ok) continue;
+          const int64_t off = (int64_t)(col - a.lo[0]) * a.u_pitch[0] + (int64_t)(y - a.lo[1]) * a.u_pitch[1] +
+                              (int64_t)(sl - a.lo[2]) * a.u_pitch[2];
+          const float* const ud = reinterpret_cast<const float*>(a.u + off);
+          const float* const uv = reinterpret_cast<const float*>(a.u2 + off);
+          pu[m][0] = __ldg(ud);
+          pu2[m][0] = __ldg(uv);
+          if (c1ok) {
+            pu[m][1] = __ldg(ud + 1);
+            pu2[m][1] = __ldg(uv + 1);
+          }
+        }
+      }
       f2_t yv[MY], yd[MY];
       {
         f2_t win[MY + 2 * R];
@@ -332,7 +354,6 @@ __global__ void __launch_bounds__(256, 2)
         }
       }
       // outputs: rows ty0 + grp*MY + m, columns col, col + 1 (inside the image only)
-      const bool c0ok = col <= a.hi[0], c1ok = col + 1 <= a.hi[0];
 #pragma unroll
       for (int m = 0; m < MY; ++m) {
         const int y = ty0 + grp * MY + m;
@@ -353,12 +374,8 @@ __global__ void __launch_bounds__(256, 2)
         } else {
           float d0, d1;
           unpack2(yd[m], d0, d1);
-          const int64_t off = (int64_t)(col - a.lo[0]) * a.u_pitch[0] + (int64_t)(y - a.lo[1]) * a.u_pitch[1] +
-                              (int64_t)(sl - a.lo[2]) * a.u_pitch[2];
-          const float* const ud = reinterpret_cast<const float*>(a.u + off);
-          const float* const uv = reinterpret_cast<const float*>(a.u2 + off);
-          float s = fmaf(v0, uv[0], d0 * ud[0]);
-          if (c1ok) s = fmaf(v1, uv[1], fmaf(d1, ud[1], s));
+          float s = fmaf(v0, pu2[m][0], d0 * pu[m][0]);
+          if (c1ok) s = fmaf(v1, pu2[m][1], fmaf(d1, pu[m][1], s));
           dot += (double)s;
         }
       }
