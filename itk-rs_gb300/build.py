@@ -30,9 +30,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-std=c++17", "-O3", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
           "-I", os.path.join(ROOT, "include"), "-I", CSRC]
 # -fmad=false: ptxas must not contract a separate multiply and add into an FMA
-# (the reference-rounding kernels rely on two roundings per tap, including the
-# packed mul.rn.f32x2 / add.rn.f32x2 pairs); FMA-rounding code uses explicit
-# fma instructions, which the flag does not touch.
+# (the reference-rounding kernels rely on two roundings per tap); FMA-rounding
+# code uses explicit fma instructions, which the flag does not touch.
 CUFLAGS = ARCH + ["-lineinfo", "--expt-relaxed-constexpr", "-fmad=false", "-Xptxas", "-warn-spills"]
 
 

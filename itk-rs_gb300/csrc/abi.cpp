@@ -340,6 +340,7 @@ static void make_fused_geom(const itkg_image& in, const itkg_region& largest,
     g.in_dtype = in.dtype;
     g.out_dtype = out.dtype;
     g.rounding = prm.rounding;
+    g.u8pix = prm.arithmetic == ITKG_ARITH_PIXEL_U8 ? 1 : 0;
   }
 }
 
@@ -418,6 +419,25 @@ static itkg_status generate_device(const itkg_image& in, const itkg_region& larg
     return run_per_axis(in, largest, requested, prm, plan, out, s);
   }
   if (plan.reps > 1) return run_rounds(in, largest, requested, prm, plan, out, s);
+  // u8 pixel arithmetic: the two-pass kernels when every tap has an f32
+  // constant that reproduces its u8 products, else the per-axis passes
+  if (prm.arithmetic == ITKG_ARITH_PIXEL_U8 && D == 3 &&
+      (prm.algorithm == ITKG_ALGO_AUTO || prm.algorithm == ITKG_ALGO_TWO_PASS)) {
+    FusedGeom g;
+    make_fused_geom(in, largest, requested, prm, plan, out, &g);
+    std::vector<float> c[kMaxDim];
+    bool ok = true;
+    for (int d = 0; d < D && ok; ++d) {
+      c[d].resize(plan.w64[d].size());
+      ok = u8_pixel_tap_consts(plan.w64[d].data(), (int)plan.w64[d].size(), c[d].data());
+    }
+    if (ok) {
+      const float* w[kMaxDim] = {c[0].data(), c[1].data(), c[2].data()};
+      if (launch_two_pass(g, w, s, /*dry_run=*/true) == ITKG_SUCCESS) return launch_two_pass(g, w, s, false);
+    }
+    if (prm.algorithm == ITKG_ALGO_TWO_PASS)
+      return set_error(ITKG_ERROR_UNSUPPORTED, "the two-pass kernels do not cover this geometry");
+  }
   if (prm.arithmetic != ITKG_ARITH_PIXEL_U8 && prm.algorithm != ITKG_ALGO_PER_AXIS) {
     FusedGeom g;
     make_fused_geom(in, largest, requested, prm, plan, out, &g);

@@ -278,6 +278,7 @@ itkg_status encode_input_map(const FusedGeom& g, int box_w, int box_h, void* map
 
 itkg_status launch_fused(const FusedGeom& g, const float* const w[kMaxDim], void* stream,
                          bool dry_run) {
+  if (g.u8pix) return ITKG_ERROR_UNSUPPORTED;  // u8 pixel arithmetic: two-pass or per-axis only
   if (g.dim == 2) return launch_fused2d(g, w, stream, dry_run);
   if (!geometry_ok(g)) return ITKG_ERROR_UNSUPPORTED;
   const Entry* e = find_entry(g.radius[0], g.radius[1], g.radius[2], g.in_dtype);

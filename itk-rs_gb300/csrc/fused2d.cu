@@ -327,6 +327,7 @@ bool fits32(int64_t v) { return v >= INT_MIN && v <= INT_MAX; }
 itkg_status launch_fused2d(const FusedGeom& g, const float* const w[kMaxDim], void* stream, bool dry_run) {
   // 2-D, or 3-D with the 1-tap kernel [1] on z (each slice filtered alone)
   const bool slices = g.dim == 3 && g.radius[2] == 0 && w[2] && w[2][0] == 1.0f;
+  if (g.u8pix) return ITKG_ERROR_UNSUPPORTED;
   if ((g.dim != 2 && !slices) || g.in_dtype != ITKG_F32 || g.out_dtype == ITKG_I16) return ITKG_ERROR_UNSUPPORTED;
   if (g.radius[0] != g.radius[1] || g.radius[0] < 1) return ITKG_ERROR_UNSUPPORTED;
   const Entry2* e = nullptr;

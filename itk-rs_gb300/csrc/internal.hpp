@@ -97,8 +97,15 @@ struct FusedGeom {
   int32_t in_dtype;
   int32_t out_dtype;
   int32_t rounding;
-  int32_t pad_;
+  int32_t u8pix;  // u8 pixel arithmetic (NumericPixel for u8); only the two-pass kernels take it
 };
+
+// two_pass.cu: the f32 constants c[k] of the u8 pixel-arithmetic kernels for
+// the f64 taps w[0 .. K): for every v in 0 .. 255, floor(f32 fma(v, c[k], 0.5))
+// must equal round(v as f64 * w[k]).clamp(0, 255) (src/pixel.rs:430-435).
+// Tries the nearest f32 first, then its neighbours; false if no f32 within 64
+// ulps qualifies for some tap (the caller then runs the per-axis passes).
+bool u8_pixel_tap_consts(const double* w, int K, float* c);
 
 // fused.cu: returns ITKG_ERROR_UNSUPPORTED (without setting an error) when no
 // fused kernel covers the geometry; the caller then uses the per-axis path.

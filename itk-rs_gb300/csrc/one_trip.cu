@@ -49,7 +49,8 @@ bool fits_i32(int64_t v) { return v >= INT_MIN && v <= INT_MAX; }
 
 itkg_status launch_one_trip(const FusedGeom& g, const float* const w[kMaxDim], void* stream, bool dry_run) {
   using namespace onetrip;
-  if (g.dim != 3 || g.comps != 1 || g.in_dtype != ITKG_F32 || g.out_dtype == ITKG_I16) return ITKG_ERROR_UNSUPPORTED;
+  if (g.dim != 3 || g.comps != 1 || g.in_dtype != ITKG_F32 || g.out_dtype == ITKG_I16 || g.u8pix)
+    return ITKG_ERROR_UNSUPPORTED;
   const int R = g.radius[0], RZ = g.radius[2];
   if (g.radius[1] != R || R < 1 || R > kMaxR || RZ < 1 || RZ > kMaxRZ) return ITKG_ERROR_UNSUPPORTED;
   const bool ref = g.rounding == ITKG_ROUND_REFERENCE;

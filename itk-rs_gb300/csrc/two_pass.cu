@@ -1,9 +1,10 @@
 // Host side of the two-kernel 3-D forward (kernels in two_pass.cuh): kernel
 // choice, the intermediate's layout and its z-chunking, and the launches.
-// This file holds the f32 x-y pass table and every z-pass instantiation; the
-// i16 / u8 / bf16 / f16 x-y pass tables are in two_pass_in.cu.
+// This file holds the f32 x-y pass table; the i16 / u8 / bf16 / f16 x-y pass
+// tables are in two_pass_in.cu, the z-pass instantiations in two_pass_z*.cu.
 #include <algorithm>
 #include <climits>
+#include <cmath>
 
 #include "two_pass.cuh"
 
@@ -11,25 +12,20 @@ namespace itkg {
 namespace twopass {
 namespace {
 const XYEntry kXYF32[] = ITKG_XY_TABLE(float, ITKG_F32);
-
-struct ZEntry {
-  int r;
-  ZFn fn[2][2];  // [ref][vec]
-};
-template <int R>
-ZEntry make_z() {
-  return ZEntry{R, {{k_z_pass<R, false, false>, k_z_pass<R, false, true>},
-                    {k_z_pass<R, true, false>, k_z_pass<R, true, true>}}};
-}
-const ZEntry kZ[] = {make_z<1>(), make_z<2>(), make_z<3>(),  make_z<4>(),  make_z<5>(),  make_z<6>(),
-                     make_z<7>(), make_z<8>(), make_z<9>(),  make_z<10>(), make_z<11>(), make_z<12>()};
 }  // namespace
 
-ZFn z_fn(int r, bool ref, bool vec, bool ush) {
+ZFn z_fn(int r, bool ref, int store, bool ush) {
   if (ush) return z_ush_fn(r, ref);
-  for (const ZEntry& z : kZ)
-    if (z.r == r) return z.fn[ref ? 1 : 0][vec ? 1 : 0];
-  return nullptr;
+  if (r < 1 || r > kMaxR) return nullptr;
+  const ZFn* row = nullptr;
+  switch (store) {
+    case kStoreAny: row = ref ? z_row_ref_any() : z_row_fma_any(); break;
+    case kStoreF32Quad: row = ref ? z_row_ref_f32q() : z_row_fma_f32q(); break;
+    case kStoreBF16Quad: row = ref ? z_row_ref_bf16q() : z_row_fma_bf16q(); break;
+    case kStoreF16Quad: row = ref ? z_row_ref_f16q() : z_row_fma_f16q(); break;
+    default: return nullptr;
+  }
+  return row[r - 1];
 }
 
 const XYEntry* xy_entries_f32(int* n) {
@@ -42,6 +38,29 @@ namespace {
 
 using twopass::XYArgs;
 using twopass::XYEntry;
+
+// floor(f32 fma(v, c, 0.5)) for v in 0 .. 255, as the u8 pixel-arithmetic
+// kernels compute it: v * c is exact in f64 (8 + 24 significant bits) and so
+// is the sum with 0.5 when c >= 2^-21 (at most 32 - log2(c) bits); the one
+// rounding to f32 is then the conversion.  Below 2^-21, v * c < 2^-13 and the
+// f32 result is below 1 whatever its rounding: floor 0.
+int u8p_device_value(int v, float c) {
+  if (!(c >= 0x1p-21f)) {
+    if (c >= 0.0f) return 0;
+    return INT_MIN;  // negative constants are never chosen
+  }
+  const float s = (float)((double)v * (double)c + 0.5);
+  return (int)std::floor(s);
+}
+
+bool u8p_tap_ok(double w, float c) {
+  for (int v = 0; v < 256; ++v) {
+    double r = std::round((double)v * w);  // f64 product, half away from zero
+    r = r < 0.0 ? 0.0 : (r > 255.0 ? 255.0 : r);
+    if (u8p_device_value(v, c) != (int)r) return false;
+  }
+  return true;
+}
 using twopass::ZArgs;
 
 // L2 share the intermediate may take; longer z ranges are processed in chunks.
@@ -119,19 +138,47 @@ int z_split(int64_t qblocks, int64_t nz, int rz, int64_t grid, int32_t* split) {
   return (int)cover(lo, split);
 }
 
+bool u8_pixel_tap_consts(const double* w, int K, float* c) {
+  for (int k = 0; k < K; ++k) {
+    const float c0 = (float)w[k];
+    bool found = u8p_tap_ok(w[k], c0);
+    float best = c0;
+    float up = c0, dn = c0;
+    for (int d = 1; d <= 64 && !found; ++d) {
+      up = std::nextafter(up, 2.0f);
+      dn = std::nextafter(dn, -1.0f);
+      if (up >= 0.0f && u8p_tap_ok(w[k], up)) found = true, best = up;
+      else if (dn >= 0.0f && u8p_tap_ok(w[k], dn)) found = true, best = dn;
+    }
+    if (!found) return false;
+    c[k] = best;
+  }
+  return true;
+}
+
 itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], void* stream, bool dry_run,
                             const UnsharpConsts* ush) {
+  const bool u8p = g.u8pix != 0;
   if (g.dim != 3 || g.comps != 1 || g.out_dtype == ITKG_I16) return ITKG_ERROR_UNSUPPORTED;
   if (g.radius[0] != g.radius[1] || g.radius[2] < 1 || g.radius[2] > twopass::kMaxR)
     return ITKG_ERROR_UNSUPPORTED;
-  const XYEntry* e = find_xy(g.radius[0], g.in_dtype);
+  if (u8p && (g.in_dtype != ITKG_U8 || g.out_dtype != ITKG_U8 || ush)) return ITKG_ERROR_UNSUPPORTED;
+  const XYEntry* e = nullptr;
+  if (u8p) {
+    int n = 0;
+    const XYEntry* t = twopass::xy_entries_u8p(&n);
+    for (int i = 0; i < n; ++i)
+      if (t[i].r == g.radius[0]) e = &t[i];
+  } else {
+    e = find_xy(g.radius[0], g.in_dtype);
+  }
   if (!e) return ITKG_ERROR_UNSUPPORTED;
   const int esz = dtype_size(g.in_dtype);
   if (g.src_pitch[0] != esz) return ITKG_ERROR_UNSUPPORTED;
   // FMA rounding reads zeros outside the input buffer as the halo and adds the
   // clamped taps back at the image's edges: the buffer must lie inside the
   // image on x and y.
-  if (g.rounding != ITKG_ROUND_REFERENCE)
+  if (g.rounding != ITKG_ROUND_REFERENCE && !u8p)
     for (int d = 0; d < 2; ++d)
       if (g.src_origin[d] < g.lo[d] || g.src_origin[d] + g.src_size[d] - 1 > g.hi[d]) return ITKG_ERROR_UNSUPPORTED;
   // TMA: 16-byte base and pitches, 16-byte aligned first tile column
@@ -147,11 +194,25 @@ itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], v
   if (!fits_i32(nx) || !fits_i32(ny)) return ITKG_ERROR_UNSUPPORTED;
   const int64_t ntx = (nx + twopass::kTileX - 1) / twopass::kTileX;
   const int64_t nty = (ny + e->ty - 1) / e->ty;
-  // 16-byte f32 stores when every quad of the output is full and aligned
+  // one store per quad (16 bytes of f32, 8 bytes of bf16 / f16) when every
+  // quad of the output is full and aligned
   char* const dst0 = static_cast<char*>(g.dst) + (g.req_index[0] - g.dst_origin[0]) * g.dst_pitch[0] +
                      (g.req_index[1] - g.dst_origin[1]) * g.dst_pitch[1];
-  const bool vec = g.out_dtype == ITKG_F32 && g.dst_pitch[0] == 4 && ((uintptr_t)dst0 & 15) == 0 &&
-                   (g.dst_pitch[1] & 15) == 0 && (g.dst_pitch[2] & 15) == 0 && nx % 4 == 0;
+  int store = twopass::kStoreAny;
+  if (u8p) {
+    if (g.dst_pitch[0] == 1 && ((uintptr_t)dst0 & 3) == 0 && g.dst_pitch[1] % 4 == 0 && g.dst_pitch[2] % 4 == 0 &&
+        nx % 4 == 0)
+      store = twopass::kStoreU8Quad;
+  } else {
+    const int osz = g.out_dtype == ITKG_F32 ? 4 : (g.out_dtype == ITKG_BF16 || g.out_dtype == ITKG_F16) ? 2 : 0;
+    const int64_t qa = 4 * osz;  // bytes per quad
+    if (osz && g.dst_pitch[0] == osz && ((uintptr_t)dst0 % qa) == 0 && g.dst_pitch[1] % qa == 0 &&
+        g.dst_pitch[2] % qa == 0 && nx % 4 == 0)
+      store = g.out_dtype == ITKG_F32    ? twopass::kStoreF32Quad
+              : g.out_dtype == ITKG_BF16 ? twopass::kStoreBF16Quad
+                                         : twopass::kStoreF16Quad;
+  }
+  const bool vec = store == twopass::kStoreF32Quad;
   // the unsharp store reads the input's quads at the output's positions (the
   // TMA checks above make them 16-byte aligned for f32 input)
   const char* const src0 = static_cast<const char*>(g.src) + (g.req_index[0] - g.src_origin[0]) * g.src_pitch[0] +
@@ -163,7 +224,7 @@ itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], v
   if (dry_run) return ITKG_SUCCESS;
 
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  const bool ref = g.rounding == ITKG_ROUND_REFERENCE;
+  const bool ref = u8p || g.rounding == ITKG_ROUND_REFERENCE;  // u8 pixel arithmetic clamps like the reference rounding
   const int rz = g.radius[2];
   // clamp bounds on z: the image within the input buffer
   const int64_t zlo = std::max<int64_t>(g.lo[2], g.src_origin[2]);
@@ -192,7 +253,9 @@ itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], v
   if (st == ITKG_SUCCESS) st = device_fault_word(&xa.fault);
   xa.wait_limit = wait_limit_cycles();
   int res_xy = 0, res_z = 0;
-  const twopass::ZFn zfn = twopass::z_fn(rz, ref, vec, ush != nullptr);
+  const twopass::ZFn zfn =
+      u8p ? (store == twopass::kStoreU8Quad ? twopass::z_row_u8p_u8q() : twopass::z_row_u8p_any())[rz - 1]
+          : twopass::z_fn(rz, ref, store, ush != nullptr);
   const twopass::XYFn xyfn = e->fn[ref ? 1 : 0];
   if (st == ITKG_SUCCESS) st = max_resident_ctas(reinterpret_cast<const void*>(xyfn), e->smem, e->nt, &res_xy);
   if (st == ITKG_SUCCESS)
@@ -262,7 +325,7 @@ itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], v
   za.dst_pitch[0] = g.dst_pitch[0];
   za.dst_pitch[1] = g.dst_pitch[1];
   za.dst_pitch[2] = g.dst_pitch[2];
-  za.vec_store = vec ? 1 : 0;
+  za.vec_store = store;
   if (ush) {
     za.ush = *ush;
     za.ush_pitch[0] = g.src_pitch[0];
@@ -297,7 +360,7 @@ itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], v
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     cudaError_t err = cudaLaunchKernelEx(&cfg, xyfn, map, xa);
-    note_launch(xy_name(g.in_dtype, ref));
+    note_launch(u8p ? "xy_pass_u8_pixel" : xy_name(g.in_dtype, ref));
     if (err == cudaSuccess) err = cudaGetLastError();
     if (err != cudaSuccess) {
       st = set_error(ITKG_ERROR_CUDA, "xy pass launch: %s", cudaGetErrorString(err));
@@ -317,7 +380,9 @@ itkg_status launch_two_pass(const FusedGeom& g, const float* const w[kMaxDim], v
     cfg.blockDim = dim3(256);
     cfg.dynamicSmemBytes = z_smem(rz, ush != nullptr);
     err = cudaLaunchKernelEx(&cfg, zfn, za);
-    note_launch(ush ? (ref ? "z_pass_unsharp_ref" : "z_pass_unsharp_fma") : (ref ? "z_pass_f32_ref" : "z_pass_f32_fma"));
+    note_launch(u8p ? "z_pass_u8_pixel"
+                    : ush ? (ref ? "z_pass_unsharp_ref" : "z_pass_unsharp_fma")
+                          : (ref ? "z_pass_f32_ref" : "z_pass_f32_fma"));
     if (err == cudaSuccess) err = cudaGetLastError();
     if (err != cudaSuccess) st = set_error(ITKG_ERROR_CUDA, "z pass launch: %s", cudaGetErrorString(err));
   }

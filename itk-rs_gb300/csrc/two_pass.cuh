@@ -32,6 +32,8 @@
 // reference pass by pass.  FMA rounding: packed fma.rn.f32x2.
 #pragma once
 
+#include <type_traits>
+
 #include "fused_kernel.cuh"
 #include "unsharp.cuh"
 
@@ -51,6 +53,8 @@ constexpr int kMaxK = 2 * kMaxR + 1;
 // x-y tile: kTileX columns and 128 rows (64 for R > 8); T is stored
 // tile-major: [slice][tile][tile rows][kTileX columns]
 constexpr int kTileX = 32;
+// z-pass store modes (k_z_pass's ST)
+constexpr int kStoreAny = 0, kStoreF32Quad = 1, kStoreBF16Quad = 2, kStoreF16Quad = 3, kStoreU8Quad = 4;
 constexpr int kMaxZSplit = 1024;  // z-pass CTAs with a per-CTA unit range
 constexpr int kTileY = 128;  // the tallest tile
 
@@ -98,7 +102,7 @@ struct ZArgs {
   char* dst;               // output voxel (x0, y0, z0)
   int64_t dst_pitch[3];    // bytes
   int32_t out_dtype;
-  int32_t vec_store;       // 1: the 16-byte store variant (see k_z_pass)
+  int32_t vec_store;       // store mode of the launched variant (kStore*, see k_z_pass)
   const char* ush_src;     // UnsharpMaskFilter variant: input voxel (x0, y0, z0)
   int64_t ush_pitch[3];    // bytes
   UnsharpConsts ush;
@@ -193,10 +197,31 @@ __device__ __forceinline__ float ld1(const __nv_bfloat16* p) { return __bfloat16
 __device__ __forceinline__ float ld1(const __half* p) { return __half2float(*p); }
 
 // ---------------------------------------------------------------------------
+// u8 pixel arithmetic (GaussianFilter<Image<u8>>, NumericPixel for u8): each
+// tap adds round(v as f64 * w).clamp(0, 255) as u8 to a u8 accumulator with a
+// wrapping add, so a pass's output is the sum of its taps' values mod 256, in
+// any order.  A tap's value is computed in f32: floor(fma(v, c, 0.5)) with a
+// per-tap constant c that the host has checked against the f64 definition for
+// all 256 values of v (an f32 near w; see u8_pixel_tap_consts).  Adding 2^23
+// rounding down leaves floor(.) in the low mantissa bits of 2^23 + floor(.), a
+// bit pattern whose low byte is the tap's value, so the taps' bit patterns are
+// summed as integers and the sum's low byte is the pass's output.
+__device__ __forceinline__ uint32_t u8p_tap(float v, float c) {
+  return __float_as_uint(__fadd_rd(__fmaf_rn(v, c, 0.5f), 8388608.0f));
+}
+// the low byte of an accumulated sum, as an exact f32 (0 .. 255)
+__device__ __forceinline__ float u8p_value(uint32_t acc) {
+  return __fsub_rn(__uint_as_float(0x4B000000u | (acc & 255u)), 8388608.0f);
+}
+
+// ---------------------------------------------------------------------------
 // xy pass
-template <int R, bool REF, typename Tin>
+// U8P (with REF and u8 input): u8 pixel arithmetic; a.wx / a.wy hold the
+// per-tap constants c, and T holds each y-pass output byte as an f32.
+template <int R, bool REF, typename Tin, bool U8P = false>
 __global__ void __launch_bounds__(288, CfgXY<R, Tin>::MINB)
     k_xy_pass(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ XYArgs a) {
+  static_assert(!U8P || (REF && std::is_same<Tin, uint8_t>::value), "u8 pixel arithmetic: clamped u8 tiles");
   using C = CfgXY<R, Tin>;
   constexpr int K = C::K, TX = C::TX, TY = C::TY, MY = C::MY, MX = C::MX, BW = C::BW, IH = C::IH,
                 XA = C::XA, S = C::S, WIN = C::WIN, WB = C::WB, OFF = C::OFF, NT = C::NT, SEGS = C::SEGS,
@@ -268,10 +293,17 @@ __global__ void __launch_bounds__(288, CfgXY<R, Tin>::MINB)
       }
 #pragma unroll
       for (int m = 0; m < MX; ++m) {
-        float ax = 0.0f;
+        if constexpr (U8P) {
+          uint32_t ia = 0;
 #pragma unroll
-        for (int k = 0; k < K; ++k) ax = tap<true>(ax, v[m + k + OFF], a.wx[k]);
-        o[m] = ax;
+          for (int k = 0; k < K; ++k) ia += u8p_tap(v[m + k + OFF], a.wx[k]);
+          o[m] = u8p_value(ia);
+        } else {
+          float ax = 0.0f;
+#pragma unroll
+          for (int k = 0; k < K; ++k) ax = tap<true>(ax, v[m + k + OFF], a.wx[k]);
+          o[m] = ax;
+        }
       }
     } else {
       (void)yedge, (void)rlo, (void)rhi;
@@ -378,7 +410,17 @@ __global__ void __launch_bounds__(288, CfgXY<R, Tin>::MINB)
         f2_t yv[MY];
 #pragma unroll
         for (int m = 0; m < MY; ++m) {
-          if constexpr (REF) {
+          if constexpr (U8P) {
+            uint32_t i0 = 0, i1 = 0;
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+              float v0, v1;
+              unpack2(win[m + k], v0, v1);
+              i0 += u8p_tap(v0, a.wy[k]);
+              i1 += u8p_tap(v1, a.wy[k]);
+            }
+            yv[m] = pack2(u8p_value(i0), u8p_value(i1));
+          } else if constexpr (REF) {
             float y0 = 0.0f, y1 = 0.0f;
 #pragma unroll
             for (int k = 0; k < K; ++k) {
@@ -456,16 +498,24 @@ timeout:
 
 // ---------------------------------------------------------------------------
 // z pass
-// VEC: f32 output whose rows allow 16-byte stores and whose width is a
-// multiple of 4 (every quad full).  USH (with VEC): store UnsharpMaskFilter's
+// ST: how a completed quad is stored.  kStoreAny: element by element, any
+// output type and width.  kStoreF32Quad: one 16-byte store (f32 output whose
+// rows allow it and whose width is a multiple of 4, every quad full).
+// kStoreBF16Quad / kStoreF16Quad: the same for bf16 / f16 output, one 8-byte
+// store of the four rounded values.  kStoreU8Quad (U8P only): one 4-byte store.
+// U8P (with REF): u8 pixel arithmetic over T's bytes (see u8p_tap), a.wz
+// holding the per-tap constants; the output is u8.
+// USH (with kStoreF32Quad): store UnsharpMaskFilter's
 // point-wise step of the input voxel and the blur instead of the blur --
 // unsharp_cheap_f32 in FMA rounding, the exact f32 test (unsharp_quad_exact,
 // one out-of-line copy) in reference rounding; the input quads travel in a
 // second cp.async ring beside the T quads (the input quad of output z rides
 // with T slice z + RZ).
-template <int RZ, bool REF, bool VEC, bool USH = false>
+template <int RZ, bool REF, int ST, bool USH = false, bool U8P = false>
 __global__ void __launch_bounds__(256, RZ <= 8 ? 2 : 1) k_z_pass(const __grid_constant__ ZArgs a) {
-  static_assert(!USH || VEC, "the unsharp variant stores whole quads");
+  static_assert(!USH || ST == kStoreF32Quad, "the unsharp variant stores whole f32 quads");
+  static_assert(!U8P || (REF && !USH && (ST == kStoreAny || ST == kStoreU8Quad)), "u8 pixel arithmetic stores u8");
+  static_assert(ST != kStoreU8Quad || U8P, "the u8 quad store is the u8 pixel arithmetic's");
   using C = CfgZ<RZ>;
   constexpr int KZ = C::KZ, S = C::S, NT = C::NT;
   static_assert(C::QPT == 1, "one quad per thread");
@@ -540,7 +590,13 @@ __global__ void __launch_bounds__(256, RZ <= 8 ? 2 : 1) k_z_pass(const __grid_co
         const int slot = (p - k + KZ) % KZ;
 #pragma unroll
         for (int m = 0; m < 2; ++m) {
-          if constexpr (REF) {
+          if constexpr (U8P) {
+            float v0, v1;
+            unpack2(v[m], v0, v1);
+            const uint32_t a0 = (uint32_t)acc[m][slot] + u8p_tap(v0, a.wz[k]);
+            const uint32_t a1 = (uint32_t)(acc[m][slot] >> 32) + u8p_tap(v1, a.wz[k]);
+            acc[m][slot] = ((f2_t)a1 << 32) | a0;
+          } else if constexpr (REF) {
             float a0, a1, v0, v1;
             unpack2(acc[m][slot], a0, a1);
             unpack2(v[m], v0, v1);
@@ -560,8 +616,21 @@ __global__ void __launch_bounds__(256, RZ <= 8 ? 2 : 1) k_z_pass(const __grid_co
       }
       if (!store) return;
       float o[4];
-      unpack2(d0, o[0], o[1]);
-      unpack2(d1, o[2], o[3]);
+      if constexpr (U8P) {
+        if constexpr (ST == kStoreU8Quad) {
+          __stcs(reinterpret_cast<unsigned int*>(dz), (uint32_t)(d0 & 255u) | (uint32_t)((d0 >> 24) & 0xFF00u) |
+                                                          (uint32_t)((d1 & 255u) << 16) | (uint32_t)((d1 >> 8) & 0xFF000000u));
+          dz += a.dst_pitch[2];
+          return;
+        }
+        o[0] = u8p_value((uint32_t)d0);
+        o[1] = u8p_value((uint32_t)(d0 >> 32));
+        o[2] = u8p_value((uint32_t)d1);
+        o[3] = u8p_value((uint32_t)(d1 >> 32));
+      } else {
+        unpack2(d0, o[0], o[1]);
+        unpack2(d1, o[2], o[3]);
+      }
       if constexpr (USH) {
         if constexpr (REF)
           __stcs(reinterpret_cast<float4*>(dz), unsharp_quad_exact(og, o[0], o[1], o[2], o[3], a.ush));
@@ -569,8 +638,16 @@ __global__ void __launch_bounds__(256, RZ <= 8 ? 2 : 1) k_z_pass(const __grid_co
           __stcs(reinterpret_cast<float4*>(dz),
                  make_float4(unsharp_cheap_f32(og.x, o[0], a.ush), unsharp_cheap_f32(og.y, o[1], a.ush),
                              unsharp_cheap_f32(og.z, o[2], a.ush), unsharp_cheap_f32(og.w, o[3], a.ush)));
-      } else if constexpr (VEC) {
+      } else if constexpr (ST == kStoreF32Quad) {
         __stcs(reinterpret_cast<float4*>(dz), make_float4(o[0], o[1], o[2], o[3]));
+      } else if constexpr (ST == kStoreBF16Quad || ST == kStoreF16Quad) {
+        uint32_t h[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          if constexpr (ST == kStoreBF16Quad) h[c] = __bfloat16_as_ushort(from_f32<__nv_bfloat16>(o[c]));
+          else h[c] = __half_as_ushort(from_f32<__half>(o[c]));
+        }
+        __stcs(reinterpret_cast<uint2*>(dz), make_uint2(h[0] | (h[1] << 16), h[2] | (h[3] << 16)));
       } else {
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
@@ -626,14 +703,35 @@ XYEntry make_xy(int dtype) {
                  C::IH};
 }
 
-// Tables: two_pass.cu (f32 and the z pass) and two_pass_in.cu (i16, u8, bf16, f16).
+// Tables: two_pass.cu (f32 x-y), two_pass_in.cu (i16, u8, bf16, f16 x-y), two_pass_z*.cu (z).
 const XYEntry* xy_entries_f32(int* n);
 const XYEntry* xy_entries_i16(int* n);
 const XYEntry* xy_entries_u8(int* n);
 const XYEntry* xy_entries_bf16(int* n);
 const XYEntry* xy_entries_f16(int* n);
-ZFn z_fn(int r, bool ref, bool vec, bool ush = false);
+ZFn z_fn(int r, bool ref, int store, bool ush = false);
+// The plain z kernels, split over translation units so they compile in
+// parallel: [r - 1] of each row is k_z_pass<r, REF, ST>.
+const ZFn* z_row_fma_any();     // two_pass_z.cu: REF false, kStoreAny
+const ZFn* z_row_fma_f32q();    //                REF false, kStoreF32Quad
+const ZFn* z_row_ref_any();     // two_pass_zref.cu: REF true, kStoreAny
+const ZFn* z_row_ref_f32q();    //                   REF true, kStoreF32Quad
+const ZFn* z_row_fma_bf16q();   // two_pass_znarrow.cu: REF false, kStoreBF16Quad
+const ZFn* z_row_fma_f16q();    //                      REF false, kStoreF16Quad
+const ZFn* z_row_ref_bf16q();   // two_pass_znarrow_ref.cu: REF true, kStoreBF16Quad
+const ZFn* z_row_ref_f16q();    //                          REF true, kStoreF16Quad
+// two_pass_u8p.cu: the u8 pixel-arithmetic kernels, [r - 1]
+const XYEntry* xy_entries_u8p(int* n);
+const ZFn* z_row_u8p_any();
+const ZFn* z_row_u8p_u8q();
 ZFn z_ush_fn(int r, bool ref);  // two_pass_ush.cu
+
+#define ITKG_Z_ROW(REF, ST)                                                                             \
+  {                                                                                                     \
+    k_z_pass<1, REF, ST>, k_z_pass<2, REF, ST>, k_z_pass<3, REF, ST>, k_z_pass<4, REF, ST>,             \
+        k_z_pass<5, REF, ST>, k_z_pass<6, REF, ST>, k_z_pass<7, REF, ST>, k_z_pass<8, REF, ST>,         \
+        k_z_pass<9, REF, ST>, k_z_pass<10, REF, ST>, k_z_pass<11, REF, ST>, k_z_pass<12, REF, ST>       \
+  }
 
 #define ITKG_XY_TABLE(T, DT)                                                                      \
   {                                                                                              \

@@ -1,5 +1,5 @@
 // The z kernels of the two-pass 3-D forward that store UnsharpMaskFilter's
-// point-wise step (k_z_pass<R, REF, true, true>), in their own translation
+// point-wise step (k_z_pass<R, REF, kStoreF32Quad, true>), in their own translation
 // unit so they compile beside the plain ones.
 #include "two_pass.cuh"
 
@@ -12,7 +12,7 @@ struct ZUshEntry {
 };
 template <int R>
 ZUshEntry make_z_ush() {
-  return ZUshEntry{R, {k_z_pass<R, false, true, true>, k_z_pass<R, true, true, true>}};
+  return ZUshEntry{R, {k_z_pass<R, false, kStoreF32Quad, true>, k_z_pass<R, true, kStoreF32Quad, true>}};
 }
 const ZUshEntry kZUsh[] = {make_z_ush<1>(), make_z_ush<2>(),  make_z_ush<3>(),  make_z_ush<4>(),
                            make_z_ush<5>(), make_z_ush<6>(),  make_z_ush<7>(),  make_z_ush<8>(),

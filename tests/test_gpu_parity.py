@@ -16,7 +16,8 @@ ALGOS = ["auto", "per_axis"]
 
 
 def _algo(itkg, name):
-    return {"auto": itkg.ALGO_AUTO, "per_axis": itkg.ALGO_PER_AXIS, "fused": itkg.ALGO_FUSED}[name]
+    return {"auto": itkg.ALGO_AUTO, "per_axis": itkg.ALGO_PER_AXIS, "fused": itkg.ALGO_FUSED,
+            "two_pass": itkg.ALGO_TWO_PASS}[name]
 
 
 def bits_equal(a, b):
@@ -202,6 +203,30 @@ def test_half_storage_outputs(gpu, out):
     # bf16 output equals rounding the f32 result to nearest-even
     f32 = oracle.gaussian_f32(arr.astype(np.float32), 1.5, spacing=(0.7, 0.7, 2.5))
     assert normwise(got, f32) <= ulp_rel
+
+
+def _f32_to_bf16_bits(v):
+    """Round f32 to bf16 to nearest, ties to even (finite values), as bits."""
+    b = np.ascontiguousarray(v, dtype=np.float32).view(np.uint32).astype(np.uint64)
+    return ((b + 0x7FFF + ((b >> 16) & 1)) >> 16).astype(np.uint16)
+
+
+@pytest.mark.parametrize("out", ["bf16", "f16"])
+@pytest.mark.parametrize("shape,req", [((14, 40, 64), None),                          # whole quads: 8-byte stores
+                                        ((14, 40, 66), None),                          # ragged width: element stores
+                                        ((20, 45, 72), ((4, 3, 2), (36, 30, 15)))])    # sub-region, whole quads
+@pytest.mark.parametrize("algo", ["two_pass", "auto"])
+def test_half_storage_bit_exact_in_reference_rounding(gpu, out, shape, req, algo):
+    """In reference rounding the bf16 / f16 output is the reference's f32
+    result rounded to nearest-even, bit for bit, whichever store the z pass
+    takes (one 8-byte store per quad, or element by element)."""
+    arr = np.random.default_rng(15).standard_normal(shape).astype(np.float32) * 40
+    code = gpu.BF16 if out == "bf16" else gpu.F16
+    raw = run_device(gpu, arr, 1.6, requested=req, out_dtype=code, algo=algo)
+    assert gpu.last_kernel().startswith("z_pass"), gpu.last_kernel()
+    want32 = oracle.gaussian_f32(arr, 1.6, requested=req)
+    want = _f32_to_bf16_bits(want32) if out == "bf16" else want32.astype(np.float16).view(np.uint16)
+    assert np.array_equal(np.asarray(raw).view(np.uint16), want)
 
 
 def test_host_buffers_through_abi(gpu):
