@@ -294,6 +294,11 @@ struct DotArgs {  // sum over the image of p * q (two pitched f32 images)
 itkg_status launch_adjoint_axis(const VjpAxisArgs& a, const float* w, const float* prefix,
                                 void* stream);
 itkg_status launch_dual_axis(const VjpAxisArgs& a, const float* w, const float* dw, void* stream);
+// vjp_lines_{dual,adj}.cu: the tiled passes for radii 13 .. 24; return
+// ITKG_ERROR_UNSUPPORTED (without setting an error) outside that range or when
+// the image does not fit their tile arithmetic.
+itkg_status launch_line_dual(const VjpAxisArgs& a, const float* w, const float* dw, void* stream);
+itkg_status launch_line_adjoint(const VjpAxisArgs& a, const float* w, const float* prefix, void* stream);
 int dot_partial_blocks(int64_t n);
 // partials: nblocks doubles of scratch; *out (device) = sum, or += with accumulate.
 itkg_status launch_dot(const DotArgs& d, double* partials, int nblocks, double* out,

@@ -16,6 +16,8 @@
 // so after the last pass dv = dy/dsigma and dL/dsigma = <ybar, dv>.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "internal.hpp"
 #include "pixel.cuh"
 
@@ -29,6 +31,12 @@ struct Taps {
   float aux[kMaxVjpTaps];  // dw/dsigma (dual pass) or prefix sums P (adjoint pass)
 };
 
+// v[i] for a runtime i by selects: indexing a kernel parameter's array with a
+// runtime index would copy the parameters to local memory.
+__host__ __device__ __forceinline__ int64_t pick3(const int64_t (&v)[kMaxDim], int i) {
+  return i == 0 ? v[0] : (i == 1 ? v[1] : v[2]);
+}
+
 __device__ __forceinline__ const char* px(const void* base, const int64_t* pitch, int64_t x,
                                           int64_t y, int64_t z) {
   return static_cast<const char*>(base) + x * pitch[0] + y * pitch[1] + z * pitch[2];
@@ -41,8 +49,8 @@ __global__ void __launch_bounds__(kThreads) k_adjoint_axis(const VjpAxisArgs a, 
   const int64_t nrows = a.size[1] * a.size[2];
   const int r = a.radius, K = 2 * r + 1;
   const int axis = a.axis;
-  const int64_t n = a.size[axis];
-  const int64_t ap = a.in_pitch[axis];
+  const int64_t n = pick3(a.size, axis);
+  const int64_t ap = pick3(a.in_pitch, axis);
   for (int64_t row = blockIdx.y; row < nrows; row += gridDim.y) {
     const int64_t y = row % a.size[1], z = row / a.size[1];
     const int64_t i = axis == 0 ? t : (axis == 1 ? y : z);
@@ -70,8 +78,8 @@ __global__ void __launch_bounds__(kThreads) k_dual_axis(const VjpAxisArgs a, con
   const int64_t nrows = a.size[1] * a.size[2];
   const int r = a.radius, K = 2 * r + 1;
   const int axis = a.axis;
-  const int64_t n = a.size[axis];
-  const int64_t ap = a.in_pitch[axis];
+  const int64_t n = pick3(a.size, axis);
+  const int64_t ap = pick3(a.in_pitch, axis);
   for (int64_t row = blockIdx.y; row < nrows; row += gridDim.y) {
     const int64_t y = row % a.size[1], z = row / a.size[1];
     const int64_t i = axis == 0 ? t : (axis == 1 ? y : z);
@@ -92,13 +100,14 @@ __global__ void __launch_bounds__(kThreads) k_dual_axis(const VjpAxisArgs a, con
   }
 }
 
-// The same two passes with the radius a template parameter (R <= 24: taps
-// unrolled, weights read from the parameter bank) and RUN outputs per thread
+// The same two passes with the radius a template parameter (R <= 12: taps
+// unrolled, weights read from the parameter bank; radii 13 .. 24 take the tiled
+// passes of vjp_lines.cuh) and RUN outputs per thread
 // along a marching axis -- y for passes along x and y, z for passes along z.
 // Along y and z the RUN outputs share one register window of K + RUN - 1
 // loads; along x the taps' offsets (and, for the adjoint, which taps fall
 // inside the image) are computed once per thread.
-constexpr int kMaxSmallVjpR = 24;
+constexpr int kMaxSmallVjpR = 12;
 
 template <int R, int RUN, bool AX0>
 __global__ void __launch_bounds__(kThreads, 2) k_adjoint_small(const VjpAxisArgs a, const Taps T) {
@@ -107,13 +116,13 @@ __global__ void __launch_bounds__(kThreads, 2) k_adjoint_small(const VjpAxisArgs
   if (x >= a.size[0]) return;
   const int axis = AX0 ? 0 : a.axis;
   const int md = axis == 2 ? 2 : 1, od = axis == 2 ? 1 : 2;
-  const int64_t n = a.size[axis], mn = a.size[md], on = a.size[od];
-  const int64_t ap = a.in_pitch[axis];
+  const int64_t n = pick3(a.size, axis), mn = pick3(a.size, md), on = pick3(a.size, od);
+  const int64_t ap = pick3(a.in_pitch, axis);
   const char* const ix = reinterpret_cast<const char*>(a.in) + x * a.in_pitch[0];
   char* const ox = reinterpret_cast<char*>(a.out) + x * a.out_pitch[0];
   for (int64_t o = blockIdx.z; o < on; o += gridDim.z) {
-    const char* const io = ix + o * a.in_pitch[od];
-    char* const oo = ox + o * a.out_pitch[od];
+    const char* const io = ix + o * pick3(a.in_pitch, od);
+    char* const oo = ox + o * pick3(a.out_pitch, od);
     for (int64_t mb = (int64_t)blockIdx.y * RUN; mb < mn; mb += (int64_t)gridDim.y * RUN) {
       const int nv = (int)(mn - mb < RUN ? mn - mb : RUN);
       float acc[RUN];
@@ -123,7 +132,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_adjoint_small(const VjpAxisArgs
 #pragma unroll
         for (int r = 0; r < RUN; ++r) {
           acc[r] = 0.0f;
-          rows[r] = io + (mb + (r < nv ? r : 0)) * a.in_pitch[md];
+          rows[r] = io + (mb + (r < nv ? r : 0)) * pick3(a.in_pitch, md);
         }
 #pragma unroll
         for (int k = 0; k < K; ++k) {
@@ -156,7 +165,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_adjoint_small(const VjpAxisArgs
         const int64_t i = AX0 ? x : m;  // position along the pass axis
         float res = acc[r];
         if (i == 0 || i == n - 1) {  // the taps the forward clamped onto the edge voxels
-          const char* const line = AX0 ? io + m * a.in_pitch[md] - x * ap : io;
+          const char* const line = AX0 ? io + m * pick3(a.in_pitch, md) - x * ap : io;
           if (i == 0)
             for (int d = 0; d < R && d < n; ++d)
               res = fmaf(T.aux[R - 1 - d], *reinterpret_cast<const float*>(line + d * ap), res);
@@ -164,7 +173,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_adjoint_small(const VjpAxisArgs
             for (int d = 0; d < R && d < n; ++d)
               res = fmaf(T.aux[R - 1 - d], *reinterpret_cast<const float*>(line + (n - 1 - d) * ap), res);
         }
-        float* const po = reinterpret_cast<float*>(oo + m * a.out_pitch[md]);
+        float* const po = reinterpret_cast<float*>(oo + m * pick3(a.out_pitch, md));
         *po = a.accumulate ? *po + res : res;
       }
     }
@@ -178,15 +187,15 @@ __global__ void __launch_bounds__(kThreads, 2) k_dual_small(const VjpAxisArgs a,
   if (x >= a.size[0]) return;
   const int axis = AX0 ? 0 : a.axis;
   const int md = axis == 2 ? 2 : 1, od = axis == 2 ? 1 : 2;
-  const int64_t n = a.size[axis], mn = a.size[md], on = a.size[od];
-  const int64_t ap = a.in_pitch[axis];
+  const int64_t n = pick3(a.size, axis), mn = pick3(a.size, md), on = pick3(a.size, od);
+  const int64_t ap = pick3(a.in_pitch, axis);
   const bool has_d = a.din != nullptr;
   const int64_t dbase = has_d ? reinterpret_cast<const char*>(a.din) - reinterpret_cast<const char*>(a.in) : 0;
   const char* const ix = reinterpret_cast<const char*>(a.in) + x * a.in_pitch[0];
   const int64_t oxo = x * a.out_pitch[0];
   for (int64_t o = blockIdx.z; o < on; o += gridDim.z) {
-    const char* const io = ix + o * a.in_pitch[od];
-    const int64_t oo = oxo + o * a.out_pitch[od];
+    const char* const io = ix + o * pick3(a.in_pitch, od);
+    const int64_t oo = oxo + o * pick3(a.out_pitch, od);
     for (int64_t mb = (int64_t)blockIdx.y * RUN; mb < mn; mb += (int64_t)gridDim.y * RUN) {
       const int nv = (int)(mn - mb < RUN ? mn - mb : RUN);
       float v[RUN], dv[RUN];
@@ -197,7 +206,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_dual_small(const VjpAxisArgs a,
         for (int r = 0; r < RUN; ++r) {
           v[r] = 0.0f;
           dv[r] = 0.0f;
-          rows[r] = io + (mb + (r < nv ? r : 0)) * a.in_pitch[md];
+          rows[r] = io + (mb + (r < nv ? r : 0)) * pick3(a.in_pitch, md);
         }
 #pragma unroll
         for (int k = 0; k < K; ++k) {
@@ -239,7 +248,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_dual_small(const VjpAxisArgs a,
 #pragma unroll
       for (int r = 0; r < RUN; ++r) {
         if (r >= nv) break;
-        const int64_t off = oo + (mb + r) * a.out_pitch[md];
+        const int64_t off = oo + (mb + r) * pick3(a.out_pitch, md);
         *reinterpret_cast<float*>(reinterpret_cast<char*>(a.out) + off) = v[r];
         *reinterpret_cast<float*>(reinterpret_cast<char*>(a.dout) + off) = dv[r];
       }
@@ -256,10 +265,8 @@ template <int R>
 constexpr VjpPair adj_fn() { return {k_adjoint_small<R, kAdjRun, true>, k_adjoint_small<R, kAdjRun, false>}; }
 template <int R>
 constexpr VjpPair dual_fn() { return {k_dual_small<R, kDualRun, true>, k_dual_small<R, kDualRun, false>}; }
-#define ITKG_VJP_TABLE(F)                                                                                    \
-  {{nullptr, nullptr}, F<1>(), F<2>(),  F<3>(),  F<4>(),  F<5>(),  F<6>(),  F<7>(),  F<8>(),  F<9>(),  F<10>(), \
-   F<11>(), F<12>(), F<13>(), F<14>(), F<15>(), F<16>(), F<17>(), F<18>(), F<19>(), F<20>(), F<21>(), F<22>(),   \
-   F<23>(), F<24>()}
+#define ITKG_VJP_TABLE(F) \
+  {{nullptr, nullptr}, F<1>(), F<2>(), F<3>(), F<4>(), F<5>(), F<6>(), F<7>(), F<8>(), F<9>(), F<10>(), F<11>(), F<12>()}
 const VjpPair kAdjSmall[kMaxSmallVjpR + 1] = ITKG_VJP_TABLE(adj_fn);
 const VjpPair kDualSmall[kMaxSmallVjpR + 1] = ITKG_VJP_TABLE(dual_fn);
 #undef ITKG_VJP_TABLE
@@ -267,8 +274,8 @@ const VjpPair kDualSmall[kMaxSmallVjpR + 1] = ITKG_VJP_TABLE(dual_fn);
 dim3 grid_small(const VjpAxisArgs& a, int run) {
   const int md = a.axis == 2 ? 2 : 1, od = a.axis == 2 ? 1 : 2;
   const int64_t gx = (a.size[0] + kThreads - 1) / kThreads;
-  const int64_t gy = (a.size[md] + run - 1) / run;
-  return dim3((unsigned)gx, (unsigned)(gy < 65535 ? gy : 65535), (unsigned)(a.size[od] < 65535 ? a.size[od] : 65535));
+  const int64_t gy = (pick3(a.size, md) + run - 1) / run;
+  return dim3((unsigned)gx, (unsigned)(gy < 65535 ? gy : 65535), (unsigned)(pick3(a.size, od) < 65535 ? pick3(a.size, od) : 65535));
 }
 
 // Per-block f64 partial sums of sum(p * q) over a pitched image.
@@ -347,6 +354,64 @@ __global__ void __launch_bounds__(kThreads) k_sqerr(const float* __restrict__ y,
   }
 }
 
+// The same over dense images whose rows are whole quads (the target too): a
+// grid-stride loop over the volume's quads, four quads per thread in flight,
+// the f32 runs folded into f64 every 8 quads.  A fixed grid makes the partials
+// deterministic.
+__global__ void __launch_bounds__(kThreads) k_sqerr_q(const float4* __restrict__ y, const float4* __restrict__ dy,
+                                                        const float4* __restrict__ t, float4* __restrict__ ybar,
+                                                        int64_t nq, double* partials) {
+  constexpr int U = 4;
+  double sl = 0.0, ss = 0.0;
+  const int64_t stride = (int64_t)gridDim.x * kThreads;
+  for (int64_t i0 = (int64_t)blockIdx.x * kThreads + threadIdx.x; i0 < nq; i0 += U * stride) {
+    float4 yv[U], tv[U], dv[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t i = i0 + u * stride;
+      if (i < nq) {
+        yv[u] = __ldcs(y + i);
+        tv[u] = __ldg(t + i);
+        dv[u] = dy ? __ldcs(dy + i) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      }
+    }
+    float fl = 0.0f, fs = 0.0f;
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t i = i0 + u * stride;
+      if (i >= nq) break;
+      const float4 d = make_float4(yv[u].x - tv[u].x, yv[u].y - tv[u].y, yv[u].z - tv[u].z, yv[u].w - tv[u].w);
+      const float4 g = make_float4(2.0f * d.x, 2.0f * d.y, 2.0f * d.z, 2.0f * d.w);
+      __stcs(ybar + i, g);
+      fl = fmaf(d.x, d.x, fl);
+      fl = fmaf(d.y, d.y, fl);
+      fl = fmaf(d.z, d.z, fl);
+      fl = fmaf(d.w, d.w, fl);
+      fs = fmaf(g.x, dv[u].x, fs);
+      fs = fmaf(g.y, dv[u].y, fs);
+      fs = fmaf(g.z, dv[u].z, fs);
+      fs = fmaf(g.w, dv[u].w, fs);
+    }
+    sl += (double)fl;
+    ss += (double)fs;
+  }
+  __shared__ double red[2][kThreads];
+  red[0][threadIdx.x] = sl;
+  red[1][threadIdx.x] = ss;
+  __syncthreads();
+  for (int w = kThreads / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) {
+      red[0][threadIdx.x] += red[0][threadIdx.x + w];
+      red[1][threadIdx.x] += red[1][threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x] = red[0][0];
+    partials[gridDim.x + blockIdx.x] = red[1][0];
+  }
+}
+
 // Fixed-order final sum of the partials (deterministic).
 __global__ void k_sum_partials(const double* partials, int n, double* out, int accumulate) {
   __shared__ double red[kThreads];
@@ -389,6 +454,10 @@ itkg_status launch_adjoint_axis(const VjpAxisArgs& a, const float* w, const floa
                                 void* stream) {
   if (2 * a.radius + 1 > kMaxVjpTaps)
     return set_error(ITKG_ERROR_UNSUPPORTED, "VJP radius %d exceeds %d", a.radius, (kMaxVjpTaps - 1) / 2);
+  {
+    const itkg_status st = launch_line_adjoint(a, w, prefix, stream);
+    if (st != ITKG_ERROR_UNSUPPORTED) return st;
+  }
   const Taps T = make_taps(w, prefix, 2 * a.radius + 1);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (a.radius >= 1 && a.radius <= kMaxSmallVjpR && a.size[0] <= INT32_MAX) {
@@ -403,6 +472,10 @@ itkg_status launch_adjoint_axis(const VjpAxisArgs& a, const float* w, const floa
 itkg_status launch_dual_axis(const VjpAxisArgs& a, const float* w, const float* dw, void* stream) {
   if (2 * a.radius + 1 > kMaxVjpTaps)
     return set_error(ITKG_ERROR_UNSUPPORTED, "VJP radius %d exceeds %d", a.radius, (kMaxVjpTaps - 1) / 2);
+  {
+    const itkg_status st = launch_line_dual(a, w, dw, stream);
+    if (st != ITKG_ERROR_UNSUPPORTED) return st;
+  }
   const Taps T = make_taps(w, dw, 2 * a.radius + 1);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (a.radius >= 1 && a.radius <= kMaxSmallVjpR && a.size[0] <= INT32_MAX) {
@@ -423,13 +496,25 @@ itkg_status launch_sqerr(const float* y, const float* dy, const DotArgs& t, floa
                          double* partials, int nblocks, double* loss_out, double* sigma_out,
                          bool accumulate_loss, void* stream) {
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  k_sqerr<<<nblocks, kThreads, 0, s>>>(y, dy, t, ybar, partials);
+  const int64_t nx = t.size[0], ny = t.size[1];
+  const bool quads = nx % 4 == 0 && t.q_pitch[0] == 4 && t.q_pitch[1] == 4 * nx && t.q_pitch[2] == 4 * nx * ny &&
+                     (((uintptr_t)y | (uintptr_t)dy | (uintptr_t)t.q | (uintptr_t)ybar) & 15) == 0;
+  // the quad kernel: about 16 quads per thread (fewer, longer-running blocks)
+  const int64_t nq = nx / 4 * ny * t.size[2];
+  const int nb = quads ? (int)std::max<int64_t>(1, std::min<int64_t>(nblocks, (nq + kThreads * 16 - 1) / (kThreads * 16)))
+                       : nblocks;
+  if (quads)
+    k_sqerr_q<<<nb, kThreads, 0, s>>>(reinterpret_cast<const float4*>(y), reinterpret_cast<const float4*>(dy),
+                                      reinterpret_cast<const float4*>(t.q), reinterpret_cast<float4*>(ybar), nq,
+                                      partials);
+  else
+    k_sqerr<<<nb, kThreads, 0, s>>>(y, dy, t, ybar, partials);
   itkg_status st = launched("sqerr_partials_f64");
   if (st != ITKG_SUCCESS) return st;
-  k_sum_partials<<<1, kThreads, 0, s>>>(partials, nblocks, loss_out, accumulate_loss ? 1 : 0);
+  k_sum_partials<<<1, kThreads, 0, s>>>(partials, nb, loss_out, accumulate_loss ? 1 : 0);
   if ((st = launched("sum_partials_f64")) != ITKG_SUCCESS) return st;
   if (!sigma_out) return ITKG_SUCCESS;
-  k_sum_partials<<<1, kThreads, 0, s>>>(partials + nblocks, nblocks, sigma_out, 0);
+  k_sum_partials<<<1, kThreads, 0, s>>>(partials + nb, nb, sigma_out, 0);
   return launched("sum_partials_f64");
 }
 

@@ -201,12 +201,14 @@ def test_vjp_scale_stack_192_sigma_1_2_4_8(gpu):
 
 
 LARGE_R = [((40, 48, 56), 4.5, None), ((36, 44, 52), 6.0, None), ((50, 54, 58), 8.0, None),
-           ((30, 70, 64), 4.0, (1.0, 0.5, 0.9)), ((60, 28, 66), 5.2, (0.8, 1.3, 1.0))]
+           ((30, 70, 64), 4.0, (1.0, 0.5, 0.9)), ((60, 28, 66), 5.2, (0.8, 1.3, 1.0)),
+           ((12, 70, 9), 8.0, None),      # lines shorter than the radius, a ragged tile of lines
+           ((130, 33, 140), 7.0, None)]   # several tiles along every pass axis
 
 
 @pytest.mark.parametrize("shape,sigma,spacing", LARGE_R)
 def test_vjp_radii_13_to_24(gpu, shape, sigma, spacing):
-    """The compile-time per-axis adjoint and dual passes for radii 13..24."""
+    """The tiled per-axis adjoint and dual passes for radii 13..24."""
     sp = list(spacing) if spacing else None
     radii = _radii(sigma, sp)
     assert max(radii) > 12 and max(radii) <= 24, radii
