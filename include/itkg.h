@@ -160,6 +160,10 @@ void itkg_debug_fail_scratch_alloc(int64_t after);
  * A wait that gives up sets the calling thread's device fault word (see
  * itkg_device_fault); the kernel still lets its loads land before it exits. */
 void itkg_debug_set_wait_limit(int64_t cycles);
+/* Test hook: which kernel runs the fused 2-D forward (2-D images and the
+ * slices of SliceBySliceFilter): 1 the tile kernel, 2 the row-marching
+ * kernel, anything else the library's choice.  Results are the same. */
+void itkg_debug_set_2d_kernel(int32_t which);
 
 /* ---- host-side geometry (no device needed) ------------------------------ */
 

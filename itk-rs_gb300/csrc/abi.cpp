@@ -91,6 +91,8 @@ std::atomic<long long> g_wait_limit{1ll << 31};
 }  // namespace
 
 long long wait_limit_cycles() { return g_wait_limit.load(std::memory_order_relaxed); }
+std::atomic<int> g_kernel2d{0};
+int kernel2d_override() { return g_kernel2d.load(std::memory_order_relaxed); }
 
 itkg_status scratch_alloc(void** p, size_t bytes, void* stream) {
   int64_t f = g_fail_after.load(std::memory_order_relaxed);
@@ -735,6 +737,7 @@ const char* itkg_last_kernel(void) { return t_kernel.c_str(); }
 uint64_t itkg_scratch_alloc_counter(void) { return g_scratch_allocs.load(std::memory_order_relaxed); }
 void itkg_debug_fail_scratch_alloc(int64_t after) { g_fail_after.store(after < 0 ? -1 : after); }
 void itkg_debug_set_wait_limit(int64_t cycles) { g_wait_limit.store(cycles > 0 ? cycles : (1ll << 31)); }
+void itkg_debug_set_2d_kernel(int32_t which) { g_kernel2d.store(which == 1 || which == 2 ? which : 0); }
 uint64_t itkg_launch_counter(void) { return g_launches.load(std::memory_order_relaxed); }
 
 uint64_t itkg_kernel_radius(double sigma, double spacing) { return kernel_radius(sigma, spacing); }

@@ -115,6 +115,12 @@ itkg_status launch_fused(const FusedGeom& g, const float* const w[kMaxDim], void
 // fused2d.cu: the 2-D counterpart (f32 input, 1 or 3 components, radius <= 12).
 itkg_status launch_fused2d(const FusedGeom& g, const float* const w[kMaxDim], void* stream,
                            bool dry_run);
+// tile2d.cu: the same geometries on 64 x 32 tiles staged at once (small and
+// medium images); launch_fused2d chooses between the two.
+itkg_status launch_tile2d(const FusedGeom& g, const float* const w[kMaxDim], void* stream, bool dry_run);
+// abi.cpp: the 2-D kernel forced by itkg_debug_set_2d_kernel (0: chosen by size,
+// 1: the tile kernel, 2: the row-marching kernel).
+int kernel2d_override();
 
 // abi.cpp: validates one 3-D request and fills its fused geometry and f32
 // weights; ITKG_ERROR_UNSUPPORTED when no multi-request fused kernel covers it.

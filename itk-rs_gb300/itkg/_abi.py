@@ -116,6 +116,7 @@ SIGNATURES = {
     "itkg_scratch_alloc_counter": (ctypes.c_uint64, []),
     "itkg_debug_fail_scratch_alloc": (None, [ctypes.c_int64]),
     "itkg_debug_set_wait_limit": (None, [ctypes.c_int64]),
+    "itkg_debug_set_2d_kernel": (None, [ctypes.c_int32]),
     "itkg_kernel_radius": (ctypes.c_uint64, [ctypes.c_double, ctypes.c_double]),
     "itkg_build_kernel": (st, [ctypes.c_double, ctypes.c_uint64, P]),
     "itkg_region_padded_per_axis": (st, [R, ctypes.c_int32, P, R]),

@@ -74,11 +74,17 @@ def test_bspline_u8(gpu):
     assert np.array_equal(run_bspline(gpu, x), oracle.bspline_downsample(x))
 
 
-def test_slices_take_the_fused_2d_kernel(gpu):
+@pytest.mark.parametrize("which,kernel", [(1, "tile2d"), (2, "fused2d")])
+def test_slices_take_the_fused_2d_kernels(gpu, which, kernel):
+    from itkg import _abi
     x = np.random.default_rng(65).standard_normal((9, 33, 70)).astype(np.float32)
-    for rounding, name in ((0, "fused2d_f32_ref"), (1, "fused2d_f32_fma")):
-        got = run_slices(gpu, x, 1.7, rounding=rounding)
-        assert gpu.last_kernel() == name
-        want = oracle.slice_by_slice(x, 1.7)
-        assert bits_equal(got, want) if rounding == 0 else normwise(got, want) <= 1e-5
+    _abi.lib().itkg_debug_set_2d_kernel(which)
+    try:
+        for rounding, suffix in ((0, "_f32_ref"), (1, "_f32_fma")):
+            got = run_slices(gpu, x, 1.7, rounding=rounding)
+            assert gpu.last_kernel() == kernel + suffix
+            want = oracle.slice_by_slice(x, 1.7)
+            assert bits_equal(got, want) if rounding == 0 else normwise(got, want) <= 1e-5
+    finally:
+        _abi.lib().itkg_debug_set_2d_kernel(0)
 

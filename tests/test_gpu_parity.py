@@ -400,30 +400,41 @@ FUSED2D_CASES = [((1, 1), 1, 1.0), ((7, 600), 1, 1.0), ((64, 64), 1, 0.3), ((130
                  ((130, 20), 3, 3.5), ((9, 600), 1, 4.0)]
 
 
+@pytest.fixture(params=[(1, "tile2d"), (2, "fused2d")], ids=["tile", "rows"])
+def kernel2d(request, gpu):
+    """Both fused 2-D kernels: the tile kernel and the row-marching kernel
+    (itkg_debug_set_2d_kernel); yields the kernel's launch-name prefix."""
+    from itkg import _abi
+    which, name = request.param
+    _abi.lib().itkg_debug_set_2d_kernel(which)
+    yield name
+    _abi.lib().itkg_debug_set_2d_kernel(0)
+
+
 @pytest.mark.parametrize("shape,comps,sigma", FUSED2D_CASES)
-def test_fused2d_reference_rounding_bit_exact(gpu, shape, comps, sigma):
-    """The fused 2-D kernel (scalar and VecPixel<f32, 3>): bit-exact with the
+def test_fused2d_reference_rounding_bit_exact(gpu, kernel2d, shape, comps, sigma):
+    """The fused 2-D kernels (scalar and VecPixel<f32, 3>): bit-exact with the
     reference pass-by-pass arithmetic."""
     rng = np.random.default_rng(sum(shape) + comps)
     arr = rng.standard_normal(shape + ((comps,) if comps > 1 else ())).astype(np.float32)
     want = oracle.gaussian_f32(arr, sigma, comps=comps)
     got = run_device(gpu, arr, sigma, comps=comps, algo="fused")
-    assert gpu.last_kernel() == "fused2d_f32_ref", gpu.last_kernel()
+    assert gpu.last_kernel() == f"{kernel2d}_f32_ref", gpu.last_kernel()
     assert bits_equal(got, want)
 
 
 @pytest.mark.parametrize("shape,comps,sigma", FUSED2D_CASES)
-def test_fused2d_fma_within_1e5(gpu, shape, comps, sigma):
+def test_fused2d_fma_within_1e5(gpu, kernel2d, shape, comps, sigma):
     rng = np.random.default_rng(3 + sum(shape) + comps)
     arr = rng.random(shape + ((comps,) if comps > 1 else ()), dtype=np.float32)
     want = oracle.gaussian_f32(arr, sigma, comps=comps)
     got = run_device(gpu, arr, sigma, comps=comps, algo="fused", rounding=gpu.ROUND_FMA)
-    assert gpu.last_kernel() == "fused2d_f32_fma", gpu.last_kernel()
+    assert gpu.last_kernel() == f"{kernel2d}_f32_fma", gpu.last_kernel()
     assert normwise(got, want) <= 1e-5
 
 
 @pytest.mark.parametrize("comps", [1, 3])
-def test_fused2d_subregions_offset_index_and_outputs(gpu, comps):
+def test_fused2d_subregions_offset_index_and_outputs(gpu, kernel2d, comps):
     """Requested sub-regions of an image with a non-zero index, and the
     converted output types, through the fused 2-D kernel."""
     rng = np.random.default_rng(17 + comps)
@@ -433,11 +444,11 @@ def test_fused2d_subregions_offset_index_and_outputs(gpu, comps):
                    ((0, 11), (513, 45)), ((679, 40), (1, 16))]:
         want = oracle.gaussian_f32(arr, 1.7, comps=comps, index=index, requested=(ri, rs))
         got = run_device(gpu, arr, 1.7, comps=comps, index=index, requested=(ri, rs), algo="fused")
-        assert gpu.last_kernel() == "fused2d_f32_ref", gpu.last_kernel()
+        assert gpu.last_kernel() == f"{kernel2d}_f32_ref", gpu.last_kernel()
         assert bits_equal(got, want), (ri, rs)
     want = oracle.gaussian_f32(arr * 255, 1.7, comps=comps)
     got = run_device(gpu, arr * 255, 1.7, comps=comps, algo="fused", out_dtype=gpu.U8)
-    assert gpu.last_kernel() == "fused2d_f32_ref", gpu.last_kernel()
+    assert gpu.last_kernel() == f"{kernel2d}_f32_ref", gpu.last_kernel()
     assert np.array_equal(got, oracle.cast_f32_to_u8(want))
 
 
