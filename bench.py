@@ -24,6 +24,8 @@ output voxels), on a bounded slab of the same workload per step.
   recursive3d  RecursiveGaussianFilter (and gradient magnitude), f64 lines
   unsharp3d    UnsharpMaskFilter, both roundings and Image<u8>
   callers3d    SliceBySliceFilter and BSplineDownsampleFilter
+  registration2d  DiffeomorphicDemons and N4 bias correction, 512^2
+  u8_3d        GaussianFilter<Image<u8>> 256^3 in u8 pixel arithmetic
 
 Prints ONE JSON line (rank 0).
 """
@@ -820,6 +822,32 @@ def extra_workload(args):
                                  "frac": best["achieved_GBs"] / peak,
                                  "note": "algorithmic 8 B per voxel per call (read the input, write the output)"},
                     "cpu_baseline": cpu})
+    elif args.workload == "u8_3d":
+        # GaussianFilter<Image<u8>> (u8 pixel arithmetic), 256^3 u8 from the
+        # blobs volume scaled to 0..255, sigma 2: two-pass kernels and per-axis passes
+        vol = np.clip(blobs_volume(SHAPE, 0) * 120.0, 0, 255).astype(np.uint8)
+        nvox = int(np.prod(SHAPE))
+        devs = [itkg.DeviceImage.from_host(itkg.Image(vol)) for _ in range(NVOL)]
+        region = devs[0].region
+        want = oracle.gaussian_u8(vol, SIGMA)
+        lines = {}
+        for name, algo in (("two_pass", itkg.ALGO_AUTO), ("per_axis", itkg.ALGO_PER_AXIS)):
+            outs = [itkg.DeviceImage(region, itkg.U8, 1) for _ in range(NVOL)]
+            calls = [_gen_call(L, itkg.GaussianFilter(d, SIGMA, arithmetic=itkg.ARITH_PIXEL_U8, algorithm=algo),
+                               region, o, sp) for d, o in zip(devs, outs)]
+            ms = _timed(stream, lambda: [c() for c in calls], args.steps, args.warmup)
+            got = outs[0].download()
+            lines[name] = {"voxels_per_s": NVOL * nvox / (ms * 1e-3), "us_per_call": ms / NVOL * 1e3,
+                           "kernel": itkg.last_kernel(), "bit_exact": bool(np.array_equal(got, want))}
+        best = lines["two_pass"]
+        out.update({"value": best["voxels_per_s"], "ms_per_step": best["us_per_call"] * NVOL * 1e-3, "dtype": "u8",
+                    "config": {"workload": "GaussianFilter<Image<u8,3>> 256^3 sigma 2, u8 pixel arithmetic "
+                                           "(wrapping u8 adds of round(x*w)), 8 volumes per step",
+                               "variants": lines},
+                    "roofline": {"bound": "fp32 issue (three instructions per tap and voxel)",
+                                 "achieved": nvox * 2 / (best["us_per_call"] * 1e-6) / 1e9, "peak": peak,
+                                 "unit": "GB/s", "frac": nvox * 2 / (best["us_per_call"] * 1e-6) / 1e9 / peak,
+                                 "note": "algorithmic 2 B per voxel (u8 in, u8 out)"}})
     elif args.workload == "callers3d":
         # the in-crate callers of GaussianFilter on the 256^3 blobs volume
         vol = blobs_volume(SHAPE, 0)
@@ -925,7 +953,7 @@ def main():
     ap.add_argument("--impl", choices=["itkg", "reference"], default="itkg")
     ap.add_argument("--workload", choices=["fwd3d", "fwd2d", "ct16", "batch", "batch_vjp", "vjp_stack",
                                            "mean3d", "binomial3d", "recursive3d", "unsharp3d", "callers3d",
-                                           "registration2d"],
+                                           "registration2d", "u8_3d"],
                     default="fwd3d")
     ap.add_argument("--rounding", choices=["fma", "reference"], default="fma")
     ap.add_argument("--algo", choices=["auto", "fused", "per_axis", "two_pass", "one_trip"], default="auto")

@@ -85,18 +85,52 @@ template <int R, bool AX0, bool CLAMP>
 __device__ __forceinline__ void stage_tile(float* s, const char* base, int64_t lp, int64_t pp, const LineGeom& g,
                                            int l0, int p0) {
   using C = LineCfg<R, AX0>;
-  for (int e = threadIdx.x; e < C::NP * kLines; e += kThreads) {
-    // AX0: consecutive threads on consecutive x of one line; else on
-    // consecutive lines (x again)
-    const int li = AX0 ? e / C::NP : e % kLines;
-    const int pi = AX0 ? e % C::NP : e / kLines;
+  // positions p0 - R .. p0 + kLen + R - 1 all inside the image: no clamping
+  const bool interior = p0 - R >= 0 && p0 + kLen + R <= g.n;
+  if constexpr (AX0) {
+    // one line after another, consecutive threads on consecutive x
+    static_assert(C::NP <= 2 * kThreads, "two positions per thread and line at most");
+#pragma unroll 4
+    for (int li = 0; li < kLines; ++li) {
+      const int l = l0 + li;
+      const bool lin = l < g.nlines;
+      const char* const row = base + (int64_t)(lin ? l : 0) * lp;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int pi = threadIdx.x + h * kThreads;
+        if (pi >= C::NP) break;
+        int p = p0 - R + pi;
+        bool in = lin;
+        if (!interior) {
+          if (CLAMP) p = clamp_i(p, 0, g.n - 1);
+          in = in && p >= 0 && p < g.n;
+        }
+        cp4(s + li * C::PP + pi, in ? row + (int64_t)p * pp : base, !in);
+      }
+    }
+  } else {
+    // this thread's line is fixed (kThreads is a multiple of kLines); its
+    // positions step by kThreads / kLines
+    constexpr int STEP = kThreads / kLines;
+    const int li = threadIdx.x % kLines;
     const int l = l0 + li;
-    int p = p0 - R + pi;
-    if (CLAMP) p = clamp_i(p, 0, g.n - 1);
-    const bool in = l < g.nlines && p >= 0 && p < g.n;
-    // a zero-filled word still names a valid address (the tile's base)
-    const char* const src = in ? base + (int64_t)l * lp + (int64_t)p * pp : base;
-    cp4(s + li * C::LS + pi * C::PS, src, !in);
+    const bool lin = l < g.nlines;
+    const char* const col = base + (int64_t)(lin ? l : 0) * lp;
+    const int pi0 = threadIdx.x / kLines;
+    if (interior && lin) {
+      const char* q = col + (int64_t)(p0 - R + pi0) * pp;
+      const int64_t dq = (int64_t)STEP * pp;
+#pragma unroll 4
+      for (int pi = pi0; pi < C::NP; pi += STEP, q += dq) cp4(s + pi * kLines + li, q, false);
+    } else {
+#pragma unroll 4
+      for (int pi = pi0; pi < C::NP; pi += STEP) {
+        int p = p0 - R + pi;
+        if (CLAMP) p = clamp_i(p, 0, g.n - 1);
+        const bool in = lin && p >= 0 && p < g.n;
+        cp4(s + pi * kLines + li, in ? col + (int64_t)p * pp : base, !in);
+      }
+    }
   }
 }
 
