@@ -116,7 +116,7 @@ typedef struct itkg_image {
     int32_t dim;
     int32_t dtype;      /* itkg_dtype */
     int32_t components; /* 1 = scalar, 3 = VecPixel<_, 3> (interleaved); 2 = VecPixel<f32, 2>
-                           (2-D gradient outputs only) */
+                           (2-D displacement fields and gradient outputs) */
     int32_t location;   /* itkg_location */
     itkg_region region; /* buffered region (BufferedRegion) */
     int64_t pitch[ITKG_MAX_DIM]; /* bytes between neighbours along each axis */

@@ -127,11 +127,11 @@ inline itkg_status validate_image(const itkg_image* im, const char* name) {
   return ITKG_SUCCESS;
 }
 
-// The smoothing filters take scalar pixels or VecPixel<_, 3> (2-component
-// images exist as the gradient filter's output only).
+// The smoothing filters take scalar pixels, VecPixel<_, 3> and VecPixel<_, 2>
+// (2-D displacement fields, DisplacementFieldToBSplineFilter).
 inline itkg_status filter_components(const itkg_image* im, const char* name) {
-  if (im->components != 1 && im->components != 3)
-    return set_error(ITKG_ERROR_UNSUPPORTED, "%s: components must be 1 or 3", name);
+  if (im->components < 1 || im->components > 3)
+    return set_error(ITKG_ERROR_UNSUPPORTED, "%s: components must be 1, 2 or 3", name);
   return ITKG_SUCCESS;
 }
 

@@ -1,6 +1,6 @@
 // Tiled 2-D Gaussian forward: both passes of GaussianFilter::generate_region
-// (src/filters/gaussian.rs:74-88) for Image<f32, 2> and
-// Image<VecPixel<f32, 3>, 2> (and every slice of a 3-D image whose z kernel is
+// (src/filters/gaussian.rs:74-88) for Image<f32, 2>, Image<VecPixel<f32, 2>, 2>
+// and Image<VecPixel<f32, 3>, 2> (and every slice of a 3-D image whose z kernel is
 // the 1-tap [1], SliceBySliceFilter), one CTA per 64 x 32 output tile:
 //   1. the tile's (64 + 2r) x (32 + 2r) input pixels, rows and columns clamped
 //      to the image (the reference's clamp-to-edge, conv.rs:31-33), arrive by
@@ -173,6 +173,9 @@ const EntryT2 kTableT2[] = {
     make_t2<7, 1>(),  make_t2<8, 1>(),  make_t2<9, 1>(),  make_t2<10, 1>(), make_t2<11, 1>(), make_t2<12, 1>(),
     make_t2<1, 3>(),  make_t2<2, 3>(),  make_t2<3, 3>(),  make_t2<4, 3>(),  make_t2<5, 3>(),  make_t2<6, 3>(),
     make_t2<7, 3>(),  make_t2<8, 3>(),  make_t2<9, 3>(),  make_t2<10, 3>(), make_t2<11, 3>(), make_t2<12, 3>(),
+    // VecPixel<f32, 2> (displacement fields)
+    make_t2<1, 2>(),  make_t2<2, 2>(),  make_t2<3, 2>(),  make_t2<4, 2>(),  make_t2<5, 2>(),  make_t2<6, 2>(),
+    make_t2<7, 2>(),  make_t2<8, 2>(),  make_t2<9, 2>(),  make_t2<10, 2>(), make_t2<11, 2>(), make_t2<12, 2>(),
 };
 
 bool fits32t(int64_t v) { return v >= INT_MIN && v <= INT_MAX; }

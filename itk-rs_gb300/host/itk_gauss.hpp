@@ -131,6 +131,10 @@ template <>
 struct PixelTraits<VecPixel<float, 3>> {
   static constexpr int dtype = ITKG_F32, comps = 3, arith = ITKG_ARITH_F32;
 };
+template <>
+struct PixelTraits<VecPixel<float, 2>> {  // 2-D displacement fields
+  static constexpr int dtype = ITKG_F32, comps = 2, arith = ITKG_ARITH_F32;
+};
 
 template <typename P, int D>
 struct Image {
@@ -613,6 +617,45 @@ struct SliceBySliceFilter {
 
 template <typename S>
 auto spacing_of(const SliceBySliceFilter<S>& f) { return f.spacing(); }
+
+// DisplacementFieldToBSplineFilter { source, sigma } (spatial.rs:1484-1525),
+// sigma 2.0 by default: each component of a 2-D VecPixel<f32, 2> field smoothed
+// by GaussianFilter { sigma } over the generated request as an image of its own
+// -- the request is the Gaussian's largest region, so its taps clamp there.
+template <typename S>
+struct DisplacementFieldToBSplineFilter {
+  S source;
+  double sigma = 2.0;
+  int rounding = ITKG_ROUND_REFERENCE;
+
+  static constexpr int Dim = std::decay_t<S>::Dim;
+  using Pixel = typename std::decay_t<S>::Pixel;
+  static_assert(Dim == 2 && std::is_same<Pixel, VecPixel<float, 2>>::value,
+                "DisplacementFieldToBSplineFilter takes a 2-D VecPixel<f32, 2> field");
+
+  explicit DisplacementFieldToBSplineFilter(S s, double sg = 2.0) : source(std::forward<S>(s)), sigma(sg) {}
+
+  Region<Dim> largest_region() const { return source.largest_region(); }
+  std::array<double, Dim> spacing() const { return spacing_of(source); }
+  Region<Dim> input_region_for_output(const Region<Dim>& out) const { return out; }
+
+  auto generate_region(const Region<Dim>& requested) const {
+    auto in = source.generate_region(requested);  // spatial.rs:1509
+    auto out = Image<Pixel, Dim>::allocate(requested, in.spacing, in.origin, Pixel{});
+    itkg_gaussian_params p;
+    std::memset(&p, 0, sizeof p);
+    p.sigma = sigma;
+    p.arithmetic = ITKG_ARITH_F32;
+    p.rounding = rounding;
+    const itkg_region r = requested.to_c();
+    itkg_image ic = in.desc(), oc = out.desc();
+    check(itkg_gaussian_generate_region(&ic, &r, &r, &p, &oc, nullptr));
+    return out;
+  }
+};
+
+template <typename S>
+auto spacing_of(const DisplacementFieldToBSplineFilter<S>& f) { return f.spacing(); }
 
 // stream_full (source.rs:81-98): allocate the full output once, fill it piece
 // by piece along the slowest axis.

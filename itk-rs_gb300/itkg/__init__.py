@@ -37,7 +37,7 @@ __all__ = [
     "GradientMagnitudeRecursiveGaussianFilter", "LaplacianRecursiveGaussianFilter",
     "DiscreteGaussianDerivativeFilter", "GradientRecursiveGaussianFilter", "HessianRecursiveGaussianFilter",
     "DifferenceOfGaussiansFilter", "UnsharpMaskFilter", "unsharp_kernel", "ZeroCrossingBasedEdgeDetectionFilter",
-    "SliceBySliceFilter", "BSplineDownsampleFilter", "DemonsRegistrationFilter",
+    "SliceBySliceFilter", "DisplacementFieldToBSplineFilter", "BSplineDownsampleFilter", "DemonsRegistrationFilter",
     "DiffeomorphicDemonsRegistrationFilter", "SyNRegistrationMethod", "N4BiasFieldCorrectionFilter",
     "MRIBiasFieldCorrectionFilter",
 ]
@@ -466,6 +466,24 @@ class SliceBySliceFilter(GaussianFilter):
         prm = self.params()
         check(lib().itkg_slice_by_slice_generate_region(ctypes.byref(src), ctypes.byref(req), ctypes.byref(prm),
                                                         ctypes.byref(out_c), stream.ptr))
+
+
+class DisplacementFieldToBSplineFilter(GaussianFilter):
+    """DisplacementFieldToBSplineFilter { source, sigma } (spatial.rs:1484-1525), sigma 2.0 by
+    default: each component of a 2-D VecPixel<f32, 2> field smoothed by GaussianFilter { sigma }.
+    The reference smooths the source's generated request as an image of its own, so the request
+    is also the Gaussian's largest region (its taps clamp at the request's edges)."""
+
+    def __init__(self, source, sigma: float = 2.0, rounding: int = ROUND_REFERENCE, algorithm: int = ALGO_AUTO):
+        super().__init__(source, sigma, rounding, algorithm)
+
+    def input_region_for_output(self, out: Region) -> Region:
+        return out  # the reference asks its source for the request itself (spatial.rs:1509)
+
+    def _call(self, src, largest, req, out_c, stream):
+        prm = self.params()
+        check(lib().itkg_gaussian_generate_region(ctypes.byref(src), ctypes.byref(req), ctypes.byref(req),
+                                                  ctypes.byref(prm), ctypes.byref(out_c), stream.ptr))
 
 
 class BSplineDownsampleFilter(GaussianFilter):

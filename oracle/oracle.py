@@ -293,6 +293,22 @@ def bspline_downsample(img, spacing=None, comps=1):
     return np.ascontiguousarray(full[tuple([slice(None, None, 2)] * D)])
 
 
+def displacement_field_to_bspline(field, sigma=2.0, spacing=None, index=None, requested=None):
+    """DisplacementFieldToBSplineFilter (spatial.rs:1484-1525) over a 2-D
+    VecPixel<f32, 2> field (numpy (y, x, 2)): the requested crop, each
+    component smoothed by GaussianFilter { sigma } over the crop as an image of
+    its own -- the crop is the Gaussian's largest region, so its taps clamp at
+    the crop's edges, not the field's."""
+    x = np.asarray(field, dtype=np.float32)
+    if x.ndim != 3 or x.shape[2] != 2:
+        raise ValueError("a 2-D VecPixel<f32, 2> field (y, x, 2)")
+    idx = tuple(index) if index is not None else (0, 0)
+    ri, rs = requested if requested is not None else (idx, (x.shape[1], x.shape[0]))
+    crop = x[ri[1] - idx[1]:ri[1] - idx[1] + rs[1], ri[0] - idx[0]:ri[0] - idx[0] + rs[0]]
+    out = [gaussian_f32(np.ascontiguousarray(crop[..., c]), sigma, spacing) for c in range(2)]
+    return np.ascontiguousarray(np.stack(out, axis=-1))
+
+
 def unsharp_kernel(sigma: float) -> np.ndarray:
     """UnsharpMaskFilter's blur kernel (edges.rs:408, 415-424): radius ceil(3 sigma),
     exp(-(d d) / (2 sigma sigma)) through the C library's exp, divided by the

@@ -225,6 +225,37 @@ static void test_slice_by_slice() {
     CHECK(std::fabs(out.get_pixel({{2, 2, z}}) - (float)z) < 1e-5f, "slice %lld", (long long)z);
 }
 
+// DisplacementFieldToBSplineFilter (spatial.rs:1484-1525): a constant field
+// comes back unchanged (the weights sum to one), and a sub-region request is
+// smoothed as an image of its own -- it equals the filter over the crop.
+static void test_displacement_field_to_bspline() {
+  using V2 = VecPixel<float, 2>;
+  std::array<int64_t, 2> z{};
+  auto field = Image<V2, 2>::allocate(Region<2>::make(z, {20, 16}), {1.0, 1.0}, {0.0, 0.0}, V2{});
+  for (int64_t y = 0; y < 16; ++y)
+    for (int64_t x = 0; x < 20; ++x) field.set_pixel({{x, y}}, V2{{0.5f, -1.25f}});
+  DisplacementFieldToBSplineFilter<Image<V2, 2>> f(field);
+  auto out = f.generate_region(f.largest_region());
+  for (int64_t y = 0; y < 16; ++y)
+    for (int64_t x = 0; x < 20; ++x) {
+      const V2 p = out.get_pixel({{x, y}});
+      CHECK(std::fabs(p.c[0] - 0.5f) < 1e-5f && std::fabs(p.c[1] + 1.25f) < 1e-5f, "constant at %lld,%lld",
+            (long long)x, (long long)y);
+    }
+  for (int64_t y = 0; y < 16; ++y)
+    for (int64_t x = 0; x < 20; ++x) field.set_pixel({{x, y}}, V2{{(float)(x * x % 7), (float)(y * 3 % 5)}});
+  const Region<2> sub = Region<2>::make({{4, 3}}, {{9, 7}});
+  auto a = f.generate_region(sub);
+  auto crop = field.generate_region(sub);
+  DisplacementFieldToBSplineFilter<Image<V2, 2>> fc(crop);
+  auto b = fc.generate_region(sub);
+  for (int64_t y = 3; y < 10; ++y)
+    for (int64_t x = 4; x < 13; ++x) {
+      const V2 pa = a.get_pixel({{x, y}}), pb = b.get_pixel({{x, y}});
+      CHECK(pa.c[0] == pb.c[0] && pa.c[1] == pb.c[1], "sub-region at %lld,%lld", (long long)x, (long long)y);
+    }
+}
+
 int main() {
   int ndev = 0;
   itkg_device_count(&ndev);
@@ -245,6 +276,7 @@ int main() {
       {"binomial_blur", test_binomial_blur},
       {"unsharp_mask", test_unsharp_mask},
       {"slice_by_slice", test_slice_by_slice},
+      {"displacement_field_to_bspline", test_displacement_field_to_bspline},
   };
   for (auto& t : tests) {
     const int before = g_fail;

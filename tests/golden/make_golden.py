@@ -20,7 +20,8 @@ and, for the rows beyond the Gaussian (case prefixes):
   recd_  its derivative users (stencils on the smoothing)    filters/edges.rs:686-950
   recz_  ZeroCrossingBasedEdgeDetectionFilter               filters/edges.rs:1019-1052, 480-514
   ush_   UnsharpMaskFilter                                  filters/edges.rs:374-452
-  cal_   SliceBySliceFilter, BSplineDownsampleFilter        filters/spatial.rs:1128-1166, 1284-1340
+  cal_   SliceBySliceFilter, BSplineDownsampleFilter,
+         DisplacementFieldToBSplineFilter                   filters/spatial.rs:1128-1166, 1284-1340, 1484-1525
   dem_   DemonsRegistrationFilter, DiffeomorphicDemons...   filters/registration_methods.rs:39-100, 126-148
   n4_    N4BiasFieldCorrectionFilter                        filters/bias_correction.rs:45-83
 
@@ -658,6 +659,23 @@ def main():
                             ([0, 0, 0], [8, 7, 3]), kind="u8"))
     cases.update(bspline_case("bspline3d_odd", c3, [1.0, 1.0, 1.0]))
     cases.update(bspline_case("bspline2d_aniso", (crng.random((9, 12), dtype=np.float32)), [0.7, 1.5]))
+
+    def dfb_case(name, field, sigma, requested):
+        """DisplacementFieldToBSplineFilter (spatial.rs:1484-1525): the requested crop of a
+        VecPixel<f32, 2> field, each component smoothed by GaussianFilter { sigma } over the crop
+        as an image of its own (whose largest region, and so clamp bounds, is the crop)."""
+        ri, rs = requested
+        out = []
+        for c in range(2):
+            pix = [(field[ri[1] + y, ri[0] + x, c],) for y in range(rs[1]) for x in range(rs[0])]
+            res = generate_region((list(ri), list(rs), pix), [1.0, 1.0], sigma, list(ri), list(rs))
+            out.append(from_ref(res, 1, np.float32))
+        return {f"cal_{name}__in": field, f"cal_{name}__out": np.stack(out, axis=-1),
+                f"cal_{name}__meta": np.array([2, sigma] + list(ri) + list(rs), dtype=np.float64)}
+
+    f2 = (crng.standard_normal((13, 17, 2)) * 1.5).astype(np.float32)
+    cases.update(dfb_case("dfbspline_s2", f2, 2.0, ([0, 0], [17, 13])))
+    cases.update(dfb_case("dfbspline_sub_s1p5", f2, 1.5, ([3, 2], [11, 8])))
     # kernels
     for s, sp in [(1.5, 1.0), (2.0, 1.0), (1.5, 0.7), (1.5, 2.5), (0.5, 1.0), (8.0, 1.0)]:
         cases[f"kernel_{s}_{sp}"] = np.array(build_kernel(s / sp, kernel_radius(s, sp)),

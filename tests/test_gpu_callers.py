@@ -8,7 +8,7 @@ import pytest
 
 import oracle
 from test_gpu_parity import bits_equal, normwise
-from test_oracle_callers import slice_meta
+from test_oracle_callers import dfb_meta, slice_meta
 
 pytestmark = pytest.mark.gpu
 
@@ -88,3 +88,35 @@ def test_slices_take_the_fused_2d_kernels(gpu, which, kernel):
     finally:
         _abi.lib().itkg_debug_set_2d_kernel(0)
 
+
+
+def run_dfb(itkg, field, sigma, requested=None, index=None, host=False, rounding=0):
+    img = itkg.Image(field, index=index, components=2)
+    src = img if host else itkg.DeviceImage.from_host(img)
+    f = itkg.DisplacementFieldToBSplineFilter(src, sigma, rounding=rounding)
+    req = itkg.Region(*requested) if requested else img.region
+    out = f.generate_region(req)
+    return out.data if host else out.download()
+
+
+@pytest.mark.parametrize("name", ["dfbspline_s2", "dfbspline_sub_s1p5"])
+def test_displacement_field_to_bspline_golden(gpu, golden, name):
+    sigma, req = dfb_meta(golden, name)
+    for host in (False, True):
+        assert bits_equal(run_dfb(gpu, golden[f"cal_{name}__in"], sigma, requested=req, host=host),
+                          golden[f"cal_{name}__out"])
+
+
+@pytest.mark.parametrize("shape", [(64, 80), (300, 257), (1700, 2000)])
+def test_displacement_field_to_bspline_random(gpu, shape):
+    """VecPixel<f32, 2> through the 2-D tile kernel (small fields) or the
+    per-axis passes (large ones), sub-regions clamped at the request."""
+    f = np.random.default_rng(sum(shape)).standard_normal(shape + (2,)).astype(np.float32)
+    index = (3, -2)
+    req = ((3 + shape[1] // 5, -2 + shape[0] // 4), (shape[1] // 2, shape[0] // 2))
+    for r in (None, req):
+        want = oracle.displacement_field_to_bspline(f, 2.0, index=index, requested=r)
+        got = run_dfb(gpu, f, 2.0, requested=r, index=index)
+        assert bits_equal(got, want), (shape, r, gpu.last_kernel())
+        got = run_dfb(gpu, f, 2.0, requested=r, index=index, rounding=1)
+        assert normwise(got, want) <= 1e-5

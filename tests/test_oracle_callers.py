@@ -1,8 +1,9 @@
 """Pin the oracle's in-crate callers of GaussianFilter -- SliceBySliceFilter
-(spatial.rs:1284-1340) and BSplineDownsampleFilter (spatial.rs:1128-1166) --
+(spatial.rs:1284-1340), BSplineDownsampleFilter (spatial.rs:1128-1166) and
+DisplacementFieldToBSplineFilter (spatial.rs:1484-1525) --
 against the `cal_*` cases of tests/golden/golden.npz (the pure-Python
 transcription in tests/golden/make_golden.py).  The reference has no tests of
-its own for either filter."""
+its own for these filters."""
 import numpy as np
 import pytest
 
@@ -40,3 +41,27 @@ def test_slice_by_slice_leaves_z_alone():
     z = np.arange(6, dtype=np.float32)[:, None, None] * np.ones((1, 5, 7), np.float32)
     out = oracle.slice_by_slice(z, 1.5)
     assert np.all(np.abs(out - z) <= 1e-6 * np.maximum(1.0, np.abs(z)))
+
+
+def dfb_meta(golden, name):
+    m = golden[f"cal_{name}__meta"]
+    return float(m[1]), ((int(m[2]), int(m[3])), (int(m[4]), int(m[5])))
+
+
+@pytest.mark.parametrize("name", ["dfbspline_s2", "dfbspline_sub_s1p5"])
+def test_displacement_field_to_bspline_oracle_matches_golden(golden, name):
+    sigma, req = dfb_meta(golden, name)
+    got = oracle.displacement_field_to_bspline(golden[f"cal_{name}__in"], sigma, requested=req)
+    assert np.array_equal(got.view(np.uint32), golden[f"cal_{name}__out"].view(np.uint32))
+
+
+def test_displacement_field_to_bspline_clamps_at_the_request():
+    """The Gaussian's largest region is the request: a sub-region result equals
+    the whole-field filter run on the crop, not the crop of the whole-field result."""
+    f = np.random.default_rng(3).standard_normal((20, 24, 2)).astype(np.float32)
+    req = ((5, 4), (12, 10))
+    sub = oracle.displacement_field_to_bspline(f, 1.5, requested=req)
+    crop = np.ascontiguousarray(f[4:14, 5:17])
+    assert np.array_equal(sub, oracle.displacement_field_to_bspline(crop, 1.5))
+    whole = oracle.displacement_field_to_bspline(f, 1.5)
+    assert not np.array_equal(sub, whole[4:14, 5:17])
