@@ -245,7 +245,8 @@ static void test_displacement_field_to_bspline() {
   for (int64_t y = 0; y < 16; ++y)
     for (int64_t x = 0; x < 20; ++x) field.set_pixel({{x, y}}, V2{{(float)(x * x % 7), (float)(y * 3 % 5)}});
   const Region<2> sub = Region<2>::make({{4, 3}}, {{9, 7}});
-  auto a = f.generate_region(sub);
+  DisplacementFieldToBSplineFilter<Image<V2, 2>> fv(field);  // the filter keeps its own copy of the field
+  auto a = fv.generate_region(sub);
   auto crop = field.generate_region(sub);
   DisplacementFieldToBSplineFilter<Image<V2, 2>> fc(crop);
   auto b = fc.generate_region(sub);
