@@ -246,7 +246,9 @@ __device__ __forceinline__ bool fused_range(const Fused3DArgs& a, const CUtensor
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nzr = a.req_hi[2] - a.req_lo[2] + 1;
   const uint32_t sbase = smem_u32(stage0);
-  double dot_acc = 0.0;  // kDot: this thread's share of <ybar, G x>
+  double dot_acc = 0.0;  // kDot: this thread's share of <ybar, G x> (f32 runs of 8 slices folded in)
+  float dot_f = 0.0f;
+  int dot_n = 0;
 
   for (int64_t u = u_begin; u < u_end;) {
     const int64_t tile = u / nzr;
@@ -572,7 +574,12 @@ __device__ __forceinline__ bool fused_range(const Fused3DArgs& a, const CUtensor
 #pragma unroll
           for (int m = 0; m < MY; ++m)
             if (m < nrows_ok) sl = fmaf(vals[m], *reinterpret_cast<const float*>(yrow + m * a.ybar_pitch[1]), sl);
-          dot_acc += (double)sl;
+          dot_f += sl;
+          if (++dot_n == 8) {
+            dot_acc += (double)dot_f;
+            dot_f = 0.0f;
+            dot_n = 0;
+          }
         } else if constexpr (MODE == kAdj) {
           char* orow = obase + (int64_t)(z - a.dst_origin[2]) * a.dst_pitch[2];
 #pragma unroll
@@ -605,6 +612,7 @@ __device__ __forceinline__ bool fused_range(const Fused3DArgs& a, const CUtensor
   }
 #undef ITKG_ON_TIMEOUT
   if constexpr (MODE == kDot) {
+    dot_acc += (double)dot_f;
     // block sum of dot_acc -> partials[blockIdx.x] (fixed order)
     __shared__ double red[NT / 32];
     for (int off = 16; off > 0; off >>= 1) dot_acc += __shfl_down_sync(0xffffffffu, dot_acc, off);

@@ -278,18 +278,29 @@ dim3 grid_small(const VjpAxisArgs& a, int run) {
   return dim3((unsigned)gx, (unsigned)(gy < 65535 ? gy : 65535), (unsigned)(pick3(a.size, od) < 65535 ? pick3(a.size, od) : 65535));
 }
 
-// Per-block f64 partial sums of sum(p * q) over a pitched image.
+// Per-block f64 partial sums of sum(p * q) over a pitched image: each thread
+// sums its products in f32 runs of 16 and folds each run into f64 (an f64
+// operation per element would hold this GPU's slow FP64 pipe for longer than
+// the loads take).
 __global__ void __launch_bounds__(kThreads) k_dot_partials(const DotArgs d, double* partials) {
   const int64_t nx = d.size[0], nxy = d.size[0] * d.size[1];
   const int64_t n = nxy * d.size[2];
   double s = 0.0;
+  float f = 0.0f;
+  int run = 0;
   for (int64_t i = (int64_t)blockIdx.x * kThreads + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * kThreads) {
     const int64_t x = i % nx, y = (i / nx) % d.size[1], z = i / nxy;
     const float a = *reinterpret_cast<const float*>(px(d.p, d.p_pitch, x, y, z));
     const float b = *reinterpret_cast<const float*>(px(d.q, d.q_pitch, x, y, z));
-    s += (double)a * (double)b;
+    f = fmaf(a, b, f);
+    if (++run == 16) {
+      s += (double)f;
+      f = 0.0f;
+      run = 0;
+    }
   }
+  s += (double)f;
   __shared__ double red[kThreads];
   red[threadIdx.x] = s;
   __syncthreads();

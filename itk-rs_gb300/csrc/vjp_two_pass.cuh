@@ -138,7 +138,12 @@ __global__ void __launch_bounds__(256, 2)
   }
   __syncthreads();
   uint32_t phase_bits = 0;
-  double dot = 0.0;  // dual-dot mode: this thread's share
+  // dual-dot mode: this thread's share, summed in f32 over 4 slices at a time
+  // and folded into f64 then (an f64 add per voxel would hold this GPU's slow
+  // FP64 pipe longer than the whole f32 arithmetic)
+  double dot = 0.0;
+  float fdot = 0.0f;
+  int fdot_n = 0;
 
   const int64_t u_begin = a.units * blockIdx.x / gridDim.x;
   const int64_t u_end = a.units * (blockIdx.x + 1) / gridDim.x;
@@ -376,13 +381,21 @@ __global__ void __launch_bounds__(256, 2)
           unpack2(yd[m], d0, d1);
           float s = fmaf(v0, pu2[m][0], d0 * pu[m][0]);
           if (c1ok) s = fmaf(v1, pu2[m][1], fmaf(d1, pu[m][1], s));
-          dot += (double)s;
+          fdot += s;
+        }
+      }
+      if constexpr (MODE == kDualDot) {
+        if (++fdot_n == 4) {
+          dot += (double)fdot;
+          fdot = 0.0f;
+          fdot_n = 0;
         }
       }
     }
     __syncthreads();
   }
   if constexpr (MODE == kDualDot) {
+    dot += (double)fdot;
     const int lane = tid & 31, warp = tid >> 5;
     for (int o = 16; o > 0; o >>= 1) dot += __shfl_down_sync(0xffffffffu, dot, o);
     if (lane == 0) red[warp] = dot;
