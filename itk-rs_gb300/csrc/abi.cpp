@@ -466,6 +466,28 @@ static itkg_status generate_device(const itkg_image& in, const itkg_region& larg
   return run_per_axis(in, largest, requested, prm, plan, out, s);
 }
 
+itkg_status tile2d_geom_for(const itkg_image& in, const itkg_region& largest, const itkg_region& requested,
+                            const itkg_gaussian_params& prm, const itkg_image& out, FusedGeom* g,
+                            std::vector<std::vector<float>>* weights) {
+  if (prm.arithmetic == ITKG_ARITH_PIXEL_U8 || prm.algorithm == ITKG_ALGO_PER_AXIS) return ITKG_ERROR_UNSUPPORTED;
+  const int D = in.dim;
+  if (D != 2) return ITKG_ERROR_UNSUPPORTED;
+  if (out.dim != D || out.components != in.components || region_len(requested, D) == 0 ||
+      !region_contains(largest, requested, D) || !region_contains(out.region, requested, D))
+    return ITKG_ERROR_UNSUPPORTED;
+  Plan plan;
+  KernelSpec ks;
+  ks.sigma = prm.sigma;
+  if (make_plan(in, requested, largest, ks, &plan) != ITKG_SUCCESS) return ITKG_ERROR_UNSUPPORTED;
+  if (!plan.symmetric || !region_contains(in.region, plan.in_reg, D)) return ITKG_ERROR_UNSUPPORTED;
+  make_fused_geom(in, largest, requested, prm, plan, out, g);
+  const float* w[kMaxDim] = {nullptr, nullptr, nullptr};
+  for (int d = 0; d < D; ++d) w[d] = plan.w32[d].data();
+  if (launch_tile2d(*g, w, nullptr, /*dry_run=*/true) != ITKG_SUCCESS) return ITKG_ERROR_UNSUPPORTED;
+  weights->assign(plan.w32, plan.w32 + D);
+  return ITKG_SUCCESS;
+}
+
 itkg_status fused_geom_for(const itkg_image& in, const itkg_region& largest,
                            const itkg_region& requested, const itkg_gaussian_params& prm,
                            const itkg_image& out, FusedGeom* g,

@@ -55,6 +55,7 @@ struct itkg_batch {
   std::string described;
   uint64_t launches_per_run = 0;
   itkg::FusedMultiPlan* fused = nullptr;  // request tables of the multi-request launches
+  itkg::Tile2DMultiPlan* tiles2d = nullptr;  // the 2-D items' multi-request tile launches
 };
 
 namespace itkg {
@@ -188,6 +189,7 @@ itkg_status itkg_batch_destroy(itkg_batch* b) {
   if (b->exec) cudaGraphExecDestroy(b->exec);
   if (b->graph) cudaGraphDestroy(b->graph);
   fused_multi_free(b->fused);
+  tile2d_multi_free(b->tiles2d);
   delete b;
   return ITKG_SUCCESS;
 }
@@ -242,11 +244,22 @@ itkg_status itkg_batch_plan(itkg_batch* b, int32_t flags, void* stream) {
   for (size_t i = 0; i < b->fwd.size(); ++i) ITKG_TRY(choose_algorithm(b->fwd[i], tune, user, &algo[i]));
   ITKG_CUDA(cudaStreamSynchronize(user));
 
-  // 2. group fused forward items by kernel class for multi-item launches
-  std::vector<FusedGeom> fused_geoms;
-  std::vector<std::vector<std::vector<float>>> fused_w;
+  // 2. group fused forward items by kernel class for multi-item launches: the
+  // 3-D items the fused kernel covers, and the 2-D items the tile kernel covers
+  std::vector<FusedGeom> fused_geoms, tile_geoms;
+  std::vector<std::vector<std::vector<float>>> fused_w, tile_w;
   std::vector<size_t> per_item;
   for (size_t i = 0; i < b->fwd.size(); ++i) {
+    if (b->fwd[i].in.dim == 2 && algo[i] != ITKG_ALGO_PER_AXIS) {
+      FusedGeom g;
+      std::vector<std::vector<float>> w;
+      if (tile2d_geom_for(b->fwd[i].in, b->fwd[i].largest, b->fwd[i].requested, b->fwd[i].prm, b->fwd[i].out, &g,
+                          &w) == ITKG_SUCCESS) {
+        tile_geoms.push_back(g);
+        tile_w.push_back(std::move(w));
+        continue;
+      }
+    }
     if (algo[i] == ITKG_ALGO_PER_AXIS || algo[i] == ITKG_ALGO_TWO_PASS) {
       per_item.push_back(i);
       continue;
@@ -264,22 +277,24 @@ itkg_status itkg_batch_plan(itkg_batch* b, int32_t flags, void* stream) {
   }
 
   if (!fused_geoms.empty()) ITKG_TRY(fused_multi_prepare(fused_geoms, fused_w, &b->fused, &b->plan_lines));
+  if (!tile_geoms.empty()) ITKG_TRY(tile2d_multi_prepare(tile_geoms, tile_w, &b->tiles2d, &b->plan_lines));
 
   // 3. spread the work over kLanes lanes, longest first onto the least loaded
   // lane; the multi-request fused launch counts as one job
   struct Job {
     double work;
-    int kind;  // 0 fused multi-request launch, 1 forward item, 2 VJP item
+    int kind;  // 0 fused multi-request launch, 1 forward item, 2 VJP item, 3 2-D tile class launch
     size_t i;
   };
   std::vector<Job> jobs;
   if (b->fused) {
     double wsum = 0.0;
     for (size_t i = 0; i < b->fwd.size(); ++i)
-      if (std::find(per_item.begin(), per_item.end(), i) == per_item.end())
+      if (b->fwd[i].in.dim == 3 && std::find(per_item.begin(), per_item.end(), i) == per_item.end())
         wsum += work_of(b->fwd[i].in, b->fwd[i].requested, b->fwd[i].prm.sigma);
     jobs.push_back({wsum, 0, 0});
   }
+  for (int q = 0; q < tile2d_multi_groups(b->tiles2d); ++q) jobs.push_back({tile2d_multi_work(b->tiles2d, q), 3, (size_t)q});
   for (size_t i : per_item) jobs.push_back({work_of(b->fwd[i].in, b->fwd[i].requested, b->fwd[i].prm.sigma), 1, i});
   for (size_t i = 0; i < b->vjp.size(); ++i)
     jobs.push_back({3.0 * work_of(b->vjp[i].x, b->vjp[i].x.region, b->vjp[i].prm.sigma), 2, i});
@@ -330,6 +345,9 @@ itkg_status itkg_batch_plan(itkg_batch* b, int32_t flags, void* stream) {
     if (jobs[j].kind == 0) {
       st = fused_multi_launch(b->fused, ls);
       if (st == ITKG_SUCCESS) b->plan_lines.push_back("fused multi-request launches" + lane);
+    } else if (jobs[j].kind == 3) {
+      st = tile2d_multi_launch(b->tiles2d, (int)jobs[j].i, ls);
+      if (st == ITKG_SUCCESS) b->plan_lines.push_back("2-D tile class " + std::to_string(jobs[j].i) + lane);
     } else if (jobs[j].kind == 1) {
       const size_t i = jobs[j].i;
       itkg_batch::Fwd f = b->fwd[i];

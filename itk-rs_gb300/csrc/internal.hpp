@@ -118,6 +118,21 @@ itkg_status launch_fused2d(const FusedGeom& g, const float* const w[kMaxDim], vo
 // tile2d.cu: the same geometries on 64 x 32 tiles staged at once (small and
 // medium images); launch_fused2d chooses between the two.
 itkg_status launch_tile2d(const FusedGeom& g, const float* const w[kMaxDim], void* stream, bool dry_run);
+// tile2d.cu: many 2-D requests as one tile-kernel launch per kernel class
+// (radius, components, rounding); the batch's 2-D items.
+struct Tile2DMultiPlan;
+itkg_status tile2d_multi_prepare(const std::vector<FusedGeom>& geoms,
+                                 const std::vector<std::vector<std::vector<float>>>& weights,
+                                 Tile2DMultiPlan** plan, std::vector<std::string>* lines);
+int tile2d_multi_groups(const Tile2DMultiPlan* plan);
+double tile2d_multi_work(const Tile2DMultiPlan* plan, int group);
+itkg_status tile2d_multi_launch(const Tile2DMultiPlan* plan, int group, void* stream);
+void tile2d_multi_free(Tile2DMultiPlan* plan);
+// abi.cpp: the 2-D geometry and f32 weights of one request for the tile
+// kernel (ITKG_ERROR_UNSUPPORTED when it does not apply).
+itkg_status tile2d_geom_for(const itkg_image& in, const itkg_region& largest, const itkg_region& requested,
+                            const itkg_gaussian_params& prm, const itkg_image& out, FusedGeom* g,
+                            std::vector<std::vector<float>>* weights);
 // abi.cpp: the 2-D kernel forced by itkg_debug_set_2d_kernel (0: chosen by size,
 // 1: the tile kernel, 2: the row-marching kernel).
 int kernel2d_override();

@@ -23,6 +23,7 @@
 #include <climits>
 #include <cstring>
 #include <mutex>
+#include <string>
 #include <utility>
 #include <vector>
 
@@ -72,14 +73,14 @@ __device__ __forceinline__ void cp4(float* dst, const void* src) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
 }
 
+// One tile t of the launch described by `a` (weights wx / wy in registers).
 template <int R, int C, bool REF>
-__global__ void __launch_bounds__(kT2Threads) k_tile2d(const Tile2DArgs a) {
+__device__ __forceinline__ void tile2d_body(const Tile2DArgs& a, const float (&wx)[2 * R + 1],
+                                            const float (&wy)[2 * R + 1], int64_t t, float* sm) {
   using G = T2Cfg<R, C>;
   constexpr int K = G::K, IW = G::IW, IWP = G::IWP, IH = G::IH, WIN = G::WIN;
-  extern __shared__ __align__(16) float sm[];
   float* const sin = sm;             // [C][IH][IWP]
   float* const sxf = sm + G::IN;     // [C][IH][kTW]
-  const int64_t t = blockIdx.x;
   const int64_t per_slice = (int64_t)a.ntx * a.nty;
   const int64_t zq = t / per_slice;
   const int ti = (int)(t - zq * per_slice);
@@ -118,7 +119,7 @@ __global__ void __launch_bounds__(kT2Threads) k_tile2d(const Tile2DArgs a) {
     for (int m = 0; m < 4; ++m) {
       float acc = 0.0f;
 #pragma unroll
-      for (int k = 0; k < K; ++k) acc = REF ? tap<true>(acc, v[m + k], a.wx[k]) : fmaf(v[m + k], a.wx[k], acc);
+      for (int k = 0; k < K; ++k) acc = REF ? tap<true>(acc, v[m + k], wx[k]) : fmaf(v[m + k], wx[k], acc);
       o[m] = acc;
     }
     *reinterpret_cast<float4*>(sxf + cr * kTW + 4 * q) = make_float4(o[0], o[1], o[2], o[3]);
@@ -146,7 +147,7 @@ __global__ void __launch_bounds__(kT2Threads) k_tile2d(const Tile2DArgs a) {
       if (gy0 + m > a.req_hi[1]) break;
       float acc = 0.0f;
 #pragma unroll
-      for (int k = 0; k < K; ++k) acc = REF ? tap<true>(acc, v[m + k], a.wy[k]) : fmaf(v[m + k], a.wy[k], acc);
+      for (int k = 0; k < K; ++k) acc = REF ? tap<true>(acc, v[m + k], wy[k]) : fmaf(v[m + k], wy[k], acc);
       char* const q = ob + (int64_t)m * a.dst_pitch[1];
       switch (a.out_dtype) {
         case ITKG_F32: *reinterpret_cast<float*>(q) = acc; break;
@@ -158,15 +159,58 @@ __global__ void __launch_bounds__(kT2Threads) k_tile2d(const Tile2DArgs a) {
   }
 }
 
+template <int R, int C, bool REF>
+__global__ void __launch_bounds__(kT2Threads) k_tile2d(const Tile2DArgs a) {
+  extern __shared__ __align__(16) float sm[];
+  float wx[2 * R + 1], wy[2 * R + 1];
+#pragma unroll
+  for (int k = 0; k < 2 * R + 1; ++k) wx[k] = a.wx[k], wy[k] = a.wy[k];
+  tile2d_body<R, C, REF>(a, wx, wy, blockIdx.x, sm);
+}
+
+// Many requests of one class (radius, components, rounding) in one launch:
+// request q owns the CTAs [starts[q], starts[q + 1]); each CTA copies its
+// request's arguments to shared memory and its weights to registers.
+template <int R, int C, bool REF>
+__global__ void __launch_bounds__(kT2Threads) k_tile2d_multi(const Tile2DArgs* reqs, const int32_t* starts, int nreq) {
+  extern __shared__ __align__(16) float sm[];
+  __shared__ Tile2DArgs sa;
+  __shared__ int sq;
+  if (threadIdx.x == 0) {
+    int lo = 0, hi = nreq - 1;  // the last q with starts[q] <= blockIdx.x
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) / 2;
+      if (starts[mid] <= (int)blockIdx.x) lo = mid;
+      else hi = mid - 1;
+    }
+    sq = lo;
+  }
+  __syncthreads();
+  const int q = sq;
+  {
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(reqs + q);
+    uint32_t* dst = reinterpret_cast<uint32_t*>(&sa);
+    for (int i = threadIdx.x; i < (int)(sizeof(Tile2DArgs) / 4); i += kT2Threads) dst[i] = src[i];
+  }
+  __syncthreads();
+  float wx[2 * R + 1], wy[2 * R + 1];
+#pragma unroll
+  for (int k = 0; k < 2 * R + 1; ++k) wx[k] = sa.wx[k], wy[k] = sa.wy[k];
+  tile2d_body<R, C, REF>(sa, wx, wy, (int64_t)blockIdx.x - starts[q], sm);
+}
+
 using FnT2 = void (*)(const Tile2DArgs);
+using FnT2M = void (*)(const Tile2DArgs*, const int32_t*, int);
 struct EntryT2 {
   int r, comps;
-  FnT2 fn[2];  // [ref]
+  FnT2 fn[2];    // [ref]
+  FnT2M multi[2];
   size_t smem;
 };
 template <int R, int C>
 EntryT2 make_t2() {
-  return EntryT2{R, C, {k_tile2d<R, C, false>, k_tile2d<R, C, true>}, T2Cfg<R, C>::SMEM};
+  return EntryT2{R, C, {k_tile2d<R, C, false>, k_tile2d<R, C, true>},
+                 {k_tile2d_multi<R, C, false>, k_tile2d_multi<R, C, true>}, T2Cfg<R, C>::SMEM};
 }
 const EntryT2 kTableT2[] = {
     make_t2<1, 1>(),  make_t2<2, 1>(),  make_t2<3, 1>(),  make_t2<4, 1>(),  make_t2<5, 1>(),  make_t2<6, 1>(),
@@ -182,8 +226,8 @@ bool fits32t(int64_t v) { return v >= INT_MIN && v <= INT_MAX; }
 
 // cudaFuncSetAttribute once per kernel and device
 std::mutex g_t2_mu;
-std::vector<std::pair<FnT2, int>> g_t2_ready;
-itkg_status prepare_t2(FnT2 fn, size_t smem) {
+std::vector<std::pair<const void*, int>> g_t2_ready;
+itkg_status prepare_t2(const void* fn, size_t smem) {
   int dev = 0;
   cudaError_t err = cudaGetDevice(&dev);
   if (err != cudaSuccess) return set_error(ITKG_ERROR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(err));
@@ -196,9 +240,10 @@ itkg_status prepare_t2(FnT2 fn, size_t smem) {
   return ITKG_SUCCESS;
 }
 
-}  // namespace
-
-itkg_status launch_tile2d(const FusedGeom& g, const float* const w[kMaxDim], void* stream, bool dry_run) {
+// The launch arguments of one request, its table entry and tile count;
+// ITKG_ERROR_UNSUPPORTED (no error set) when the tile kernel does not cover it.
+itkg_status build_t2(const FusedGeom& g, const float* const w[kMaxDim], Tile2DArgs* out, const EntryT2** entry,
+                     int64_t* ntiles) {
   const bool slices = g.dim == 3 && g.radius[2] == 0 && w[2] && w[2][0] == 1.0f;
   if (g.u8pix) return ITKG_ERROR_UNSUPPORTED;
   if ((g.dim != 2 && !slices) || g.in_dtype != ITKG_F32 || g.out_dtype == ITKG_I16) return ITKG_ERROR_UNSUPPORTED;
@@ -217,9 +262,7 @@ itkg_status launch_tile2d(const FusedGeom& g, const float* const w[kMaxDim], voi
   const int64_t nz = slices ? g.req_size[2] : 1;
   const int64_t ntx = (g.req_size[0] + kTW - 1) / kTW, nty = (g.req_size[1] + kTH - 1) / kTH;
   if (ntx * nty * nz > INT_MAX) return ITKG_ERROR_UNSUPPORTED;
-  if (dry_run) return ITKG_SUCCESS;
-
-  Tile2DArgs a;
+  Tile2DArgs& a = *out;
   std::memset(&a, 0, sizeof a);
   a.src = static_cast<const char*>(g.src);
   a.dst = static_cast<char*>(g.dst);
@@ -244,17 +287,120 @@ itkg_status launch_tile2d(const FusedGeom& g, const float* const w[kMaxDim], voi
   a.out_dtype = g.out_dtype;
   a.out_esz = dtype_size(g.out_dtype);
   for (int k = 0; k < 2 * e->r + 1; ++k) a.wx[k] = w[0][k], a.wy[k] = w[1][k];
+  *entry = e;
+  *ntiles = ntx * nty * nz;
+  return ITKG_SUCCESS;
+}
+
+}  // namespace
+
+itkg_status launch_tile2d(const FusedGeom& g, const float* const w[kMaxDim], void* stream, bool dry_run) {
+  Tile2DArgs a;
+  const EntryT2* e = nullptr;
+  int64_t ntiles = 0;
+  {
+    const itkg_status st = build_t2(g, w, &a, &e, &ntiles);
+    if (st != ITKG_SUCCESS) return st;
+  }
+  if (dry_run) return ITKG_SUCCESS;
   const bool ref = g.rounding == ITKG_ROUND_REFERENCE;
   const FnT2 fn = e->fn[ref ? 1 : 0];
   {
-    const itkg_status pst = prepare_t2(fn, e->smem);
+    const itkg_status pst = prepare_t2(reinterpret_cast<const void*>(fn), e->smem);
     if (pst != ITKG_SUCCESS) return pst;
   }
-  fn<<<(unsigned)(ntx * nty * nz), kT2Threads, e->smem, static_cast<cudaStream_t>(stream)>>>(a);
+  fn<<<(unsigned)ntiles, kT2Threads, e->smem, static_cast<cudaStream_t>(stream)>>>(a);
   const cudaError_t err = cudaGetLastError();
   note_launch(ref ? "tile2d_f32_ref" : "tile2d_f32_fma");
   if (err != cudaSuccess) return set_error(ITKG_ERROR_CUDA, "tile2d launch: %s", cudaGetErrorString(err));
   return ITKG_SUCCESS;
+}
+
+// Multi-request launches: the requests grouped by kernel class, one launch per
+// class with the requests' arguments and CTA ranges in device tables.
+struct Tile2DMultiGroup {
+  const EntryT2* e = nullptr;
+  bool ref = false;
+  std::vector<Tile2DArgs> reqs;
+  std::vector<int32_t> starts;  // CTA ranges, starts.back() = CTAs in all
+  Tile2DArgs* d_reqs = nullptr;
+  int32_t* d_starts = nullptr;
+  double work = 0.0;
+};
+struct Tile2DMultiPlan {
+  std::vector<Tile2DMultiGroup> groups;
+};
+
+itkg_status tile2d_multi_prepare(const std::vector<FusedGeom>& geoms,
+                                 const std::vector<std::vector<std::vector<float>>>& weights,
+                                 Tile2DMultiPlan** out, std::vector<std::string>* lines) {
+  Tile2DMultiPlan* plan = new Tile2DMultiPlan();
+  *out = plan;
+  for (size_t i = 0; i < geoms.size(); ++i) {
+    const FusedGeom& g = geoms[i];
+    const float* w[kMaxDim] = {nullptr, nullptr, nullptr};
+    for (int d = 0; d < g.dim && d < (int)weights[i].size(); ++d) w[d] = weights[i][d].data();
+    Tile2DArgs a;
+    const EntryT2* e = nullptr;
+    int64_t ntiles = 0;
+    const itkg_status st = build_t2(g, w, &a, &e, &ntiles);
+    if (st != ITKG_SUCCESS) return st == ITKG_ERROR_UNSUPPORTED ? set_error(st, "no tile kernel for 2-D item %zu", i) : st;
+    const bool ref = g.rounding == ITKG_ROUND_REFERENCE;
+    Tile2DMultiGroup* grp = nullptr;
+    for (Tile2DMultiGroup& q : plan->groups)
+      if (q.e == e && q.ref == ref) grp = &q;
+    if (!grp) {
+      plan->groups.push_back(Tile2DMultiGroup());
+      grp = &plan->groups.back();
+      grp->e = e;
+      grp->ref = ref;
+      grp->starts.push_back(0);
+    }
+    if ((int64_t)grp->starts.back() + ntiles > INT_MAX) return set_error(ITKG_ERROR_UNSUPPORTED, "too many tiles");
+    grp->reqs.push_back(a);
+    grp->starts.push_back(grp->starts.back() + (int32_t)ntiles);
+    grp->work += (double)g.req_size[0] * g.req_size[1] * g.comps * (double)(2 * e->r + 1 + 4);
+  }
+  for (Tile2DMultiGroup& q : plan->groups) {
+    cudaError_t err = cudaMalloc(&q.d_reqs, sizeof(Tile2DArgs) * q.reqs.size());
+    if (err == cudaSuccess) err = cudaMalloc(&q.d_starts, sizeof(int32_t) * q.starts.size());
+    if (err == cudaSuccess)
+      err = cudaMemcpy(q.d_reqs, q.reqs.data(), sizeof(Tile2DArgs) * q.reqs.size(), cudaMemcpyHostToDevice);
+    if (err == cudaSuccess)
+      err = cudaMemcpy(q.d_starts, q.starts.data(), sizeof(int32_t) * q.starts.size(), cudaMemcpyHostToDevice);
+    if (err != cudaSuccess) return set_error(ITKG_ERROR_CUDA, "tile2d multi tables: %s", cudaGetErrorString(err));
+    const itkg_status pst = prepare_t2(reinterpret_cast<const void*>(q.e->multi[q.ref ? 1 : 0]), q.e->smem);
+    if (pst != ITKG_SUCCESS) return pst;
+    if (lines)
+      lines->push_back(std::string(q.ref ? "tile2d_f32_ref" : "tile2d_f32_fma") + " multi-request launch: r=" +
+                       std::to_string(q.e->r) + ", " + std::to_string(q.e->comps) + " components, " +
+                       std::to_string(q.reqs.size()) + " requests, " + std::to_string(q.starts.back()) + " CTAs");
+  }
+  return ITKG_SUCCESS;
+}
+
+int tile2d_multi_groups(const Tile2DMultiPlan* plan) { return plan ? (int)plan->groups.size() : 0; }
+
+double tile2d_multi_work(const Tile2DMultiPlan* plan, int group) { return plan->groups[group].work; }
+
+itkg_status tile2d_multi_launch(const Tile2DMultiPlan* plan, int group, void* stream) {
+  const Tile2DMultiGroup& q = plan->groups[group];
+  const FnT2M fn = q.e->multi[q.ref ? 1 : 0];
+  fn<<<(unsigned)q.starts.back(), kT2Threads, q.e->smem, static_cast<cudaStream_t>(stream)>>>(
+      q.d_reqs, q.d_starts, (int)q.reqs.size());
+  note_launch(q.ref ? "tile2d_multi_f32_ref" : "tile2d_multi_f32_fma");
+  const cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess) return set_error(ITKG_ERROR_CUDA, "tile2d multi launch: %s", cudaGetErrorString(err));
+  return ITKG_SUCCESS;
+}
+
+void tile2d_multi_free(Tile2DMultiPlan* plan) {
+  if (!plan) return;
+  for (Tile2DMultiGroup& q : plan->groups) {
+    if (q.d_reqs) cudaFree(q.d_reqs);
+    if (q.d_starts) cudaFree(q.d_starts);
+  }
+  delete plan;
 }
 
 }  // namespace itkg

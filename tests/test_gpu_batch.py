@@ -74,6 +74,50 @@ def test_batch_mixed_2d_vecpixel_and_3d(gpu):
         assert np.array_equal(o.download().view(np.uint32), want.view(np.uint32))
 
 
+@pytest.mark.parametrize("rounding", ["reference", "fma"])
+def test_batch_2d_items_in_multi_request_tile_launches(gpu, rounding):
+    """2-D items (1, 2 and 3 components, radii 1..12, sub-regions of images
+    with offset indices, several items per kernel class) run as multi-request
+    tile launches, one per class; each output equals the oracle (bit-exact in
+    reference rounding) and replays rewrite it."""
+    from itkg import _abi
+    rnd = gpu.ROUND_REFERENCE if rounding == "reference" else gpu.ROUND_FMA
+    rng = np.random.default_rng(77)
+    b = gpu.Batch()
+    cases = []
+    for i in range(24):
+        comps = (1, 2, 3)[i % 3]
+        shape = tuple(int(v) for v in rng.integers(20, 300, 2))
+        arr = rng.standard_normal(shape + ((comps,) if comps > 1 else ())).astype(np.float32)
+        sigma = (0.6, 1.5, 2.2, 4.0)[i % 4]
+        index = (int(rng.integers(-5, 5)), int(rng.integers(-5, 5)))
+        img = gpu.Image(arr, index=index, components=comps)
+        d = gpu.DeviceImage.from_host(img)
+        req = None
+        if i % 2:
+            ri = (index[0] + shape[1] // 4, index[1] + shape[0] // 3)
+            req = (ri, (shape[1] // 2, shape[0] // 2))
+        o = b.add(d, sigma, rounding=rnd, requested=gpu.Region(*req) if req else None)
+        cases.append((arr, sigma, comps, index, req, o))
+    b.plan()
+    plan = b.describe()
+    assert "tile2d" in plan and "multi-request" in plan, plan
+    for rep in range(2):
+        for *_, o in cases:  # poison the outputs so the replay must rewrite them
+            sx, sy = o.region.size[:2]
+            nbytes = (sy - 1) * o.c.pitch[1] + sx * o.c.pitch[0]
+            _abi.check(_abi.lib().itkg_memset_device(ctypes.c_void_p(o.c.data), 0xFF, nbytes, None))
+        b.run()
+        gpu.Stream().synchronize()
+        for arr, sigma, comps, index, req, o in cases:
+            want = oracle.gaussian_f32(arr, sigma, comps=comps, index=index, requested=req)
+            got = o.download()
+            if rnd == gpu.ROUND_REFERENCE:
+                assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), (arr.shape, sigma, req)
+            else:
+                assert np.abs(got - want).max() / np.abs(want).max() <= 1e-5
+
+
 def test_batch_vjp_items_match_single_vjp(gpu):
     from itkg import _abi
     L = _abi.lib()
