@@ -1183,8 +1183,10 @@ itkg_status itkg_unsharp_mask_generate_region(const itkg_image* input, const itk
   if (!params) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "params is NULL");
   ITKG_TRY(validate_image(input, "input"));
   ITKG_TRY(validate_image(output, "output"));
-  ITKG_TRY(filter_components(input, "input"));
-  ITKG_TRY(filter_components(output, "output"));
+  // the point-wise kernels take scalar and 3-component pixels
+  for (const itkg_image* im : {input, output})
+    if (im->components != 1 && im->components != 3)
+      return set_error(ITKG_ERROR_UNSUPPORTED, "UnsharpMaskFilter: components must be 1 or 3");
   if (!largest || !requested) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "region is NULL");
   if (params->reserved != 0) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "reserved must be 0");
   if (params->rounding != ITKG_ROUND_REFERENCE && params->rounding != ITKG_ROUND_FMA)
