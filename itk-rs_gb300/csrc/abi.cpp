@@ -1184,7 +1184,8 @@ itkg_status itkg_unsharp_mask_generate_region(const itkg_image* input, const itk
   ITKG_TRY(validate_image(input, "input"));
   ITKG_TRY(validate_image(output, "output"));
   // the point-wise kernels take scalar and 3-component pixels
-  for (const itkg_image* im : {input, output})
+  const itkg_image* const ims[2] = {input, output};
+  for (const itkg_image* im : ims)
     if (im->components != 1 && im->components != 3)
       return set_error(ITKG_ERROR_UNSUPPORTED, "UnsharpMaskFilter: components must be 1 or 3");
   if (!largest || !requested) return set_error(ITKG_ERROR_INVALID_ARGUMENT, "region is NULL");
