@@ -18,6 +18,7 @@ struct Entry {
   size_t xy_smem[2];
   int bw, ih, tx, ty;
   ZAFn z;
+  ZAFn z2;  // both z adjoints in one pass
 };
 
 template <int R>
@@ -25,7 +26,7 @@ Entry make() {
   using A = CfgXYV<R, kAdjoint>;
   using Dd = CfgXYV<R, kDualDot>;
   return Entry{R, {k_xy_vjp<R, kAdjoint>, k_xy_vjp<R, kDualDot>}, {A::SMEM, Dd::SMEM}, A::BW, A::IH, A::TX, A::TY,
-               k_z_adj<R>};
+               k_z_adj<R>, k_z_adj2<R>};
 }
 
 const Entry kTable[] = {make<1>(), make<2>(), make<3>(),  make<4>(),  make<5>(),  make<6>(),
@@ -38,6 +39,7 @@ const Entry* find(int r) {
 }
 
 size_t z_smem(int r) { return (size_t)(2 * r + 1) * 256 * 16; }
+size_t z2_smem(int r) { return (size_t)(2 * r + 1) * 256 * 8; }
 
 bool aligned16(const itkg_image& im) {
   return ((uintptr_t)im.data & 15) == 0 && im.pitch[0] == 4 && (im.pitch[1] & 15) == 0 && (im.pitch[2] & 15) == 0;
@@ -107,18 +109,35 @@ itkg_status launch_vjp_two_pass(const VjpTwoPass& v, void* stream, bool dry_run)
   za.nqx = (int32_t)((nx + 3) / 4);
   za.units = ((int64_t)za.nqx * ny + 255) / 256 * nz;
   int res_z = 0, res_xy = 0;
-  if (st == ITKG_SUCCESS)
-    st = max_resident_ctas(reinterpret_cast<const void*>(ez->z), vjp2::z_smem(RZ), 256, &res_z);
-  for (int pass = 0; pass < (want_s ? 2 : 1) && st == ITKG_SUCCESS; ++pass) {
-    const float* wz = pass == 0 ? v.w[2] : v.dw[2];
-    for (int k = 0; k < 2 * RZ + 1; ++k) za.wz2[k] = splat2_host(wz[k]);
-    vjp2::prefix(wz, RZ, za.pz);
-    za.out = static_cast<char*>(pass == 0 ? pu : pu2);
-    const int64_t g = std::min<int64_t>(za.units, res_z);
-    ez->z<<<(unsigned)g, 256, vjp2::z_smem(RZ), s>>>(za);
-    note_launch("z_adjoint_f32");
-    const cudaError_t err = cudaGetLastError();
-    if (err != cudaSuccess) st = set_error(ITKG_ERROR_CUDA, "z adjoint launch: %s", cudaGetErrorString(err));
+  for (int k = 0; k < 2 * RZ + 1; ++k) za.wz2[k] = splat2_host(v.w[2][k]);
+  vjp2::prefix(v.w[2], RZ, za.pz);
+  za.out = static_cast<char*>(pu);
+  if (want_s) {
+    // U and U' in one pass over ybar (two columns per thread, both weight sets)
+    for (int k = 0; k < 2 * RZ + 1; ++k) za.wz2d[k] = splat2_host(v.dw[2][k]);
+    vjp2::prefix(v.dw[2], RZ, za.pzd);
+    za.out2 = static_cast<char*>(pu2);
+    za.npx = (int32_t)((nx + 1) / 2);
+    za.units = ((int64_t)za.npx * ny + 255) / 256 * nz;
+    if (st == ITKG_SUCCESS)
+      st = max_resident_ctas(reinterpret_cast<const void*>(ez->z2), vjp2::z2_smem(RZ), 256, &res_z);
+    if (st == ITKG_SUCCESS) {
+      const int64_t g = std::min<int64_t>(za.units, res_z);
+      ez->z2<<<(unsigned)g, 256, vjp2::z2_smem(RZ), s>>>(za);
+      note_launch("z_adjoint2_f32");
+      const cudaError_t err = cudaGetLastError();
+      if (err != cudaSuccess) st = set_error(ITKG_ERROR_CUDA, "z adjoint launch: %s", cudaGetErrorString(err));
+    }
+  } else {
+    if (st == ITKG_SUCCESS)
+      st = max_resident_ctas(reinterpret_cast<const void*>(ez->z), vjp2::z_smem(RZ), 256, &res_z);
+    if (st == ITKG_SUCCESS) {
+      const int64_t g = std::min<int64_t>(za.units, res_z);
+      ez->z<<<(unsigned)g, 256, vjp2::z_smem(RZ), s>>>(za);
+      note_launch("z_adjoint_f32");
+      const cudaError_t err = cudaGetLastError();
+      if (err != cudaSuccess) st = set_error(ITKG_ERROR_CUDA, "z adjoint launch: %s", cudaGetErrorString(err));
+    }
   }
 
   // x-y kernels

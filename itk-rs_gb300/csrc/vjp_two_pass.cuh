@@ -70,6 +70,12 @@ struct ZAArgs {
   int64_t units;           // quad blocks * nz
   f2_t wz2[kMaxK];         // z weights (w or dw) as splat pairs
   float pz[kMaxR + 1];     // their exclusive prefix sums
+  // k_z_adj2: the second output (U' = dGz^T ybar) and its weights
+  char* out2;
+  int32_t npx;             // column pairs per row
+  int32_t pad2_;
+  f2_t wz2d[kMaxK];
+  float pzd[kMaxR + 1];
 };
 
 template <int R, int MODE>
@@ -506,6 +512,107 @@ __global__ void __launch_bounds__(256, RZ <= 8 ? 2 : 1) k_z_adj(const __grid_con
               if (c < ncols) reinterpret_cast<float*>(dz)[c] = o[c];
           }
           dz += a.out_pitch[2];
+        }
+      }
+    }
+    fusedk::cp_async_wait<0>();
+  }
+}
+
+// Both z adjoints at once: U = Gz^T ybar and U' = dGz^T ybar from one pass over
+// ybar.  One thread marches one pair of columns (8-byte loads into its own
+// cp.async ring) with two rings of 2 RZ + 1 packed accumulators, one per
+// weight set; otherwise as k_z_adj.
+__device__ __forceinline__ void cp_async8(uint32_t s, const void* g) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(g) : "memory");
+}
+
+template <int RZ>
+__global__ void __launch_bounds__(256, RZ <= 6 ? 2 : 1) k_z_adj2(const __grid_constant__ ZAArgs a) {
+  constexpr int KZ = 2 * RZ + 1, S = KZ, NT = 256;
+  extern __shared__ __align__(16) float2 zring2[];  // [S][NT]
+  const int tid = threadIdx.x;
+  const int64_t u_begin = a.units * blockIdx.x / gridDim.x;
+  const int64_t u_end = a.units * (blockIdx.x + 1) / gridDim.x;
+  const uint32_t my_slot0 = smem_u32(zring2 + tid);
+  const int64_t np = (int64_t)a.npx * a.ny;
+
+  for (int64_t u = u_begin; u < u_end;) {
+    const int64_t blk = u / a.nz;
+    const int zs = (int)(u - blk * a.nz);
+    const int64_t zrem = zs + (u_end - u);
+    const int ze = zrem < a.nz ? (int)zrem : a.nz;
+    u += ze - zs;
+    const int64_t q = blk * NT + tid;
+    if (q >= np) continue;
+    const int cy = (int)(q / a.npx), px = (int)(q - (int64_t)cy * a.npx);
+    const int cx = 2 * px;
+    const int jb = zs - RZ, je = ze - 1 + RZ;
+    const char* const src = a.in + (int64_t)cx * a.in_pitch[0] + (int64_t)cy * a.in_pitch[1];
+    int jn = jb;
+    auto prefetch = [&](int stage) {  // slice jn, clamped to the image (a valid address)
+      cp_async8(my_slot0 + (uint32_t)(stage * NT * 8), src + (int64_t)clampi(jn, 0, a.nz - 1) * a.in_pitch[2]);
+      fusedk::cp_async_commit();
+      ++jn;
+    };
+#pragma unroll
+    for (int i = 0; i < S; ++i) prefetch(i);
+    f2_t acc[2][KZ];  // [weight set][slot]
+#pragma unroll
+    for (int m = 0; m < 2; ++m)
+#pragma unroll
+      for (int k = 0; k < KZ; ++k) acc[m][k] = 0ull;
+    f2_t flo[2] = {0ull, 0ull}, fhi[2] = {0ull, 0ull};
+    const bool two = cx + 1 < a.nx;
+    const int64_t ooff = (int64_t)cx * a.out_pitch[0] + (int64_t)cy * a.out_pitch[1] + (int64_t)zs * a.out_pitch[2];
+    char* dz = a.out + ooff;
+    char* dz2 = a.out2 + ooff;
+    for (int jbase = jb; jbase <= je; jbase += KZ) {
+#pragma unroll
+      for (int p = 0; p < KZ; ++p) {
+        const int j = jbase + p;
+        if (j > je) break;
+        fusedk::cp_async_wait<S - 1>();
+        const float2 f = zring2[p * NT + tid];
+        prefetch(p);
+        const bool inside = j >= 0 && j < a.nz;  // outside: zero (no contribution)
+        const f2_t v = inside ? pack2(f.x, f.y) : 0ull;
+#pragma unroll
+        for (int k = 0; k < KZ; ++k) {
+          const int slot = (p - k + KZ) % KZ;
+          const int kk = k <= RZ ? k : 2 * RZ - k;
+          acc[0][slot] = k == 0 ? mul2(v, a.wz2[kk]) : fma2(v, a.wz2[kk], acc[0][slot]);
+          acc[1][slot] = k == 0 ? mul2(v, a.wz2d[kk]) : fma2(v, a.wz2d[kk], acc[1][slot]);
+        }
+        // folds: the clamped taps of slices 0 .. R-1 onto slice 0, of the last R onto the last
+        if (inside && j < RZ) {
+          const float c = a.pz[RZ - j], cd = a.pzd[RZ - j];
+          flo[0] = fma2(v, pack2(c, c), flo[0]);
+          flo[1] = fma2(v, pack2(cd, cd), flo[1]);
+        }
+        if (inside && j > a.nz - 1 - RZ) {
+          const float c = a.pz[RZ - (a.nz - 1 - j)], cd = a.pzd[RZ - (a.nz - 1 - j)];
+          fhi[0] = fma2(v, pack2(c, c), fhi[0]);
+          fhi[1] = fma2(v, pack2(cd, cd), fhi[1]);
+        }
+        const int D = (p + 1) % KZ;
+        const int z = j - RZ;
+        if (z >= zs) {
+          f2_t d0 = acc[0][D], d1 = acc[1][D];
+          if (z == 0) d0 = add2(d0, flo[0]), d1 = add2(d1, flo[1]);
+          if (z == a.nz - 1) d0 = add2(d0, fhi[0]), d1 = add2(d1, fhi[1]);
+          float o0, o1, e0, e1;
+          unpack2(d0, o0, o1);
+          unpack2(d1, e0, e1);
+          if (two) {
+            *reinterpret_cast<float2*>(dz) = make_float2(o0, o1);
+            *reinterpret_cast<float2*>(dz2) = make_float2(e0, e1);
+          } else {
+            *reinterpret_cast<float*>(dz) = o0;
+            *reinterpret_cast<float*>(dz2) = e0;
+          }
+          dz += a.out_pitch[2];
+          dz2 += a.out_pitch[2];
         }
       }
     }
