@@ -196,3 +196,20 @@ def test_host_buffers_staged(gpu, reps):
     want = oracle.binomial_f32(x, reps)
     got, k = run(gpu, lambda s, **kw: gpu.BinomialBlurFilter(s, reps, **kw), x, host=True)
     assert bits_equal(got, want), k
+
+
+@pytest.mark.parametrize("r", [1, 2, 5])
+def test_mean_u8_pixel_arithmetic_takes_the_two_pass_kernels(gpu, r):
+    """MeanFilter over Image<u8, 3> in u8 pixel arithmetic (one round of a
+    symmetric kernel): the two-pass u8 kernels, bit-identical to the oracle
+    and to the per-axis passes."""
+    x = np.random.default_rng(40 + r).integers(0, 256, (18, 30, 48), dtype=np.uint8)
+    k = oracle.box_kernel(r)
+    want = oracle.separable_u8(x, [k, k, k])
+    make = lambda s, **kw: gpu.MeanFilter(s, r, **kw)
+    got, kern = run(gpu, make, x, arithmetic=gpu.ARITH_PIXEL_U8, out_dtype=gpu.U8)
+    assert kern == "z_pass_u8_pixel", kern
+    assert np.array_equal(got, want)
+    got, kern = run(gpu, make, x, algo="per_axis", arithmetic=gpu.ARITH_PIXEL_U8, out_dtype=gpu.U8)
+    assert kern != "z_pass_u8_pixel", kern
+    assert np.array_equal(got, want)
