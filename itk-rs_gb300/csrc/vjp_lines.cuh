@@ -13,11 +13,14 @@
 // thread filters kRun consecutive outputs of one line, reading each of the
 // kRun + 2r staged values its outputs reach once (push form, accumulators in
 // registers).  Each input value is read from global memory (kLen + 2r) / kLen
-// times instead of once per tap and output run.
+// times instead of once per tap and output run.  The accumulators are packed
+// pairs of adjacent outputs, so one fma.rn.f32x2 adds a staged value to two
+// outputs (each lane's sum is the scalar fmaf chain's, bit for bit).
 #pragma once
 
 #include <cuda_runtime.h>
 
+#include "f32x2.cuh"
 #include "internal.hpp"
 
 namespace itkg {
@@ -33,7 +36,19 @@ constexpr int kThreads = kLines * kSegs;   // 128
 struct LineTaps {
   float w[2 * kMaxR + 1];
   float aux[2 * kMaxR + 1];  // dw/dsigma (dual pass) or the prefix sums P (adjoint pass)
+  // tap pairs of an output pair (j, j + 1) and the staged value j + d:
+  // wp[d] = (w[d], w[d - 1]), ap[d] = (aux[d], aux[d - 1]), for 1 <= d <= 2r
+  f2_t wp[2 * kMaxR + 1];
+  f2_t ap[2 * kMaxR + 1];
 };
+
+// Host: fills the tap pairs from w and aux (k = 0 .. 2r).
+inline void line_taps_pairs(LineTaps* T, int r) {
+  for (int d = 1; d <= 2 * r; ++d) {
+    T->wp[d] = pack2_host(T->w[d], T->w[d - 1]);
+    T->ap[d] = pack2_host(T->aux[d], T->aux[d - 1]);
+  }
+}
 
 struct LineGeom {
   int32_t n;           // image size along the pass axis
@@ -157,26 +172,48 @@ __device__ __forceinline__ void tile_pitches(const int64_t* pitch, int axis, int
 // Push-form filtering of one line's window: staged value q (positions
 // p0 + seg kRun - R + q) is read from shared memory once and added, times the
 // tap weight, to every output j of the thread's run that it reaches (tap
-// k = q - j), so each output still sums its taps in ascending order.  W2 adds
-// T.aux's taps into acc2 (the dual pass's G' of the same values).
+// k = q - j), so each output still sums its taps in ascending order.  acc[h]
+// packs outputs 2h and 2h + 1: where both taps exist (1 <= q - 2h <= 2R) one
+// packed fma adds the value to both, at q - 2h = 0 (2R + 1) only the first
+// (second) output takes it.  W2 adds T.aux's taps into acc2 the same way (the
+// dual pass's G' of the same values).
 template <int R, bool AX0, bool W2>
-__device__ __forceinline__ void filter_run(const float* s, int li, int seg, const LineTaps& T, float (&acc)[kRun],
-                                           float (&acc2)[kRun]) {
+__device__ __forceinline__ void filter_run(const float* s, int li, int seg, const LineTaps& T,
+                                           f2_t (&acc)[kRun / 2], f2_t (&acc2)[kRun / 2]) {
   using C = LineCfg<R, AX0>;
   constexpr int K = C::K;
   const float* const p = s + li * C::LS + seg * kRun * C::PS;
 #pragma unroll
   for (int q = 0; q < C::WIN; ++q) {
     const float x = p[q * C::PS];
+    const f2_t xx = pack2(x, x);
 #pragma unroll
-    for (int j = 0; j < kRun; ++j) {
-      const int k = q - j;
-      if (k >= 0 && k < K) {
-        acc[j] = fmaf(T.w[k], x, acc[j]);
-        if constexpr (W2) acc2[j] = fmaf(T.aux[k], x, acc2[j]);
+    for (int h = 0; h < kRun / 2; ++h) {
+      const int d = q - 2 * h;  // output 2h takes tap d, output 2h + 1 tap d - 1
+      if (d >= 1 && d < K) {
+        acc[h] = fma2(xx, T.wp[d], acc[h]);
+        if constexpr (W2) acc2[h] = fma2(xx, T.ap[d], acc2[h]);
+      } else if (d == 0 || d == K) {
+        float lo, hi;
+        unpack2(acc[h], lo, hi);
+        if (d == 0) lo = fmaf(T.w[0], x, lo);
+        else hi = fmaf(T.w[K - 1], x, hi);
+        acc[h] = pack2(lo, hi);
+        if constexpr (W2) {
+          unpack2(acc2[h], lo, hi);
+          if (d == 0) lo = fmaf(T.aux[0], x, lo);
+          else hi = fmaf(T.aux[K - 1], x, hi);
+          acc2[h] = pack2(lo, hi);
+        }
       }
     }
   }
+}
+
+// The run's outputs as scalars.
+__device__ __forceinline__ void unpack_run(const f2_t (&a)[kRun / 2], float (&v)[kRun]) {
+#pragma unroll
+  for (int h = 0; h < kRun / 2; ++h) unpack2(a[h], v[2 * h], v[2 * h + 1]);
 }
 
 // Tile index -> (first line, first pass position, other).
@@ -254,11 +291,14 @@ __global__ void __launch_bounds__(kThreads) k_line_dual(const VjpAxisArgs a, con
   if (has_d) stage_tile<R, AX0, true>(sd, reinterpret_cast<const char*>(a.din) + oo, lp, pp, g, l0, p0);
   stage_wait();
   const int li = threadIdx.x % kLines, seg = threadIdx.x / kLines;
-  float v[kRun], dv[kRun];
+  f2_t v2[kRun / 2], d2[kRun / 2];
 #pragma unroll
-  for (int j = 0; j < kRun; ++j) v[j] = 0.0f, dv[j] = 0.0f;
-  filter_run<R, AX0, true>(sx, li, seg, T, v, dv);
-  if (has_d) filter_run<R, AX0, false>(sd, li, seg, T, dv, dv);
+  for (int h = 0; h < kRun / 2; ++h) v2[h] = 0ull, d2[h] = 0ull;
+  filter_run<R, AX0, true>(sx, li, seg, T, v2, d2);
+  if (has_d) filter_run<R, AX0, false>(sd, li, seg, T, d2, d2);
+  float v[kRun], dv[kRun];
+  unpack_run(v2, v);
+  unpack_run(d2, dv);
   if constexpr (AX0) __syncthreads();  // the staged input is free for the output rows
   store_runs<AX0>(a, g, smem, l0, p0, o, li, seg, v, dv, true, false);
 }
@@ -276,10 +316,12 @@ __global__ void __launch_bounds__(kThreads) k_line_adjoint(const VjpAxisArgs a, 
   stage_tile<R, AX0, false>(smem, reinterpret_cast<const char*>(a.in) + oo, lp, pp, g, l0, p0);
   stage_wait();
   const int li = threadIdx.x % kLines, seg = threadIdx.x / kLines;
-  float acc[kRun];
+  f2_t a2[kRun / 2];
 #pragma unroll
-  for (int j = 0; j < kRun; ++j) acc[j] = 0.0f;
-  filter_run<R, AX0, false>(smem, li, seg, T, acc, acc);
+  for (int h = 0; h < kRun / 2; ++h) a2[h] = 0ull;
+  filter_run<R, AX0, false>(smem, li, seg, T, a2, a2);
+  float acc[kRun];
+  unpack_run(a2, acc);
   // the edge folds (rare: only the tiles holding position 0 or n - 1)
   if (l0 + li < g.nlines && (p0 == 0 || p0 + kLen >= g.n)) {
     const float* const sl = smem + li * C::LS;

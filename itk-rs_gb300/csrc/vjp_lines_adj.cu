@@ -24,6 +24,7 @@ itkg_status launch_line_adjoint(const VjpAxisArgs& a, const float* w, const floa
   LineTaps T;
   std::memset(&T, 0, sizeof T);
   for (int k = 0; k < 2 * a.radius + 1; ++k) T.w[k] = w[k], T.aux[k] = prefix[k];
+  line_taps_pairs(&T, a.radius);
   const Row& r = kAdj[a.radius - kMinR];
   const LineFn fn = a.axis == 0 ? r.ax0 : r.ax12;
   const size_t smem = sizeof(float) *

@@ -24,6 +24,7 @@ itkg_status launch_line_dual(const VjpAxisArgs& a, const float* w, const float* 
   LineTaps T;
   std::memset(&T, 0, sizeof T);
   for (int k = 0; k < 2 * a.radius + 1; ++k) T.w[k] = w[k], T.aux[k] = dw[k];
+  line_taps_pairs(&T, a.radius);
   const Row& r = kDual[a.radius - kMinR];
   const LineFn fn = a.axis == 0 ? r.ax0 : r.ax12;
   const size_t smem = 2 * sizeof(float) *
