@@ -103,24 +103,25 @@ __device__ __forceinline__ void stage_tile(float* s, const char* base, int64_t l
   // positions p0 - R .. p0 + kLen + R - 1 all inside the image: no clamping
   const bool interior = p0 - R >= 0 && p0 + kLen + R <= g.n;
   if constexpr (AX0) {
-    // one line after another, consecutive threads on consecutive x
-    static_assert(C::NP <= 2 * kThreads, "two positions per thread and line at most");
+    // thread pi stages position pi of every line (consecutive threads on
+    // consecutive x): its position, clamp and in-image test are fixed, and
+    // its source steps by one line pitch
+    static_assert(C::NP <= kThreads, "one position per thread and line");
+    const int pi = threadIdx.x;
+    if (pi < C::NP) {
+      int p = p0 - R + pi;
+      bool pin = true;
+      if (!interior) {
+        if (CLAMP) p = clamp_i(p, 0, g.n - 1);
+        pin = p >= 0 && p < g.n;
+      }
+      const int nl = min(kLines, g.nlines - l0);  // lines of the tile inside the image (>= 1)
+      const char* src = base + (int64_t)(pin ? p : 0) * pp + (int64_t)l0 * lp;
+      float* dst = s + pi;
 #pragma unroll 4
-    for (int li = 0; li < kLines; ++li) {
-      const int l = l0 + li;
-      const bool lin = l < g.nlines;
-      const char* const row = base + (int64_t)(lin ? l : 0) * lp;
-#pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const int pi = threadIdx.x + h * kThreads;
-        if (pi >= C::NP) break;
-        int p = p0 - R + pi;
-        bool in = lin;
-        if (!interior) {
-          if (CLAMP) p = clamp_i(p, 0, g.n - 1);
-          in = in && p >= 0 && p < g.n;
-        }
-        cp4(s + li * C::PP + pi, in ? row + (int64_t)p * pp : base, !in);
+      for (int li = 0; li < kLines; ++li, src += lp, dst += C::PP) {
+        const bool in = pin && li < nl;
+        cp4(dst, in ? src : base, !in);
       }
     }
   } else {
@@ -246,15 +247,22 @@ __device__ __forceinline__ void store_runs(const VjpAxisArgs& a, const LineGeom&
       if (two) s[(kLines + li) * kOutPitch + seg * kRun + j] = dv[j];
     }
     __syncthreads();
-    for (int e = threadIdx.x; e < kLines * kLen; e += kThreads) {
-      const int lj = e / kLen, pj = e % kLen;
-      const int l = l0 + lj, p = p0 + pj;
-      if (l >= g.nlines || p >= g.n) continue;
-      const int64_t off = line_off<true>(a.out_pitch, 0, l, p, o);
-      float* const po = reinterpret_cast<float*>(ob + off);
-      const float r = s[lj * kOutPitch + pj];
-      *po = acc ? *po + r : r;
-      if (two) *reinterpret_cast<float*>(db + off) = s[(kLines + lj) * kOutPitch + pj];
+    // thread t writes position t % kLen of lines t / kLen, + kThreads / kLen, ...
+    static_assert(kThreads % kLen == 0, "whole rows per step");
+    constexpr int LSTEP = kThreads / kLen;
+    const int pj = threadIdx.x % kLen;
+    const int p = p0 + pj;
+    if (p < g.n) {
+      const int nl = min(kLines, g.nlines - l0);  // lines of the tile inside the image
+      int lj = threadIdx.x / kLen;
+      int64_t off = line_off<true>(a.out_pitch, 0, l0 + lj, p, o);
+      const int64_t step = (int64_t)LSTEP * a.out_pitch[1];
+      for (; lj < nl; lj += LSTEP, off += step) {
+        float* const po = reinterpret_cast<float*>(ob + off);
+        const float r = s[lj * kOutPitch + pj];
+        *po = acc ? *po + r : r;
+        if (two) *reinterpret_cast<float*>(db + off) = s[(kLines + lj) * kOutPitch + pj];
+      }
     }
   } else {
     const int l = l0 + li;
